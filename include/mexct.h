@@ -1,0 +1,180 @@
+/*
+ * mexct.h -- C ABI of libmexct, a GB300 (sm_103a) implementation of the
+ * mex-cuda-CT projection-operator path.
+ *
+ * Conventions shared by every entry point
+ *   - Arrays are MATLAB column-major float32 ("single"):
+ *       volume   [W,W,H]   index x + W*y + W*W*z
+ *       sinogram [W,H,nP]  index u + W*v + W*H*view
+ *       pts      [W,H,6]   planes x1,y1,z1,x2,y2,z2 (or [W,H,6,nP] per view)
+ *   - Angles are float32 radians (MATLAB single), one per view.
+ *   - geom: 0 parallel, 1 stacked fan, 2 cone (the reference's geomFlag).
+ *   - Host entry points (no suffix) take host pointers, copy in, compute on
+ *     the GPU and copy out before returning (the MEX gateway contract).
+ *     Pinned host buffers give full-speed copies; pageable ones work too.
+ *   - Device entry points (suffix _dev) take device pointers and a CUDA
+ *     stream (cudaStream_t passed as void*, NULL = legacy default stream);
+ *     they are stream-ordered and return without synchronising.
+ *   - ctx may be NULL: a per-device default context is used.
+ *   - Every call returns a mexct_status; mexct_last_error() gives the text of
+ *     the last failure on the calling thread.  Nothing aborts, longjmps or
+ *     resets the device (the reference's CUDAmex_oscIter.cu:582 calls
+ *     cudaDeviceReset; this library never does).
+ */
+#ifndef MEXCT_H
+#define MEXCT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int mexct_status;
+#define MEXCT_OK 0
+#define MEXCT_ERR_ARG 1         /* invalid argument (dims, geom, null, ...) */
+#define MEXCT_ERR_CUDA 2        /* CUDA runtime error */
+#define MEXCT_ERR_OOM 3         /* device allocation failed */
+#define MEXCT_ERR_UNSUPPORTED 4 /* valid in the reference but not supported */
+#define MEXCT_ERR_TIMEOUT 5     /* a bounded device-side wait gave up */
+#define MEXCT_ERR_BUDGET 6      /* request exceeds the admission budget */
+
+/* Storage types for the _ex entry points. */
+#define MEXCT_F32 0
+#define MEXCT_F16 1
+#define MEXCT_BF16 2
+
+/* FP implementation variants for the _ex entry points. */
+#define MEXCT_FP_EXPLICIT 0 /* FP32 trilinear in software (parity path) */
+#define MEXCT_FP_TEXTURE 1  /* hardware 3D texture, 8-bit filter weights */
+
+typedef struct mexct_ctx mexct_ctx;
+
+const char* mexct_last_error(void);
+const char* mexct_version(void);
+
+/* Context: owns the stream used by host entry points, grow-only device
+ * workspaces and the autotune cache.  One context per device and thread
+ * (or serialise calls on a shared one). */
+mexct_status mexct_ctx_create(int device, mexct_ctx** out);
+mexct_status mexct_ctx_destroy(mexct_ctx* ctx);
+/* Release the context's workspaces (they are re-created on demand). */
+mexct_status mexct_ctx_trim(mexct_ctx* ctx);
+
+/* ---- MEX-equivalent host entry points --------------------------------- */
+
+/* fp = CUDAmex_FP(vol, SAD, angles, nProj, geomFlag)
+ * Replaces projection_kernels/CUDAmex_FP.cu:350-477 (kernels :56-346).
+ * vol [W,W,H] -> out [W,H,nP].  Clamp addressing; step 0.5 (par, fan) or 1.0
+ * (cone).  Every detector row is computed (the reference skips rows
+ * iy >= 32*ceil(W/32), CUDAmex_FP.cu:432-440). */
+mexct_status mexct_fp(mexct_ctx* ctx, const float* vol, int W, int H,
+                      float sad, const float* angles, int nP, int geom,
+                      float* out);
+
+/* bp = CUDAmex_BP(sino, SAD, angles, geomFlag)
+ * Replaces projection_kernels/CUDAmex_BP.cu:223-324 (kernels :44-221).
+ * sino [W,H,nP] -> vol [W,W,H] (zero outside the circle h = W/2-1). */
+mexct_status mexct_bp(mexct_ctx* ctx, const float* sino, int W, int H,
+                      int nP, float sad, const float* angles, int geom,
+                      float* vol);
+
+/* fp = CUDAmex_general3D_FP(vol, angles, pts, nProj)
+ * Replaces projection_kernels/CUDAmex_general3D_FP.cu:154-252 (kernel
+ * :59-150).  vol [S,S,Z], pts [W,H,6] shared by all views (pts_per_view=0,
+ * the reference's form) or [W,H,6,nP] (pts_per_view=1, an extension for
+ * helical scans).  Border addressing, step 0.5. */
+mexct_status mexct_g3d_fp(mexct_ctx* ctx, const float* vol, int S, int Z,
+                          const float* angles, const float* pts, int W,
+                          int H, int nP, int pts_per_view, float* out);
+
+/* bp = CUDAmex_general3D_BP(sino, angles, pts, S, Z)
+ * Replaces projection_kernels/CUDAmex_general3D_BP.cu:194-282 (kernel
+ * :61-188): ray-driven two-corner scatter, transcribed exactly. */
+mexct_status mexct_g3d_bp(mexct_ctx* ctx, const float* sino, int W, int H,
+                          int nP, const float* angles, const float* pts,
+                          int pts_per_view, int S, int Z, float* vol);
+
+/* CUDAmex_oscIter(mu, pre, post, nSub, subsetPicks, angles, SAD, geomFlag)
+ * Replaces iterative_reconstruction/CUDAmex_oscIter.cu:362-584 (kernels
+ * :94-358).  mu [W,W,H] is updated in place; pre/post [W,H,nP] are NOT
+ * modified (the reference overwrites them, :527-528). */
+mexct_status mexct_osc_iter(mexct_ctx* ctx, float* mu, const float* pre,
+                            const float* post, int W, int H, int nP,
+                            int nSub, const int32_t* picks,
+                            const float* angles, float sad, int geom);
+
+/* out = CUDAmex_TVmin_3D(vol, c)
+ * Replaces iterative_reconstruction/CUDAmex_TVmin_3D.cu:162-246 (kernel
+ * :101-158, thrust norm/saxpy :221-234).  n_steps = 20 in the reference.
+ * Border gradient is 0 (the reference leaves it uninitialised); the
+ * gradient norm is reduced in FP64. */
+mexct_status mexct_tvmin3d(mexct_ctx* ctx, const float* vol, int Nx, int Ny,
+                           int Nz, float c, int n_steps, float* out);
+
+/* filteredSino = preFilterSinogram(sino, geom, angles, filter, cutoff, q)
+ * Replaces fbp_reconstruction/preFilterSinogram.m:1-90 and
+ * parker_weight.m:1-98.  filter: 0 none, 1 ramp, 2 shepp-logan, 3 cosine,
+ * 4 hamming, 5 hann.  Requires W == H and nP >= 2, as the reference does.
+ * log_input != 0 first applies FBP_recon.m:26-28 (sino = -log(post/pre),
+ * NaN/Inf -> 0) with sino = post and pre_or_null = pre. */
+mexct_status mexct_prefilter(mexct_ctx* ctx, const float* sino,
+                             const float* pre_or_null, int W, int H, int nP,
+                             const float* angles, int geom, float sad,
+                             int filter, float cutoff, float q, float* out);
+
+/* recon = FBP_recon(pre, post, angles, geom, filter, cutoff, q)
+ * Replaces fbp_reconstruction/FBP_recon.m:1-41 on the device: log
+ * transform, pre-filter and BP with no host round trip. */
+mexct_status mexct_fbp(mexct_ctx* ctx, const float* pre, const float* post,
+                       int W, int H, int nP, const float* angles, int geom,
+                       float sad, int filter, float cutoff, float q,
+                       float* recon);
+
+/* ---- device-pointer twins (stream-ordered) ---------------------------- */
+
+mexct_status mexct_fp_dev(mexct_ctx* ctx, const float* d_vol, int W, int H,
+                          float sad, const float* angles, int nP, int geom,
+                          float* d_out, void* stream);
+mexct_status mexct_bp_dev(mexct_ctx* ctx, const float* d_sino, int W, int H,
+                          int nP, float sad, const float* angles, int geom,
+                          float* d_vol, void* stream);
+mexct_status mexct_g3d_fp_dev(mexct_ctx* ctx, const float* d_vol, int S,
+                              int Z, const float* angles, const float* d_pts,
+                              int W, int H, int nP, int pts_per_view,
+                              float* d_out, void* stream);
+mexct_status mexct_g3d_bp_dev(mexct_ctx* ctx, const float* d_sino, int W,
+                              int H, int nP, const float* angles,
+                              const float* d_pts, int pts_per_view, int S,
+                              int Z, float* d_vol, void* stream);
+mexct_status mexct_osc_iter_dev(mexct_ctx* ctx, float* d_mu,
+                                const float* d_pre, const float* d_post,
+                                int W, int H, int nP, int nSub,
+                                const int32_t* picks, const float* angles,
+                                float sad, int geom, void* stream);
+mexct_status mexct_tvmin3d_dev(mexct_ctx* ctx, const float* d_vol, int Nx,
+                               int Ny, int Nz, float c, int n_steps,
+                               float* d_out, void* stream);
+mexct_status mexct_prefilter_dev(mexct_ctx* ctx, const float* d_sino,
+                                 const float* d_pre_or_null, int W, int H,
+                                 int nP, const float* angles, int geom,
+                                 float sad, int filter, float cutoff,
+                                 float q, float* d_out, void* stream);
+
+/* Extended FP/BP: storage type of the volume and sinogram (MEXCT_F32,
+ * MEXCT_F16, MEXCT_BF16; accumulation is always FP32) and the FP variant
+ * (MEXCT_FP_EXPLICIT or MEXCT_FP_TEXTURE, FP32 storage only). */
+mexct_status mexct_fp_dev_ex(mexct_ctx* ctx, const void* d_vol, int vol_type,
+                             int W, int H, float sad, const float* angles,
+                             int nP, int geom, void* d_out, int out_type,
+                             int variant, void* stream);
+mexct_status mexct_bp_dev_ex(mexct_ctx* ctx, const void* d_sino,
+                             int sino_type, int W, int H, int nP, float sad,
+                             const float* angles, int geom, void* d_vol,
+                             int vol_type, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MEXCT_H */

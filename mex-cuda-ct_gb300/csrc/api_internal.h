@@ -1,0 +1,84 @@
+// api_internal.h -- context and helpers shared by the host translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <initializer_list>
+#include <mutex>
+#include <vector>
+
+#include "../../include/mexct.h"
+#include "kernels.h"
+
+namespace mexct {
+
+// Grow-only device buffer.
+struct Buf {
+  void* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t bytes);
+  void release();
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+}  // namespace mexct
+
+struct mexct_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;     // stream of the host entry points
+  std::recursive_mutex mu;           // serialises calls on this context
+  // Host entry points: staged inputs / outputs.
+  mexct::Buf in, in2, in3, out;
+  // Device entry points: transposed volume, subset residuals / TV ping-pong,
+  // filter tables, FP64 reduction partials, counter and scalars.
+  mexct::Buf volT, r1, r2, r3, tabs, red, cnt, scal;
+  // Texture variant: cached 3D array + texture object.
+  cudaArray_t tex_arr = nullptr;
+  cudaTextureObject_t tex = 0;
+  int tex_w = 0, tex_h = 0;
+  // Pre-filter kernel cache.
+  int filt_w = -1, filt_type = -1;
+  float filt_cut = -1.f;
+  std::vector<float> filt_kern;
+
+  std::vector<mexct::Buf*> all_bufs() {
+    return {&in, &in2, &in3, &out, &volT, &r1, &r2, &r3, &tabs, &red, &cnt, &scal};
+  }
+};
+
+namespace mexct {
+
+mexct_status set_err(mexct_status code, const char* fmt, ...);
+mexct_status cuda_err(cudaError_t e, const char* what);
+void trig_of(float beta, Trig* t);
+mexct_ctx* resolve(mexct_ctx* ctx);
+cudaError_t ensure_reduction(mexct_ctx* c, size_t nparts);
+void fill_std_rays(RayArgs& a, int W, int H, float sad, int geom, bool osc);
+void fill_vox(VoxArgs& a, int W, int H, float sad);
+
+// Scoped device switch to the context's device.
+struct DevGuard {
+  int prev = -1;
+  explicit DevGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DevGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+inline size_t dsize(int t) { return t == kF32 ? 4 : 2; }
+
+}  // namespace mexct
+
+#define MEXCT_TRY_CUDA(expr, what)                         \
+  do {                                                     \
+    cudaError_t _e = (expr);                               \
+    if (_e != cudaSuccess) return ::mexct::cuda_err(_e, what); \
+  } while (0)

@@ -1,0 +1,363 @@
+// k_iter.cu -- TV descent, FP64 reductions and the FDK/FBP pre-filter.
+//
+// TV (CUDAmex_TVmin_3D.cu:101-234).  The reference runs three full-volume
+// passes per step (gradient kernel -> thrust norm -> thrust saxpy) and stores
+// the gradient.  Here a step is two passes and no gradient volume:
+//   tv_norm_kernel   gradient recomputed per voxel, ||g||^2 reduced in FP64
+//                    (warp shuffles, per-CTA partials, last-CTA fixed-order
+//                    sum: deterministic), step scale -c/||g|| written to HBM;
+//   tv_update_kernel gradient recomputed, y = x + scale*g into the other
+//                    buffer of a ping-pong pair.
+// Algorithmic traffic is 12 bytes per voxel per step (read x twice, write y).
+#include <cstdio>
+
+#include "kernels.h"
+
+namespace mexct {
+
+// ---------------------------------------------------------------------------
+// TV gradient of one interior voxel (CUDAmex_TVmin_3D.cu:121-152), FP32.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ float tv_grad(const T* __restrict__ v, size_t i,
+                                         size_t sy, size_t sz) {
+  const float eps = 1.0e-6f;
+  const float x = ldf(v + i);
+  const float xm = ldf(v + i - 1), xp = ldf(v + i + 1);
+  const float ym = ldf(v + i - sy), yp = ldf(v + i + sy);
+  const float zm = ldf(v + i - sz), zp = ldf(v + i + sz);
+  const float xmyp = ldf(v + i - 1 + sy), xpym = ldf(v + i + 1 - sy);
+  const float ymzp = ldf(v + i - sy + sz), ypzm = ldf(v + i + sy - sz);
+  const float xmzp = ldf(v + i - 1 + sz), xpzm = ldf(v + i + 1 - sz);
+  const float a = x - xm, b = x - ym, c = x - zm;
+  float t = ((a + b) + c) / (eps + sqrtf(a * a + b * b + c * c));
+  const float d1 = xp - x, e1 = xp - xpym, f1 = xp - xpzm;
+  t -= d1 / (eps + sqrtf(d1 * d1 + e1 * e1 + f1 * f1));
+  const float d2 = yp - x, e2 = yp - xmyp, f2 = yp - ypzm;
+  t -= d2 / (eps + sqrtf(d2 * d2 + e2 * e2 + f2 * f2));
+  const float d3 = zp - x, e3 = zp - xmzp, f3 = zp - ymzp;
+  t -= d3 / (eps + sqrtf(d3 * d3 + e3 * e3 + f3 * f3));
+  return t;
+}
+
+__device__ __forceinline__ bool tv_interior(int ix, int iy, int iz, int Nx,
+                                            int Ny, int Nz) {
+  return ix >= 1 && iy >= 1 && iz >= 1 && ix < Nx - 1 && iy < Ny - 1 &&
+         iz < Nz - 1;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-level FP64 sum with a fixed tree (deterministic); blockDim.x*y*z
+// threads, result valid in thread 0.
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double red[32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  v = warp_sum(v);
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (tid < 32) {
+    r = (tid < (nt + 31) / 32) ? red[tid] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// Last-CTA finalisation: every CTA stores its partial, the last one to arrive
+// sums all partials in index order (deterministic).  Returns true in thread 0
+// of the last CTA with *total set.
+__device__ __forceinline__ bool finish_partials(double mine, double* partials,
+                                                unsigned* counter,
+                                                double* total) {
+  __shared__ bool last;
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nt = blockDim.x * blockDim.y * blockDim.z;
+  const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (tid == 0) {
+    partials[bid] = mine;
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == nb - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double acc = 0.0;
+  for (unsigned i = tid; i < nb; i += nt) acc += __ldcg(partials + i);
+  acc = block_sum(acc);
+  if (tid == 0) {
+    *total = acc;
+    *counter = 0u;  // ready for the next launch on this stream
+  }
+  return tid == 0;
+}
+
+constexpr int kTvBx = 32, kTvBy = 8, kTvZ = 4;  // each thread: kTvZ voxels in z
+
+template <typename T>
+__global__ void __launch_bounds__(256) tv_norm_kernel(
+    const T* __restrict__ x, int Nx, int Ny, int Nz, float c,
+    double* __restrict__ partials, unsigned* __restrict__ counter,
+    float* __restrict__ scale, double* __restrict__ norm) {
+  const int ix = blockIdx.x * kTvBx + threadIdx.x;
+  const int iy = blockIdx.y * kTvBy + threadIdx.y;
+  const size_t sy = (size_t)Nx, sz = (size_t)Nx * Ny;
+  double ss = 0.0;
+  for (int j = 0; j < kTvZ; ++j) {
+    const int iz = blockIdx.z * kTvZ + j;
+    if (ix < Nx && iy < Ny && iz < Nz && tv_interior(ix, iy, iz, Nx, Ny, Nz)) {
+      const float g = tv_grad(x, (size_t)ix + iy * sy + iz * sz, sy, sz);
+      ss += (double)g * (double)g;
+    }
+  }
+  const double blk = block_sum(ss);
+  double total;
+  if (finish_partials(blk, partials, counter, &total)) {
+    const double m = sqrt(total);
+    *norm = m;
+    *scale = (float)(-(double)c / m);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) tv_update_kernel(
+    const T* __restrict__ x, T* __restrict__ y, int Nx, int Ny, int Nz,
+    const float* __restrict__ scale) {
+  const int ix = blockIdx.x * kTvBx + threadIdx.x;
+  const int iy = blockIdx.y * kTvBy + threadIdx.y;
+  if (ix >= Nx || iy >= Ny) return;
+  const float a = __ldg(scale);
+  const size_t sy = (size_t)Nx, sz = (size_t)Nx * Ny;
+  for (int j = 0; j < kTvZ; ++j) {
+    const int iz = blockIdx.z * kTvZ + j;
+    if (iz >= Nz) break;
+    const size_t i = (size_t)ix + iy * sy + iz * sz;
+    const float xv = ldf(x + i);
+    // x <- a*g + x (thrust saxpy, CUDAmex_TVmin_3D.cu:232); border g = 0.
+    const float g = tv_interior(ix, iy, iz, Nx, Ny, Nz) ? tv_grad(x, i, sy, sz) : 0.f;
+    stf(y + i, fmaf(a, g, xv));
+  }
+}
+
+size_t tv_partials_needed(int Nx, int Ny, int Nz) {
+  return (size_t)((Nx + kTvBx - 1) / kTvBx) * ((Ny + kTvBy - 1) / kTvBy) *
+         ((Nz + kTvZ - 1) / kTvZ);
+}
+
+cudaError_t launch_tv_norm(const void* x, int xt, int Nx, int Ny, int Nz,
+                           float c, double* partials, unsigned* counter,
+                           float* scale, double* norm, cudaStream_t st) {
+  dim3 blk(kTvBx, kTvBy), grd((Nx + kTvBx - 1) / kTvBx, (Ny + kTvBy - 1) / kTvBy,
+                              (Nz + kTvZ - 1) / kTvZ);
+  if (xt == kF32)
+    tv_norm_kernel<float><<<grd, blk, 0, st>>>((const float*)x, Nx, Ny, Nz, c,
+                                               partials, counter, scale, norm);
+  else if (xt == kF16)
+    tv_norm_kernel<__half><<<grd, blk, 0, st>>>((const __half*)x, Nx, Ny, Nz,
+                                                c, partials, counter, scale, norm);
+  else
+    tv_norm_kernel<__nv_bfloat16><<<grd, blk, 0, st>>>(
+        (const __nv_bfloat16*)x, Nx, Ny, Nz, c, partials, counter, scale, norm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tv_update(const void* x, void* y, int xt, int Nx, int Ny,
+                             int Nz, const float* scale, cudaStream_t st) {
+  dim3 blk(kTvBx, kTvBy), grd((Nx + kTvBx - 1) / kTvBx, (Ny + kTvBy - 1) / kTvBy,
+                              (Nz + kTvZ - 1) / kTvZ);
+  if (xt == kF32)
+    tv_update_kernel<float><<<grd, blk, 0, st>>>((const float*)x, (float*)y,
+                                                 Nx, Ny, Nz, scale);
+  else if (xt == kF16)
+    tv_update_kernel<__half><<<grd, blk, 0, st>>>((const __half*)x,
+                                                  (__half*)y, Nx, Ny, Nz, scale);
+  else
+    tv_update_kernel<__nv_bfloat16><<<grd, blk, 0, st>>>(
+        (const __nv_bfloat16*)x, (__nv_bfloat16*)y, Nx, Ny, Nz, scale);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// ||a - b||^2 in FP64 with NaN differences dropped and, optionally, a[0]
+// taken as 0 (OSC_TV_recon.m:45,65-67: mu_old(1) = 0, mu_old(isnan) = 0).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) ssd_kernel(
+    const T* __restrict__ a, const T* __restrict__ b, long long n,
+    int zero_first, double* partials, unsigned* counter, double* out) {
+  double ss = 0.0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += stride) {
+    const float av = (zero_first && i == 0) ? 0.f : ldf(a + i);
+    const float d = av - ldf(b + i);
+    if (!isnan(d)) ss += (double)d * (double)d;
+  }
+  const double blk = block_sum(ss);
+  double total;
+  if (finish_partials(blk, partials, counter, &total)) *out = sqrt(total);
+}
+
+cudaError_t launch_ssd(const void* a, const void* b, int dt, long long n,
+                       int zero_first, double* partials, unsigned* counter,
+                       double* out, cudaStream_t st) {
+  const int blocks = 152 * 4;
+  if (dt == kF32)
+    ssd_kernel<float><<<blocks, 256, 0, st>>>((const float*)a, (const float*)b,
+                                              n, zero_first, partials, counter, out);
+  else if (dt == kF16)
+    ssd_kernel<__half><<<blocks, 256, 0, st>>>((const __half*)a,
+                                               (const __half*)b, n, zero_first,
+                                               partials, counter, out);
+  else
+    ssd_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(
+        (const __nv_bfloat16*)a, (const __nv_bfloat16*)b, n, zero_first,
+        partials, counter, out);
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void finite_kernel(T* x, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += stride) {
+    const float v = ldp(x + i);
+    if (!isfinite(v)) stf(x + i, 0.f);
+  }
+}
+
+cudaError_t launch_finite(void* x, int dt, long long n, cudaStream_t st) {
+  const int blocks = 152 * 8;
+  if (dt == kF32) finite_kernel<float><<<blocks, 256, 0, st>>>((float*)x, n);
+  else if (dt == kF16) finite_kernel<__half><<<blocks, 256, 0, st>>>((__half*)x, n);
+  else finite_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>((__nv_bfloat16*)x, n);
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void fill_kernel(T* x, long long n, float v) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += stride)
+    stf(x + i, v);
+}
+
+cudaError_t launch_fill(void* x, int dt, long long n, float v,
+                        cudaStream_t st) {
+  const int blocks = 152 * 8;
+  if (dt == kF32) fill_kernel<float><<<blocks, 256, 0, st>>>((float*)x, n, v);
+  else if (dt == kF16) fill_kernel<__half><<<blocks, 256, 0, st>>>((__half*)x, n, v);
+  else fill_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>((__nv_bfloat16*)x, n, v);
+  return cudaGetLastError();
+}
+
+template <typename S, typename D>
+__global__ void convert_kernel(const S* __restrict__ s, D* __restrict__ d,
+                               long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += stride)
+    stf(d + i, ldp(s + i));
+}
+
+cudaError_t launch_convert(const void* src, int st_, void* dst, int dt,
+                           long long n, cudaStream_t st) {
+  const int blocks = 152 * 8;
+#define CV(SA, DA) convert_kernel<SA, DA><<<blocks, 256, 0, st>>>((const SA*)src, (DA*)dst, n)
+  if (st_ == kF32 && dt == kF16) CV(float, __half);
+  else if (st_ == kF32 && dt == kBF16) CV(float, __nv_bfloat16);
+  else if (st_ == kF16 && dt == kF32) CV(__half, float);
+  else if (st_ == kBF16 && dt == kF32) CV(__nv_bfloat16, float);
+  else if (st_ == kF32 && dt == kF32) CV(float, float);
+  else return cudaErrorInvalidValue;
+#undef CV
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FDK/FBP pre-filter: per detector row, the cosine weight
+// (preFilterSinogram.m:38-57, 1-based U/V as written), the Parker window of
+// the row element (parker_weight.m:216-226, a host-built [nP, W] table), the
+// zero-padded ramp x window filter as a direct linear convolution with the
+// spatial kernel real(ifft(H)) (preFilterSinogram.m:72-78: padding to
+// order >= 2W makes the circular convolution linear), and the dbeta/2 factor
+// (:80-84).  Optional FBP_recon.m:26-28 log transform on load.
+// ---------------------------------------------------------------------------
+constexpr int kFiltRows = 4;
+
+__global__ void __launch_bounds__(256) prefilter_kernel(
+    const FiltArgs A, const float* __restrict__ sino,
+    const float* __restrict__ pre, const float* __restrict__ parker,
+    const float* __restrict__ dbeta, const float* __restrict__ kern,
+    float* __restrict__ out) {
+  extern __shared__ float sm[];
+  float* ks = sm;                       // order
+  float* xs = sm + A.order;             // kFiltRows * W
+  const int view = blockIdx.y;
+  const int v0 = blockIdx.x * kFiltRows;
+  const int W = A.W, H = A.H;
+  for (int i = threadIdx.x; i < A.order; i += blockDim.x) ks[i] = __ldg(kern + i);
+  const size_t vbase = (size_t)view * W * H;
+  const float db = __ldg(dbeta + view);
+  for (int r = 0; r < kFiltRows; ++r) {
+    const int v = v0 + r;
+    for (int u = threadIdx.x; u < W; u += blockDim.x) {
+      float w = 0.f;
+      if (v < H) {
+        const size_t gi = vbase + (size_t)v * W + u;
+        float s = __ldg(sino + gi);
+        if (A.log_input) {
+          s = -logf(s / __ldg(pre + gi));
+          if (!isfinite(s)) s = 0.f;
+        }
+        const float U = (float)(u + 1) - (float)(W - 1) * 0.5f;
+        const float V = (float)(v + 1) - (float)(H - 1) * 0.5f;
+        if (A.geom == 1) s *= A.sad / sqrtf(A.sad * A.sad + U * U);
+        if (A.geom == 2) s *= A.sad / sqrtf(A.sad * A.sad + U * U + V * V);
+        w = s * __ldg(parker + (size_t)view * W + u);
+      }
+      xs[r * W + u] = w;
+    }
+  }
+  __syncthreads();
+  const int mask = A.order - 1;
+  for (int u = threadIdx.x; u < W; u += blockDim.x) {
+    float acc[kFiltRows];
+#pragma unroll
+    for (int r = 0; r < kFiltRows; ++r) acc[r] = 0.f;
+    for (int j = 0; j < W; ++j) {
+      const float k = ks[(u - j) & mask];
+#pragma unroll
+      for (int r = 0; r < kFiltRows; ++r) acc[r] = fmaf(xs[r * W + j], k, acc[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < kFiltRows; ++r) {
+      const int v = v0 + r;
+      if (v < H) out[vbase + (size_t)v * W + u] = acc[r] * db;
+    }
+  }
+}
+
+cudaError_t launch_prefilter(const FiltArgs& a, const float* sino,
+                             const float* pre, const float* parker,
+                             const float* dbeta, const float* kern, float* out,
+                             cudaStream_t st) {
+  dim3 grd((a.H + kFiltRows - 1) / kFiltRows, a.nP);
+  const size_t smem = sizeof(float) * ((size_t)a.order + (size_t)kFiltRows * a.W);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(
+        prefilter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  prefilter_kernel<<<grd, 256, smem, st>>>(a, sino, pre, parker, dbeta, kern, out);
+  return cudaGetLastError();
+}
+
+}  // namespace mexct

@@ -1,0 +1,571 @@
+// k_proj.cu -- ray-driven forward projectors, voxel-driven backprojector and
+// the general3D scatter backprojector for sm_103a.
+//
+// Forward projection (CUDAmex_FP.cu:56-346, CUDAmex_general3D_FP.cu:59-150)
+//   One thread per detector pixel; a warp owns 32 consecutive pixels of one
+//   detector row, a CTA an 32x8 pixel tile of one view.  blockIdx.x is the
+//   view, so CTAs that are resident together march the same detector tile at
+//   neighbouring angles through the same part of the volume (L2 reuse).
+//   Samples are explicit FP32 trilinear fetches (the texture unit's 8-bit
+//   filter weights would miss a 1e-5 tolerance).  The volume is kept in two
+//   layouts, x-fastest and y-fastest: a view whose rays run mostly along x
+//   reads the y-fastest copy, so the 32 lanes of a warp (neighbouring u, i.e.
+//   neighbouring y) touch consecutive addresses.
+//
+// Backprojection (CUDAmex_BP.cu:44-221)
+//   One thread per (x, y) voxel column and a chunk of ZC voxels along z held
+//   in registers across all views; per-view geometry comes from the kernel
+//   parameter block (constant bank), the volume is written once.
+#include <cstdio>
+
+#include "kernels.h"
+
+namespace mexct {
+
+template <typename T>
+struct DT;
+template <>
+struct DT<float> {
+  static constexpr int id = kF32;
+};
+template <>
+struct DT<__half> {
+  static constexpr int id = kF16;
+};
+template <>
+struct DT<__nv_bfloat16> {
+  static constexpr int id = kBF16;
+};
+
+// ---------------------------------------------------------------------------
+// xy transpose (x-fastest <-> y-fastest), 32x32 tiles per z slice.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) transpose_xy_kernel(
+    const T* __restrict__ src, T* __restrict__ dst, int W) {
+  __shared__ T tile[32][33];
+  const size_t zoff = (size_t)blockIdx.z * W * W;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int x = x0 + threadIdx.x, y = y0 + j;
+    if (x < W && y < W) tile[j][threadIdx.x] = src[zoff + (size_t)y * W + x];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int y = y0 + threadIdx.x, x = x0 + j;
+    if (x < W && y < W) dst[zoff + (size_t)x * W + y] = tile[threadIdx.x][j];
+  }
+}
+
+cudaError_t launch_transpose_xy(const void* src, void* dst, int W, int H,
+                                int dtype, cudaStream_t st) {
+  dim3 blk(32, 8), grd((W + 31) / 32, (W + 31) / 32, H);
+  switch (dtype) {
+    case kF32:
+      transpose_xy_kernel<float>
+          <<<grd, blk, 0, st>>>((const float*)src, (float*)dst, W);
+      break;
+    case kF16:
+      transpose_xy_kernel<__half>
+          <<<grd, blk, 0, st>>>((const __half*)src, (__half*)dst, W);
+      break;
+    default:
+      transpose_xy_kernel<__nv_bfloat16><<<grd, blk, 0, st>>>(
+          (const __nv_bfloat16*)src, (__nv_bfloat16*)dst, W);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Ray march: sum of n trilinear samples at c + k*d (texture coordinates).
+// ---------------------------------------------------------------------------
+template <bool BORDER, typename T>
+__device__ __forceinline__ float march(const T* __restrict__ v, int nf,
+                                       int ns, int nz, float cf, float cs,
+                                       float cz, float df, float ds, float dz,
+                                       int n) {
+  float a0 = 0.f, a1 = 0.f;
+  int k = 0;
+  for (; k + 1 < n; k += 2) {
+    const float k0 = (float)k, k1 = (float)(k + 1);
+    a0 += tri<BORDER>(v, nf, ns, nz, fmaf(k0, df, cf), fmaf(k0, ds, cs),
+                      fmaf(k0, dz, cz));
+    a1 += tri<BORDER>(v, nf, ns, nz, fmaf(k1, df, cf), fmaf(k1, ds, cs),
+                      fmaf(k1, dz, cz));
+  }
+  if (k < n) {
+    const float k0 = (float)k;
+    a0 += tri<BORDER>(v, nf, ns, nz, fmaf(k0, df, cf), fmaf(k0, ds, cs),
+                      fmaf(k0, dz, cz));
+  }
+  return a0 + a1;
+}
+
+// Build the binary32 ray of detector pixel (ix, iy) of launch view `view`.
+// GEOM 0/1/2: standard geometries; GEOM 3: general3D points.
+template <int GEOM>
+__device__ __forceinline__ Ray make_ray(const RayArgs& A, int view, int ix,
+                                        int iy, const float* __restrict__ pts) {
+  const Trig t = A.trig[view];
+  float s[3], e[3];
+  if (GEOM < 3) {
+    std_ray<GEOM>(ix, iy, A.u0, A.v0, t.s, t.c, A.SR, A.RD, s, e);
+  } else {
+    const long long pix = (long long)iy * A.det_w + ix;
+    const float* p =
+        pts + (A.pts_per_view ? (size_t)6 * A.P * (A.view0 + view * A.vstride) : 0);
+    g3d_ray(p, pix, A.P, t.s, t.c, s, e);
+  }
+  return clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], A.bx, A.by, A.bz,
+                  A.step);
+}
+
+// Warp-uniform choice of the volume layout: the y-fastest copy when the rays
+// of this warp run mostly along x.
+template <int GEOM>
+__device__ __forceinline__ bool pick_y_layout(const RayArgs& A, int view,
+                                              const Ray& r, bool valid,
+                                              bool have_y) {
+  if (!have_y) return false;
+  if (GEOM < 3) {
+    const Trig t = A.trig[view];
+    return fabsf(t.c) >= fabsf(t.s);
+  }
+  const bool live = valid && r.n > 0;
+  const unsigned all = __ballot_sync(0xffffffffu, live);
+  const unsigned xs =
+      __ballot_sync(0xffffffffu, live && fabsf(r.dx) >= fabsf(r.dy));
+  return all != 0u && 2 * __popc(xs) >= __popc(all);
+}
+
+template <int GEOM, bool BORDER, typename TV, typename TO>
+__global__ void __launch_bounds__(256) fp_kernel(
+    const __grid_constant__ RayArgs A, const TV* __restrict__ vx,
+    const TV* __restrict__ vy, const float* __restrict__ pts,
+    TO* __restrict__ out) {
+  const int view = blockIdx.x;
+  const int tiles_u = (A.det_w + 31) >> 5;
+  const int ix = (blockIdx.y % tiles_u) * 32 + threadIdx.x;
+  const int iy = (blockIdx.y / tiles_u) * blockDim.y + threadIdx.y;
+  const bool valid = ix < A.det_w && iy < A.det_h;
+  const Ray r = make_ray<GEOM>(A, view, min(ix, A.det_w - 1),
+                               min(iy, A.det_h - 1), pts);
+  const bool use_y = pick_y_layout<GEOM>(A, view, r, valid, vy != nullptr);
+  if (!valid) return;
+  const float cx = r.cx - A.bx, cy = r.cy - A.by, cz = r.cz - A.bz;
+  float acc;
+  if (use_y)
+    acc = march<BORDER>(vy, A.S, A.S, A.Z, cy, cx, cz, r.dy, r.dx, r.dz, r.n);
+  else
+    acc = march<BORDER>(vx, A.S, A.S, A.Z, cx, cy, cz, r.dx, r.dy, r.dz, r.n);
+  stf(out + (size_t)(A.view0 + view * A.vstride) * A.P + (size_t)iy * A.det_w + ix,
+      acc * A.step);
+}
+
+template <int GEOM, bool BORDER, typename TV, typename TO>
+static void fp_go(const RayArgs& a, const void* vx, const void* vy,
+                  const float* pts, void* out, cudaStream_t st) {
+  const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
+  dim3 blk(32, 8), grd(a.nviews, tiles);
+  fp_kernel<GEOM, BORDER, TV, TO><<<grd, blk, 0, st>>>(
+      a, (const TV*)vx, (const TV*)vy, pts, (TO*)out);
+}
+
+template <int GEOM, bool BORDER>
+static cudaError_t fp_types(const RayArgs& a, const void* vx, const void* vy,
+                            int vt, const float* pts, void* out, int ot,
+                            cudaStream_t st) {
+  if (vt == kF32 && ot == kF32)
+    fp_go<GEOM, BORDER, float, float>(a, vx, vy, pts, out, st);
+  else if (vt == kF16 && ot == kF16)
+    fp_go<GEOM, BORDER, __half, __half>(a, vx, vy, pts, out, st);
+  else if (vt == kF16 && ot == kF32)
+    fp_go<GEOM, BORDER, __half, float>(a, vx, vy, pts, out, st);
+  else if (vt == kBF16 && ot == kBF16)
+    fp_go<GEOM, BORDER, __nv_bfloat16, __nv_bfloat16>(a, vx, vy, pts, out,
+                                                       st);
+  else if (vt == kBF16 && ot == kF32)
+    fp_go<GEOM, BORDER, __nv_bfloat16, float>(a, vx, vy, pts, out, st);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fp(int geom, bool border, const RayArgs& a,
+                      const void* vx, const void* vy, int vt,
+                      const float* pts, void* out, int ot, cudaStream_t st) {
+  if (a.nviews <= 0) return cudaSuccess;
+  switch (geom * 2 + (border ? 1 : 0)) {
+    case 0: return fp_types<0, false>(a, vx, vy, vt, pts, out, ot, st);
+    case 1: return fp_types<0, true>(a, vx, vy, vt, pts, out, ot, st);
+    case 2: return fp_types<1, false>(a, vx, vy, vt, pts, out, ot, st);
+    case 3: return fp_types<1, true>(a, vx, vy, vt, pts, out, ot, st);
+    case 4: return fp_types<2, false>(a, vx, vy, vt, pts, out, ot, st);
+    case 5: return fp_types<2, true>(a, vx, vy, vt, pts, out, ot, st);
+    case 7: return fp_types<3, true>(a, vx, vy, vt, pts, out, ot, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Hardware-texture FP variant (tex3D with linear filtering): the reference's
+// own sampling path, kept for comparison.  Its 8-bit filter weights put it
+// ~1e-4..1e-3 away from the FP64 oracle.
+// ---------------------------------------------------------------------------
+template <int GEOM>
+__global__ void __launch_bounds__(256) fp_tex_kernel(
+    const __grid_constant__ RayArgs A, cudaTextureObject_t tex,
+    float* __restrict__ out) {
+  const int view = blockIdx.x;
+  const int tiles_u = (A.det_w + 31) >> 5;
+  const int ix = (blockIdx.y % tiles_u) * 32 + threadIdx.x;
+  const int iy = (blockIdx.y / tiles_u) * blockDim.y + threadIdx.y;
+  if (ix >= A.det_w || iy >= A.det_h) return;
+  const Ray r = make_ray<GEOM>(A, view, ix, iy, nullptr);
+  const float cx = r.cx - A.bx, cy = r.cy - A.by, cz = r.cz - A.bz;
+  float a0 = 0.f, a1 = 0.f;
+  int k = 0;
+  for (; k + 1 < r.n; k += 2) {
+    const float k0 = (float)k, k1 = (float)(k + 1);
+    a0 += tex3D<float>(tex, fmaf(k0, r.dx, cx), fmaf(k0, r.dy, cy),
+                       fmaf(k0, r.dz, cz));
+    a1 += tex3D<float>(tex, fmaf(k1, r.dx, cx), fmaf(k1, r.dy, cy),
+                       fmaf(k1, r.dz, cz));
+  }
+  if (k < r.n) {
+    const float k0 = (float)k;
+    a0 += tex3D<float>(tex, fmaf(k0, r.dx, cx), fmaf(k0, r.dy, cy),
+                       fmaf(k0, r.dz, cz));
+  }
+  out[(size_t)(A.view0 + view * A.vstride) * A.P + (size_t)iy * A.det_w + ix] =
+      (a0 + a1) * A.step;
+}
+
+cudaError_t launch_fp_tex(int geom, const RayArgs& a, cudaTextureObject_t tex,
+                          float* out, cudaStream_t st) {
+  if (a.nviews <= 0) return cudaSuccess;
+  const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
+  dim3 blk(32, 8), grd(a.nviews, tiles);
+  switch (geom) {
+    case 0: fp_tex_kernel<0><<<grd, blk, 0, st>>>(a, tex, out); break;
+    case 1: fp_tex_kernel<1><<<grd, blk, 0, st>>>(a, tex, out); break;
+    case 2: fp_tex_kernel<2><<<grd, blk, 0, st>>>(a, tex, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Voxel-driven BP.  Per view: s, t and U of the column (CUDAmex_BP.cu:79-94,
+// :137-154, :199-212), then the projection column is sampled along z.
+// ---------------------------------------------------------------------------
+template <int GEOM>
+struct ColGeom {
+  float w, py, pz0, dpz;
+};
+
+template <int GEOM>
+__device__ __forceinline__ ColGeom<GEOM> col_geom(float x, float y, Trig t,
+                                                  float SR, float v0,
+                                                  uint32_t hw) {
+  ColGeom<GEOM> g;
+  const float s = fmaf(x, t.c, y * t.s);
+  const float tt = fmaf(-x, t.s, y * t.c);
+  if (GEOM == 0) {
+    g.w = 1.f;
+    g.py = tt + (float)hw + 1.f;
+    g.pz0 = 0.5f;
+    g.dpz = 1.f;
+  } else {
+    const float U = SR / (SR - s);
+    g.w = U * U;
+    g.py = fmaf(tt, U, (float)hw) + 1.f;
+    if (GEOM == 1) {
+      g.pz0 = 0.5f;
+      g.dpz = 1.f;
+    } else {
+      g.pz0 = fmaf(-v0, U, v0) + 0.5f;
+      g.dpz = U;
+    }
+  }
+  return g;
+}
+
+// Sample one projection along a voxel column: acc[j] += w * B(py, pz(z0+j)).
+// Par/fan columns hit texel rows exactly (pz = iz + 0.5): one row, no v
+// interpolation.
+template <int GEOM, bool BORDER, int ZC, typename TS>
+__device__ __forceinline__ void bp_column(const TS* __restrict__ p, int W,
+                                          int H, int z0,
+                                          const ColGeom<GEOM>& g,
+                                          float* acc) {
+  const Tap tu = tap<BORDER>(g.py, W);
+  const float w0 = g.w * tu.w0, w1 = g.w * tu.w1;
+  if (GEOM < 2) {
+#pragma unroll
+    for (int j = 0; j < ZC; ++j) {
+      const int row = min(z0 + j, H - 1);
+      const TS* r = p + (size_t)row * W;
+      acc[j] = fmaf(w0, ldf(r + tu.i0), fmaf(w1, ldf(r + tu.i1), acc[j]));
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < ZC; ++j) {
+      const float pz = fmaf((float)(z0 + j), g.dpz, g.pz0);
+      const Tap tv = tap<BORDER>(pz, H);
+      const TS* r0 = p + (size_t)tv.i0 * W;
+      const TS* r1 = p + (size_t)tv.i1 * W;
+      const float a = fmaf(w0, ldf(r0 + tu.i0), w1 * ldf(r0 + tu.i1));
+      const float b = fmaf(w0, ldf(r1 + tu.i0), w1 * ldf(r1 + tu.i1));
+      acc[j] = fmaf(tv.w0, a, fmaf(tv.w1, b, acc[j]));
+    }
+  }
+}
+
+template <int GEOM, int ZC, typename TS, typename TV>
+__global__ void __launch_bounds__(256) bp_kernel(
+    const __grid_constant__ VoxArgs A, const TS* __restrict__ sino,
+    TV* __restrict__ vol, int accumulate) {
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z0 = blockIdx.z * ZC;
+  if (ix >= A.W || iy >= A.W) return;
+  float acc[ZC];
+#pragma unroll
+  for (int j = 0; j < ZC; ++j) acc[j] = 0.f;
+  if (in_circle(ix, iy, A.hw)) {
+    const float x = (float)ix - ((float)A.hw + 0.5f);
+    const float y = (float)iy - ((float)A.hw + 0.5f);
+    for (int v = 0; v < A.nviews; ++v) {
+      const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
+      bp_column<GEOM, false, ZC>(sino + (size_t)(A.view0 + v) * A.P, A.W,
+                                 A.H, z0, g, acc);
+    }
+  }
+  const size_t base = (size_t)iy * A.W + ix;
+  const size_t sz = (size_t)A.W * A.W;
+#pragma unroll
+  for (int j = 0; j < ZC; ++j) {
+    if (z0 + j < A.H) {
+      TV* o = vol + base + (size_t)(z0 + j) * sz;
+      stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
+    }
+  }
+}
+
+constexpr int kBpZc = 16;
+
+template <int GEOM, typename TS, typename TV>
+static void bp_go(const VoxArgs& a, const void* sino, void* vol, bool accum,
+                  cudaStream_t st) {
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + kBpZc - 1) / kBpZc);
+  bp_kernel<GEOM, kBpZc, TS, TV>
+      <<<grd, blk, 0, st>>>(a, (const TS*)sino, (TV*)vol, accum ? 1 : 0);
+}
+
+template <int GEOM>
+static cudaError_t bp_types(const VoxArgs& a, const void* sino, int stype,
+                            void* vol, int vtype, bool accum,
+                            cudaStream_t st) {
+  if (stype == kF32 && vtype == kF32)
+    bp_go<GEOM, float, float>(a, sino, vol, accum, st);
+  else if (stype == kF16 && vtype == kF16)
+    bp_go<GEOM, __half, __half>(a, sino, vol, accum, st);
+  else if (stype == kF16 && vtype == kF32)
+    bp_go<GEOM, __half, float>(a, sino, vol, accum, st);
+  else if (stype == kBF16 && vtype == kBF16)
+    bp_go<GEOM, __nv_bfloat16, __nv_bfloat16>(a, sino, vol, accum, st);
+  else if (stype == kBF16 && vtype == kF32)
+    bp_go<GEOM, __nv_bfloat16, float>(a, sino, vol, accum, st);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp(int geom, const VoxArgs& a, const void* sino,
+                      int stype, void* vol, int vtype, bool accumulate,
+                      cudaStream_t st) {
+  switch (geom) {
+    case 0: return bp_types<0>(a, sino, stype, vol, vtype, accumulate, st);
+    case 1: return bp_types<1>(a, sino, stype, vol, vtype, accumulate, st);
+    case 2: return bp_types<2>(a, sino, stype, vol, vtype, accumulate, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// general3D BP (CUDAmex_general3D_BP.cu:61-188): ray-driven, two-corner
+// scatter with atomics.  Positions advance incrementally in binary32 and the
+// voxel indices / weights / deposits are binary32 exactly as written, because
+// floor()/ceil() of the position are discontinuous.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) g3d_bp_kernel(
+    const __grid_constant__ RayArgs A, const float* __restrict__ sino,
+    const float* __restrict__ pts, float* __restrict__ vol) {
+  const int view = blockIdx.x;
+  const int tiles_u = (A.det_w + 31) >> 5;
+  const int ix = (blockIdx.y % tiles_u) * 32 + threadIdx.x;
+  const int iy = (blockIdx.y / tiles_u) * blockDim.y + threadIdx.y;
+  if (ix >= A.det_w || iy >= A.det_h) return;
+  const float p = __ldg(sino + (size_t)(A.view0 + view * A.vstride) * A.P +
+                        (size_t)iy * A.det_w + ix);
+  if (p == 0.f) return;  // adds +0 only; the sum is unchanged
+  const Ray r = make_ray<3>(A, view, ix, iy, pts);
+  const int S = A.S, Z = A.Z;
+  const size_t SS = (size_t)S * S;
+  const float ps = fmul(p, A.step);
+  float cx = r.cx, cy = r.cy, cz = r.cz;
+  for (int k = 0; k < r.n; ++k) {
+    const float fx = fsub(cx, A.bx), fy = fsub(cy, A.by), fz = fsub(cz, A.bz);
+    const float flx = floorf(fx), fly = floorf(fy), flz = floorf(fz);
+    const int iL = (int)flx, iU = (int)ceilf(fx);
+    const int jL = (int)fly, jU = (int)ceilf(fy);
+    const int kL = (int)flz, kU = (int)ceilf(fz);
+    if (!(iL < 0 || jL < 0 || kL < 0 || iU >= S || jU >= S || kU >= Z)) {
+      const float wxx = fadd(fsub(fx, (float)iL), 0.5f);
+      const float wyy = fadd(fsub(fy, (float)jL), 0.5f);
+      const float wz = fadd(fsub(fz, (float)kL), 0.5f);
+      const float wzz = fsub(1.0f, wz);
+      const float pxy = fmul(fmul(ps, wxx), wyy);
+      const size_t base = (size_t)jL * S + (size_t)iL;
+      atomicAdd(vol + base + (size_t)kL * SS, fmul(pxy, wzz));
+      atomicAdd(vol + base + (size_t)kU * SS, fmul(pxy, wz));
+    }
+    cx = fadd(cx, r.dx);
+    cy = fadd(cy, r.dy);
+    cz = fadd(cz, r.dz);
+  }
+}
+
+cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
+                          const float* pts, float* vol, cudaStream_t st) {
+  if (a.nviews <= 0) return cudaSuccess;
+  const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
+  dim3 blk(32, 8), grd(a.nviews, tiles);
+  g3d_bp_kernel<<<grd, blk, 0, st>>>(a, sino, pts, vol);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// OSC kernels.
+// ---------------------------------------------------------------------------
+// FP of mu with border addressing and step 0.5 for every geometry
+// (CUDAmex_oscIter.cu:140-259), then pre' = pre e^-l - post and
+// post' = pre e^-l l (:262-268), written to the subset residual buffers.
+template <int GEOM, typename TM>
+__global__ void __launch_bounds__(256) osc_fp_kernel(
+    const __grid_constant__ RayArgs A, const TM* __restrict__ mx,
+    const TM* __restrict__ my, const float* __restrict__ pre,
+    const float* __restrict__ post, float* __restrict__ rpre,
+    float* __restrict__ rpost) {
+  const int view = blockIdx.x;
+  const int tiles_u = (A.det_w + 31) >> 5;
+  const int ix = (blockIdx.y % tiles_u) * 32 + threadIdx.x;
+  const int iy = (blockIdx.y / tiles_u) * blockDim.y + threadIdx.y;
+  const bool valid = ix < A.det_w && iy < A.det_h;
+  const Ray r = make_ray<GEOM>(A, view, min(ix, A.det_w - 1),
+                               min(iy, A.det_h - 1), nullptr);
+  const bool use_y = pick_y_layout<GEOM>(A, view, r, valid, my != nullptr);
+  if (!valid) return;
+  const float cx = r.cx - A.bx, cy = r.cy - A.by, cz = r.cz - A.bz;
+  float l;
+  if (use_y)
+    l = march<true>(my, A.S, A.S, A.Z, cy, cx, cz, r.dy, r.dx, r.dz, r.n);
+  else
+    l = march<true>(mx, A.S, A.S, A.Z, cx, cy, cz, r.dx, r.dy, r.dz, r.n);
+  l *= A.step;
+  const size_t pix = (size_t)iy * A.det_w + ix;
+  const size_t gi = (size_t)(A.view0 + view * A.vstride) * A.P + pix;
+  const float pv = __ldg(pre + gi), qv = __ldg(post + gi);
+  const float e = pv * expf(-l);
+  rpre[(size_t)view * A.P + pix] = e - qv;
+  rpost[(size_t)view * A.P + pix] = e * l;
+}
+
+cudaError_t launch_osc_fp(int geom, const RayArgs& a, const void* mx,
+                          const void* my, int mt, const float* pre,
+                          const float* post, float* rpre, float* rpost,
+                          cudaStream_t st) {
+  if (a.nviews <= 0) return cudaSuccess;
+  const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
+  dim3 blk(32, 8), grd(a.nviews, tiles);
+#define OSC_FP(G, T)                                                   \
+  osc_fp_kernel<G, T><<<grd, blk, 0, st>>>(a, (const T*)mx, (const T*)my, \
+                                           pre, post, rpre, rpost)
+  if (mt == kF32) {
+    if (geom == 0) OSC_FP(0, float);
+    else if (geom == 1) OSC_FP(1, float);
+    else OSC_FP(2, float);
+  } else if (mt == kF16) {
+    if (geom == 0) OSC_FP(0, __half);
+    else if (geom == 1) OSC_FP(1, __half);
+    else OSC_FP(2, __half);
+  } else {
+    if (geom == 0) OSC_FP(0, __nv_bfloat16);
+    else if (geom == 1) OSC_FP(1, __nv_bfloat16);
+    else OSC_FP(2, __nv_bfloat16);
+  }
+#undef OSC_FP
+  return cudaGetLastError();
+}
+
+// Dual BP of the residuals with border addressing (CUDAmex_oscIter.cu:305-356)
+// into register accumulators, then mu <- max(mu + mu*num/den, 0) inside the
+// circle (:119-134).  num/den never touch memory.
+template <int GEOM, int ZC, typename TM>
+__global__ void __launch_bounds__(256) osc_bp_update_kernel(
+    const __grid_constant__ VoxArgs A, const float* __restrict__ rpre,
+    const float* __restrict__ rpost, TM* __restrict__ mu) {
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z0 = blockIdx.z * ZC;
+  if (ix >= A.W || iy >= A.W) return;
+  if (!in_circle(ix, iy, A.hw)) return;
+  float num[ZC], den[ZC];
+#pragma unroll
+  for (int j = 0; j < ZC; ++j) num[j] = den[j] = 0.f;
+  const float x = (float)ix - ((float)A.hw + 0.5f);
+  const float y = (float)iy - ((float)A.hw + 0.5f);
+  for (int v = 0; v < A.nviews; ++v) {
+    const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
+    bp_column<GEOM, true, ZC>(rpre + (size_t)v * A.P, A.W, A.H, z0, g, num);
+    bp_column<GEOM, true, ZC>(rpost + (size_t)v * A.P, A.W, A.H, z0, g, den);
+  }
+  const size_t base = (size_t)iy * A.W + ix;
+  const size_t sz = (size_t)A.W * A.W;
+#pragma unroll
+  for (int j = 0; j < ZC; ++j) {
+    if (z0 + j < A.H) {
+      TM* o = mu + base + (size_t)(z0 + j) * sz;
+      const float f = ldp(o);
+      stf(o, fmaxf(f + (f * num[j] / den[j]), 0.f));
+    }
+  }
+}
+
+cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
+                                 const float* rpre, const float* rpost,
+                                 void* mu, int mt, cudaStream_t st) {
+  constexpr int ZC = 8;
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + ZC - 1) / ZC);
+#define OSC_BP(G, T) \
+  osc_bp_update_kernel<G, ZC, T><<<grd, blk, 0, st>>>(a, rpre, rpost, (T*)mu)
+  if (mt == kF32) {
+    if (geom == 0) OSC_BP(0, float);
+    else if (geom == 1) OSC_BP(1, float);
+    else OSC_BP(2, float);
+  } else if (mt == kF16) {
+    if (geom == 0) OSC_BP(0, __half);
+    else if (geom == 1) OSC_BP(1, __half);
+    else OSC_BP(2, __half);
+  } else {
+    if (geom == 0) OSC_BP(0, __nv_bfloat16);
+    else if (geom == 1) OSC_BP(1, __nv_bfloat16);
+    else OSC_BP(2, __nv_bfloat16);
+  }
+#undef OSC_BP
+  return cudaGetLastError();
+}
+
+}  // namespace mexct

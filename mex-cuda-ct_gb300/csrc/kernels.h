@@ -1,0 +1,100 @@
+// kernels.h -- launch interface between the host library and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "geom.cuh"
+
+namespace mexct {
+
+// Ray-driven projector launch (standard FP, general3D FP/BP, OSC FP).
+struct RayArgs {
+  int det_w, det_h;        // detector W x H
+  int S, Z;                // volume S x S x Z
+  float u0, v0;            // detector centre (W-1)/2, (H-1)/2
+  float bx, by, bz;        // volume corner -S/2, -S/2, -Z/2
+  float SR, RD, step;
+  int nviews;              // views in this launch
+  int view0, vstride;      // launch view i is global view view0 + i*vstride
+  long long P;             // det_w * det_h
+  int pts_per_view;        // general3D: per-view points
+  Trig trig[kMaxViews];
+};
+
+// Voxel-driven BP launch (standard BP, OSC dual BP).
+struct VoxArgs {
+  int W, H;       // volume W x W x H, detector W x H
+  int nviews;
+  float v0, SR;
+  uint32_t hw;    // circle half width W/2 - 1 (unsigned, as the reference)
+  int view0;      // launch view i reads sinogram slot view0 + i
+  long long P;
+  Trig trig[kMaxViews];
+};
+
+// Storage type tags.
+enum Dtype { kF32 = 0, kF16 = 1, kBF16 = 2 };
+
+cudaError_t launch_transpose_xy(const void* src, void* dst, int W, int H,
+                                int dtype, cudaStream_t st);
+
+cudaError_t launch_fp(int geom, bool border, const RayArgs& a,
+                      const void* vol_x, const void* vol_y, int vol_type,
+                      const float* pts, void* out, int out_type,
+                      cudaStream_t st);
+
+cudaError_t launch_fp_tex(int geom, const RayArgs& a,
+                          cudaTextureObject_t tex, float* out,
+                          cudaStream_t st);
+
+cudaError_t launch_bp(int geom, const VoxArgs& a, const void* sino,
+                      int sino_type, void* vol, int vol_type, bool accumulate,
+                      cudaStream_t st);
+
+cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
+                          const float* pts, float* vol, cudaStream_t st);
+
+// OSC: FP of mu for the subset's views with the residual epilogue
+// (CUDAmex_oscIter.cu:140-271) and the dual BP + update
+// (CUDAmex_oscIter.cu:94-136,272-358).
+cudaError_t launch_osc_fp(int geom, const RayArgs& a, const void* mu_x,
+                          const void* mu_y, int mu_type, const float* pre,
+                          const float* post, float* rpre, float* rpost,
+                          cudaStream_t st);
+cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
+                                 const float* rpre, const float* rpost,
+                                 void* mu, int mu_type, cudaStream_t st);
+
+// TV (CUDAmex_TVmin_3D.cu:101-234).  tv_norm computes ||g||^2 in FP64 and the
+// step scale -c/||g|| into *scale; tv_update writes y = x + scale*g(x).
+size_t tv_partials_needed(int Nx, int Ny, int Nz);
+cudaError_t launch_tv_norm(const void* x, int x_type, int Nx, int Ny, int Nz,
+                           float c, double* partials, unsigned* counter,
+                           float* scale, double* norm, cudaStream_t st);
+cudaError_t launch_tv_update(const void* x, void* y, int x_type, int Nx,
+                             int Ny, int Nz, const float* scale,
+                             cudaStream_t st);
+
+// Sum of squared differences in FP64 (OSC_TV_recon.m:65-67), deterministic.
+cudaError_t launch_ssd(const void* a, const void* b, int dtype, long long n,
+                       int zero_first, double* partials, unsigned* counter,
+                       double* out, cudaStream_t st);
+// NaN/Inf -> 0 in place (OSC_TV_recon.m:69-70).
+cudaError_t launch_finite(void* x, int dtype, long long n, cudaStream_t st);
+cudaError_t launch_fill(void* x, int dtype, long long n, float v,
+                        cudaStream_t st);
+cudaError_t launch_convert(const void* src, int src_type, void* dst,
+                           int dst_type, long long n, cudaStream_t st);
+
+// FDK/FBP pre-filter (preFilterSinogram.m, parker_weight.m, FBP_recon.m).
+struct FiltArgs {
+  int W, H, nP, order, geom, log_input;
+  float sad;
+};
+cudaError_t launch_prefilter(const FiltArgs& a, const float* sino,
+                             const float* pre, const float* parker,
+                             const float* dbeta, const float* kern,
+                             float* out, cudaStream_t st);
+
+}  // namespace mexct

@@ -1,0 +1,702 @@
+// ops.cu -- operator entry points of the C ABI (include/mexct.h).
+//
+// Device twins (*_dev) run stream-ordered on caller memory; host entry points
+// stage the MATLAB arrays through the context's workspaces on the context's
+// stream and synchronise before returning (the MEX gateway contract).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "../../include/mexct.h"
+#include "api_internal.h"
+#include "kernels.h"
+
+using namespace mexct;
+
+namespace {
+
+bool bad_geom(int g) { return g < 0 || g > 2; }
+bool bad_type(int t) { return t != kF32 && t != kF16 && t != kBF16; }
+
+// Shape limits: every index below fits the int/size_t arithmetic used by the
+// kernels and a detector tile grid fits gridDim.y.
+bool bad_dims(long long W, long long H) {
+  return W <= 0 || H <= 0 || W > 16384 || H > 16384;
+}
+
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+mexct_status upload(Buf& b, const void* src, size_t bytes, cudaStream_t st,
+                    const char* what) {
+  MEXCT_TRY_CUDA(b.ensure(bytes), what);
+  if (bytes) MEXCT_TRY_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, st), what);
+  return MEXCT_OK;
+}
+
+mexct_status finish(mexct_ctx* c, void* dst, const Buf& b, size_t bytes,
+                    const char* what) {
+  if (bytes)
+    MEXCT_TRY_CUDA(cudaMemcpyAsync(dst, b.p, bytes, cudaMemcpyDeviceToHost, c->stream), what);
+  MEXCT_TRY_CUDA(cudaStreamSynchronize(c->stream), what);
+  return MEXCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP
+// ---------------------------------------------------------------------------
+mexct_status fp_tex(mexct_ctx* c, const float* d_vol, int W, int H, int geom,
+                    RayArgs& a, const float* angles, int nP, float* d_out,
+                    cudaStream_t st) {
+  if (!c->tex_arr || c->tex_w != W || c->tex_h != H) {
+    if (c->tex) cudaDestroyTextureObject(c->tex);
+    if (c->tex_arr) cudaFreeArray(c->tex_arr);
+    c->tex = 0;
+    c->tex_arr = nullptr;
+    cudaChannelFormatDesc ch = cudaCreateChannelDesc<float>();
+    MEXCT_TRY_CUDA(cudaMalloc3DArray(&c->tex_arr, &ch, make_cudaExtent(W, W, H), 0),
+                   "fp(texture): 3D array");
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof rd);
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = c->tex_arr;
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof td);
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    MEXCT_TRY_CUDA(cudaCreateTextureObject(&c->tex, &rd, &td, nullptr),
+                   "fp(texture): texture object");
+    c->tex_w = W;
+    c->tex_h = H;
+  }
+  cudaMemcpy3DParms p;
+  std::memset(&p, 0, sizeof p);
+  p.srcPtr = make_cudaPitchedPtr((void*)d_vol, (size_t)W * sizeof(float), W, W);
+  p.dstArray = c->tex_arr;
+  p.extent = make_cudaExtent(W, W, H);
+  p.kind = cudaMemcpyDeviceToDevice;
+  MEXCT_TRY_CUDA(cudaMemcpy3DAsync(&p, st), "fp(texture): copy to array");
+  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+    a.nviews = std::min(kMaxViews, nP - v0);
+    a.view0 = v0;
+    for (int i = 0; i < a.nviews; ++i) trig_of(angles[v0 + i], &a.trig[i]);
+    MEXCT_TRY_CUDA(launch_fp_tex(geom, a, c->tex, d_out, st), "fp(texture): launch");
+  }
+  return MEXCT_OK;
+}
+
+mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
+                         int H, float sad, const float* angles, int nP,
+                         int geom, void* d_out, int ot, int variant,
+                         cudaStream_t st) {
+  if (!d_vol || !d_out || !angles) return set_err(MEXCT_ERR_ARG, "fp: NULL pointer");
+  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "fp: bad volume dims %d x %d x %d", W, W, H);
+  if (nP < 0) return set_err(MEXCT_ERR_ARG, "fp: nProj must be >= 0 (got %d)", nP);
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "fp: invalid geometry %d", geom);
+  if (bad_type(vt) || bad_type(ot)) return set_err(MEXCT_ERR_ARG, "fp: bad storage type");
+  if (variant != MEXCT_FP_EXPLICIT && variant != MEXCT_FP_TEXTURE)
+    return set_err(MEXCT_ERR_ARG, "fp: unknown variant %d", variant);
+  if (!c || nP == 0) return MEXCT_OK;  // c == NULL: validate only
+  std::unique_ptr<RayArgs> a(new RayArgs);
+  fill_std_rays(*a, W, H, sad, geom, false);
+  if (variant == MEXCT_FP_TEXTURE) {
+    if (vt != kF32 || ot != kF32)
+      return set_err(MEXCT_ERR_UNSUPPORTED, "fp(texture): FP32 storage only");
+    return fp_tex(c, (const float*)d_vol, W, H, geom, *a, angles, nP, (float*)d_out, st);
+  }
+  const size_t N = (size_t)W * W * H;
+  MEXCT_TRY_CUDA(c->volT.ensure(N * dsize(vt)), "fp: workspace");
+  MEXCT_TRY_CUDA(launch_transpose_xy(d_vol, c->volT.p, W, H, vt, st), "fp: transpose");
+  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+    a->nviews = std::min(kMaxViews, nP - v0);
+    a->view0 = v0;
+    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+    MEXCT_TRY_CUDA(launch_fp(geom, false, *a, d_vol, c->volT.p, vt, nullptr, d_out, ot, st),
+                   "fp: launch");
+  }
+  return MEXCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// BP
+// ---------------------------------------------------------------------------
+mexct_status bp_dev_impl(mexct_ctx* c, const void* d_sino, int stype, int W,
+                         int H, int nP, float sad, const float* angles,
+                         int geom, void* d_vol, int vt, cudaStream_t st) {
+  if (!d_sino || !d_vol || (!angles && nP > 0)) return set_err(MEXCT_ERR_ARG, "bp: NULL pointer");
+  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "bp: bad sinogram dims %d x %d", W, H);
+  if (nP < 0) return set_err(MEXCT_ERR_ARG, "bp: bad view count %d", nP);
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "bp: invalid geometry %d", geom);
+  if (bad_type(stype) || bad_type(vt)) return set_err(MEXCT_ERR_ARG, "bp: bad storage type");
+  if (!c) return MEXCT_OK;  // validate only
+  std::unique_ptr<VoxArgs> a(new VoxArgs);
+  fill_vox(*a, W, H, sad);
+  if (nP == 0) {
+    MEXCT_TRY_CUDA(launch_fill(d_vol, vt, (long long)W * W * H, 0.f, st), "bp: zero");
+    return MEXCT_OK;
+  }
+  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+    a->nviews = std::min(kMaxViews, nP - v0);
+    a->view0 = v0;
+    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+    MEXCT_TRY_CUDA(launch_bp(geom, *a, d_sino, stype, d_vol, vt, v0 > 0, st), "bp: launch");
+  }
+  return MEXCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// general3D
+// ---------------------------------------------------------------------------
+void fill_g3d(RayArgs& a, int S, int Z, int W, int H, int per_view) {
+  std::memset(&a, 0, sizeof a);
+  a.det_w = W;
+  a.det_h = H;
+  a.S = S;
+  a.Z = Z;
+  a.bx = -(float)S / 2.0f;  // CUDAmex_general3D_FP.cu:175-177
+  a.by = a.bx;
+  a.bz = -(float)Z / 2.0f;
+  a.step = 0.5f;            // :132
+  a.P = (long long)W * H;
+  a.pts_per_view = per_view;
+  a.vstride = 1;
+}
+
+mexct_status g3d_fp_dev_impl(mexct_ctx* c, const float* d_vol, int S, int Z,
+                             const float* angles, const float* d_pts, int W,
+                             int H, int nP, int per_view, float* d_out,
+                             cudaStream_t st) {
+  if (!d_vol || !d_pts || !d_out || (!angles && nP > 0))
+    return set_err(MEXCT_ERR_ARG, "g3d_fp: NULL pointer");
+  if (bad_dims(S, Z) || bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "g3d_fp: bad dims");
+  if (nP < 0) return set_err(MEXCT_ERR_ARG, "g3d_fp: bad view count %d", nP);
+  if (!c || nP == 0) return MEXCT_OK;  // c == NULL: validate only
+  const size_t N = (size_t)S * S * Z;
+  MEXCT_TRY_CUDA(c->volT.ensure(N * sizeof(float)), "g3d_fp: workspace");
+  MEXCT_TRY_CUDA(launch_transpose_xy(d_vol, c->volT.p, S, Z, kF32, st), "g3d_fp: transpose");
+  std::unique_ptr<RayArgs> a(new RayArgs);
+  fill_g3d(*a, S, Z, W, H, per_view ? 1 : 0);
+  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+    a->nviews = std::min(kMaxViews, nP - v0);
+    a->view0 = v0;
+    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+    MEXCT_TRY_CUDA(launch_fp(3, true, *a, d_vol, c->volT.p, kF32, d_pts, d_out, kF32, st),
+                   "g3d_fp: launch");
+  }
+  return MEXCT_OK;
+}
+
+mexct_status g3d_bp_dev_impl(mexct_ctx* c, const float* d_sino, int W, int H,
+                             int nP, const float* angles, const float* d_pts,
+                             int per_view, int S, int Z, float* d_vol,
+                             cudaStream_t st) {
+  if (!d_sino || !d_pts || !d_vol || (!angles && nP > 0))
+    return set_err(MEXCT_ERR_ARG, "g3d_bp: NULL pointer");
+  if (bad_dims(S, Z) || bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "g3d_bp: bad dims");
+  if (nP < 0) return set_err(MEXCT_ERR_ARG, "g3d_bp: bad view count %d", nP);
+  if (!c) return MEXCT_OK;  // validate only
+  MEXCT_TRY_CUDA(cudaMemsetAsync(d_vol, 0, (size_t)S * S * Z * sizeof(float), st), "g3d_bp: zero");
+  std::unique_ptr<RayArgs> a(new RayArgs);
+  fill_g3d(*a, S, Z, W, H, per_view ? 1 : 0);
+  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+    a->nviews = std::min(kMaxViews, nP - v0);
+    a->view0 = v0;
+    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+    MEXCT_TRY_CUDA(launch_g3d_bp(*a, d_sino, d_pts, d_vol, st), "g3d_bp: launch");
+  }
+  return MEXCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// OSC iteration (CUDAmex_oscIter.cu:504-557): per subset, the fused FP +
+// residual over the subset's views, then the fused dual BP + update.
+// ---------------------------------------------------------------------------
+mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
+                          const float* d_pre, const float* d_post, int W,
+                          int H, int nP, int nSub, const int32_t* picks,
+                          const float* angles, float sad, int geom,
+                          cudaStream_t st) {
+  if (!d_mu || !d_pre || !d_post || !picks || (!angles && nP > 0))
+    return set_err(MEXCT_ERR_ARG, "osc_iter: NULL pointer");
+  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "osc_iter: bad dims");
+  if (nP < 0 || nSub <= 0) return set_err(MEXCT_ERR_ARG, "osc_iter: bad nProj %d / nSub %d", nP, nSub);
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "osc_iter: invalid geometry %d", geom);
+  if (bad_type(mu_type)) return set_err(MEXCT_ERR_ARG, "osc_iter: bad storage type");
+  const size_t N = (size_t)W * W * H;
+  const size_t P = (size_t)W * H;
+  int maxv = 0;
+  for (int si = 0; si < nSub; ++si) {
+    const int sel = picks[si];
+    const int nv = (sel < 0 || sel >= nP) ? 0 : (nP - 1 - sel) / nSub + 1;
+    maxv = std::max(maxv, nv);
+  }
+  if (maxv > kMaxViews)
+    return set_err(MEXCT_ERR_UNSUPPORTED, "osc_iter: %d views in one subset (max %d)", maxv, kMaxViews);
+  if (!c) return MEXCT_OK;  // validate only
+  MEXCT_TRY_CUDA(c->volT.ensure(N * dsize(mu_type)), "osc_iter: workspace");
+  if (maxv > 0) {
+    MEXCT_TRY_CUDA(c->r1.ensure(P * maxv * sizeof(float)), "osc_iter: workspace");
+    MEXCT_TRY_CUDA(c->r2.ensure(P * maxv * sizeof(float)), "osc_iter: workspace");
+  }
+  std::unique_ptr<RayArgs> ra(new RayArgs);
+  std::unique_ptr<VoxArgs> va(new VoxArgs);
+  fill_std_rays(*ra, W, H, sad, geom, /*osc=*/true);
+  fill_vox(*va, W, H, sad);
+  for (int si = 0; si < nSub; ++si) {
+    const int sel = picks[si];
+    const int nv = (sel < 0 || sel >= nP) ? 0 : (nP - 1 - sel) / nSub + 1;
+    ra->nviews = nv;
+    ra->view0 = sel;
+    ra->vstride = nSub;
+    va->nviews = nv;
+    for (int i = 0; i < nv; ++i) {
+      trig_of(angles[sel + i * nSub], &ra->trig[i]);
+      va->trig[i] = ra->trig[i];
+    }
+    if (nv > 0) {
+      MEXCT_TRY_CUDA(launch_transpose_xy(d_mu, c->volT.p, W, H, mu_type, st), "osc_iter: transpose");
+      MEXCT_TRY_CUDA(launch_osc_fp(geom, *ra, d_mu, c->volT.p, mu_type, d_pre, d_post,
+                                   c->r1.as<float>(), c->r2.as<float>(), st),
+                     "osc_iter: fp");
+    }
+    // An empty subset still runs the update: num = den = 0 gives
+    // max(mu + mu*0/0, 0) = 0 inside the circle, as in the reference.
+    MEXCT_TRY_CUDA(launch_osc_bp_update(geom, *va, c->r1.as<float>(), c->r2.as<float>(),
+                                        d_mu, mu_type, st),
+                   "osc_iter: bp/update");
+  }
+  return MEXCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// TV descent: n_steps of (norm, update) on a ping-pong pair whose last write
+// lands in d_out.
+// ---------------------------------------------------------------------------
+mexct_status tv_dev_impl(mexct_ctx* c, const void* d_in, int t, int Nx,
+                         int Ny, int Nz, float cval, int n_steps,
+                         void* d_out, cudaStream_t st) {
+  if (!d_in || !d_out) return set_err(MEXCT_ERR_ARG, "tvmin3d: NULL pointer");
+  if (Nx <= 0 || Ny <= 0 || Nz <= 0) return set_err(MEXCT_ERR_ARG, "tvmin3d: bad dims");
+  if (n_steps < 0) return set_err(MEXCT_ERR_ARG, "tvmin3d: n_steps < 0");
+  if (bad_type(t)) return set_err(MEXCT_ERR_ARG, "tvmin3d: bad storage type");
+  if (!c) return MEXCT_OK;  // validate only
+  const size_t N = (size_t)Nx * Ny * Nz;
+  const size_t bytes = N * dsize(t);
+  if (n_steps == 0) {
+    if (d_in != d_out)
+      MEXCT_TRY_CUDA(cudaMemcpyAsync(d_out, d_in, bytes, cudaMemcpyDeviceToDevice, st), "tvmin3d: copy");
+    return MEXCT_OK;
+  }
+  MEXCT_TRY_CUDA(ensure_reduction(c, tv_partials_needed(Nx, Ny, Nz)), "tvmin3d: workspace");
+  MEXCT_TRY_CUDA(c->r1.ensure(bytes), "tvmin3d: workspace");
+  const void* src = d_in;
+  if (d_in == d_out && (n_steps % 2) == 1) {
+    // The first write would land on the input: read it from a copy.
+    MEXCT_TRY_CUDA(c->r2.ensure(bytes), "tvmin3d: workspace");
+    MEXCT_TRY_CUDA(cudaMemcpyAsync(c->r2.p, d_in, bytes, cudaMemcpyDeviceToDevice, st), "tvmin3d: copy");
+    src = c->r2.p;
+  }
+  float* scale = c->scal.as<float>();
+  double* norm = reinterpret_cast<double*>(c->scal.as<char>() + 8);
+  for (int k = 0; k < n_steps; ++k) {
+    void* dst = ((n_steps - 1 - k) % 2 == 0) ? d_out : c->r1.p;
+    MEXCT_TRY_CUDA(launch_tv_norm(src, t, Nx, Ny, Nz, cval, c->red.as<double>(),
+                                  c->cnt.as<unsigned>(), scale, norm, st),
+                   "tvmin3d: norm");
+    MEXCT_TRY_CUDA(launch_tv_update(src, dst, t, Nx, Ny, Nz, scale, st), "tvmin3d: update");
+    src = dst;
+  }
+  return MEXCT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pre-filter tables: designFilter (preFilterSinogram.m:95-152) -> spatial
+// kernel real(ifft(H)); Parker window (parker_weight.m:181-240); dbeta/2.
+// ---------------------------------------------------------------------------
+int filter_order(int W) {
+  int order = 64;
+  while (order < 2 * W) order *= 2;  // max(64, 2^nextpow2(2*len))
+  return order;
+}
+
+void filter_kernel(int W, int filter, double d, std::vector<float>& out) {
+  const double pi = 3.14159265358979323846;
+  const int order = filter_order(W), half = order / 2;
+  std::vector<double> ct(order);
+  for (int i = 0; i < order; ++i) ct[i] = std::cos(2.0 * pi * i / order);
+  std::vector<double> H(order, 1.0);
+  if (filter != 0) {
+    std::vector<double> h(order, 0.0);
+    h[0] = 0.25;  // DC term
+    for (int n = 1; n <= half; n += 2) {
+      const double v = -1.0 / ((pi * n) * (pi * n));
+      h[n] = v;
+      if (n < half) h[order - n] = v;
+    }
+    std::vector<double> filt(half + 1);
+    for (int m = 0; m <= half; ++m) {
+      double acc = 0.0;
+      for (int n = 0; n < order; ++n) acc += h[n] * ct[((long long)m * n) % order];
+      filt[m] = 2.0 * acc;
+    }
+    for (int m = 1; m <= half; ++m) {
+      const double w = 2.0 * pi * m / order;
+      if (filter == 2) filt[m] *= std::sin(w / (2 * d)) / (w / (2 * d));
+      else if (filter == 3) filt[m] *= std::cos(w / (2 * d));
+      else if (filter == 4) filt[m] *= (.54 + .46 * std::cos(w / d));
+      else if (filter == 5) filt[m] *= (1 + std::cos(w / d)) / 2;
+    }
+    for (int m = 0; m <= half; ++m)
+      if (2.0 * pi * m / order > pi * d) filt[m] = 0.0;
+    for (int m = 0; m <= half; ++m) H[m] = filt[m];
+    for (int m = 1; m < half; ++m) H[half + m] = filt[half - m];
+  }
+  out.assign(order, 0.f);
+  for (int n = 0; n < order; ++n) {
+    double acc = 0.0;
+    for (int m = 0; m < order; ++m) acc += H[m] * ct[((long long)m * n) % order];
+    out[n] = (float)(acc / order);
+  }
+}
+
+double s_window(double b) {
+  if (std::fabs(b) < 0.5) return 0.5 * (1 + std::sin(3.14159265358979323846 * b));
+  if (b >= 0.5) return 1.0;
+  return 0.0;
+}
+
+mexct_status prefilter_dev_impl(mexct_ctx* c, const float* d_sino,
+                                const float* d_pre, int W, int H, int nP,
+                                const float* angles, int geom, float sad,
+                                int filter, float cutoff, float q,
+                                float* d_out, cudaStream_t st) {
+  if (!d_sino || !d_out || !angles) return set_err(MEXCT_ERR_ARG, "prefilter: NULL pointer");
+  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "prefilter: bad dims");
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "prefilter: invalid geometry %d", geom);
+  if (filter < 0 || filter > 5) return set_err(MEXCT_ERR_ARG, "prefilter: unknown filter %d", filter);
+  if (nP < 2) return set_err(MEXCT_ERR_ARG, "prefilter: needs at least 2 views (dbeta)");
+  if (W != H)
+    return set_err(MEXCT_ERR_UNSUPPORTED,
+                   "prefilter: W (%d) != H (%d); the Parker weighting of the reference "
+                   "(parker_weight.m:225) needs a square detector", W, H);
+  if (!c) return MEXCT_OK;  // validate only
+  const double pi = 3.14159265358979323846;
+  const int order = filter_order(W);
+  if (c->filt_w != W || c->filt_type != filter || c->filt_cut != cutoff) {
+    filter_kernel(W, filter, cutoff, c->filt_kern);
+    c->filt_w = W;
+    c->filt_type = filter;
+    c->filt_cut = cutoff;
+  }
+  // Parker window per (view, row element) and dbeta/2 per view.
+  std::vector<double> alpha(H, 0.0);
+  if (geom != 0)
+    for (int j = 0; j < H; ++j) alpha[j] = std::atan((-H / 2.0 + 0.5 + j) / (double)sad);
+  bool incr = true;
+  for (int i = 1; i < nP; ++i)
+    if (!(angles[i] - angles[i - 1] >= 0)) incr = false;
+  if (incr)
+    for (double& a : alpha) a = -a;
+  const double delta = std::fabs(alpha[H - 1] - alpha[0]) / 2;
+  const double extent = std::fabs((double)(angles[nP - 1] - angles[0]));
+  const double eps = std::max(extent - (pi + 2 * delta), 0.0);
+  auto b2 = [&](double a) { return (double)q * (2 * delta - 2 * a + eps); };
+  std::vector<float> tab((size_t)order + (size_t)nP * W + nP);
+  std::memcpy(tab.data(), c->filt_kern.data(), sizeof(float) * order);
+  float* parker = tab.data() + order;
+  float* dbeta = parker + (size_t)nP * W;
+  for (int i = 0; i < nP; ++i) {
+    const double beta = std::fabs((double)(angles[i] - angles[0]));
+    for (int j = 0; j < W; ++j) {
+      const double a = alpha[j];
+      parker[(size_t)i * W + j] = (float)(
+          0.5 * (s_window(beta / b2(a) - 0.5) +
+                 s_window((beta - 2 * delta + 2 * a - eps) / b2(a) + 0.5) -
+                 s_window((beta - pi + 2 * a) / b2(-a) - 0.5) -
+                 s_window((beta - pi - 2 * delta - eps) / b2(-a) + 0.5)));
+    }
+    dbeta[i] = (i > 0) ? (angles[i] - angles[i - 1]) / 2 : (angles[1] - angles[0]) / 2;
+  }
+  MEXCT_TRY_CUDA(c->tabs.ensure(tab.size() * sizeof(float)), "prefilter: workspace");
+  MEXCT_TRY_CUDA(cudaMemcpyAsync(c->tabs.p, tab.data(), tab.size() * sizeof(float),
+                                 cudaMemcpyHostToDevice, st),
+                 "prefilter: tables");
+  FiltArgs fa;
+  fa.W = W;
+  fa.H = H;
+  fa.nP = nP;
+  fa.order = order;
+  fa.geom = geom;
+  fa.log_input = d_pre ? 1 : 0;
+  fa.sad = sad;
+  const float* dt = c->tabs.as<float>();
+  MEXCT_TRY_CUDA(launch_prefilter(fa, d_sino, d_pre, dt + order, dt + order + (size_t)nP * W, dt,
+                                  d_out, st),
+                 "prefilter: launch");
+  // The tables are read from a pageable host vector: keep it alive until the
+  // copy has been staged (cudaMemcpyAsync from pageable memory returns after
+  // staging), nothing more to wait for.
+  return MEXCT_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// Every entry point validates its arguments first (the impl functions with a
+// NULL context only validate), then resolves the device context.
+extern "C" {
+
+#define VALIDATE(call)              \
+  do {                              \
+    mexct_status _v = (call);       \
+    if (_v != MEXCT_OK) return _v;  \
+  } while (0)
+
+#define CTX_OR_FAIL(c, name)                                                \
+  mexct_ctx* c = resolve(ctx);                                              \
+  if (!c) return set_err(MEXCT_ERR_CUDA, name ": no CUDA device / context"); \
+  std::lock_guard<std::recursive_mutex> _lk(c->mu);                         \
+  DevGuard _dg(c->device)
+
+mexct_status mexct_fp_dev(mexct_ctx* ctx, const float* d_vol, int W, int H,
+                          float sad, const float* angles, int nP, int geom,
+                          float* d_out, void* stream) {
+  VALIDATE(fp_dev_impl(nullptr, d_vol, kF32, W, H, sad, angles, nP, geom, d_out, kF32,
+                       MEXCT_FP_EXPLICIT, nullptr));
+  CTX_OR_FAIL(c, "fp");
+  return fp_dev_impl(c, d_vol, kF32, W, H, sad, angles, nP, geom, d_out, kF32,
+                     MEXCT_FP_EXPLICIT, as_stream(stream));
+}
+
+mexct_status mexct_fp_dev_ex(mexct_ctx* ctx, const void* d_vol, int vt, int W,
+                             int H, float sad, const float* angles, int nP,
+                             int geom, void* d_out, int ot, int variant,
+                             void* stream) {
+  VALIDATE(fp_dev_impl(nullptr, d_vol, vt, W, H, sad, angles, nP, geom, d_out, ot, variant,
+                       nullptr));
+  CTX_OR_FAIL(c, "fp");
+  return fp_dev_impl(c, d_vol, vt, W, H, sad, angles, nP, geom, d_out, ot, variant,
+                     as_stream(stream));
+}
+
+mexct_status mexct_fp(mexct_ctx* ctx, const float* vol, int W, int H,
+                      float sad, const float* angles, int nP, int geom,
+                      float* out) {
+  VALIDATE(fp_dev_impl(nullptr, vol, kF32, W, H, sad, angles, nP, geom, out, kF32,
+                       MEXCT_FP_EXPLICIT, nullptr));
+  CTX_OR_FAIL(c, "fp");
+  const size_t N = (size_t)W * W * H, M = (size_t)W * H * nP;
+  mexct_status s = upload(c->in, vol, N * 4, c->stream, "fp: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->out.ensure(M * 4), "fp: workspace");
+  s = fp_dev_impl(c, c->in.p, kF32, W, H, sad, angles, nP, geom, c->out.p, kF32,
+                  MEXCT_FP_EXPLICIT, c->stream);
+  if (s) return s;
+  return finish(c, out, c->out, M * 4, "fp: download");
+}
+
+mexct_status mexct_bp_dev(mexct_ctx* ctx, const float* d_sino, int W, int H,
+                          int nP, float sad, const float* angles, int geom,
+                          float* d_vol, void* stream) {
+  VALIDATE(bp_dev_impl(nullptr, d_sino, kF32, W, H, nP, sad, angles, geom, d_vol, kF32,
+                       nullptr));
+  CTX_OR_FAIL(c, "bp");
+  return bp_dev_impl(c, d_sino, kF32, W, H, nP, sad, angles, geom, d_vol, kF32,
+                     as_stream(stream));
+}
+
+mexct_status mexct_bp_dev_ex(mexct_ctx* ctx, const void* d_sino, int stype,
+                             int W, int H, int nP, float sad,
+                             const float* angles, int geom, void* d_vol,
+                             int vt, void* stream) {
+  VALIDATE(bp_dev_impl(nullptr, d_sino, stype, W, H, nP, sad, angles, geom, d_vol, vt,
+                       nullptr));
+  CTX_OR_FAIL(c, "bp");
+  return bp_dev_impl(c, d_sino, stype, W, H, nP, sad, angles, geom, d_vol, vt,
+                     as_stream(stream));
+}
+
+mexct_status mexct_bp(mexct_ctx* ctx, const float* sino, int W, int H, int nP,
+                      float sad, const float* angles, int geom, float* vol) {
+  VALIDATE(bp_dev_impl(nullptr, sino, kF32, W, H, nP, sad, angles, geom, vol, kF32, nullptr));
+  CTX_OR_FAIL(c, "bp");
+  const size_t N = (size_t)W * W * H, M = (size_t)W * H * nP;
+  mexct_status s = upload(c->in, sino, M * 4, c->stream, "bp: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "bp: workspace");
+  s = bp_dev_impl(c, c->in.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, c->stream);
+  if (s) return s;
+  return finish(c, vol, c->out, N * 4, "bp: download");
+}
+
+mexct_status mexct_g3d_fp_dev(mexct_ctx* ctx, const float* d_vol, int S,
+                              int Z, const float* angles, const float* d_pts,
+                              int W, int H, int nP, int per_view,
+                              float* d_out, void* stream) {
+  VALIDATE(g3d_fp_dev_impl(nullptr, d_vol, S, Z, angles, d_pts, W, H, nP, per_view, d_out,
+                           nullptr));
+  CTX_OR_FAIL(c, "g3d_fp");
+  return g3d_fp_dev_impl(c, d_vol, S, Z, angles, d_pts, W, H, nP, per_view, d_out,
+                         as_stream(stream));
+}
+
+mexct_status mexct_g3d_fp(mexct_ctx* ctx, const float* vol, int S, int Z,
+                          const float* angles, const float* pts, int W, int H,
+                          int nP, int per_view, float* out) {
+  VALIDATE(g3d_fp_dev_impl(nullptr, vol, S, Z, angles, pts, W, H, nP, per_view, out, nullptr));
+  CTX_OR_FAIL(c, "g3d_fp");
+  const size_t N = (size_t)S * S * Z, M = (size_t)W * H * nP;
+  const size_t npts = (size_t)W * H * 6 * (per_view ? nP : 1);
+  mexct_status s = upload(c->in, vol, N * 4, c->stream, "g3d_fp: upload");
+  if (s) return s;
+  s = upload(c->in2, pts, npts * 4, c->stream, "g3d_fp: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->out.ensure(M * 4), "g3d_fp: workspace");
+  s = g3d_fp_dev_impl(c, c->in.as<float>(), S, Z, angles, c->in2.as<float>(), W, H, nP,
+                      per_view, c->out.as<float>(), c->stream);
+  if (s) return s;
+  return finish(c, out, c->out, M * 4, "g3d_fp: download");
+}
+
+mexct_status mexct_g3d_bp_dev(mexct_ctx* ctx, const float* d_sino, int W,
+                              int H, int nP, const float* angles,
+                              const float* d_pts, int per_view, int S, int Z,
+                              float* d_vol, void* stream) {
+  VALIDATE(g3d_bp_dev_impl(nullptr, d_sino, W, H, nP, angles, d_pts, per_view, S, Z, d_vol,
+                           nullptr));
+  CTX_OR_FAIL(c, "g3d_bp");
+  return g3d_bp_dev_impl(c, d_sino, W, H, nP, angles, d_pts, per_view, S, Z, d_vol,
+                         as_stream(stream));
+}
+
+mexct_status mexct_g3d_bp(mexct_ctx* ctx, const float* sino, int W, int H,
+                          int nP, const float* angles, const float* pts,
+                          int per_view, int S, int Z, float* vol) {
+  VALIDATE(g3d_bp_dev_impl(nullptr, sino, W, H, nP, angles, pts, per_view, S, Z, vol, nullptr));
+  CTX_OR_FAIL(c, "g3d_bp");
+  const size_t N = (size_t)S * S * Z, M = (size_t)W * H * nP;
+  const size_t npts = (size_t)W * H * 6 * (per_view ? nP : 1);
+  mexct_status s = upload(c->in, sino, M * 4, c->stream, "g3d_bp: upload");
+  if (s) return s;
+  s = upload(c->in2, pts, npts * 4, c->stream, "g3d_bp: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "g3d_bp: workspace");
+  s = g3d_bp_dev_impl(c, c->in.as<float>(), W, H, nP, angles, c->in2.as<float>(), per_view,
+                      S, Z, c->out.as<float>(), c->stream);
+  if (s) return s;
+  return finish(c, vol, c->out, N * 4, "g3d_bp: download");
+}
+
+mexct_status mexct_osc_iter_dev(mexct_ctx* ctx, float* d_mu,
+                                const float* d_pre, const float* d_post,
+                                int W, int H, int nP, int nSub,
+                                const int32_t* picks, const float* angles,
+                                float sad, int geom, void* stream) {
+  VALIDATE(osc_dev_impl(nullptr, d_mu, kF32, d_pre, d_post, W, H, nP, nSub, picks, angles, sad,
+                        geom, nullptr));
+  CTX_OR_FAIL(c, "osc_iter");
+  return osc_dev_impl(c, d_mu, kF32, d_pre, d_post, W, H, nP, nSub, picks, angles, sad,
+                      geom, as_stream(stream));
+}
+
+mexct_status mexct_osc_iter(mexct_ctx* ctx, float* mu, const float* pre,
+                            const float* post, int W, int H, int nP,
+                            int nSub, const int32_t* picks,
+                            const float* angles, float sad, int geom) {
+  VALIDATE(osc_dev_impl(nullptr, mu, kF32, pre, post, W, H, nP, nSub, picks, angles, sad, geom,
+                        nullptr));
+  CTX_OR_FAIL(c, "osc_iter");
+  const size_t N = (size_t)W * W * H, M = (size_t)W * H * nP;
+  mexct_status s = upload(c->out, mu, N * 4, c->stream, "osc_iter: upload");
+  if (s) return s;
+  s = upload(c->in, pre, M * 4, c->stream, "osc_iter: upload");
+  if (s) return s;
+  s = upload(c->in2, post, M * 4, c->stream, "osc_iter: upload");
+  if (s) return s;
+  s = osc_dev_impl(c, c->out.as<float>(), kF32, c->in.as<float>(), c->in2.as<float>(), W, H,
+                   nP, nSub, picks, angles, sad, geom, c->stream);
+  if (s) return s;
+  return finish(c, mu, c->out, N * 4, "osc_iter: download");
+}
+
+mexct_status mexct_tvmin3d_dev(mexct_ctx* ctx, const float* d_vol, int Nx,
+                               int Ny, int Nz, float cval, int n_steps,
+                               float* d_out, void* stream) {
+  VALIDATE(tv_dev_impl(nullptr, d_vol, kF32, Nx, Ny, Nz, cval, n_steps, d_out, nullptr));
+  CTX_OR_FAIL(c, "tvmin3d");
+  return tv_dev_impl(c, d_vol, kF32, Nx, Ny, Nz, cval, n_steps, d_out, as_stream(stream));
+}
+
+mexct_status mexct_tvmin3d(mexct_ctx* ctx, const float* vol, int Nx, int Ny,
+                           int Nz, float cval, int n_steps, float* out) {
+  VALIDATE(tv_dev_impl(nullptr, vol, kF32, Nx, Ny, Nz, cval, n_steps, out, nullptr));
+  CTX_OR_FAIL(c, "tvmin3d");
+  const size_t N = (size_t)Nx * Ny * Nz;
+  mexct_status s = upload(c->in, vol, N * 4, c->stream, "tvmin3d: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "tvmin3d: workspace");
+  s = tv_dev_impl(c, c->in.p, kF32, Nx, Ny, Nz, cval, n_steps, c->out.p, c->stream);
+  if (s) return s;
+  return finish(c, out, c->out, N * 4, "tvmin3d: download");
+}
+
+mexct_status mexct_prefilter_dev(mexct_ctx* ctx, const float* d_sino,
+                                 const float* d_pre, int W, int H, int nP,
+                                 const float* angles, int geom, float sad,
+                                 int filter, float cutoff, float q,
+                                 float* d_out, void* stream) {
+  VALIDATE(prefilter_dev_impl(nullptr, d_sino, d_pre, W, H, nP, angles, geom, sad, filter,
+                              cutoff, q, d_out, nullptr));
+  CTX_OR_FAIL(c, "prefilter");
+  return prefilter_dev_impl(c, d_sino, d_pre, W, H, nP, angles, geom, sad, filter, cutoff, q,
+                            d_out, as_stream(stream));
+}
+
+mexct_status mexct_prefilter(mexct_ctx* ctx, const float* sino,
+                             const float* pre, int W, int H, int nP,
+                             const float* angles, int geom, float sad,
+                             int filter, float cutoff, float q, float* out) {
+  VALIDATE(prefilter_dev_impl(nullptr, sino, pre, W, H, nP, angles, geom, sad, filter, cutoff,
+                              q, out, nullptr));
+  CTX_OR_FAIL(c, "prefilter");
+  const size_t M = (size_t)W * H * nP;
+  mexct_status s = upload(c->in, sino, M * 4, c->stream, "prefilter: upload");
+  if (s) return s;
+  if (pre) {
+    s = upload(c->in2, pre, M * 4, c->stream, "prefilter: upload");
+    if (s) return s;
+  }
+  MEXCT_TRY_CUDA(c->out.ensure(M * 4), "prefilter: workspace");
+  s = prefilter_dev_impl(c, c->in.as<float>(), pre ? c->in2.as<float>() : nullptr, W, H, nP,
+                         angles, geom, sad, filter, cutoff, q, c->out.as<float>(), c->stream);
+  if (s) return s;
+  return finish(c, out, c->out, M * 4, "prefilter: download");
+}
+
+mexct_status mexct_fbp(mexct_ctx* ctx, const float* pre, const float* post,
+                       int W, int H, int nP, const float* angles, int geom,
+                       float sad, int filter, float cutoff, float q,
+                       float* recon) {
+  if (!pre) return set_err(MEXCT_ERR_ARG, "fbp: NULL pointer");
+  VALIDATE(prefilter_dev_impl(nullptr, post, pre, W, H, nP, angles, geom, sad, filter, cutoff,
+                              q, recon, nullptr));
+  CTX_OR_FAIL(c, "fbp");
+  const size_t N = (size_t)W * W * H, M = (size_t)W * H * nP;
+  mexct_status s = upload(c->in, post, M * 4, c->stream, "fbp: upload");
+  if (s) return s;
+  s = upload(c->in2, pre, M * 4, c->stream, "fbp: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->in3.ensure(M * 4), "fbp: workspace");
+  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "fbp: workspace");
+  s = prefilter_dev_impl(c, c->in.as<float>(), c->in2.as<float>(), W, H, nP, angles, geom, sad,
+                         filter, cutoff, q, c->in3.as<float>(), c->stream);
+  if (s) return s;
+  s = bp_dev_impl(c, c->in3.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, c->stream);
+  if (s) return s;
+  return finish(c, recon, c->out, N * 4, "fbp: download");
+}
+
+}  // extern "C"

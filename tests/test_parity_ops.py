@@ -1,0 +1,226 @@
+"""GPU parity of every operator against the FP64 oracle, through the C ABI.
+
+FP32 results must be within 1e-5 relative L2 of the oracle (spec tolerance);
+the per-operator tolerance is written next to each assertion.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5  # FP32 vs FP64 oracle, relative L2
+
+
+def _phantom(W, H, seed=3, count=6):
+    from mexct import phantoms
+
+    return phantoms.ellipsoids(W, count=count, seed=seed, nz=H)
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+@pytest.mark.parametrize("W,H,nP", [(48, 40, 24), (37, 29, 13), (64, 64, 32)])
+def test_fp_matches_oracle(cuda, orc, geom, W, H, nP):
+    import mexct
+    from mexct import phantoms
+
+    vol = _phantom(W, H)
+    ang = phantoms.angles_full(nP)
+    got = mexct.CUDAmex_FP(vol, 1000.0, ang, nP, geom)
+    ref = orc.fp(vol, 1000.0, ang, nP, geom)
+    assert got.shape == (W, H, nP)
+    assert rel_l2(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+def test_fp_short_sad_and_odd_angles(cuda, orc, geom):
+    """Strong magnification (SAD = 60 voxels) and irregular angles exercise the clip."""
+    import mexct
+
+    W, H, nP = 40, 36, 11
+    vol = _phantom(W, H, seed=9)
+    ang = np.random.default_rng(1).uniform(-7, 7, nP).astype(np.float32)
+    got = mexct.CUDAmex_FP(vol, 60.0, ang, nP, geom)
+    ref = orc.fp(vol, 60.0, ang, nP, geom)
+    assert rel_l2(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+@pytest.mark.parametrize("W,H,nP", [(48, 40, 24), (37, 29, 13), (64, 64, 32)])
+def test_bp_matches_oracle(cuda, orc, geom, W, H, nP):
+    import mexct
+    from mexct import phantoms
+
+    rng = np.random.default_rng(W + H + geom)
+    sino = np.asfortranarray(rng.uniform(-1, 2, (W, H, nP)).astype(np.float32))
+    ang = phantoms.angles_full(nP)
+    got = mexct.CUDAmex_BP(sino, 1000.0, ang, geom)
+    ref = orc.bp(sino, 1000.0, ang, geom)
+    assert got.shape == (W, W, H)
+    assert rel_l2(got, ref) <= TOL
+
+
+def test_config1_cylinder_cone_fp_then_bp(cuda, orc):
+    """Cone FP then BP of the 128^3 uniform cylinder (0.02 inside x^2+y^2 <= 47^2),
+    256 float32 angles linspace(0, 2*pi), SAD 1000, against the FP64 oracle."""
+    import mexct
+    from mexct import phantoms
+
+    vol = phantoms.cylinder(128, 128, radius=47.0, value=0.02)
+    ang = phantoms.angles_full(256)
+    fp = mexct.CUDAmex_FP(vol, 1000.0, ang, 256, 2)
+    ref_fp = orc.fp(vol, 1000.0, ang, 256, 2)
+    assert rel_l2(fp, ref_fp) <= TOL
+    bp = mexct.CUDAmex_BP(fp, 1000.0, ang, 2)
+    ref_bp = orc.bp(fp, 1000.0, ang, 2)
+    assert rel_l2(bp, ref_bp) <= TOL
+
+
+def test_fp_texture_variant_difference(cuda, orc):
+    """The hardware-texture FP (8-bit filter weights) is measured, not exact: its
+    distance to the oracle is bounded loosely and reported."""
+    import torch
+    from mexct import ops, phantoms
+
+    W, H, nP = 64, 64, 32
+    vol = _phantom(W, H)
+    ang = phantoms.angles_full(nP)
+    dvol = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    out = ops.fp_dev(dvol, 1000.0, ang, 2, variant=1)
+    got = out.cpu().numpy().transpose(2, 1, 0)
+    ref = orc.fp(vol, 1000.0, ang, nP, 2)
+    err = rel_l2(got, ref)
+    print("texture FP rel-L2 vs oracle: %.3g" % err)
+    assert err <= 5e-3
+
+
+def test_general3d_fp_parallel_pts_matches_oracle(cuda, orc):
+    import mexct
+    from mexct import phantoms
+
+    S, Z = 40, 32
+    vol = _phantom(S, Z, seed=5)
+    pts = phantoms.parallel_pts(S, Z, L=1000.0)
+    ang = phantoms.angles_full(9)
+    got = mexct.CUDAmex_general3D_FP(vol, ang, pts, 9)
+    ref = orc.g3d_fp(vol, ang, pts, 9)
+    assert rel_l2(got, ref) <= TOL
+
+
+def test_general3d_fp_helix_per_view(cuda, orc):
+    import mexct
+    from mexct import phantoms
+
+    S, Z = 40, 36
+    vol = _phantom(S, Z, seed=6)
+    pts, ang = phantoms.helix_pts(24, 20, 10, Z, sad=300.0, seed=2)
+    got = mexct.CUDAmex_general3D_FP(vol, ang, pts, 10)
+    ref = orc.g3d_fp(vol, ang, pts, 10)
+    assert rel_l2(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("kind", ["parallel", "helix"])
+def test_general3d_bp_matches_oracle(cuda, orc, kind):
+    """Two-corner scatter: voxel indices/weights are binary32-exact, only the
+    accumulation order (atomics vs FP64 sum) differs."""
+    import mexct
+    from mexct import phantoms
+
+    S, Z = 36, 28
+    if kind == "parallel":
+        pts = phantoms.parallel_pts(S, Z, L=1000.0)
+        ang = phantoms.angles_full(8)
+        W, H = S, Z
+    else:
+        W, H = 20, 16
+        pts, ang = phantoms.helix_pts(W, H, 8, Z, sad=300.0, seed=4)
+    rng = np.random.default_rng(7)
+    sino = np.asfortranarray(rng.uniform(0, 1, (W, H, 8)).astype(np.float32))
+    got = mexct.CUDAmex_general3D_BP(sino, ang, pts, S, Z)
+    ref = orc.g3d_bp(sino, ang, pts, S, Z)
+    assert rel_l2(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+def test_osc_iteration_matches_oracle(cuda, orc, geom):
+    """One full OSC iteration (all subsets, in the given order) from the driver's
+    initial state mu = 1e-10; FP32 GPU vs FP64 oracle."""
+    import mexct
+    from mexct import phantoms
+
+    W, H, nP, nsub = 40, 32, 24, 6
+    vol = _phantom(W, H, seed=11)
+    ang = phantoms.angles_full(nP)
+    fp = orc.fp(vol, 1000.0, ang, nP, geom).astype(np.float32)
+    pre, post = phantoms.poisson_counts(fp, 1e5, seed=1)
+    mu = np.full((W, W, H), np.float32(1e-10), dtype=np.float32, order="F")
+    picks = orc.subset_order(nsub, 2)
+    ref = orc.osc_iter(mu, pre, post, nsub, picks, ang, 1000.0, geom)
+    pre0, post0 = pre.copy(), post.copy()
+    mexct.CUDAmex_oscIter(mu, pre, post, nsub, picks, ang, 1000.0, geom)
+    assert np.array_equal(pre, pre0) and np.array_equal(post, post0)
+    assert rel_l2(mu, ref) <= TOL
+
+
+def test_osc_empty_subset_zeroes_circle(cuda, orc):
+    """A subset with no views divides 0 by 0 in the update: the reference's fmaxf
+    turns the NaN into 0 inside the circle; outside it mu is untouched."""
+    import mexct
+    from mexct import phantoms
+
+    W, H, nP = 24, 16, 6
+    ang = phantoms.angles_full(nP)
+    pre = np.full((W, H, nP), 1e5, dtype=np.float32, order="F")
+    post = np.full((W, H, nP), 9e4, dtype=np.float32, order="F")
+    mu = np.full((W, W, H), np.float32(0.01), dtype=np.float32, order="F")
+    picks = np.array([7], dtype=np.int32)  # subset 7 of 1: no view
+    ref = orc.osc_iter(mu, pre, post, 1, picks, ang, 1000.0, 2)
+    mexct.CUDAmex_oscIter(mu, pre, post, 1, picks, ang, 1000.0, 2)
+    assert np.array_equal(mu, ref.astype(np.float32))
+    assert mu[W // 2, W // 2, 0] == 0.0 and mu[0, 0, 0] == np.float32(0.01)
+
+
+@pytest.mark.parametrize("shape", [(32, 32, 32), (33, 27, 19), (64, 48, 40)])
+def test_tvmin3d_matches_oracle(cuda, orc, shape):
+    import mexct
+    from mexct import phantoms
+
+    vol = phantoms.ellipsoids(shape[0], count=5, seed=2, nz=shape[2])[:, : shape[1], :]
+    vol = np.asfortranarray(vol + np.random.default_rng(0).normal(0, 1e-3, vol.shape).astype(np.float32))
+    got = mexct.CUDAmex_TVmin_3D(vol, 0.05)
+    ref = orc.tvmin3d(vol, 0.05, 20)
+    assert rel_l2(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+@pytest.mark.parametrize("filt", ["ramp", "hamming", "shepp-logan"])
+def test_prefilter_matches_oracle(cuda, orc, geom, filt):
+    import mexct
+    from mexct import phantoms
+
+    W, nP = 48, 40
+    rng = np.random.default_rng(geom)
+    sino = np.asfortranarray(rng.uniform(0, 3, (W, W, nP)).astype(np.float32))
+    ang = phantoms.angles_full(nP)
+    gs = {"type": ["par3d", "fan3d", "cone3d"][geom], "SAD": 1000.0}
+    got = mexct.preFilterSinogram(sino, gs, ang, filt, 0.9, 1.0)
+    ref = orc.prefilter(sino, geom, ang, filt, 0.9, 1.0, sad=1000.0)
+    assert rel_l2(got, ref) <= TOL
+
+
+def test_fbp_recon_matches_oracle_chain(cuda, orc):
+    import mexct
+    from mexct import phantoms
+
+    W, nP = 48, 64
+    vol = _phantom(W, W, seed=4)
+    ang = phantoms.angles_full(nP)
+    fp = orc.fp(vol, 1000.0, ang, nP, 2).astype(np.float32)
+    pre, post = phantoms.poisson_counts(fp, 1e5, seed=3)
+    got = mexct.FBP_recon(pre, post, ang, {"type": "cone3d", "SAD": 1000.0}, "hamming", 1.0, 1.0)
+    sino = -np.log(post.astype(np.float32) / pre.astype(np.float32))
+    sino[~np.isfinite(sino)] = 0
+    filt = orc.prefilter(np.asfortranarray(sino.astype(np.float32)), 2, ang, "hamming", 1.0, 1.0)
+    ref = orc.bp(filt.astype(np.float32), 1000.0, ang, 2)
+    assert rel_l2(got, ref) <= 2 * TOL
