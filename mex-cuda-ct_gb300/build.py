@@ -74,5 +74,31 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+MEX_DIR = os.path.join(HERE, "mex")
+MEX_LIB = os.path.join(BUILD, "libmexct_mex.so")
+
+
+def build_mex_stub(force: bool = False) -> str:
+    """The six MEX gateways against the stub mex.h, linked into one shared
+    library with a by-name call interface (mxs_call), for testing without MATLAB."""
+    lib = build(force=force)
+    srcs = sorted(os.path.join(MEX_DIR, f) for f in os.listdir(MEX_DIR) if f.endswith(".cpp"))
+    srcs.append(os.path.join(MEX_DIR, "mexstub", "mexstub.cpp"))
+    deps = srcs + [os.path.join(MEX_DIR, "gateway.h"), os.path.join(MEX_DIR, "mexstub", "mex.h"),
+                   os.path.join(ROOT, "include", "mexct.h"), lib]
+    if (not force and os.path.exists(MEX_LIB)
+            and os.path.getmtime(MEX_LIB) >= max(os.path.getmtime(d) for d in deps)):
+        return MEX_LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-DMEXCT_STUB",
+           "-I", os.path.join(MEX_DIR, "mexstub"), "-I", os.path.join(ROOT, "include"),
+           "-o", MEX_LIB + ".tmp", *srcs, "-L", BUILD, "-lmexct", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("MEX stub build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(MEX_LIB + ".tmp", MEX_LIB)
+    return MEX_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_mex_stub())
