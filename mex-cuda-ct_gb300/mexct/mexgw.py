@@ -102,6 +102,6 @@ def call(name: str, *args, nlhs: int = 1, inplace: tuple = ()):
         for i in range(nlhs):
             if plhs[i]:
                 m.mxs_destroy(plhs[i])
-    if nlhs == 1:
+    if nlhs <= 1:
         return outs[0] if outs else None
     return tuple(outs)
