@@ -174,6 +174,32 @@ mexct_status mexct_bp_dev_ex(mexct_ctx* ctx, const void* d_sino,
                              const float* angles, int geom, void* d_vol,
                              int vol_type, void* stream);
 
+/* ---- allocation-free variant ------------------------------------------ */
+
+/* TV descent for callers that cannot allocate device memory while they run.
+ * This entry point has no counterpart in the reference.
+ *
+ * It returns the same volume as mexct_tvmin3d_dev. Its scratch is one fixed
+ * array compiled into the library (about 8.5 MiB, kept by every GPU that
+ * loads the library until the process exits), so it never calls cudaMalloc
+ * or cudaFree. That suits a serving loop that reserves its whole HBM budget
+ * at start-up, where an allocation on the request path can synchronise the
+ * device and stall other streams. It also suits a host whose GPU memory is
+ * held by another allocator (MATLAB's gpuArray pool, for one).
+ *
+ * - The caller passes the input and output volumes (device pointers, float32,
+ *   Nx*Ny*Nz voxels; d_vol == d_out is allowed).
+ * - It runs on the current device and the given stream.
+ * - Volumes above 2^21 voxels (e.g. 128^3) are rejected with
+ *   MEXCT_ERR_UNSUPPORTED. So is a shape that needs more than 65536 reduction
+ *   partials.
+ * - The first call on a device looks up the array's device address, with
+ *   that device current. Make that first call before any stream capture.
+ * - All calls share the array. Calls that overlap on the GPU race. */
+mexct_status mexct_tvmin3d_dev_noalloc(const float* d_vol, int Nx, int Ny,
+                                       int Nz, float c, int n_steps,
+                                       float* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

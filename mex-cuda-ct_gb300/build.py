@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmexct.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["k_proj.cu", "k_iter.cu", "k_sched.cu", "api.cu", "ops.cu", "solver.cu"]
+SOURCES = ["k_proj.cu", "k_iter.cu", "k_sched.cu", "api.cu", "ops.cu", "solver.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:
