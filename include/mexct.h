@@ -46,8 +46,9 @@ typedef int mexct_status;
 #define MEXCT_BF16 2
 
 /* FP implementation variants for the _ex entry points. */
-#define MEXCT_FP_EXPLICIT 0 /* FP32 trilinear in software (parity path) */
+#define MEXCT_FP_EXPLICIT 0 /* FP32 trilinear, TMA slab-staged (parity path) */
 #define MEXCT_FP_TEXTURE 1  /* hardware 3D texture, 8-bit filter weights */
+#define MEXCT_FP_RAY 2      /* FP32 trilinear, one ray per thread via L1 */
 
 typedef struct mexct_ctx mexct_ctx;
 

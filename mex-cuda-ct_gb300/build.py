@@ -19,7 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmexct.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["k_proj.cu", "k_iter.cu", "k_sched.cu", "api.cu", "ops.cu", "solver.cu", "noalloc.cu"]
+SOURCES = ["k_proj.cu", "k_slab.cu", "k_iter.cu", "k_sched.cu", "api.cu", "ops.cu", "solver.cu",
+           "noalloc.cu"]
 
 
 def nvcc() -> str:
@@ -31,7 +32,8 @@ def nvcc() -> str:
 
 def _deps(src: str) -> list[str]:
     hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    return [src] + hdrs + [os.path.join(ROOT, "include", "mexct.h")]
+    incs = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    return [src] + hdrs + incs
 
 
 def _compile(src: str, verbose: bool) -> str:

@@ -35,6 +35,9 @@ struct mexct_ctx {
   // Device entry points: transposed volume, subset residuals / TV ping-pong,
   // filter tables, FP64 reduction partials, counter and scalars.
   mexct::Buf volT, r1, r2, r3, tabs, red, cnt, scal;
+  // Padded volumes of the slab FP (x-fastest and y-fastest) and the device
+  // error word of bounded waits.
+  mexct::Buf padx, pady, err;
   // Texture variant: cached 3D array + texture object.
   cudaArray_t tex_arr = nullptr;
   cudaTextureObject_t tex = 0;
@@ -45,7 +48,8 @@ struct mexct_ctx {
   std::vector<float> filt_kern;
 
   std::vector<mexct::Buf*> all_bufs() {
-    return {&in, &in2, &in3, &out, &volT, &r1, &r2, &r3, &tabs, &red, &cnt, &scal};
+    return {&in, &in2, &in3, &out, &volT, &r1, &r2, &r3, &tabs, &red, &cnt, &scal,
+            &padx, &pady, &err};
   }
 };
 
@@ -74,6 +78,13 @@ struct DevGuard {
 };
 
 inline size_t dsize(int t) { return t == kF32 ? 4 : 2; }
+
+mexct_status prepare_slab_bufs(Buf& px, Buf& py, Buf& err, const void* d_vol, int vt, int W,
+                               int H, bool border, CUtensorMap* mx, CUtensorMap* my,
+                               int* Pf_out, cudaStream_t st);
+mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
+                          bool border, CUtensorMap* mx, CUtensorMap* my, int* Pf_out,
+                          cudaStream_t st);
 
 }  // namespace mexct
 

@@ -104,8 +104,9 @@ constexpr int kTvBx = 32, kTvBy = 8, kTvZ = 4;  // each thread: kTvZ voxels in z
 template <typename T>
 __global__ void __launch_bounds__(256) tv_norm_kernel(
     const T* __restrict__ x, int Nx, int Ny, int Nz, float c,
-    double* __restrict__ partials, unsigned* __restrict__ counter,
-    float* __restrict__ scale, double* __restrict__ norm) {
+    const double* __restrict__ cmul, double* __restrict__ partials,
+    unsigned* __restrict__ counter, float* __restrict__ scale,
+    double* __restrict__ norm) {
   const int ix = blockIdx.x * kTvBx + threadIdx.x;
   const int iy = blockIdx.y * kTvBy + threadIdx.y;
   const size_t sy = (size_t)Nx, sz = (size_t)Nx * Ny;
@@ -121,8 +122,11 @@ __global__ void __launch_bounds__(256) tv_norm_kernel(
   double total;
   if (finish_partials(blk, partials, counter, &total)) {
     const double m = sqrt(total);
+    // c_eff = c * (*cmul): the OSC-TV driver passes TV_constant * d_a with d_a
+    // computed on the device (OSC_TV_recon.m:68).
+    const double ce = cmul ? (double)c * __ldcg(cmul) : (double)c;
     *norm = m;
-    *scale = (float)(-(double)c / m);
+    *scale = (float)(-ce / m);
   }
 }
 
@@ -151,21 +155,34 @@ size_t tv_partials_needed(int Nx, int Ny, int Nz) {
          ((Nz + kTvZ - 1) / kTvZ);
 }
 
-cudaError_t launch_tv_norm(const void* x, int xt, int Nx, int Ny, int Nz,
-                           float c, double* partials, unsigned* counter,
-                           float* scale, double* norm, cudaStream_t st) {
+static cudaError_t tv_norm_go(const void* x, int xt, int Nx, int Ny, int Nz, float c,
+                              const double* cmul, double* partials, unsigned* counter,
+                              float* scale, double* norm, cudaStream_t st) {
   dim3 blk(kTvBx, kTvBy), grd((Nx + kTvBx - 1) / kTvBx, (Ny + kTvBy - 1) / kTvBy,
                               (Nz + kTvZ - 1) / kTvZ);
   if (xt == kF32)
-    tv_norm_kernel<float><<<grd, blk, 0, st>>>((const float*)x, Nx, Ny, Nz, c,
+    tv_norm_kernel<float><<<grd, blk, 0, st>>>((const float*)x, Nx, Ny, Nz, c, cmul,
                                                partials, counter, scale, norm);
   else if (xt == kF16)
-    tv_norm_kernel<__half><<<grd, blk, 0, st>>>((const __half*)x, Nx, Ny, Nz,
-                                                c, partials, counter, scale, norm);
+    tv_norm_kernel<__half><<<grd, blk, 0, st>>>((const __half*)x, Nx, Ny, Nz, c, cmul,
+                                                partials, counter, scale, norm);
   else
     tv_norm_kernel<__nv_bfloat16><<<grd, blk, 0, st>>>(
-        (const __nv_bfloat16*)x, Nx, Ny, Nz, c, partials, counter, scale, norm);
+        (const __nv_bfloat16*)x, Nx, Ny, Nz, c, cmul, partials, counter, scale, norm);
   return cudaGetLastError();
+}
+
+cudaError_t launch_tv_norm(const void* x, int xt, int Nx, int Ny, int Nz,
+                           float c, double* partials, unsigned* counter,
+                           float* scale, double* norm, cudaStream_t st) {
+  return tv_norm_go(x, xt, Nx, Ny, Nz, c, nullptr, partials, counter, scale, norm, st);
+}
+
+cudaError_t launch_tv_norm_scaled(const void* x, int xt, int Nx, int Ny, int Nz,
+                                  float c, const double* cmul, double* partials,
+                                  unsigned* counter, float* scale, double* norm,
+                                  cudaStream_t st) {
+  return tv_norm_go(x, xt, Nx, Ny, Nz, c, cmul, partials, counter, scale, norm, st);
 }
 
 cudaError_t launch_tv_update(const void* x, void* y, int xt, int Nx, int Ny,
@@ -255,6 +272,22 @@ cudaError_t launch_fill(void* x, int dt, long long n, float v,
   if (dt == kF32) fill_kernel<float><<<blocks, 256, 0, st>>>((float*)x, n, v);
   else if (dt == kF16) fill_kernel<__half><<<blocks, 256, 0, st>>>((__half*)x, n, v);
   else fill_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>((__nv_bfloat16*)x, n, v);
+  return cudaGetLastError();
+}
+
+// OSC_TV_recon.m:35-37: x(x < eps) = eps (NaN stays NaN, as in MATLAB).
+__global__ void clamp_copy_kernel(const float* __restrict__ s, float* __restrict__ d,
+                                  long long n, float eps) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float v = s[i];
+    d[i] = (v < eps) ? eps : v;
+  }
+}
+
+cudaError_t launch_clamp_copy(const float* src, float* dst, long long n, float eps,
+                              cudaStream_t st) {
+  clamp_copy_kernel<<<152 * 8, 256, 0, st>>>(src, dst, n, eps);
   return cudaGetLastError();
 }
 

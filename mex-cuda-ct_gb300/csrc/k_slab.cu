@@ -1,0 +1,509 @@
+// k_slab.cu -- slab-staged forward projection with TMA for the standard
+// geometries (CUDAmex_FP.cu:56-346) and the OSC forward pass
+// (CUDAmex_oscIter.cu:140-271).
+//
+// Why: a ray-per-thread march that fetches its 8 trilinear taps through L1
+// issues ~28 L1 wavefronts per warp-sample, because the 32 rays of a warp
+// enter the volume through different faces and are spread along the ray
+// direction.  Here a CTA (32 x 8 detector pixels of one view) sweeps the
+// volume along the view's dominant axis a (x or y) in slabs of kSlabT tap
+// planes.  For each slab one thread computes the bounding box of the tile's
+// ray bundle (from the 4 corner rays: the coordinates across a plane are
+// monotone in the detector coordinates), and TMA copies that box from a
+// padded volume into shared memory ([z][a][f] with f fastest); every lane
+// then takes its samples whose a-tap lies in the slab from shared memory
+// with constant-offset loads.  Two buffers and two mbarriers overlap the copy
+// of slab j+1 with the sampling of slab j.
+//
+// The padded volume has a one-voxel border (replicated edge for clamp
+// addressing, zeros for border addressing) and a fast-axis pitch rounded up
+// to 8 elements, so taps never need clamping and every TMA box starts on a
+// 16-byte boundary.  A slab whose bundle does not fit the box falls back to
+// loads from the padded volume in global memory.
+//
+// Samples are the reference's: p_k = entry + k*step*dir for k < n with the
+// binary32 ray set-up of geom.cuh; only the order in which a thread visits
+// its samples is unchanged (increasing k), the accumulation is FP32.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstdio>
+#include <cstring>
+
+#include "kernels.h"
+
+namespace mexct {
+
+// ---------------------------------------------------------------------------
+// Padded volumes.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) pad_x_kernel(const T* __restrict__ src,
+                                                    T* __restrict__ dst, int W,
+                                                    int H, int Pf, int border) {
+  const int xp = blockIdx.x * 32 + threadIdx.x;
+  const int yp = blockIdx.y * 8 + threadIdx.y;
+  const int zp = blockIdx.z;
+  const int Ps = W + 2;
+  if (xp >= Pf || yp >= Ps) return;
+  float v = 0.f;
+  if (xp < Ps) {
+    int x = xp - 1, y = yp - 1, z = zp - 1;
+    const bool out = x < 0 || x >= W || y < 0 || y >= W || z < 0 || z >= H;
+    if (!(border && out)) {
+      x = min(max(x, 0), W - 1);
+      y = min(max(y, 0), W - 1);
+      z = min(max(z, 0), H - 1);
+      v = ldf(src + (size_t)x + (size_t)W * ((size_t)y + (size_t)W * z));
+    }
+  }
+  stf(dst + (size_t)xp + (size_t)Pf * ((size_t)yp + (size_t)Ps * zp), v);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) pad_transpose_kernel(
+    const T* __restrict__ px, T* __restrict__ py, int Ps, int Pf) {
+  __shared__ float tile[32][33];
+  const size_t zoff = (size_t)blockIdx.z * Pf * Ps;
+  const int a0 = blockIdx.x * 32, b0 = blockIdx.y * 32;  // a: x, b: y
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int x = a0 + threadIdx.x, y = b0 + j;
+    tile[j][threadIdx.x] = (x < Pf && y < Ps) ? ldp(px + zoff + (size_t)y * Pf + x) : 0.f;
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int y = b0 + threadIdx.x, x = a0 + j;
+    if (y < Pf && x < Ps) stf(py + zoff + (size_t)x * Pf + y, (y < Ps) ? tile[threadIdx.x][j] : 0.f);
+  }
+}
+
+cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
+                              bool border, void* px, void* py, cudaStream_t st) {
+  const int Ps = W + 2, Pz = H + 2;
+  dim3 blk(32, 8), g1((Pf + 31) / 32, (Ps + 7) / 8, Pz);
+  dim3 g2((Pf + 31) / 32, (Pf + 31) / 32, Pz);
+#define PAD(T)                                                                        \
+  pad_x_kernel<T><<<g1, blk, 0, st>>>((const T*)src, (T*)px, W, H, Pf, border ? 1 : 0); \
+  pad_transpose_kernel<T><<<g2, blk, 0, st>>>((const T*)px, (T*)py, Ps, Pf)
+  if (dtype == kF32) {
+    PAD(float);
+  } else if (dtype == kF16) {
+    PAD(__half);
+  } else {
+    PAD(__nv_bfloat16);
+  }
+#undef PAD
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// TMA / mbarrier helpers (inline PTX).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1,
+                                            int c2, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait: gives up after ~2^22 polls (seconds), records the failure and
+// reports it to the caller, which then samples the slab from global memory.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  unsigned* err) {
+  for (int i = 0; i < (1 << 22); ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicOr(err, 1u);
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Slab kernel.
+// ---------------------------------------------------------------------------
+constexpr int kSlabT = 8;                     // a-taps per slab
+constexpr int kSlabA = kSlabT + 1;            // a-planes in a box
+constexpr int kBoxF = 96;                     // box extent along f (elements)
+constexpr int kBoxZ = 2;                      // z rows per TMA box
+constexpr int kBZ = 16;                       // z rows per slab buffer
+constexpr int kPlane = kSlabA * kBoxF;        // elements per z row of a buffer
+constexpr int kBufElems = kBZ * kPlane;       // elements per buffer
+constexpr int kMaxIdx = kBufElems - 1 - (kPlane + kBoxF + 1);
+
+struct SlabPlan {
+  int alo, ahi;  // a-taps sampled in this slab
+  int a0;        // first a-plane in the buffer (= alo)
+  int f0, z0;    // first f column / z row in the buffer
+  int fb;        // 1: sample from global memory
+};
+
+size_t slab_smem_bytes(int dtype) {
+  return 2 * (size_t)kBufElems * (dtype == kF32 ? 4 : 2) + 256;
+}
+
+template <typename T>
+__device__ __forceinline__ float ld_any(const T* p) {
+  return ldp(p);
+}
+
+// One trilinear (or, with Z2 = false, bilinear in the a/f plane) sample at
+// tap-space coordinates ta/tf/tz from a [z][a][f] array with strides.
+template <bool Z2, typename T>
+__device__ __forceinline__ float sample_at(const T* base, int sa, int sz, float wa,
+                                           float wf, float wz) {
+  const float v00 = ld_any(base), v01 = ld_any(base + 1);
+  const float v10 = ld_any(base + sa), v11 = ld_any(base + sa + 1);
+  const float r0 = fmaf(wf, v01 - v00, v00);
+  const float r1 = fmaf(wf, v11 - v10, v10);
+  const float s0 = fmaf(wa, r1 - r0, r0);
+  if (!Z2) return s0;
+  const T* b = base + sz;
+  const float u00 = ld_any(b), u01 = ld_any(b + 1);
+  const float u10 = ld_any(b + sa), u11 = ld_any(b + sa + 1);
+  const float q0 = fmaf(wf, u01 - u00, u00);
+  const float q1 = fmaf(wf, u11 - u10, u10);
+  const float s1 = fmaf(wa, q1 - q0, q0);
+  return fmaf(wz, s1 - s0, s0);
+}
+
+template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
+__global__ void __launch_bounds__(256, 2) fp_slab_kernel(
+    const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
+    const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
+    const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  TV* buf0 = reinterpret_cast<TV*>(smem_raw);
+  TV* buf1 = buf0 + kBufElems;
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ SlabPlan plan[2];
+  __shared__ float corner[4][6];
+  __shared__ int s_amin, s_amax, s_pos, s_neg, s_nslab;
+
+  constexpr bool Z2 = (GEOM == 2);  // par/fan rays sample exact z texel rows
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const int view = blockIdx.x;
+  const int tiles_u = (A.det_w + 31) >> 5;
+  const int u0 = (blockIdx.y % tiles_u) * 32, v0 = (blockIdx.y / tiles_u) * 8;
+  const int ix = u0 + threadIdx.x, iy = v0 + threadIdx.y;
+  const bool valid = ix < A.det_w && iy < A.det_h;
+  const Trig tr = A.trig[view];
+  const bool xdom = fabsf(tr.c) >= fabsf(tr.s);  // rays run mostly along x
+  const int Ps = A.S + 2, Pz = A.Z + 2;
+
+  float s[3], e[3];
+  std_ray<GEOM < 3 ? GEOM : 2>(min(ix, A.det_w - 1), min(iy, A.det_h - 1), A.u0, A.v0, tr.s,
+                               tr.c, A.SR, A.RD, s, e);
+  const Ray r = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], A.bx, A.by, A.bz, A.step);
+  // Tap space: padded texture coordinate minus 0.5, i.e. world - b + 0.5.
+  const float ca = xdom ? r.cx - A.bx : r.cy - A.by;
+  const float cf = xdom ? r.cy - A.by : r.cx - A.bx;
+  const float ta0 = ca + 0.5f, tf0 = cf + 0.5f, tz0 = (r.cz - A.bz) + 0.5f;
+  const float da = xdom ? r.dx : r.dy, df = xdom ? r.dy : r.dx, dz = r.dz;
+  const int n = valid ? r.n : 0;
+
+  if (tid == 0) {
+    s_amin = 0x7fffffff;
+    s_amax = -0x7fffffff;
+    s_pos = 0;
+    s_neg = 0;
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // Corner rays of the valid part of the tile bound the bundle.
+  const int lx = min(31, A.det_w - 1 - u0), ly = min(7, A.det_h - 1 - v0);
+  const int cid = (threadIdx.x == 0 && threadIdx.y == 0)     ? 0
+                  : (threadIdx.x == lx && threadIdx.y == 0)  ? 1
+                  : (threadIdx.x == 0 && threadIdx.y == ly)  ? 2
+                  : (threadIdx.x == lx && threadIdx.y == ly) ? 3
+                                                             : -1;
+  __syncthreads();
+  if (cid >= 0) {
+    corner[cid][0] = s[0]; corner[cid][1] = s[1]; corner[cid][2] = s[2];
+    corner[cid][3] = e[0]; corner[cid][4] = e[1]; corner[cid][5] = e[2];
+  }
+  if (n > 0) {
+    const int t_first = __float2int_rd(ta0);
+    const int t_last = __float2int_rd(fmaf((float)(n - 1), da, ta0));
+    atomicMin(&s_amin, min(t_first, t_last));
+    atomicMax(&s_amax, max(t_first, t_last));
+    if (da > 0.f) atomicAdd(&s_pos, 1);
+    else atomicAdd(&s_neg, 1);
+  }
+  __syncthreads();
+  const bool any = s_amax >= s_amin;
+  const int dir = s_neg == 0 ? 1 : -1;
+  const bool mixed = s_pos > 0 && s_neg > 0;
+  const int nslab = any ? (s_amax - s_amin) / kSlabT + 1 : 0;
+  const TV* gv = xdom ? py : px;            // padded layout with f fastest
+  const CUtensorMap* tm = xdom ? &tmy : &tmx;
+  const float bfw = xdom ? A.by : A.bx;     // world offset of the f axis
+  const float baw = xdom ? A.bx : A.by;     // world offset of the a axis
+
+  // Plan slab j into slot j&1 and start its copy.  Called by all of warp 0:
+  // lanes 0-7 evaluate the 4 corner rays at the 2 ends of the slab in FP32
+  // (error ~1e-4 voxel, covered by the 1-voxel margin), lane 0 issues the TMA.
+  auto plan_and_issue = [&](int j) {
+    const int lane = threadIdx.x;
+    int alo, ahi;
+    if (dir > 0) {
+      alo = s_amin + j * kSlabT;
+      ahi = alo + kSlabT - 1;
+    } else {
+      ahi = s_amax - j * kSlabT;
+      alo = ahi - kSlabT + 1;
+    }
+    float fv = 0.f, zv = 0.f;
+    if (lane < 8) {
+      const int c = lane & 3, w = lane >> 2;
+      const float aw = w ? (float)ahi + 0.5f + baw : (float)alo - 0.5f + baw;
+      const float sa = xdom ? corner[c][0] : corner[c][1];
+      const float sf = xdom ? corner[c][1] : corner[c][0];
+      const float ea = xdom ? corner[c][3] : corner[c][4];
+      const float ef = xdom ? corner[c][4] : corner[c][3];
+      const float den = ea - sa;
+      const float t = den != 0.f ? (aw - sa) / den : 0.f;
+      fv = fmaf(t, ef - sf, sf);
+      zv = fmaf(t, corner[c][5] - corner[c][2], corner[c][2]);
+    }
+    float fmn = lane < 8 ? fv : 3.0e38f, fmx = lane < 8 ? fv : -3.0e38f;
+    float zmn = lane < 8 ? zv : 3.0e38f, zmx = lane < 8 ? zv : -3.0e38f;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      fmn = fminf(fmn, __shfl_xor_sync(0xffffffffu, fmn, o));
+      fmx = fmaxf(fmx, __shfl_xor_sync(0xffffffffu, fmx, o));
+      zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
+      zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
+    }
+    if (lane != 0) return;
+    SlabPlan p;
+    p.alo = alo;
+    p.ahi = ahi;
+    p.a0 = alo;
+    const int align = sizeof(TV) == 4 ? 4 : 8;
+    const float flo = floorf(fmn - bfw + 0.5f) - 1.0f;
+    const float fhi = floorf(fmx - bfw + 0.5f) + 2.0f;
+    const float zlo = floorf(zmn - A.bz + 0.5f) - 1.0f;
+    const float zhi = floorf(zmx - A.bz + 0.5f) + 2.0f;
+    bool fits = isfinite(flo) && isfinite(fhi) && isfinite(zlo) && isfinite(zhi) && !mixed &&
+                fhi >= 0.f && zhi >= 0.f && flo <= (float)(Pf - 1) && zlo <= (float)(Pz - 1);
+    int f0 = 0, z0 = 0, nzr = 0;
+    if (fits) {
+      const int fl = (int)fmaxf(flo, 0.f), zl = (int)fmaxf(zlo, 0.f);
+      const int fh = (int)fminf(fhi, (float)(Pf - 1)), zh = (int)fminf(zhi, (float)(Pz - 1));
+      f0 = (fl / align) * align;
+      z0 = zl;
+      nzr = zh - z0 + 1;
+      fits = (fh - f0 + 1 <= kBoxF) && (nzr <= kBZ) && nzr > 0;
+    }
+    p.f0 = f0;
+    p.z0 = z0;
+    p.fb = fits ? 0 : 1;
+    plan[j & 1] = p;
+    if (fits) {
+      const int nbox = (nzr + kBoxZ - 1) / kBoxZ;
+      TV* dst = (j & 1) ? buf1 : buf0;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&bar[j & 1], (uint32_t)(nbox * kBoxZ * kPlane * sizeof(TV)));
+      for (int bx = 0; bx < nbox; ++bx)
+        tma_load_3d(dst + (size_t)bx * kBoxZ * kPlane, tm, f0, p.a0, z0 + bx * kBoxZ,
+                    &bar[j & 1]);
+    }
+  };
+
+  if (threadIdx.y == 0 && nslab > 0) plan_and_issue(0);
+  __syncthreads();
+
+  float acc0 = 0.f, acc1 = 0.f;
+  int k = 0;
+  uint32_t phase[2] = {0u, 0u};
+  for (int j = 0; j < nslab; ++j) {
+    if (threadIdx.y == 0 && j + 1 < nslab) plan_and_issue(j + 1);
+    const SlabPlan p = plan[j & 1];
+    const TV* b = (j & 1) ? buf1 : buf0;
+    bool from_smem = !p.fb;
+    if (from_smem) {
+      from_smem = mbar_wait_bounded(&bar[j & 1], phase[j & 1], E.err);
+      phase[j & 1] ^= 1u;
+    }
+    // Two samples per iteration (independent loads and FMA chains).
+    while (k < n) {
+      const float k0 = (float)k, k1 = (float)(k + 1);
+      const float ta = fmaf(k0, da, ta0), tb = fmaf(k1, da, ta0);
+      const int ia = __float2int_rd(ta), ib = __float2int_rd(tb);
+      if (dir > 0 ? ia > p.ahi : ia < p.alo) break;
+      const bool two = (k + 1 < n) && (dir > 0 ? ib <= p.ahi : ib >= p.alo);
+      const float tfa = fmaf(k0, df, tf0), tfb = fmaf(k1, df, tf0);
+      const float tza = Z2 ? fmaf(k0, dz, tz0) : tz0, tzb = Z2 ? fmaf(k1, dz, tz0) : tz0;
+      const int fa = __float2int_rd(tfa), fb = __float2int_rd(tfb);
+      const int za = __float2int_rd(tza), zb = __float2int_rd(tzb);
+      const float wa0 = ta - (float)ia, wf0 = tfa - (float)fa, wz0 = tza - (float)za;
+      const float wa1 = tb - (float)ib, wf1 = tfb - (float)fb, wz1 = tzb - (float)zb;
+      float v0, v1;
+      if (from_smem) {
+        int i0 = (za - p.z0) * kPlane + (ia - p.a0) * kBoxF + (fa - p.f0);
+        int i1 = (zb - p.z0) * kPlane + (ib - p.a0) * kBoxF + (fb - p.f0);
+        i0 = min(max(i0, 0), kMaxIdx);
+        i1 = min(max(i1, 0), kMaxIdx);
+        v0 = sample_at<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
+        v1 = sample_at<Z2>(b + i1, kBoxF, kPlane, wa1, wf1, wz1);
+      } else {
+        const int ga = min(max(ia, 0), Ps - 2), gf = min(max(fa, 0), Pf - 2);
+        const int gz = min(max(za, 0), Pz - 2);
+        const int ha = min(max(ib, 0), Ps - 2), hf = min(max(fb, 0), Pf - 2);
+        const int hz = min(max(zb, 0), Pz - 2);
+        v0 = sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
+                           Pf * Ps, wa0, wf0, wz0);
+        v1 = sample_at<Z2>(gv + (size_t)hf + (size_t)Pf * ((size_t)ha + (size_t)Ps * hz), Pf,
+                           Pf * Ps, wa1, wf1, wz1);
+      }
+      acc0 += v0;
+      if (two) {
+        acc1 += v1;
+        k += 2;
+      } else {
+        k += 1;
+        break;
+      }
+    }
+    __syncthreads();
+  }
+  if (!valid) return;
+  const float l = (acc0 + acc1) * A.step;
+  const size_t pix = (size_t)iy * A.det_w + ix;
+  const size_t gi = (size_t)(A.view0 + view * A.vstride) * A.P + pix;
+  if (EPI == 0) {
+    stf(out + gi, l);
+  } else {
+    // CUDAmex_oscIter.cu:262-268: pre' = pre e^-l - post, post' = pre e^-l l.
+    const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
+    const float ehat = pv * expf(-l);
+    E.rpre[(size_t)view * A.P + pix] = ehat - qv;
+    E.rpost[(size_t)view * A.P + pix] = ehat * l;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side: tensor maps and launch.
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype, int Pf, int Ps,
+                           int Pz) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  const size_t es = dtype == kF32 ? 4 : 2;
+  cuuint64_t dims[3] = {(cuuint64_t)Pf, (cuuint64_t)Ps, (cuuint64_t)Pz};
+  cuuint64_t strides[2] = {(cuuint64_t)Pf * es, (cuuint64_t)Pf * Ps * es};
+  cuuint32_t box[3] = {(cuuint32_t)kBoxF, (cuuint32_t)kSlabA, (cuuint32_t)kBoxZ};
+  cuuint32_t estr[3] = {1, 1, 1};
+  const CUtensorMapDataType dt = dtype == kF32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                 : dtype == kF16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  CUresult r = fn(map, dt, 3, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+int slab_pitch(int W) { return ((W + 2 + 7) / 8) * 8; }
+
+template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
+static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtensorMap& my,
+                           const void* px, const void* py, int Pf, void* out,
+                           const SlabEpi& e, cudaStream_t st) {
+  auto k = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO>;
+  const size_t smem = 2 * (size_t)kBufElems * sizeof(TV) + 128;
+  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
+  dim3 blk(32, 8), grd(a.nviews, tiles);
+  k<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
+                           const CUtensorMap& mx, const CUtensorMap& my, const void* px,
+                           const void* py, int Pf, int vt, void* out, int ot,
+                           const SlabEpi& e, cudaStream_t st) {
+  if (a.nviews <= 0) return cudaSuccess;
+#define GO(G, B, EP, TV, TO) return slab_go<G, B, EP, TV, TO>(a, mx, my, px, py, Pf, out, e, st)
+  if (osc) {
+    if (vt == kF32) {
+      if (geom == 0) GO(0, true, 1, float, float);
+      if (geom == 1) GO(1, true, 1, float, float);
+      GO(2, true, 1, float, float);
+    }
+    if (vt == kF16) {
+      if (geom == 0) GO(0, true, 1, __half, float);
+      if (geom == 1) GO(1, true, 1, __half, float);
+      GO(2, true, 1, __half, float);
+    }
+    if (geom == 0) GO(0, true, 1, __nv_bfloat16, float);
+    if (geom == 1) GO(1, true, 1, __nv_bfloat16, float);
+    GO(2, true, 1, __nv_bfloat16, float);
+  }
+  (void)border;
+  if (vt == kF32 && ot == kF32) {
+    if (geom == 0) GO(0, false, 0, float, float);
+    if (geom == 1) GO(1, false, 0, float, float);
+    GO(2, false, 0, float, float);
+  }
+  if (vt == kF16 && ot == kF16) {
+    if (geom == 0) GO(0, false, 0, __half, __half);
+    if (geom == 1) GO(1, false, 0, __half, __half);
+    GO(2, false, 0, __half, __half);
+  }
+  if (vt == kF16 && ot == kF32) {
+    if (geom == 0) GO(0, false, 0, __half, float);
+    if (geom == 1) GO(1, false, 0, __half, float);
+    GO(2, false, 0, __half, float);
+  }
+  if (vt == kBF16 && ot == kBF16) {
+    if (geom == 0) GO(0, false, 0, __nv_bfloat16, __nv_bfloat16);
+    if (geom == 1) GO(1, false, 0, __nv_bfloat16, __nv_bfloat16);
+    GO(2, false, 0, __nv_bfloat16, __nv_bfloat16);
+  }
+  if (vt == kBF16 && ot == kF32) {
+    if (geom == 0) GO(0, false, 0, __nv_bfloat16, float);
+    if (geom == 1) GO(1, false, 0, __nv_bfloat16, float);
+    GO(2, false, 0, __nv_bfloat16, float);
+  }
+#undef GO
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace mexct

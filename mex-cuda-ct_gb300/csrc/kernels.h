@@ -1,6 +1,7 @@
 // kernels.h -- launch interface between the host library and the kernels.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -44,6 +45,27 @@ cudaError_t launch_fp(int geom, bool border, const RayArgs& a,
                       const float* pts, void* out, int out_type,
                       cudaStream_t st);
 
+// Slab-staged FP (k_slab.cu): padded volumes in both layouts, TMA tensor maps
+// over them, and the kernel.  With osc = true the kernel samples the
+// zero-padded mu with step 0.5 and writes the OSC residuals instead.
+struct SlabEpi {
+  const float* pre;  // OSC: pre/post counts and residual outputs
+  const float* post;
+  float* rpre;
+  float* rpost;
+  unsigned* err;     // set to non-zero when a bounded wait gave up
+};
+int slab_pitch(int W);
+cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
+                              bool border, void* px, void* py, cudaStream_t st);
+cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype,
+                           int Pf, int Ps, int Pz);
+cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
+                           const CUtensorMap& mx, const CUtensorMap& my,
+                           const void* px, const void* py, int Pf, int vt,
+                           void* out, int ot, const SlabEpi& e,
+                           cudaStream_t st);
+
 cudaError_t launch_fp_tex(int geom, const RayArgs& a,
                           cudaTextureObject_t tex, float* out,
                           cudaStream_t st);
@@ -72,6 +94,11 @@ size_t tv_partials_needed(int Nx, int Ny, int Nz);
 cudaError_t launch_tv_norm(const void* x, int x_type, int Nx, int Ny, int Nz,
                            float c, double* partials, unsigned* counter,
                            float* scale, double* norm, cudaStream_t st);
+// As launch_tv_norm with c multiplied by the FP64 value at *cmul (device).
+cudaError_t launch_tv_norm_scaled(const void* x, int x_type, int Nx, int Ny,
+                                  int Nz, float c, const double* cmul,
+                                  double* partials, unsigned* counter,
+                                  float* scale, double* norm, cudaStream_t st);
 cudaError_t launch_tv_update(const void* x, void* y, int x_type, int Nx,
                              int Ny, int Nz, const float* scale,
                              cudaStream_t st);
@@ -84,6 +111,8 @@ cudaError_t launch_ssd(const void* a, const void* b, int dtype, long long n,
 cudaError_t launch_finite(void* x, int dtype, long long n, cudaStream_t st);
 cudaError_t launch_fill(void* x, int dtype, long long n, float v,
                         cudaStream_t st);
+cudaError_t launch_clamp_copy(const float* src, float* dst, long long n,
+                              float eps, cudaStream_t st);
 cudaError_t launch_convert(const void* src, int src_type, void* dst,
                            int dst_type, long long n, cudaStream_t st);
 

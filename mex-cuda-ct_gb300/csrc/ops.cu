@@ -88,6 +88,40 @@ mexct_status fp_tex(mexct_ctx* c, const float* d_vol, int W, int H, int geom,
   return MEXCT_OK;
 }
 
+}  // namespace
+
+namespace mexct {
+// Padded copies of a W x W x H volume in both layouts (clamp: replicated edge;
+// border: zeros) in the given buffers, and TMA maps over them.
+mexct_status prepare_slab_bufs(Buf& px, Buf& py, Buf& err, const void* d_vol, int vt, int W,
+                               int H, bool border, CUtensorMap* mx, CUtensorMap* my,
+                               int* Pf_out, cudaStream_t st) {
+  const int Pf = slab_pitch(W);
+  const size_t bytes = (size_t)Pf * (W + 2) * (H + 2) * dsize(vt);
+  MEXCT_TRY_CUDA(px.ensure(bytes), "fp: workspace");
+  MEXCT_TRY_CUDA(py.ensure(bytes), "fp: workspace");
+  if (!err.p) {
+    MEXCT_TRY_CUDA(err.ensure(64), "fp: workspace");
+    MEXCT_TRY_CUDA(cudaMemset(err.p, 0, 64), "fp: workspace");
+  }
+  MEXCT_TRY_CUDA(launch_pad_volume(d_vol, vt, W, H, Pf, border, px.p, py.p, st),
+                 "fp: pad volume");
+  MEXCT_TRY_CUDA(make_slab_tmap(mx, px.p, vt, Pf, W + 2, H + 2), "fp: tensor map");
+  MEXCT_TRY_CUDA(make_slab_tmap(my, py.p, vt, Pf, W + 2, H + 2), "fp: tensor map");
+  *Pf_out = Pf;
+  return MEXCT_OK;
+}
+
+mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
+                          bool border, CUtensorMap* mx, CUtensorMap* my, int* Pf_out,
+                          cudaStream_t st) {
+  return prepare_slab_bufs(c->padx, c->pady, c->err, d_vol, vt, W, H, border, mx, my, Pf_out,
+                           st);
+}
+}  // namespace mexct
+
+namespace {
+
 mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
                          int H, float sad, const float* angles, int nP,
                          int geom, void* d_out, int ot, int variant,
@@ -97,7 +131,7 @@ mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
   if (nP < 0) return set_err(MEXCT_ERR_ARG, "fp: nProj must be >= 0 (got %d)", nP);
   if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "fp: invalid geometry %d", geom);
   if (bad_type(vt) || bad_type(ot)) return set_err(MEXCT_ERR_ARG, "fp: bad storage type");
-  if (variant != MEXCT_FP_EXPLICIT && variant != MEXCT_FP_TEXTURE)
+  if (variant != MEXCT_FP_EXPLICIT && variant != MEXCT_FP_TEXTURE && variant != MEXCT_FP_RAY)
     return set_err(MEXCT_ERR_ARG, "fp: unknown variant %d", variant);
   if (!c || nP == 0) return MEXCT_OK;  // c == NULL: validate only
   std::unique_ptr<RayArgs> a(new RayArgs);
@@ -106,6 +140,22 @@ mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
     if (vt != kF32 || ot != kF32)
       return set_err(MEXCT_ERR_UNSUPPORTED, "fp(texture): FP32 storage only");
     return fp_tex(c, (const float*)d_vol, W, H, geom, *a, angles, nP, (float*)d_out, st);
+  }
+  if (variant == MEXCT_FP_EXPLICIT) {
+    CUtensorMap mx, my;
+    int Pf = 0;
+    mexct_status s = prepare_slab(c, d_vol, vt, W, H, false, &mx, &my, &Pf, st);
+    if (s) return s;
+    SlabEpi e{nullptr, nullptr, nullptr, nullptr, c->err.as<unsigned>()};
+    for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+      a->nviews = std::min(kMaxViews, nP - v0);
+      a->view0 = v0;
+      for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+      MEXCT_TRY_CUDA(launch_fp_slab(geom, false, false, *a, mx, my, c->padx.p, c->pady.p, Pf, vt,
+                                    d_out, ot, e, st),
+                     "fp: launch");
+    }
+    return MEXCT_OK;
   }
   const size_t N = (size_t)W * W * H;
   MEXCT_TRY_CUDA(c->volT.ensure(N * dsize(vt)), "fp: workspace");
@@ -236,7 +286,7 @@ mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
   if (maxv > kMaxViews)
     return set_err(MEXCT_ERR_UNSUPPORTED, "osc_iter: %d views in one subset (max %d)", maxv, kMaxViews);
   if (!c) return MEXCT_OK;  // validate only
-  MEXCT_TRY_CUDA(c->volT.ensure(N * dsize(mu_type)), "osc_iter: workspace");
+  (void)N;
   if (maxv > 0) {
     MEXCT_TRY_CUDA(c->r1.ensure(P * maxv * sizeof(float)), "osc_iter: workspace");
     MEXCT_TRY_CUDA(c->r2.ensure(P * maxv * sizeof(float)), "osc_iter: workspace");
@@ -257,9 +307,13 @@ mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
       va->trig[i] = ra->trig[i];
     }
     if (nv > 0) {
-      MEXCT_TRY_CUDA(launch_transpose_xy(d_mu, c->volT.p, W, H, mu_type, st), "osc_iter: transpose");
-      MEXCT_TRY_CUDA(launch_osc_fp(geom, *ra, d_mu, c->volT.p, mu_type, d_pre, d_post,
-                                   c->r1.as<float>(), c->r2.as<float>(), st),
+      CUtensorMap mx, my;
+      int Pf = 0;
+      mexct_status ps = prepare_slab(c, d_mu, mu_type, W, H, /*border=*/true, &mx, &my, &Pf, st);
+      if (ps) return ps;
+      SlabEpi e{d_pre, d_post, c->r1.as<float>(), c->r2.as<float>(), c->err.as<unsigned>()};
+      MEXCT_TRY_CUDA(launch_fp_slab(geom, true, true, *ra, mx, my, c->padx.p, c->pady.p, Pf,
+                                    mu_type, nullptr, kF32, e, st),
                      "osc_iter: fp");
     }
     // An empty subset still runs the update: num = den = 0 gives

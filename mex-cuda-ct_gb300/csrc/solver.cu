@@ -1,0 +1,398 @@
+// solver.cu -- device-resident OSC-TV: OSC_TV_recon.m on the GPU.
+//
+// iterative_reconstruction/OSC_TV_recon.m:33-74 runs one MEX call per OSC
+// iteration and one per TV call, re-uploading mu and pre/post every time; the
+// reference's oscIter also resets the device (CUDAmex_oscIter.cu:582), so no
+// state survives.  Here mu, mu_old, pre and post stay on the device for the
+// whole reconstruction; an iteration is a fixed sequence of kernels:
+//
+//   mu_old <- mu                                     (:45)
+//   per subset: transpose(mu), osc_fp (FP + residual), osc_bp_update   (:51-59)
+//   k > 1: d_a = ||mu_old - mu|| in FP64 (mu_old(1) = 0, NaN dropped)  (:64-67)
+//          20 TV steps with c = TV_constant * d_a read on the device    (:68)
+//          NaN/Inf -> 0                                                 (:69-70)
+//
+// and is captured once as a CUDA graph per (subset count, subset order)
+// and replayed, so a reconstruction issues a handful of graph launches
+// instead of ~70 kernel launches per iteration.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "../../include/mexct.h"
+#include "../../include/mexct_solver.h"
+#include "api_internal.h"
+#include "kernels.h"
+
+using namespace mexct;
+
+struct mexct_osctv {
+  mexct_ctx* ctx = nullptr;
+  int device = 0;
+  int W = 0, H = 0, nP = 0, geom = 0, mu_type = kF32;
+  float sad = 0.f;
+  std::vector<float> angles;
+  Buf mu, mu_old, pre, post, padx, pady, err, r1, r2, tvbuf, red, cnt, scal;
+  int k_done = 0;
+  bool pre_zeroed = false;
+  struct Key {
+    int k_gt1, nsub, use_obj;
+    float tvc;
+    std::vector<int> picks;
+    bool operator<(const Key& o) const {
+      if (k_gt1 != o.k_gt1) return k_gt1 < o.k_gt1;
+      if (nsub != o.nsub) return nsub < o.nsub;
+      if (tvc != o.tvc) return tvc < o.tvc;
+      if (use_obj != o.use_obj) return use_obj < o.use_obj;
+      return picks < o.picks;
+    }
+  };
+  std::map<Key, cudaGraphExec_t> graphs;
+  ~mexct_osctv() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    for (Buf* b : {&mu, &mu_old, &pre, &post, &padx, &pady, &err, &r1, &r2, &tvbuf, &red, &cnt, &scal})
+      b->release();
+  }
+  size_t N() const { return (size_t)W * W * H; }
+  size_t M() const { return (size_t)W * H * nP; }
+  // Scalars on the device: [0] d_a (double), [1] TV scale (float, as double
+  // slot), [2] ||g|| (double), [3] objective (double).
+  double* d_a() { return scal.as<double>(); }
+  float* tv_scale() { return reinterpret_cast<float*>(scal.as<double>() + 1); }
+  double* tv_norm() { return scal.as<double>() + 2; }
+};
+
+namespace {
+
+constexpr int kTvSteps = 20;  // CUDAmex_TVmin_3D.cu:221
+
+int num_subsets(int s_init, int s_final, double p, int max_iters, int k) {
+  if (max_iters <= 1) return s_final;
+  const double v = (double)(s_init - s_final) / std::pow((double)(max_iters - 1), p) *
+                       std::pow((double)(max_iters - k), p) +
+                   (double)s_final;
+  return (int)std::round(v);  // MATLAB round: half away from zero
+}
+
+bool subset_order(int n, int first, int32_t* picks) {
+  if (n <= 0 || first < 0 || first >= n) return false;
+  std::vector<int> rest;  // 1-based subset numbers still to pick
+  for (int i = 1; i <= n; ++i)
+    if (i != first + 1) rest.push_back(i);
+  int cur = first + 1;
+  picks[0] = first;
+  for (int s = 1; s < n; ++s) {
+    std::vector<int> lo, hi;
+    for (int v : rest) (v < cur ? lo : hi).push_back(v);
+    std::vector<int>& side = lo.size() > hi.size() ? lo : hi;
+    if (side.empty()) return false;
+    const size_t pos = (side.size() + 1) / 2 - 1;  // ceil(numel/2), 1-based
+    cur = side[pos];
+    side.erase(side.begin() + pos);
+    rest.clear();
+    rest.insert(rest.end(), lo.begin(), lo.end());
+    rest.insert(rest.end(), hi.begin(), hi.end());
+    picks[s] = cur - 1;
+  }
+  return true;
+}
+
+mexct_status enqueue_iteration(mexct_osctv* s, bool k_gt1, int nsub,
+                               const int32_t* picks, float tvc,
+                               cudaStream_t st) {
+  const size_t N = s->N();
+  const size_t P = (size_t)s->W * s->H;
+  const size_t vb = N * dsize(s->mu_type);
+  MEXCT_TRY_CUDA(cudaMemcpyAsync(s->mu_old.p, s->mu.p, vb, cudaMemcpyDeviceToDevice, st),
+                 "osctv: mu_old");
+  std::unique_ptr<RayArgs> ra(new RayArgs);
+  std::unique_ptr<VoxArgs> va(new VoxArgs);
+  fill_std_rays(*ra, s->W, s->H, s->sad, s->geom, /*osc=*/true);
+  fill_vox(*va, s->W, s->H, s->sad);
+  for (int si = 0; si < nsub; ++si) {
+    const int sel = picks[si];
+    const int nv = (sel < 0 || sel >= s->nP) ? 0 : (s->nP - 1 - sel) / nsub + 1;
+    ra->nviews = nv;
+    ra->view0 = sel;
+    ra->vstride = nsub;
+    va->nviews = nv;
+    for (int i = 0; i < nv; ++i) {
+      trig_of(s->angles[sel + i * nsub], &ra->trig[i]);
+      va->trig[i] = ra->trig[i];
+    }
+    if (nv > 0) {
+      CUtensorMap mx, my;
+      int Pf = 0;
+      mexct_status ps = prepare_slab_bufs(s->padx, s->pady, s->err, s->mu.p, s->mu_type, s->W,
+                                          s->H, /*border=*/true, &mx, &my, &Pf, st);
+      if (ps) return ps;
+      SlabEpi e{s->pre.as<float>(), s->post.as<float>(), s->r1.as<float>(), s->r2.as<float>(),
+                s->err.as<unsigned>()};
+      MEXCT_TRY_CUDA(launch_fp_slab(s->geom, true, true, *ra, mx, my, s->padx.p, s->pady.p, Pf,
+                                    s->mu_type, nullptr, kF32, e, st),
+                     "osctv: fp");
+    }
+    MEXCT_TRY_CUDA(launch_osc_bp_update(s->geom, *va, s->r1.as<float>(), s->r2.as<float>(),
+                                        s->mu.p, s->mu_type, st),
+                   "osctv: bp/update");
+  }
+  (void)P;
+  if (k_gt1) {
+    MEXCT_TRY_CUDA(launch_ssd(s->mu_old.p, s->mu.p, s->mu_type, (long long)N, 1,
+                              s->red.as<double>(), s->cnt.as<unsigned>(), s->d_a(), st),
+                   "osctv: d_a");
+    // 20 steps on the ping-pong pair (mu, tvbuf); an even count ends in mu.
+    const void* src = s->mu.p;
+    for (int k = 0; k < kTvSteps; ++k) {
+      void* dst = ((kTvSteps - 1 - k) % 2 == 0) ? s->mu.p : s->tvbuf.p;
+      MEXCT_TRY_CUDA(launch_tv_norm_scaled(src, s->mu_type, s->W, s->W, s->H, tvc, s->d_a(),
+                                           s->red.as<double>(), s->cnt.as<unsigned>(),
+                                           s->tv_scale(), s->tv_norm(), st),
+                     "osctv: tv norm");
+      MEXCT_TRY_CUDA(launch_tv_update(src, dst, s->mu_type, s->W, s->W, s->H, s->tv_scale(), st),
+                     "osctv: tv update");
+      src = dst;
+    }
+    MEXCT_TRY_CUDA(launch_finite(s->mu.p, s->mu_type, (long long)N, st), "osctv: finite");
+  }
+  return MEXCT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mexct_num_subsets(int s_init, int s_final, float p_val, int max_iters, int k) {
+  return num_subsets(s_init, s_final, (double)p_val, max_iters, k);
+}
+
+mexct_status mexct_subset_order(int n_sub, int first_pick, int32_t* picks) {
+  if (!picks) return set_err(MEXCT_ERR_ARG, "subset_order: NULL pointer");
+  if (!subset_order(n_sub, first_pick, picks))
+    return set_err(MEXCT_ERR_ARG, "subset_order: bad n_sub %d / first pick %d", n_sub, first_pick);
+  return MEXCT_OK;
+}
+
+mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float* d_post,
+                                int W, int H, int nP, const float* angles, float sad, int geom,
+                                int mu_type, void* stream, mexct_osctv** out) {
+  if (!out) return set_err(MEXCT_ERR_ARG, "osctv_create: out is NULL");
+  *out = nullptr;
+  if (!d_pre || !d_post || !angles) return set_err(MEXCT_ERR_ARG, "osctv_create: NULL pointer");
+  if (W <= 0 || H <= 0 || nP <= 0 || W > 16384 || H > 16384)
+    return set_err(MEXCT_ERR_ARG, "osctv_create: bad dims %d x %d x %d", W, H, nP);
+  if (geom < 0 || geom > 2) return set_err(MEXCT_ERR_ARG, "osctv_create: invalid geometry %d", geom);
+  if (mu_type != kF32 && mu_type != kF16 && mu_type != kBF16)
+    return set_err(MEXCT_ERR_ARG, "osctv_create: bad storage type %d", mu_type);
+  mexct_ctx* c = resolve(ctx);
+  if (!c) return set_err(MEXCT_ERR_CUDA, "osctv_create: no CUDA device / context");
+  DevGuard dg(c->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  std::unique_ptr<mexct_osctv> s(new mexct_osctv);
+  s->ctx = c;
+  s->device = c->device;
+  s->W = W;
+  s->H = H;
+  s->nP = nP;
+  s->geom = geom;
+  s->sad = sad;
+  s->mu_type = mu_type;
+  s->angles.assign(angles, angles + nP);
+  const size_t N = s->N(), M = s->M(), vb = N * dsize(mu_type);
+  const size_t P = (size_t)W * H;
+  const size_t maxv = (size_t)nP;  // a subset holds at most nP views
+  if (maxv > (size_t)kMaxViews)
+    return set_err(MEXCT_ERR_UNSUPPORTED, "osctv_create: %d views (max %d)", nP, kMaxViews);
+  MEXCT_TRY_CUDA(s->mu.ensure(vb), "osctv_create: mu");
+  MEXCT_TRY_CUDA(s->mu_old.ensure(vb), "osctv_create: mu_old");
+  const size_t pb = (size_t)slab_pitch(W) * (W + 2) * (H + 2) * dsize(mu_type);
+  MEXCT_TRY_CUDA(s->padx.ensure(pb), "osctv_create: padded mu");
+  MEXCT_TRY_CUDA(s->pady.ensure(pb), "osctv_create: padded mu");
+  MEXCT_TRY_CUDA(s->err.ensure(64), "osctv_create: error word");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->err.p, 0, 64, st), "osctv_create: error word");
+  MEXCT_TRY_CUDA(s->tvbuf.ensure(vb), "osctv_create: tv");
+  MEXCT_TRY_CUDA(s->pre.ensure(M * 4), "osctv_create: pre");
+  MEXCT_TRY_CUDA(s->post.ensure(M * 4), "osctv_create: post");
+  MEXCT_TRY_CUDA(s->r1.ensure(P * maxv * 4), "osctv_create: residual");
+  MEXCT_TRY_CUDA(s->r2.ensure(P * maxv * 4), "osctv_create: residual");
+  const size_t parts = std::max<size_t>(tv_partials_needed(W, W, H), 152 * 4) + 8;
+  MEXCT_TRY_CUDA(s->red.ensure(parts * sizeof(double)), "osctv_create: reduction");
+  MEXCT_TRY_CUDA(s->cnt.ensure(64), "osctv_create: counter");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->cnt.p, 0, 64, st), "osctv_create: counter");
+  MEXCT_TRY_CUDA(s->scal.ensure(64), "osctv_create: scalars");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->scal.p, 0, 64, st), "osctv_create: scalars");
+  // OSC_TV_recon.m:33 mu = 1e-10; :35-37 pre/post clamped to >= 1e-6.
+  MEXCT_TRY_CUDA(launch_fill(s->mu.p, mu_type, (long long)N, 1e-10f, st), "osctv_create: mu");
+  MEXCT_TRY_CUDA(launch_clamp_copy(d_pre, s->pre.as<float>(), (long long)M, 1e-6f, st),
+                 "osctv_create: pre");
+  MEXCT_TRY_CUDA(launch_clamp_copy(d_post, s->post.as<float>(), (long long)M, 1e-6f, st),
+                 "osctv_create: post");
+  *out = s.release();
+  return MEXCT_OK;
+}
+
+mexct_status mexct_osctv_run(mexct_osctv* s, const mexct_osctv_params* p,
+                             const int32_t* first_picks, int n, void* stream) {
+  if (!s || !p || (!first_picks && n > 0)) return set_err(MEXCT_ERR_ARG, "osctv_run: NULL pointer");
+  if (n < 0 || p->n_iter < 1) return set_err(MEXCT_ERR_ARG, "osctv_run: bad iteration count");
+  DevGuard dg(s->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  for (int i = 0; i < n; ++i) {
+    const int k = s->k_done + 1;  // 1-based iteration number
+    const int nsub = num_subsets(p->n_sub_init, p->n_sub_final, p->p_val, p->n_iter, k);
+    if (nsub <= 0) return set_err(MEXCT_ERR_ARG, "osctv_run: %d subsets at iteration %d", nsub, k);
+    if ((size_t)((s->nP + nsub - 1) / nsub) > (size_t)kMaxViews)
+      return set_err(MEXCT_ERR_UNSUPPORTED, "osctv_run: subset too large");
+    int fp = first_picks[i];
+    fp = ((fp % nsub) + nsub) % nsub;
+    std::vector<int32_t> picks(nsub);
+    if (!subset_order(nsub, fp, picks.data()))
+      return set_err(MEXCT_ERR_ARG, "osctv_run: subset order");
+    if (k >= 2 && !s->pre_zeroed) {
+      // OSC_TV_recon.m:41,62: from iteration 2 on, pre(1) = post(1) = 0.
+      MEXCT_TRY_CUDA(cudaMemsetAsync(s->pre.p, 0, sizeof(float), st), "osctv_run: pre(1)");
+      MEXCT_TRY_CUDA(cudaMemsetAsync(s->post.p, 0, sizeof(float), st), "osctv_run: post(1)");
+      s->pre_zeroed = true;
+    }
+    const bool kg1 = k > 1;
+    if (p->use_graph) {
+      mexct_osctv::Key key{kg1 ? 1 : 0, nsub, p->objective ? 1 : 0, p->tv_const,
+                           std::vector<int>(picks.begin(), picks.end())};
+      auto it = s->graphs.find(key);
+      if (it == s->graphs.end()) {
+        cudaGraph_t g = nullptr;
+        MEXCT_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal),
+                       "osctv_run: begin capture");
+        mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const, st);
+        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (e != MEXCT_OK) {
+          if (g) cudaGraphDestroy(g);
+          return e;
+        }
+        MEXCT_TRY_CUDA(ce, "osctv_run: end capture");
+        cudaGraphExec_t ex = nullptr;
+        ce = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        MEXCT_TRY_CUDA(ce, "osctv_run: instantiate");
+        it = s->graphs.emplace(key, ex).first;
+      }
+      MEXCT_TRY_CUDA(cudaGraphLaunch(it->second, st), "osctv_run: graph launch");
+    } else {
+      mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const, st);
+      if (e != MEXCT_OK) return e;
+    }
+    s->k_done = k;
+  }
+  return MEXCT_OK;
+}
+
+mexct_status mexct_osctv_mu(mexct_osctv* s, float* d_out, void* stream) {
+  if (!s || !d_out) return set_err(MEXCT_ERR_ARG, "osctv_mu: NULL pointer");
+  DevGuard dg(s->device);
+  MEXCT_TRY_CUDA(launch_convert(s->mu.p, s->mu_type, d_out, kF32, (long long)s->N(),
+                                static_cast<cudaStream_t>(stream)),
+                 "osctv_mu: convert");
+  return MEXCT_OK;
+}
+
+mexct_status mexct_osctv_stats(mexct_osctv* s, int* iters, double* d_a, double* obj) {
+  if (!s) return set_err(MEXCT_ERR_ARG, "osctv_stats: NULL solver");
+  DevGuard dg(s->device);
+  double h[4] = {0, 0, 0, 0};
+  MEXCT_TRY_CUDA(cudaMemcpy(h, s->scal.p, sizeof h, cudaMemcpyDeviceToHost), "osctv_stats");
+  if (iters) *iters = s->k_done;
+  if (d_a) *d_a = h[0];
+  if (obj) *obj = std::nan("");
+  return MEXCT_OK;
+}
+
+size_t mexct_osctv_state_bytes(const mexct_osctv* s) {
+  if (!s) return 0;
+  return 64 + 2 * s->N() * dsize(s->mu_type);
+}
+
+mexct_status mexct_osctv_snapshot(mexct_osctv* s, void* host, void* stream) {
+  if (!s || !host) return set_err(MEXCT_ERR_ARG, "osctv_snapshot: NULL pointer");
+  DevGuard dg(s->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int64_t hdr[8] = {0x4d455843, s->W, s->H, s->nP, s->mu_type, s->k_done, s->pre_zeroed, 0};
+  std::memcpy(host, hdr, sizeof hdr);
+  const size_t vb = s->N() * dsize(s->mu_type);
+  unsigned char* h = static_cast<unsigned char*>(host) + 64;
+  MEXCT_TRY_CUDA(cudaMemcpyAsync(h, s->mu.p, vb, cudaMemcpyDeviceToHost, st), "osctv_snapshot");
+  MEXCT_TRY_CUDA(cudaMemcpyAsync(h + vb, s->mu_old.p, vb, cudaMemcpyDeviceToHost, st),
+                 "osctv_snapshot");
+  MEXCT_TRY_CUDA(cudaStreamSynchronize(st), "osctv_snapshot");
+  return MEXCT_OK;
+}
+
+mexct_status mexct_osctv_restore(mexct_osctv* s, const void* host, void* stream) {
+  if (!s || !host) return set_err(MEXCT_ERR_ARG, "osctv_restore: NULL pointer");
+  int64_t hdr[8];
+  std::memcpy(hdr, host, sizeof hdr);
+  if (hdr[0] != 0x4d455843 || hdr[1] != s->W || hdr[2] != s->H || hdr[3] != s->nP ||
+      hdr[4] != s->mu_type)
+    return set_err(MEXCT_ERR_ARG, "osctv_restore: snapshot does not match this solver");
+  DevGuard dg(s->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t vb = s->N() * dsize(s->mu_type);
+  const unsigned char* h = static_cast<const unsigned char*>(host) + 64;
+  MEXCT_TRY_CUDA(cudaMemcpyAsync(s->mu.p, h, vb, cudaMemcpyHostToDevice, st), "osctv_restore");
+  MEXCT_TRY_CUDA(cudaMemcpyAsync(s->mu_old.p, h + vb, vb, cudaMemcpyHostToDevice, st),
+                 "osctv_restore");
+  if (hdr[6] && !s->pre_zeroed) {
+    MEXCT_TRY_CUDA(cudaMemsetAsync(s->pre.p, 0, sizeof(float), st), "osctv_restore");
+    MEXCT_TRY_CUDA(cudaMemsetAsync(s->post.p, 0, sizeof(float), st), "osctv_restore");
+    s->pre_zeroed = true;
+  }
+  MEXCT_TRY_CUDA(cudaStreamSynchronize(st), "osctv_restore");
+  s->k_done = (int)hdr[5];
+  return MEXCT_OK;
+}
+
+mexct_status mexct_osctv_destroy(mexct_osctv* s) {
+  if (!s) return MEXCT_OK;
+  DevGuard dg(s->device);
+  delete s;
+  return MEXCT_OK;
+}
+
+mexct_status mexct_osc_tv_recon(mexct_ctx* ctx, const float* pre, const float* post, int W,
+                                int H, int nP, const float* angles, float sad, int geom,
+                                int n_iter, float tv_const, int n_sub_init, int n_sub_final,
+                                float p_val, const int32_t* first_picks, float* recon) {
+  if (!pre || !post || !angles || !recon || !first_picks)
+    return set_err(MEXCT_ERR_ARG, "osc_tv_recon: NULL pointer");
+  if (W <= 0 || H <= 0 || nP <= 0 || n_iter < 1)
+    return set_err(MEXCT_ERR_ARG, "osc_tv_recon: bad dims / iterations");
+  mexct_ctx* c = resolve(ctx);
+  if (!c) return set_err(MEXCT_ERR_CUDA, "osc_tv_recon: no CUDA device / context");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  DevGuard dg(c->device);
+  const size_t M = (size_t)W * H * nP, N = (size_t)W * W * H;
+  MEXCT_TRY_CUDA(c->in.ensure(M * 4), "osc_tv_recon: upload");
+  MEXCT_TRY_CUDA(c->in2.ensure(M * 4), "osc_tv_recon: upload");
+  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "osc_tv_recon: workspace");
+  MEXCT_TRY_CUDA(cudaMemcpyAsync(c->in.p, pre, M * 4, cudaMemcpyHostToDevice, c->stream),
+                 "osc_tv_recon: upload");
+  MEXCT_TRY_CUDA(cudaMemcpyAsync(c->in2.p, post, M * 4, cudaMemcpyHostToDevice, c->stream),
+                 "osc_tv_recon: upload");
+  mexct_osctv* s = nullptr;
+  mexct_status r = mexct_osctv_create(c, c->in.as<float>(), c->in2.as<float>(), W, H, nP, angles,
+                                      sad, geom, kF32, c->stream, &s);
+  if (r) return r;
+  mexct_osctv_params p{n_iter, tv_const, n_sub_init, n_sub_final, p_val, 1, 0};
+  r = mexct_osctv_run(s, &p, first_picks, n_iter, c->stream);
+  if (!r) r = mexct_osctv_mu(s, c->out.as<float>(), c->stream);
+  if (!r) {
+    cudaError_t e = cudaMemcpyAsync(recon, c->out.p, N * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) r = cuda_err(e, "osc_tv_recon: download");
+  }
+  mexct_osctv_destroy(s);
+  return r;
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+"""Device-resident OSC-TV (include/mexct_solver.h) and the OSC_TV_recon mirror.
+
+``OSC_TV_recon(pre, post, angles, geom, numIter, TV_constant, numSubsInit,
+numSubsFinal, pVal, first_picks)`` keeps the MATLAB driver's argument list
+(iterative_reconstruction/OSC_TV_recon.m:1); the randperm draw of each iteration's
+first subset is passed explicitly (``first_picks``, 0-based) so results are
+reproducible.  ``OscTvSolver`` keeps mu, pre and post on the device across calls,
+can capture iterations as CUDA graphs, and snapshots / restores its state.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .ops import _angles, _f32F, _geom_struct, _ptr
+
+_P, _i, _f, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("n_iter", _i), ("tv_const", _f), ("n_sub_init", _i), ("n_sub_final", _i),
+                ("p_val", _f), ("use_graph", _i), ("objective", _i)]
+
+
+_lib.register("mexct_osctv_create", [_P, _P, _P, _i, _i, _i, _P, _f, _i, _i, _P, ctypes.POINTER(_P)])
+_lib.register("mexct_osctv_run", [_P, ctypes.POINTER(Params), _P, _i, _P])
+_lib.register("mexct_osctv_mu", [_P, _P, _P])
+_lib.register("mexct_osctv_stats", [_P, ctypes.POINTER(_i), ctypes.POINTER(_d), ctypes.POINTER(_d)])
+_lib.register("mexct_osctv_state_bytes", [_P], ctypes.c_size_t)
+_lib.register("mexct_osctv_snapshot", [_P, _P, _P])
+_lib.register("mexct_osctv_restore", [_P, _P, _P])
+_lib.register("mexct_osctv_destroy", [_P])
+_lib.register("mexct_osc_tv_recon", [_P, _P, _P, _i, _i, _i, _P, _f, _i, _i, _f, _i, _i, _f, _P, _P])
+_lib.register("mexct_num_subsets", [_i, _i, _f, _i, _i])
+_lib.register("mexct_subset_order", [_i, _i, _P])
+
+
+def num_subsets(s_init, s_final, p_val, max_iters, k):
+    return int(_lib.load().mexct_num_subsets(int(s_init), int(s_final), float(p_val),
+                                             int(max_iters), int(k)))
+
+
+def subset_order(n, first):
+    out = np.zeros(int(n), dtype=np.int32)
+    _lib.call("mexct_subset_order", int(n), int(first), _ptr(out))
+    return out
+
+
+def OSC_TV_recon(pre, post, scanAngles, geom, numIter, TV_constant, numSubsInit, numSubsFinal,
+                 pVal, first_picks):
+    """recon = OSC_TV_recon(...) on the GPU (host arrays in, float32 [W, W, H] out)."""
+    pre = _f32F(pre, "pre")
+    post = _f32F(post, "post")
+    W, H, nP = post.shape
+    g, sad = _geom_struct(geom)
+    ang = _angles(scanAngles, nP)
+    fp = np.ascontiguousarray(np.asarray(first_picks, dtype=np.int32).ravel())
+    if fp.size < int(numIter):
+        raise ValueError("first_picks needs one entry per iteration")
+    out = np.empty((W, W, H), dtype=np.float32, order="F")
+    _lib.call("mexct_osc_tv_recon", None, _ptr(pre), _ptr(post), W, H, nP, _ptr(ang), float(sad),
+              g, int(numIter), float(TV_constant), int(numSubsInit), int(numSubsFinal),
+              float(pVal), _ptr(fp), _ptr(out))
+    return out
+
+
+class OscTvSolver:
+    """Resident OSC-TV state for device tensors pre/post (nP, H, W) float32."""
+
+    def __init__(self, pre, post, angles, sad, geom, mu_dtype=None, stream=None):
+        import torch
+
+        self._torch = torch
+        nP, H, W = pre.shape
+        self.W, self.H, self.nP = W, H, nP
+        self.angles = _angles(angles, nP)
+        code = {None: _lib.F32, torch.float32: _lib.F32, torch.float16: _lib.F16,
+                torch.bfloat16: _lib.BF16}[mu_dtype]
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        h = _P()
+        _lib.call("mexct_osctv_create", None, _P(pre.data_ptr()), _P(post.data_ptr()), W, H, nP,
+                  _ptr(self.angles), float(sad), int(geom), code, _P(self.stream.cuda_stream),
+                  ctypes.byref(h))
+        self.h = h
+
+    def run(self, first_picks, n_iter, tv_const, n_sub_init, n_sub_final, p_val, use_graph=True,
+            count=None):
+        fp = np.ascontiguousarray(np.asarray(first_picks, dtype=np.int32).ravel())
+        count = fp.size if count is None else int(count)
+        p = Params(int(n_iter), float(tv_const), int(n_sub_init), int(n_sub_final), float(p_val),
+                   1 if use_graph else 0, 0)
+        _lib.call("mexct_osctv_run", self.h, ctypes.byref(p), _ptr(fp), count,
+                  _P(self.stream.cuda_stream))
+
+    def mu(self):
+        out = self._torch.empty((self.H, self.W, self.W), dtype=self._torch.float32, device="cuda")
+        _lib.call("mexct_osctv_mu", self.h, _P(out.data_ptr()), _P(self.stream.cuda_stream))
+        return out
+
+    def stats(self):
+        it, da, ob = _i(), _d(), _d()
+        _lib.call("mexct_osctv_stats", self.h, ctypes.byref(it), ctypes.byref(da), ctypes.byref(ob))
+        return it.value, da.value
+
+    def snapshot(self):
+        n = _lib.load().mexct_osctv_state_bytes(self.h)
+        buf = np.zeros(n, dtype=np.uint8)
+        _lib.call("mexct_osctv_snapshot", self.h, _ptr(buf), _P(self.stream.cuda_stream))
+        return buf
+
+    def restore(self, buf):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        _lib.call("mexct_osctv_restore", self.h, _ptr(buf), _P(self.stream.cuda_stream))
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.load().mexct_osctv_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -255,3 +255,47 @@ def test_osc_tv_driver_runs_and_stays_finite(orc):
                     callback=lambda k, m: seen.append(k))
     assert seen == [1, 2, 3]
     assert np.all(np.isfinite(mu))
+
+
+def test_osc_tv_trajectory_is_rounding_sensitive(orc):
+    """Conditioning of OSC_TV_recon.m: rounding only the FP64 state mu to binary32
+    after each OSC and TV step (all arithmetic FP64) moves the trajectory by orders
+    of magnitude more than one rounding, growing about tenfold per iteration.  No
+    FP32 implementation can hold the later iterates to 1e-5 of the FP64 oracle;
+    per-iterate errors are reported instead."""
+    from mexct import phantoms
+
+    W, H, nP, geom = 32, 24, 24, 0
+    vol = phantoms.ellipsoids(W, count=4, seed=0, nz=H)
+    ang = phantoms.angles_full(nP)
+    fp = orc.fp(vol, 1000.0, ang, nP, geom).astype(np.float32)
+    pre, post = phantoms.poisson_counts(fp, 1e5, seed=1)
+
+    def run(round32):
+        pc, qc = np.maximum(pre, 1e-6), np.maximum(post, 1e-6)
+        p2, q2 = pc.copy(order="F"), qc.copy(order="F")
+        p2.flat[0] = 0
+        q2.flat[0] = 0
+        mu = np.full((W, W, H), float(np.float32(1e-10)), order="F")
+        out = []
+        for k, first in enumerate([1, 4, 0, 2], start=1):
+            old = mu.copy()
+            old.flat[0] = 0
+            ns = orc.num_subsets(6, 3, 1.0, 4, k)
+            a, b = (pc, qc) if k == 1 else (p2, q2)
+            mu = orc.osc_iter(mu, a, b, ns, orc.subset_order(ns, first % ns), ang, 1000.0, geom)
+            if round32:
+                mu = mu.astype(np.float32).astype(np.float64)
+            if k > 1:
+                d = old - mu
+                d[np.isnan(d)] = 0
+                mu = orc.tvmin3d(mu, 0.2 * np.sqrt((d * d).sum()), 20)
+                mu[~np.isfinite(mu)] = 0
+                if round32:
+                    mu = mu.astype(np.float32).astype(np.float64)
+            out.append(mu)
+        return out
+
+    a, b = run(False), run(True)
+    e = [np.linalg.norm(x - y) / np.linalg.norm(x) for x, y in zip(a, b)]
+    assert e[0] < 1e-7 and e[3] > 1e-4 and e[3] > 100 * e[1]

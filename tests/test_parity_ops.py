@@ -224,3 +224,59 @@ def test_fbp_recon_matches_oracle_chain(cuda, orc):
     filt = orc.prefilter(np.asfortranarray(sino.astype(np.float32)), 2, ang, "hamming", 1.0, 1.0)
     ref = orc.bp(filt.astype(np.float32), 1000.0, ang, 2)
     assert rel_l2(got, ref) <= 2 * TOL
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+def test_fp_slab_large_detector_multiple_tiles(cuda, orc, geom):
+    """Several detector tiles and slabs per ray (160^2 x 96, 7 views): the
+    TMA slab path, its bounding boxes and the slab hand-over are exercised."""
+    import mexct
+    from mexct import phantoms
+
+    W, H, nP = 160, 96, 7
+    vol = _phantom(W, H, seed=21, count=8)
+    ang = np.array([0.0, 0.3, 0.7854, 1.2, 2.0, 3.9, 5.5], np.float32)
+    got = mexct.CUDAmex_FP(vol, 1000.0, ang, nP, geom)
+    ref = orc.fp(vol, 1000.0, ang, nP, geom)
+    assert rel_l2(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("variant", [0, 2])
+def test_fp_variants_agree(cuda, orc, variant):
+    """Slab-staged (0) and one-ray-per-thread (2) explicit FP32 paths both meet
+    the 1e-5 bar."""
+    import torch
+    from mexct import ops, phantoms
+
+    W, H, nP = 96, 64, 16
+    vol = _phantom(W, H, seed=13)
+    ang = phantoms.angles_full(nP)
+    dvol = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    for geom in (0, 1, 2):
+        out = ops.fp_dev(dvol, 1000.0, ang, geom, variant=variant)
+        got = out.cpu().numpy().transpose(2, 1, 0)
+        assert rel_l2(got, orc.fp(vol, 1000.0, ang, nP, geom)) <= TOL
+
+
+@pytest.mark.parametrize("dt,tol", [("float16", 1e-3), ("bfloat16", 1e-2)])
+def test_fp_bp_low_precision_storage(cuda, orc, dt, tol):
+    """FP16/BF16 storage of volume and sinogram, FP32 accumulation: relative L2 to
+    the FP64 oracle within 1e-3 (FP16; BF16 has an 8-bit mantissa: 1e-2)."""
+    import torch
+    from mexct import ops, phantoms
+
+    W, H, nP = 64, 48, 24
+    vol = _phantom(W, H, seed=17)
+    ang = phantoms.angles_full(nP)
+    t = getattr(torch, dt)
+    dvol = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda().to(t)
+    for geom in (0, 2):
+        fp = ops.fp_dev(dvol, 1000.0, ang, geom, out_dtype=torch.float32)
+        ref = orc.fp(dvol.float().cpu().numpy().transpose(2, 1, 0).copy(order="F"), 1000.0, ang,
+                     nP, geom)
+        assert rel_l2(fp.cpu().numpy().transpose(2, 1, 0), ref) <= tol
+        sino = fp.to(t)
+        bp = ops.bp_dev(sino, 1000.0, ang, geom, out_dtype=torch.float32)
+        refb = orc.bp(sino.float().cpu().numpy().transpose(2, 1, 0).copy(order="F"), 1000.0, ang,
+                      geom)
+        assert rel_l2(bp.cpu().numpy().transpose(2, 1, 0), refb) <= tol
