@@ -1,20 +1,27 @@
-"""Benchmark: cone-beam FP + BP GUPS at 512^3 x 720 views on one GB300.
+"""Benchmark of the mex-cuda-CT projection-operator path on one GB300.
 
-A step is one forward projection (volume -> 720-view sinogram) plus one
-backprojection (sinogram -> volume) of a 512^3 float32 random-ellipsoid phantom,
-geomFlag 2 (cone), SAD 1000, through the C ABI of libmexct.
+Headline step: one cone-beam (geomFlag 2) forward projection of a 512^3 float32
+random-ellipsoid phantom over 720 views (SAD 1000) plus one backprojection of
+that sinogram, through the C ABI of libmexct, plain FP32 form (explicit FP32
+trilinear, the 1e-5 parity path).
 
-  value  = whole-job GUPS = 2 * 512^3 * 720 * steps * n_ranks / max-rank time
-           (device-resident inputs, CUDA events on the launching stream)
-  e2e    = the same metric through the host entry points mexct_fp / mexct_bp
-           with pinned host buffers: H2D and D2H copies inside the timed region
-  --impl reference times the FP64 C++/OpenMP CPU implementation on a bounded
-  sample of the same workload (the reference has no CPU path of its own; the
-  oracle restates its algorithm).
+  value   whole-job GUPS = 2 * 512^3 * 720 * steps * ranks / max-rank time,
+          device-resident inputs, CUDA events on the launching stream
+  e2e     the same metric through the host entry points mexct_fp / mexct_bp with
+          pinned host buffers (H2D and D2H inside the timed region)
+  extra   FP/BP GUPS for geomFlag 0 and 1; the chosen forms (hardware-texture FP,
+          FP16 storage) with their relative L2 to the plain FP32 result; OSC-TV
+          p50/p99 seconds per reconstruction (256^3, 60 views, 20 iterations x 10
+          subsets) plain (FP32, eager launches) vs chosen (CUDA graphs); the FP64
+          C++/OpenMP CPU implementation on a bounded sample (cpu_baseline).
+
+--impl reference times the CPU implementation alone (the reference has no CPU
+path of its own; its CUDA code uses texture references removed in CUDA 12, so the
+FP64 oracle that restates its algorithms is the CPU reference).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-Multi-GPU: one process per GPU (torchrun); every rank runs the full problem
-(replicas: the path is independent per problem), value aggregates all ranks.
+Multi-GPU: one process per GPU (torchrun); every rank runs its own full problem
+(replicas: the path is independent per problem); value aggregates all ranks.
 """
 from __future__ import annotations
 
@@ -37,12 +44,16 @@ for p in (ROOT, PKG):
 
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes (read + write) per launch of the slab FP kernel, cone 512^3, from the
+# ncu capture summarised in profiles/fp_slab_kernel_cone_512cube_32views.md (32 views),
+# scaled to 720 views (traffic grows with the number of views).
+FP_SLAB_DRAM_BYTES_PER_VIEW = 8.130620e9 / 32
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=512)
@@ -50,6 +61,8 @@ def parse():
     ap.add_argument("--geom", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--osc-reps", type=int, default=5)
     return ap.parse_args()
 
 
@@ -125,40 +138,46 @@ def cpu_sample(size, views, geom, seconds_target=15.0):
     n = size
     vol = phantoms.ellipsoids(n, count=12, seed=2024, nz=n)
     ang_all = phantoms.angles_full(views)
-    k = 1
-    gups = []
-    t_used = 0.0
+    k, used = 1, 0.0
     while True:
-        ang = ang_all[: k]
+        ang = ang_all[::max(1, views // k)][:k]
         t0 = time.perf_counter()
         sino = oracle.fp(vol, 1000.0, ang, k, geom).astype(np.float32)
         oracle.bp(sino, 1000.0, ang, geom)
         dt = time.perf_counter() - t0
-        t_used += dt
-        gups.append(2.0 * n ** 3 * k / dt / 1e9)
-        if t_used > seconds_target or k >= views:
+        used += dt
+        gups = 2.0 * n ** 3 * k / dt / 1e9
+        if used + 2.2 * dt > seconds_target or k >= views:
             break
         k = min(views, k * 2)
-    return {"value": round(gups[-1], 4), "unit": "GUPS", "cores": threads, "kind": "port",
-            "sample": "%d^3 volume, FP+BP over %d of %d cone views (FP64 C++/OpenMP oracle, "
-                      "%d threads)" % (n, k, views, threads)}
+    return {"value": round(gups, 4), "unit": "GUPS", "cores": threads, "kind": "port",
+            "sample": "%d^3 volume, FP+BP over %d of %d views, geomFlag %d (FP64 C++/OpenMP "
+                      "restatement of the reference, %d threads)" % (n, k, views, geom, threads)}
 
 
 def run_reference(args, rank):
     if rank != 0:
         return
-    s = cpu_sample(args.size, args.views, args.geom)
-    steps, warm = args.steps, args.warmup
-    line = {"metric": "FP+BP GUPS, cone geomFlag 2, %d^3 x %d views" % (args.size, args.views),
-            "value": s["value"], "unit": "GUPS", "n_gpus": args.gpus, "steps": steps,
-            "warmup": warm, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ellipsoid phantom)",
-            "impl": "reference",
+    s = cpu_sample(args.size, args.views, args.geom, seconds_target=20.0)
+    line = {"metric": "FP+BP GUPS, cone geomFlag %d, %d^3 x %d views" % (args.geom, args.size,
+                                                                        args.views),
+            "value": s["value"], "unit": "GUPS", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded 12-ellipsoid phantom)", "impl": "reference",
             "config": {"workload": "cone FP+BP %d^3 x %d views, SAD 1000" % (args.size, args.views)},
             "cpu_baseline": s,
             "e2e": {"value": s["value"], "unit": "GUPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def rel(a, b):
+    import torch
+
+    a = a.double()
+    b = b.double()
+    return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
 
 
 def main():
@@ -175,8 +194,7 @@ def main():
     import __graft_entry__ as ge
 
     ge._builder().build()
-    from mexct import _lib, phantoms
-    from mexct import ops
+    from mexct import _lib, ops, phantoms
 
     torch.cuda.set_device(local)
     dist = None
@@ -185,6 +203,7 @@ def main():
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     lib = _lib.load()
+    V = ctypes.c_void_p
 
     n, views, geom = args.size, args.views, args.geom
     N = n * n * n
@@ -196,34 +215,37 @@ def main():
     sino = torch.empty((views, n, n), dtype=torch.float32, device=dev)
     rec = torch.empty((n, n, n), dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
-    sptr = ctypes.c_void_p(stream.cuda_stream)
-    angp = ctypes.c_void_p(ang.ctypes.data)
+    sptr = V(stream.cuda_stream)
+    angp = V(ang.ctypes.data)
+
+    def fp(g=geom, out=sino):
+        _lib.check(lib.mexct_fp_dev(None, V(vol.data_ptr()), n, n, 1000.0, angp, views, g,
+                                    V(out.data_ptr()), sptr))
+
+    def bp(g=geom, src=sino):
+        _lib.check(lib.mexct_bp_dev(None, V(src.data_ptr()), n, n, views, 1000.0, angp, g,
+                                    V(rec.data_ptr()), sptr))
 
     def step():
-        _lib.check(lib.mexct_fp_dev(None, ctypes.c_void_p(vol.data_ptr()), n, n, 1000.0, angp,
-                                    views, geom, ctypes.c_void_p(sino.data_ptr()), sptr))
-        _lib.check(lib.mexct_bp_dev(None, ctypes.c_void_p(sino.data_ptr()), n, n, views, 1000.0,
-                                    angp, geom, ctypes.c_void_p(rec.data_ptr()), sptr))
+        fp()
+        bp()
+
+    def timed(fn, reps=1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-
-    # Per-operator timing (events on the launching stream) for the roofline.
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    fp_ms, bp_ms = [], []
-    for _ in range(max(1, min(2, args.steps))):
-        with torch.cuda.stream(stream):
-            ev[0].record(stream)
-            _lib.check(lib.mexct_fp_dev(None, ctypes.c_void_p(vol.data_ptr()), n, n, 1000.0, angp,
-                                        views, geom, ctypes.c_void_p(sino.data_ptr()), sptr))
-            ev[1].record(stream)
-            _lib.check(lib.mexct_bp_dev(None, ctypes.c_void_p(sino.data_ptr()), n, n, views,
-                                        1000.0, angp, geom, ctypes.c_void_p(rec.data_ptr()), sptr))
-            ev[2].record(stream)
-        stream.synchronize()
-        fp_ms.append(ev[0].elapsed_time(ev[1]))
-        bp_ms.append(ev[1].elapsed_time(ev[2]))
+    # Per-operator times (events on the launching stream) for the roofline.
+    fp_t = float(np.median([timed(fp) for _ in range(2)]))
+    bp_t = float(np.median([timed(bp) for _ in range(2)]))
 
     clocks = ClockSampler(local)
     if dist is not None:
@@ -257,10 +279,10 @@ def main():
         rec_pin = torch.empty((n, n, n), dtype=torch.float32).pin_memory()
 
         def e2e_step():
-            _lib.check(lib.mexct_fp(None, ctypes.c_void_p(vol_pin.data_ptr()), n, n, 1000.0, angp,
-                                    views, geom, ctypes.c_void_p(sino_pin.data_ptr())))
-            _lib.check(lib.mexct_bp(None, ctypes.c_void_p(sino_pin.data_ptr()), n, n, views,
-                                    1000.0, angp, geom, ctypes.c_void_p(rec_pin.data_ptr())))
+            _lib.check(lib.mexct_fp(None, V(vol_pin.data_ptr()), n, n, 1000.0, angp, views, geom,
+                                    V(sino_pin.data_ptr())))
+            _lib.check(lib.mexct_bp(None, V(sino_pin.data_ptr()), n, n, views, 1000.0, angp, geom,
+                                    V(rec_pin.data_ptr())))
 
         e2e_step()
         if dist is not None:
@@ -275,42 +297,139 @@ def main():
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             el = float(tt.item())
         e2e = {"value": round(2.0 * N * views * k * world / el / 1e9, 3), "unit": "GUPS",
-               "h2d_bytes_per_step": 4 * (N + P * views), "d2h_bytes_per_step": 4 * (P * views + N)}
+               "h2d_bytes_per_step": 4 * (N + P * views), "d2h_bytes_per_step": 4 * (P * views + N),
+               "path": "mexct_fp + mexct_bp host entry points, pinned buffers"}
 
     peak, peak_kind = hbm_peak()
-    fp_t = float(np.median(fp_ms)) / 1e3
-    bp_t = float(np.median(bp_ms)) / 1e3
     fp_bytes = 4.0 * (N + P * views)
     bp_bytes = 4.0 * (P * views + N)
-    dom = ("fp", fp_t, fp_bytes) if fp_t >= bp_t else ("bp", bp_t, bp_bytes)
+    dom = ("fp_slab_kernel (cone FP)", fp_t, fp_bytes, FP_SLAB_DRAM_BYTES_PER_VIEW * views) \
+        if fp_t >= bp_t else ("bp_kernel (cone BP)", bp_t, bp_bytes, None)
     achieved = dom[2] / dom[1] / 1e9
     line = {
-        "metric": "FP+BP GUPS, cone geomFlag 2, %d^3 x %d views" % (n, views),
+        "metric": "FP+BP GUPS at %d^3 x %d views (cone geomFlag %d), plain FP32" % (n, views, geom),
         "value": round(gups, 3), "unit": "GUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded 12-ellipsoid phantom)",
         "config": {"workload": "cone FP+BP %d^3 x %d views, SAD 1000, float32" % (n, views),
-                   "l2": "inputs larger than L2 (volume 512 MiB, sinogram 720 MiB)",
+                   "l2": "inputs larger than L2 (volume %d MiB, sinogram %d MiB)"
+                         % (4 * N >> 20, 4 * P * views >> 20),
                    "parallelism": "replicas" if world > 1 else "single"},
         "fp_gups": round(N * views / fp_t / 1e9, 3), "bp_gups": round(N * views / bp_t / 1e9, 3),
         "fp_ms": round(fp_t * 1e3, 3), "bp_ms": round(bp_t * 1e3, 3),
         "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": round(achieved, 2),
-                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "traffic": None},
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5),
+                     "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
+                     if peak_kind == "measured" else "fallback 6.8 TB/s",
+                     "traffic": dom[3],
+                     "note": "gather-bound projector: compulsory bytes 4(N+P*nP) over the launch"},
         "clocks": clk,
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": 4 * args.steps,
         "e2e": e2e,
     }
+
+    if not args.no_extra and rank == 0:
+        extra = {}
+        # geomFlag 0 and 1 at the same size.
+        for g in (0, 1):
+            if g == geom:
+                continue
+            fp(g)
+            tf = timed(lambda: fp(g))
+            tb = timed(lambda: bp(g))
+            extra["geom%d" % g] = {"fp_gups": round(N * views / tf / 1e9, 3),
+                                   "bp_gups": round(N * views / tb / 1e9, 3)}
+        # Chosen forms of FP: hardware texture (8-bit filter weights) and FP16 storage.
+        fp()
+        ref_sino = sino.clone()
+        tex = torch.empty_like(sino)
+        _lib.check(lib.mexct_fp_dev_ex(None, V(vol.data_ptr()), 0, n, n, 1000.0, angp, views, geom,
+                                       V(tex.data_ptr()), 0, 1, sptr))
+        tt = timed(lambda: lib.mexct_fp_dev_ex(None, V(vol.data_ptr()), 0, n, n, 1000.0, angp,
+                                               views, geom, V(tex.data_ptr()), 0, 1, sptr))
+        extra["fp_texture"] = {"fp_gups": round(N * views / tt / 1e9, 3),
+                               "rel_l2_vs_fp32": rel(tex, ref_sino)}
+        del tex
+        vol16 = vol.half()
+        s16 = torch.empty((views, n, n), dtype=torch.float16, device=dev)
+        r16 = torch.empty((n, n, n), dtype=torch.float16, device=dev)
+
+        def fp16():
+            _lib.check(lib.mexct_fp_dev_ex(None, V(vol16.data_ptr()), 1, n, n, 1000.0, angp, views,
+                                           geom, V(s16.data_ptr()), 1, 0, sptr))
+
+        def bp16():
+            _lib.check(lib.mexct_bp_dev_ex(None, V(s16.data_ptr()), 1, n, n, views, 1000.0, angp,
+                                           geom, V(r16.data_ptr()), 1, sptr))
+
+        fp16()
+        bp16()
+        t16f, t16b = timed(fp16), timed(bp16)
+        bp()
+        extra["fp16_storage"] = {"fp_gups": round(N * views / t16f / 1e9, 3),
+                                 "bp_gups": round(N * views / t16b / 1e9, 3),
+                                 "fp_rel_l2_vs_fp32": rel(s16.float(), ref_sino),
+                                 "bp_rel_l2_vs_fp32": rel(r16.float(), rec)}
+        del vol16, s16, r16
+        # OSC-TV reconstruction latency (config: 256^3, 60 views, 20 it x 10 subsets).
+        try:
+            extra["osc_tv"] = osc_tv_latency(args.osc_reps)
+        except Exception as ex:
+            extra["osc_tv"] = {"error": str(ex)}
+        line["extra"] = extra
     if rank == 0 and not args.no_cpu:
         try:
-            line["cpu_baseline"] = cpu_sample(min(n, 256), views, geom, seconds_target=10.0)
+            line["cpu_baseline"] = cpu_sample(n, views, geom, seconds_target=12.0)
         except Exception as ex:  # reported, never fatal
             line["cpu_baseline"] = {"error": str(ex)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def osc_tv_latency(reps):
+    """p50/p99 seconds per OSC-TV reconstruction, plain (eager, FP32) vs chosen (graphs)."""
+    import torch
+
+    from mexct import ops, phantoms, solver
+
+    n, nv = 256, 60
+    vol = phantoms.ellipsoids(n, count=10, seed=7, nz=n)
+    ang = phantoms.angles_full(nv)
+    dvol = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    fp = ops.fp_dev(dvol, 1000.0, ang, 2)
+    rng = np.random.default_rng(11)
+    pre = torch.full_like(fp, 1e5)
+    post = torch.from_numpy(rng.poisson(1e5 * np.exp(-fp.double().cpu().numpy())).astype(np.float32)).cuda()
+    picks = rng.integers(0, 10, 20)
+    out = {}
+    for name, graph, dt in (("plain_fp32", False, None), ("chosen_graph_fp32", True, None),
+                            ("chosen_graph_bf16", True, torch.bfloat16)):
+        times = []
+        mu_last = None
+        for r in range(reps + 1):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            s = solver.OscTvSolver(pre, post, ang, 1000.0, 2, mu_dtype=dt)
+            s.run(picks, n_iter=20, tv_const=0.2, n_sub_init=10, n_sub_final=10, p_val=1.0,
+                  use_graph=graph)
+            mu_last = s.mu()
+            torch.cuda.synchronize()
+            el = time.perf_counter() - t
+            s.close()
+            if r > 0:  # first run warms up (graph capture, lazy module load)
+                times.append(el)
+        out[name] = {"p50_s": round(float(np.percentile(times, 50)), 4),
+                     "p99_s": round(float(np.percentile(times, 99)), 4),
+                     "volumes_per_s": round(1.0 / float(np.mean(times)), 3), "reps": reps}
+        out[name]["_mu"] = mu_last
+    ref = out["plain_fp32"].pop("_mu")
+    for k in ("chosen_graph_fp32", "chosen_graph_bf16"):
+        out[k]["rel_l2_vs_plain"] = rel(out[k].pop("_mu"), ref)
+    out["workload"] = "256^3, 60 cone views, 20 iterations x 10 subsets, TV 20 steps at 0.2*d_a"
+    return out
 
 
 if __name__ == "__main__":

@@ -569,3 +569,187 @@ cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
 }
 
 }  // namespace mexct
+
+namespace mexct {
+
+// ---------------------------------------------------------------------------
+// Voxel-driven BP with projection footprints staged in shared memory.
+// A CTA owns a 32 x 8 x kSmZc voxel brick.  For a block of kSmVb views it
+// copies, per view, the rectangle of detector texels the brick projects onto
+// (u from the four column corners -- u is linear-fractional in (x, y), so its
+// extremes sit at the corners -- and v from the two end slices at the extreme
+// magnifications), with the reference's clamp applied at load time; the
+// threads then take all bilinear taps from shared memory.  A view whose
+// footprint exceeds the staging rectangle is sampled from global memory.
+// ---------------------------------------------------------------------------
+constexpr int kSmZc = 16;        // z voxels per thread
+constexpr int kSmVb = 4;         // views per staged block
+constexpr int kSmU = 64;         // staging rectangle: columns (pitch kSmU + 1)
+constexpr int kSmV = 56;         //                    rows
+constexpr int kSmPitch = kSmU + 1;
+constexpr int kSmView = kSmV * kSmPitch;
+
+struct SmFoot {
+  int u0, v0, fb;
+};
+
+template <int GEOM, typename TS, typename TV>
+__global__ void __launch_bounds__(256, 2) bp_smem_kernel(
+    const __grid_constant__ VoxArgs A, const TS* __restrict__ sino,
+    TV* __restrict__ vol, int accumulate) {
+  extern __shared__ float stage[];  // kSmVb * kSmView floats
+  __shared__ SmFoot foot[kSmVb];
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const int bx0 = blockIdx.x * 32, by0 = blockIdx.y * 8;
+  const int ix = bx0 + threadIdx.x, iy = by0 + threadIdx.y;
+  const int z0 = blockIdx.z * kSmZc;
+  const bool live = ix < A.W && iy < A.W && in_circle(ix, iy, A.hw);
+  float acc[kSmZc];
+#pragma unroll
+  for (int j = 0; j < kSmZc; ++j) acc[j] = 0.f;
+  const float hwf = (float)A.hw + 0.5f;
+  const float x = (float)ix - hwf, y = (float)iy - hwf;
+  const int xl = bx0, xh = min(bx0 + 31, A.W - 1), yl = by0, yh = min(by0 + 7, A.W - 1);
+  const int zl = z0, zh = min(z0 + kSmZc - 1, A.H - 1);
+  for (int vb = 0; vb < A.nviews; vb += kSmVb) {
+    const int nvb = min(kSmVb, A.nviews - vb);
+    // Footprints: warp w < nvb computes view vb + w (lanes 0-3: corners).
+    if (threadIdx.y < nvb) {
+      const Trig t = A.trig[vb + threadIdx.y];
+      const int lane = threadIdx.x;
+      float umn = 3e38f, umx = -3e38f, Umn = 3e38f, Umx = -3e38f;
+      if (lane < 4) {
+        const float cx = (float)((lane & 1) ? xh : xl) - hwf;
+        const float cy = (float)((lane & 2) ? yh : yl) - hwf;
+        const ColGeom<GEOM> g = col_geom<GEOM>(cx, cy, t, A.SR, A.v0, A.hw);
+        umn = umx = g.py;
+        Umn = Umx = (GEOM == 2) ? g.dpz : 1.f;
+      }
+#pragma unroll
+      for (int o = 2; o > 0; o >>= 1) {
+        umn = fminf(umn, __shfl_xor_sync(0xffffffffu, umn, o));
+        umx = fmaxf(umx, __shfl_xor_sync(0xffffffffu, umx, o));
+        Umn = fminf(Umn, __shfl_xor_sync(0xffffffffu, Umn, o));
+        Umx = fmaxf(Umx, __shfl_xor_sync(0xffffffffu, Umx, o));
+      }
+      if (lane == 0) {
+        float vmn, vmx;
+        if (GEOM == 2) {
+          const float a = ((float)zl - A.v0), b = ((float)zh - A.v0);
+          vmn = fminf(fminf(a * Umn, a * Umx), fminf(b * Umn, b * Umx)) + A.v0 + 0.5f;
+          vmx = fmaxf(fmaxf(a * Umn, a * Umx), fmaxf(b * Umn, b * Umx)) + A.v0 + 0.5f;
+        } else {
+          vmn = (float)zl + 0.5f;
+          vmx = (float)zh + 0.5f;
+        }
+        const float ulo = floorf(umn - 0.5f) - 1.f, uhi = floorf(umx - 0.5f) + 2.f;
+        const float vlo = floorf(vmn - 0.5f) - 1.f, vhi = floorf(vmx - 0.5f) + 2.f;
+        SmFoot f;
+        f.fb = !(isfinite(ulo) && isfinite(uhi) && isfinite(vlo) && isfinite(vhi) &&
+                 uhi - ulo + 1.f <= (float)kSmU && vhi - vlo + 1.f <= (float)kSmV &&
+                 fabsf(ulo) < 1e6f && fabsf(vlo) < 1e6f);
+        f.u0 = f.fb ? 0 : (int)ulo;
+        f.v0 = f.fb ? 0 : (int)vlo;
+        foot[threadIdx.y] = f;
+      }
+    }
+    __syncthreads();
+    // Stage: clamped texel (u, v) of view vb+q at stage[q][v - v0][u - u0].
+    for (int q = 0; q < nvb; ++q) {
+      const SmFoot f = foot[q];
+      if (f.fb) continue;
+      const TS* p = sino + (size_t)(A.view0 + vb + q) * A.P;
+      float* s = stage + q * kSmView;
+      for (int e = tid; e < kSmU * kSmV; e += 256) {
+        const int r = e / kSmU, c = e - r * kSmU;
+        const int u = min(max(f.u0 + c, 0), A.W - 1), v = min(max(f.v0 + r, 0), A.H - 1);
+        s[r * kSmPitch + c] = ldf(p + (size_t)v * A.W + u);
+      }
+    }
+    __syncthreads();
+    if (live) {
+      for (int q = 0; q < nvb; ++q) {
+        const SmFoot f = foot[q];
+        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[vb + q], A.SR, A.v0, A.hw);
+        if (f.fb) {
+          bp_column<GEOM, false, kSmZc>(sino + (size_t)(A.view0 + vb + q) * A.P, A.W, A.H, z0, g,
+                                        acc);
+          continue;
+        }
+        const float* s = stage + q * kSmView;
+        const float tu = g.py - 0.5f;
+        const float fu = floorf(tu);
+        const float au = tu - fu;
+        const float w0 = g.w * (1.f - au), w1 = g.w * au;
+        const int cu = (int)fu - f.u0;
+        if (GEOM < 2) {
+          // Par/fan rows are exact texel rows (pz = iz + 0.5).
+#pragma unroll
+          for (int j = 0; j < kSmZc; ++j) {
+            const int r = min(z0 + j, A.H - 1) - f.v0;
+            const int o = min(max(r * kSmPitch + cu, 0), kSmView - 2);
+            acc[j] = fmaf(w0, s[o], fmaf(w1, s[o + 1], acc[j]));
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < kSmZc; ++j) {
+            const float tv = fmaf((float)(z0 + j), g.dpz, g.pz0) - 0.5f;
+            const float fv = floorf(tv);
+            const float av = tv - fv;
+            const int o = min(max(((int)fv - f.v0) * kSmPitch + cu, 0), kSmView - kSmPitch - 2);
+            const float a = fmaf(w0, s[o], w1 * s[o + 1]);
+            const float b = fmaf(w0, s[o + kSmPitch], w1 * s[o + kSmPitch + 1]);
+            acc[j] = fmaf(1.f - av, a, fmaf(av, b, acc[j]));
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (ix >= A.W || iy >= A.W) return;
+  const size_t base = (size_t)iy * A.W + ix;
+  const size_t sz = (size_t)A.W * A.W;
+#pragma unroll
+  for (int j = 0; j < kSmZc; ++j) {
+    if (z0 + j < A.H) {
+      TV* o = vol + base + (size_t)(z0 + j) * sz;
+      stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
+    }
+  }
+}
+
+template <int GEOM, typename TS, typename TV>
+static cudaError_t bp_smem_go(const VoxArgs& a, const void* sino, void* vol, bool accum,
+                              cudaStream_t st) {
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + kSmZc - 1) / kSmZc);
+  const int smem = kSmVb * kSmView * (int)sizeof(float);
+  static bool attr_set = false;  // once per instantiation
+  if (!attr_set) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        bp_smem_kernel<GEOM, TS, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  bp_smem_kernel<GEOM, TS, TV>
+      <<<grd, blk, smem, st>>>(a, (const TS*)sino, (TV*)vol, accum ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_smem(int geom, const VoxArgs& a, const void* sino, int stype,
+                           void* vol, int vtype, bool accumulate, cudaStream_t st) {
+#define BPS(G, S, T) return bp_smem_go<G, S, T>(a, sino, vol, accumulate, st)
+#define BPG(S, T)                          \
+  if (geom == 0) BPS(0, S, T);             \
+  if (geom == 1) BPS(1, S, T);             \
+  BPS(2, S, T)
+  if (stype == kF32 && vtype == kF32) { BPG(float, float); }
+  else if (stype == kF16 && vtype == kF16) { BPG(__half, __half); }
+  else if (stype == kF16 && vtype == kF32) { BPG(__half, float); }
+  else if (stype == kBF16 && vtype == kBF16) { BPG(__nv_bfloat16, __nv_bfloat16); }
+  else if (stype == kBF16 && vtype == kF32) { BPG(__nv_bfloat16, float); }
+  return cudaErrorInvalidValue;
+#undef BPG
+#undef BPS
+}
+
+}  // namespace mexct

@@ -143,7 +143,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // ---------------------------------------------------------------------------
 // Slab kernel.
 // ---------------------------------------------------------------------------
-constexpr int kSlabT = 8;                     // a-taps per slab
+constexpr int kSlabT = 5;                     // a-taps per slab
 constexpr int kSlabA = kSlabT + 1;            // a-planes in a box
 constexpr int kBoxF = 96;                     // box extent along f (elements)
 constexpr int kBoxZ = 2;                      // z rows per TMA box
@@ -189,7 +189,7 @@ __device__ __forceinline__ float sample_at(const T* base, int sa, int sz, float 
 }
 
 template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
-__global__ void __launch_bounds__(256, 2) fp_slab_kernel(
+__global__ void __launch_bounds__(256, 3) fp_slab_kernel(
     const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
     const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
     const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E) {
@@ -348,45 +348,53 @@ __global__ void __launch_bounds__(256, 2) fp_slab_kernel(
       from_smem = mbar_wait_bounded(&bar[j & 1], phase[j & 1], E.err);
       phase[j & 1] ^= 1u;
     }
-    // Two samples per iteration (independent loads and FMA chains).
+    // Samples of this lane whose a-tap lies in [alo, ahi], two per iteration
+    // where possible.  Tap indices are kept as floats (exact below 2^24) so a
+    // sample costs one float->int conversion for its shared-memory index.
+    const float alo_f = (float)p.alo, ahi_f = (float)p.ahi;
+    const float off = -(float)(p.z0 * kPlane + p.a0 * kBoxF + p.f0);
     while (k < n) {
-      const float k0 = (float)k, k1 = (float)(k + 1);
-      const float ta = fmaf(k0, da, ta0), tb = fmaf(k1, da, ta0);
-      const int ia = __float2int_rd(ta), ib = __float2int_rd(tb);
-      if (dir > 0 ? ia > p.ahi : ia < p.alo) break;
-      const bool two = (k + 1 < n) && (dir > 0 ? ib <= p.ahi : ib >= p.alo);
-      const float tfa = fmaf(k0, df, tf0), tfb = fmaf(k1, df, tf0);
-      const float tza = Z2 ? fmaf(k0, dz, tz0) : tz0, tzb = Z2 ? fmaf(k1, dz, tz0) : tz0;
-      const int fa = __float2int_rd(tfa), fb = __float2int_rd(tfb);
-      const int za = __float2int_rd(tza), zb = __float2int_rd(tzb);
-      const float wa0 = ta - (float)ia, wf0 = tfa - (float)fa, wz0 = tza - (float)za;
-      const float wa1 = tb - (float)ib, wf1 = tfb - (float)fb, wz1 = tzb - (float)zb;
-      float v0, v1;
+      const float k0 = (float)k;
+      const float ta = fmaf(k0, da, ta0);
+      const float fa_ = floorf(ta);
+      if (dir > 0 ? fa_ > ahi_f : fa_ < alo_f) break;
+      const float tb = ta + da;
+      const float fb_ = floorf(tb);
+      const bool two = (k + 1 < n) && (dir > 0 ? fb_ <= ahi_f : fb_ >= alo_f);
+      const float tf0_ = fmaf(k0, df, tf0), tz0_ = Z2 ? fmaf(k0, dz, tz0) : tz0;
+      const float ff0 = floorf(tf0_), fz0 = floorf(tz0_);
       if (from_smem) {
-        int i0 = (za - p.z0) * kPlane + (ia - p.a0) * kBoxF + (fa - p.f0);
-        int i1 = (zb - p.z0) * kPlane + (ib - p.a0) * kBoxF + (fb - p.f0);
+        const float wa0 = ta - fa_, wf0 = tf0_ - ff0, wz0 = tz0_ - fz0;
+        int i0 = __float2int_rn(fmaf(fz0, (float)kPlane, fmaf(fa_, (float)kBoxF, ff0 + off)));
         i0 = min(max(i0, 0), kMaxIdx);
-        i1 = min(max(i1, 0), kMaxIdx);
-        v0 = sample_at<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
-        v1 = sample_at<Z2>(b + i1, kBoxF, kPlane, wa1, wf1, wz1);
+        if (two) {
+          const float tf1 = tf0_ + df, tz1 = Z2 ? tz0_ + dz : tz0;
+          const float ff1 = floorf(tf1), fz1 = floorf(tz1);
+          const float wa1 = tb - fb_, wf1 = tf1 - ff1, wz1 = tz1 - fz1;
+          int i1 = __float2int_rn(fmaf(fz1, (float)kPlane, fmaf(fb_, (float)kBoxF, ff1 + off)));
+          i1 = min(max(i1, 0), kMaxIdx);
+          const float v0 = sample_at<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
+          const float v1 = sample_at<Z2>(b + i1, kBoxF, kPlane, wa1, wf1, wz1);
+          acc0 += v0;
+          acc1 += v1;
+        } else {
+          acc0 += sample_at<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
+        }
       } else {
-        const int ga = min(max(ia, 0), Ps - 2), gf = min(max(fa, 0), Pf - 2);
-        const int gz = min(max(za, 0), Pz - 2);
-        const int ha = min(max(ib, 0), Ps - 2), hf = min(max(fb, 0), Pf - 2);
-        const int hz = min(max(zb, 0), Pz - 2);
-        v0 = sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
-                           Pf * Ps, wa0, wf0, wz0);
-        v1 = sample_at<Z2>(gv + (size_t)hf + (size_t)Pf * ((size_t)ha + (size_t)Ps * hz), Pf,
-                           Pf * Ps, wa1, wf1, wz1);
+        // Fallback: the same taps from the padded volume in global memory.
+        for (int q = 0; q < (two ? 2 : 1); ++q) {
+          const float kq = k0 + (float)q;
+          const float tq = fmaf(kq, da, ta0), tfq = fmaf(kq, df, tf0);
+          const float tzq = Z2 ? fmaf(kq, dz, tz0) : tz0;
+          const float fq = floorf(tq), ffq = floorf(tfq), fzq = floorf(tzq);
+          const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
+          const int gz = min(max((int)fzq, 0), Pz - 2);
+          acc0 += sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
+                                Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
+        }
       }
-      acc0 += v0;
-      if (two) {
-        acc1 += v1;
-        k += 2;
-      } else {
-        k += 1;
-        break;
-      }
+      k += two ? 2 : 1;
+      if (!two) break;
     }
     __syncthreads();
   }
@@ -447,8 +455,14 @@ static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtens
                            const SlabEpi& e, cudaStream_t st) {
   auto k = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO>;
   const size_t smem = 2 * (size_t)kBufElems * sizeof(TV) + 128;
-  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
+  static bool attr_set = false;  // once per instantiation (before any capture)
+  if (!attr_set) {
+    cudaError_t err =
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    attr_set = true;
+  }
+  if (a.nviews <= 0) return cudaSuccess;
   const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
   dim3 blk(32, 8), grd(a.nviews, tiles);
   k<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e);
@@ -459,7 +473,6 @@ cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
                            const CUtensorMap& mx, const CUtensorMap& my, const void* px,
                            const void* py, int Pf, int vt, void* out, int ot,
                            const SlabEpi& e, cudaStream_t st) {
-  if (a.nviews <= 0) return cudaSuccess;
 #define GO(G, B, EP, TV, TO) return slab_go<G, B, EP, TV, TO>(a, mx, my, px, py, Pf, out, e, st)
   if (osc) {
     if (vt == kF32) {

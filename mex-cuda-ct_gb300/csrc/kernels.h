@@ -74,6 +74,11 @@ cudaError_t launch_bp(int geom, const VoxArgs& a, const void* sino,
                       int sino_type, void* vol, int vol_type, bool accumulate,
                       cudaStream_t st);
 
+// BP with per-brick projection footprints staged in shared memory.
+cudaError_t launch_bp_smem(int geom, const VoxArgs& a, const void* sino,
+                           int sino_type, void* vol, int vol_type,
+                           bool accumulate, cudaStream_t st);
+
 cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
                           const float* pts, float* vol, cudaStream_t st);
 

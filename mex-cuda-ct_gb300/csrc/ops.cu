@@ -192,7 +192,7 @@ mexct_status bp_dev_impl(mexct_ctx* c, const void* d_sino, int stype, int W,
     a->nviews = std::min(kMaxViews, nP - v0);
     a->view0 = v0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-    MEXCT_TRY_CUDA(launch_bp(geom, *a, d_sino, stype, d_vol, vt, v0 > 0, st), "bp: launch");
+    MEXCT_TRY_CUDA(launch_bp_smem(geom, *a, d_sino, stype, d_vol, vt, v0 > 0, st), "bp: launch");
   }
   return MEXCT_OK;
 }

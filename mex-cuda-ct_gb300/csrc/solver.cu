@@ -7,7 +7,7 @@
 // whole reconstruction; an iteration is a fixed sequence of kernels:
 //
 //   mu_old <- mu                                     (:45)
-//   per subset: transpose(mu), osc_fp (FP + residual), osc_bp_update   (:51-59)
+//   per subset: pad(mu), slab FP + residual, dual BP + update         (:51-59)
 //   k > 1: d_a = ||mu_old - mu|| in FP64 (mu_old(1) = 0, NaN dropped)  (:64-67)
 //          20 TV steps with c = TV_constant * d_a read on the device    (:68)
 //          NaN/Inf -> 0                                                 (:69-70)
@@ -50,8 +50,15 @@ struct mexct_osctv {
     }
   };
   std::map<Key, cudaGraphExec_t> graphs;
+  // Graphs are captured and launched on this stream (capture is not allowed
+  // on the legacy default stream), joined to the caller's stream by events.
+  cudaStream_t own = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   ~mexct_osctv() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (own) cudaStreamDestroy(own);
     for (Buf* b : {&mu, &mu_old, &pre, &post, &padx, &pady, &err, &r1, &r2, &tvbuf, &red, &cnt, &scal})
       b->release();
   }
@@ -200,6 +207,9 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   s->sad = sad;
   s->mu_type = mu_type;
   s->angles.assign(angles, angles + nP);
+  MEXCT_TRY_CUDA(cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking), "osctv_create: stream");
+  MEXCT_TRY_CUDA(cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming), "osctv_create: event");
+  MEXCT_TRY_CUDA(cudaEventCreateWithFlags(&s->ev_out, cudaEventDisableTiming), "osctv_create: event");
   const size_t N = s->N(), M = s->M(), vb = N * dsize(mu_type);
   const size_t P = (size_t)W * H;
   const size_t maxv = (size_t)nP;  // a subset holds at most nP views
@@ -229,6 +239,23 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
                  "osctv_create: pre");
   MEXCT_TRY_CUDA(launch_clamp_copy(d_post, s->post.as<float>(), (long long)M, 1e-6f, st),
                  "osctv_create: post");
+  // Run one eager iteration-free launch setup so kernel attributes are set
+  // outside any later stream capture.
+  {
+    CUtensorMap mx, my;
+    int Pf = 0;
+    mexct_status ps = prepare_slab_bufs(s->padx, s->pady, s->err, s->mu.p, mu_type, W, H, true,
+                                        &mx, &my, &Pf, st);
+    if (ps) return ps;
+    std::unique_ptr<RayArgs> ra(new RayArgs);
+    fill_std_rays(*ra, W, H, sad, geom, true);
+    ra->nviews = 0;  // no work: sets attributes only
+    SlabEpi e{s->pre.as<float>(), s->post.as<float>(), s->r1.as<float>(), s->r2.as<float>(),
+              s->err.as<unsigned>()};
+    MEXCT_TRY_CUDA(launch_fp_slab(geom, true, true, *ra, mx, my, s->padx.p, s->pady.p, Pf,
+                                  mu_type, nullptr, kF32, e, st),
+                   "osctv_create: kernel setup");
+  }
   *out = s.release();
   return MEXCT_OK;
 }
@@ -263,10 +290,10 @@ mexct_status mexct_osctv_run(mexct_osctv* s, const mexct_osctv_params* p,
       auto it = s->graphs.find(key);
       if (it == s->graphs.end()) {
         cudaGraph_t g = nullptr;
-        MEXCT_TRY_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal),
+        MEXCT_TRY_CUDA(cudaStreamBeginCapture(s->own, cudaStreamCaptureModeThreadLocal),
                        "osctv_run: begin capture");
-        mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const, st);
-        cudaError_t ce = cudaStreamEndCapture(st, &g);
+        mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const, s->own);
+        cudaError_t ce = cudaStreamEndCapture(s->own, &g);
         if (e != MEXCT_OK) {
           if (g) cudaGraphDestroy(g);
           return e;
@@ -278,7 +305,11 @@ mexct_status mexct_osctv_run(mexct_osctv* s, const mexct_osctv_params* p,
         MEXCT_TRY_CUDA(ce, "osctv_run: instantiate");
         it = s->graphs.emplace(key, ex).first;
       }
-      MEXCT_TRY_CUDA(cudaGraphLaunch(it->second, st), "osctv_run: graph launch");
+      MEXCT_TRY_CUDA(cudaEventRecord(s->ev_in, st), "osctv_run: join");
+      MEXCT_TRY_CUDA(cudaStreamWaitEvent(s->own, s->ev_in, 0), "osctv_run: join");
+      MEXCT_TRY_CUDA(cudaGraphLaunch(it->second, s->own), "osctv_run: graph launch");
+      MEXCT_TRY_CUDA(cudaEventRecord(s->ev_out, s->own), "osctv_run: join");
+      MEXCT_TRY_CUDA(cudaStreamWaitEvent(st, s->ev_out, 0), "osctv_run: join");
     } else {
       mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const, st);
       if (e != MEXCT_OK) return e;
