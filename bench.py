@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--osc-reps", type=int, default=5)
+    ap.add_argument("--batch-problems", type=int, default=48)
+    ap.add_argument("--serve-requests", type=int, default=60)
     return ap.parse_args()
 
 
@@ -325,7 +327,7 @@ def main():
                      "traffic": dom[3],
                      "note": "gather-bound projector: compulsory bytes 4(N+P*nP) over the launch"},
         "clocks": clk,
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 4 * args.steps,  # per step: pad_x, pad_transpose, fp_slab, bp
         "e2e": e2e,
     }
 
@@ -341,13 +343,16 @@ def main():
             extra["geom%d" % g] = {"fp_gups": round(N * views / tf / 1e9, 3),
                                    "bp_gups": round(N * views / tb / 1e9, 3)}
         # Chosen forms of FP: hardware texture (8-bit filter weights) and FP16 storage.
+        # (Every launch goes to `stream`; it is synchronised before torch reads.)
         fp()
+        stream.synchronize()
         ref_sino = sino.clone()
         tex = torch.empty_like(sino)
         _lib.check(lib.mexct_fp_dev_ex(None, V(vol.data_ptr()), 0, n, n, 1000.0, angp, views, geom,
                                        V(tex.data_ptr()), 0, 1, sptr))
         tt = timed(lambda: lib.mexct_fp_dev_ex(None, V(vol.data_ptr()), 0, n, n, 1000.0, angp,
                                                views, geom, V(tex.data_ptr()), 0, 1, sptr))
+        stream.synchronize()
         extra["fp_texture"] = {"fp_gups": round(N * views / tt / 1e9, 3),
                                "rel_l2_vs_fp32": rel(tex, ref_sino)}
         del tex
@@ -367,16 +372,22 @@ def main():
         bp16()
         t16f, t16b = timed(fp16), timed(bp16)
         bp()
+        stream.synchronize()
         extra["fp16_storage"] = {"fp_gups": round(N * views / t16f / 1e9, 3),
                                  "bp_gups": round(N * views / t16b / 1e9, 3),
                                  "fp_rel_l2_vs_fp32": rel(s16.float(), ref_sino),
                                  "bp_rel_l2_vs_fp32": rel(r16.float(), rec)}
         del vol16, s16, r16
         # OSC-TV reconstruction latency (config: 256^3, 60 views, 20 it x 10 subsets).
-        try:
-            extra["osc_tv"] = osc_tv_latency(args.osc_reps)
-        except Exception as ex:
-            extra["osc_tv"] = {"error": str(ex)}
+        del ref_sino
+        for name, fn in (("osc_tv", lambda: osc_tv_latency(args.osc_reps)),
+                         ("batched", lambda: batched_uneven(args.batch_problems)),
+                         ("serving", lambda: serving(args.serve_requests))):
+            try:
+                extra[name] = fn()
+            except Exception as ex:  # reported, never fatal
+                extra[name] = {"error": "%s: %s" % (type(ex).__name__, ex)}
+            torch.cuda.empty_cache()
         line["extra"] = extra
     if rank == 0 and not args.no_cpu:
         try:
@@ -400,6 +411,7 @@ def osc_tv_latency(reps):
     ang = phantoms.angles_full(nv)
     dvol = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
     fp = ops.fp_dev(dvol, 1000.0, ang, 2)
+    torch.cuda.synchronize()
     rng = np.random.default_rng(11)
     pre = torch.full_like(fp, 1e5)
     post = torch.from_numpy(rng.poisson(1e5 * np.exp(-fp.double().cpu().numpy())).astype(np.float32)).cuda()
@@ -430,6 +442,187 @@ def osc_tv_latency(reps):
         out[k]["rel_l2_vs_plain"] = rel(out[k].pop("_mu"), ref)
     out["workload"] = "256^3, 60 cone views, 20 iterations x 10 subsets, TV 20 steps at 0.2*d_a"
     return out
+
+
+def batched_uneven(count, seed=2026):
+    """48 uneven problems (geom 0/1/2, 64^3..256^3, 90..720 views): FP + BP + 5 OSC-TV
+    iterations (8 subsets) each.  plain: one problem at a time, one launch per
+    operator call, eager OSC-TV.  chosen: all FPs in one persistent launch and all
+    BPs in another, captured in one CUDA graph; OSC-TV solvers replay per-iteration
+    graphs on 8 concurrent streams."""
+    import torch
+
+    from mexct import batch, ops, phantoms, solver
+
+    rng = np.random.default_rng(seed)
+    probs = []
+    for i in range(count):
+        n = int(rng.choice([64, 96, 128, 192, 256]))
+        nv = int(rng.integers(90, 721))
+        g = int(rng.integers(0, 3))
+        vol = phantoms.ellipsoids(n, count=6, seed=seed + i, nz=n)
+        ang = phantoms.angles_full(nv)
+        d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+        probs.append({"vol": d, "sino": torch.empty((nv, n, n), device="cuda"),
+                      "rec": torch.empty((n, n, n), device="cuda"), "angles": ang, "sad": 1000.0,
+                      "geom": g, "picks": rng.integers(0, 8, 5)})
+    vu = sum(p["vol"].numel() * p["angles"].size for p in probs)  # voxel-view updates per op
+    # Counts for OSC-TV: pre = 1e5, post = noiseless 1e5*exp(-FP) (the FP is computed once).
+    for p in probs:
+        ops.fp_dev(p["vol"], p["sad"], p["angles"], p["geom"], out=p["sino"])
+    torch.cuda.synchronize()
+    pre = [torch.full_like(p["sino"], 1e5) for p in probs]
+    post = [1e5 * torch.exp(-p["sino"]) for p in probs]
+    kw = dict(n_iter=5, tv_const=0.2, n_sub_init=8, n_sub_final=8, p_val=1.0)
+
+    def plain():
+        for p in probs:
+            ops.fp_dev(p["vol"], p["sad"], p["angles"], p["geom"], out=p["sino"])
+            ops.bp_dev(p["sino"], p["sad"], p["angles"], p["geom"], out=p["rec"])
+        torch.cuda.synchronize()
+        t_fb = time.perf_counter()
+        for k, p in enumerate(probs):
+            sv = solver.OscTvSolver(pre[k], post[k], p["angles"], p["sad"], p["geom"])
+            sv.run(p["picks"], use_graph=False, **kw)
+            torch.cuda.synchronize()
+            sv.close()
+        return t_fb
+
+    b = batch.Batch(probs)
+    st = torch.cuda.Stream()
+    b.fp(st)
+    b.bp(st)
+    st.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=st):
+        b.fp(st)
+        b.bp(st)
+    streams = [torch.cuda.Stream() for _ in range(8)]
+
+    def chosen():
+        graph.replay()
+        torch.cuda.synchronize()
+        t_fb = time.perf_counter()
+        solvers = []
+        for k, p in enumerate(probs):
+            s_ = streams[k % len(streams)]
+            sv = solver.OscTvSolver(pre[k], post[k], p["angles"], p["sad"], p["geom"], stream=s_)
+            sv.run(p["picks"], use_graph=True, **kw)
+            solvers.append(sv)
+        torch.cuda.synchronize()
+        for sv in solvers:
+            sv.close()
+        return t_fb
+
+    out = {"problems": count, "voxel_view_updates_per_op": vu}
+    for name, fn in (("plain", plain), ("chosen", chosen)):
+        fn()  # warm-up (graph capture, lazy loading)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t_fb = fn()
+        t1 = time.perf_counter()
+        out[name] = {"total_s": round(t1 - t0, 4), "fp_bp_s": round(t_fb - t0, 4),
+                     "osc_tv_s": round(t1 - t_fb, 4),
+                     "fp_bp_gups": round(2.0 * vu / (t_fb - t0) / 1e9, 3)}
+    out["speedup_total"] = round(out["plain"]["total_s"] / out["chosen"]["total_s"], 3)
+    out["workload"] = ("%d problems: geom 0/1/2, 64^3..256^3, 90..720 views, SAD 1000; FP, BP, "
+                       "5 OSC-TV iterations x 8 subsets each" % count)
+    b.close()
+    return out
+
+
+def serving(count, seed=7):
+    """Open-loop Poisson arrivals of FDK / OSC-TV (10 iterations x 10 subsets)
+    requests on 128^3 / 256^3 volumes with 60..360 views, random geometry, FP32 or
+    BF16 mu; lambda set for ~80% of the serial service rate.  Reports p50/p99
+    latency and volumes/s against the same requests run serially, one at a time,
+    through the one-request entry points (identical results)."""
+    import torch
+
+    import mexct
+    from mexct import ops, phantoms, serve, solver
+
+    rng = np.random.default_rng(seed)
+    datasets = {}
+    for n in (128, 256):
+        for nv in (60, 180, 360):
+            vol = phantoms.ellipsoids(n, count=8, seed=n + nv, nz=n)
+            ang = phantoms.angles_full(nv)
+            d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+            fpd = ops.fp_dev(d, 1000.0, ang, 2)
+            torch.cuda.synchronize()
+            fp = fpd.cpu().numpy().transpose(2, 1, 0)
+            pre = np.full(fp.shape, 1e5, dtype=np.float32, order="F")
+            post = np.asfortranarray(rng.poisson(1e5 * np.exp(-fp.astype(np.float64)))
+                                     .astype(np.float32))
+            datasets[(n, nv)] = (pre, post, ang)
+    reqs = []
+    for i in range(count):
+        n = int(rng.choice([128, 256], p=[0.7, 0.3]))
+        nv = int(rng.choice([60, 180, 360]))
+        reqs.append({"kind": int(rng.integers(0, 2)), "key": (n, nv), "geom": int(rng.integers(0, 3)),
+                     "mu": int(rng.choice([0, 2])), "picks": rng.integers(0, 10, 10)})
+    gs = {0: "par3d", 1: "fan3d", 2: "cone3d"}
+
+    def alone(r):
+        pre, post, ang = datasets[r["key"]]
+        if r["kind"] == 0:
+            return mexct.FBP_recon(pre, post, ang, {"type": gs[r["geom"]], "SAD": 1000.0},
+                                   "hamming", 1.0, 1.0)
+        if r["mu"] == 0:
+            return solver.OSC_TV_recon(pre, post, ang, {"type": gs[r["geom"]], "SAD": 1000.0}, 10,
+                                       0.2, 10, 10, 1.0, r["picks"])
+        srv = serve.Server(slots=1, budget_bytes=64 << 30)
+        t = srv.submit_osctv(pre, post, ang, r["geom"], r["picks"], n_iter=10, n_sub=10, mu_type=2)
+        out = srv.wait(t)[0]
+        srv.close()
+        return out
+
+    alone(reqs[0])  # warm-up
+    t0 = time.perf_counter()
+    serial = []
+    for r in reqs:
+        a = time.perf_counter()
+        serial.append((alone(r), time.perf_counter() - a))
+    t_serial = time.perf_counter() - t0
+    mean_s = t_serial / count
+    lam = 0.8 / mean_s
+    gaps = rng.exponential(1.0 / lam, count)
+    srv = serve.Server(slots=4, budget_bytes=48 << 30)
+    tickets = []
+    t0 = time.perf_counter()
+    due = t0
+    for r, gap in zip(reqs, gaps):
+        due += gap
+        now = time.perf_counter()
+        if due > now:
+            time.sleep(due - now)
+        pre, post, ang = datasets[r["key"]]
+        if r["kind"] == 0:
+            tickets.append(srv.submit_fdk(pre, post, ang, r["geom"]))
+        else:
+            tickets.append(srv.submit_osctv(pre, post, ang, r["geom"], r["picks"], n_iter=10,
+                                            n_sub=10, mu_type=r["mu"]))
+    lat, same = [], 0
+    for (a, _), t in zip(serial, tickets):
+        rec, tm = srv.wait(t)
+        lat.append(tm["total_s"])
+        same += int(np.array_equal(rec, a))
+    makespan = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    s_lat = [x[1] for x in serial]
+    return {"requests": count, "slots": 4, "lambda_per_s": round(lam, 3),
+            "p50_s": round(float(np.percentile(lat, 50)), 4),
+            "p99_s": round(float(np.percentile(lat, 99)), 4),
+            "volumes_per_s": round(count / makespan, 3),
+            "serial": {"p50_s": round(float(np.percentile(s_lat, 50)), 4),
+                       "p99_s": round(float(np.percentile(s_lat, 99)), 4),
+                       "volumes_per_s": round(count / t_serial, 3)},
+            "identical_to_alone": "%d/%d" % (same, count),
+            "max_concurrent": st["max_concurrent"], "peak_hbm_gb": round(st["peak_bytes"] / 2**30, 2),
+            "workload": "FDK or OSC-TV (10 it x 10 subsets) on 128^3/256^3, 60/180/360 views, "
+                        "geom 0/1/2, FP32/BF16 mu, Poisson arrivals at 80% of serial rate"}
 
 
 if __name__ == "__main__":

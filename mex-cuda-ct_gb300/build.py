@@ -19,8 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmexct.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["k_proj.cu", "k_slab.cu", "k_iter.cu", "k_sched.cu", "api.cu", "ops.cu", "solver.cu",
-           "noalloc.cu"]
+SOURCES = ["k_proj.cu", "k_slab.cu", "k_iter.cu", "batch.cu", "api.cu", "ops.cu", "solver.cu",
+           "serve.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -44,9 +44,29 @@ mexct_status cuda_err(cudaError_t e, const char* what) {
 }
 
 void Buf::release() {
-  if (p) cudaFree(p);
+  if (p) {
+    if (ast) cudaFreeAsync(p, ast);
+    else cudaFree(p);
+  }
   p = nullptr;
   n = 0;
+  ast = nullptr;
+}
+
+cudaError_t Buf::ensure_async(size_t bytes, cudaStream_t st) {
+  if (bytes <= n && p) return cudaSuccess;
+  release();
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocAsync(&p, bytes, st);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    n = 0;
+    cudaGetLastError();
+    return e;
+  }
+  n = bytes;
+  ast = st;
+  return cudaSuccess;
 }
 
 cudaError_t Buf::ensure(size_t bytes) {

@@ -16,7 +16,12 @@ namespace mexct {
 struct Buf {
   void* p = nullptr;
   size_t n = 0;
+  cudaStream_t ast = nullptr;  // set when allocated stream-ordered
   cudaError_t ensure(size_t bytes);
+  // Stream-ordered allocation (cudaMallocAsync): no device-wide
+  // synchronisation on allocation or release, so work on other streams keeps
+  // running.  The buffer is released with cudaFreeAsync on the same stream.
+  cudaError_t ensure_async(size_t bytes, cudaStream_t st);
   void release();
   template <typename T>
   T* as() const {
@@ -82,6 +87,10 @@ inline size_t dsize(int t) { return t == kF32 ? 4 : 2; }
 mexct_status prepare_slab_bufs(Buf& px, Buf& py, Buf& err, const void* d_vol, int vt, int W,
                                int H, bool border, CUtensorMap* mx, CUtensorMap* my,
                                int* Pf_out, cudaStream_t st);
+mexct_status osc_tv_recon_typed(mexct_ctx* ctx, const float* pre, const float* post, int W, int H,
+                                int nP, const float* angles, float sad, int geom, int n_iter,
+                                float tv_const, int n_sub_init, int n_sub_final, float p_val,
+                                const int32_t* first_picks, int mu_type, float* recon);
 mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
                           bool border, CUtensorMap* mx, CUtensorMap* my, int* Pf_out,
                           cudaStream_t st);

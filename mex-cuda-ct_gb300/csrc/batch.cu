@@ -1,0 +1,171 @@
+// batch.cu -- batched FP / BP over many independent problems of different
+// sizes and geometries (include/mexct_batch.h).
+//
+// A batch is planned once (padded-volume buffers, per-problem device
+// descriptors with TMA maps and trig tables); each operator then runs as a
+// fixed, capturable sequence: one batched padding launch plus one persistent
+// FP launch, or one persistent BP launch.  Persistent CTAs take work items
+// (problem, view, tile) / (problem, brick) from a global counter, so uneven
+// problems load-balance inside one launch.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "../../include/mexct.h"
+#include "../../include/mexct_batch.h"
+#include "api_internal.h"
+#include "kernels.h"
+
+using namespace mexct;
+
+struct mexct_batch {
+  int device = 0;
+  int n = 0;
+  std::vector<Buf> pads;  // 2 per problem
+  Buf fp_desc, bp_desc, trig, counters, err;
+  long long fp_items = 0, bp_items = 0, pad_items = 0;
+  int sms = 152;
+  ~mexct_batch() {
+    for (Buf& b : pads) b.release();
+    for (Buf* b : {&fp_desc, &bp_desc, &trig, &counters, &err}) b->release();
+  }
+};
+
+extern "C" {
+
+mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int n,
+                                mexct_batch** out) {
+  if (!out) return set_err(MEXCT_ERR_ARG, "batch_create: out is NULL");
+  *out = nullptr;
+  if (!probs || n <= 0) return set_err(MEXCT_ERR_ARG, "batch_create: no problems");
+  for (int i = 0; i < n; ++i) {
+    const mexct_problem& p = probs[i];
+    if (p.W <= 0 || p.H <= 0 || p.nP <= 0 || p.W > 16384 || p.H > 16384 || p.nP > 1 << 20)
+      return set_err(MEXCT_ERR_ARG, "batch_create: problem %d has bad dims", i);
+    if (p.geom < 0 || p.geom > 2)
+      return set_err(MEXCT_ERR_ARG, "batch_create: problem %d: invalid geometry %d", i, p.geom);
+    if (!p.angles || !p.d_vol || !p.d_sino || !p.d_rec)
+      return set_err(MEXCT_ERR_ARG, "batch_create: problem %d: NULL pointer", i);
+  }
+  mexct_ctx* c = resolve(ctx);
+  if (!c) return set_err(MEXCT_ERR_CUDA, "batch_create: no CUDA device / context");
+  DevGuard dg(c->device);
+  std::unique_ptr<mexct_batch> b(new mexct_batch);
+  b->device = c->device;
+  b->n = n;
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, c->device);
+  size_t ntrig = 0;
+  for (int i = 0; i < n; ++i) ntrig += probs[i].nP;
+  std::vector<Trig> trig(ntrig);
+  std::vector<BatchFp> fd(n);
+  std::vector<BatchBp> bd(n);
+  b->pads.resize(2 * n);
+  size_t toff = 0;
+  MEXCT_TRY_CUDA(b->trig.ensure(ntrig * sizeof(Trig)), "batch_create: trig");
+  const Trig* dtrig = b->trig.as<Trig>();
+  for (int i = 0; i < n; ++i) {
+    const mexct_problem& p = probs[i];
+    const int W = p.W, H = p.H;
+    const int Pf = slab_pitch(W);
+    const size_t pb = (size_t)Pf * (W + 2) * (H + 2) * sizeof(float);
+    MEXCT_TRY_CUDA(b->pads[2 * i].ensure(pb), "batch_create: padded volume");
+    MEXCT_TRY_CUDA(b->pads[2 * i + 1].ensure(pb), "batch_create: padded volume");
+    for (int v = 0; v < p.nP; ++v) trig_of(p.angles[v], &trig[toff + v]);
+    BatchFp& f = fd[i];
+    std::memset(&f, 0, sizeof f);
+    MEXCT_TRY_CUDA(make_slab_tmap(&f.tmx, b->pads[2 * i].p, kF32, Pf, W + 2, H + 2),
+                   "batch_create: tensor map");
+    MEXCT_TRY_CUDA(make_slab_tmap(&f.tmy, b->pads[2 * i + 1].p, kF32, Pf, W + 2, H + 2),
+                   "batch_create: tensor map");
+    f.W = W;
+    f.H = H;
+    f.geom = p.geom;
+    f.nviews = p.nP;
+    f.Pf = Pf;
+    f.tiles_u = (W + 31) / 32;
+    f.u0 = float(W - 1) / 2;  // CUDAmex_FP.cu:378-379
+    f.v0 = float(H - 1) / 2;
+    f.bx = -(float)W / 2.0f;  // :424-426
+    f.by = -(float)W / 2.0f;
+    f.bz = -(float)H / 2.0f;
+    f.sad = p.sad;
+    f.step = p.geom == 2 ? 1.0f : 0.5f;
+    f.item0 = b->fp_items;
+    b->fp_items += (long long)p.nP * f.tiles_u * ((H + 7) / 8);
+    f.px = b->pads[2 * i].p;
+    f.py = b->pads[2 * i + 1].p;
+    f.out = p.d_sino;
+    f.trig = dtrig + toff;
+    f.vol = p.d_vol;
+    f.pad_item0 = b->pad_items;
+    const long long nt = (Pf + 31) / 32;
+    b->pad_items += nt * nt * (H + 2);
+    BatchBp& g = bd[i];
+    std::memset(&g, 0, sizeof g);
+    g.W = W;
+    g.H = H;
+    g.geom = p.geom;
+    g.nviews = p.nP;
+    g.bx = (W + 31) / 32;
+    g.by = (W + 7) / 8;
+    g.bz = (H + bp_brick_z() - 1) / bp_brick_z();
+    g.v0 = float(H - 1) / 2;   // CUDAmex_BP.cu:249
+    g.sad = p.sad;
+    g.hw = (uint32_t)W / 2u - 1u;  // :73
+    g.item0 = b->bp_items;
+    b->bp_items += (long long)g.bx * g.by * g.bz;
+    g.sino = p.d_sino;
+    g.vol = p.d_rec;
+    g.trig = dtrig + toff;
+    toff += p.nP;
+  }
+  MEXCT_TRY_CUDA(b->fp_desc.ensure(n * sizeof(BatchFp)), "batch_create: descriptors");
+  MEXCT_TRY_CUDA(b->bp_desc.ensure(n * sizeof(BatchBp)), "batch_create: descriptors");
+  MEXCT_TRY_CUDA(b->counters.ensure(64), "batch_create: counters");
+  MEXCT_TRY_CUDA(b->err.ensure(64), "batch_create: error word");
+  MEXCT_TRY_CUDA(cudaMemcpy(b->trig.p, trig.data(), ntrig * sizeof(Trig), cudaMemcpyHostToDevice),
+                 "batch_create: upload");
+  MEXCT_TRY_CUDA(cudaMemcpy(b->fp_desc.p, fd.data(), n * sizeof(BatchFp), cudaMemcpyHostToDevice),
+                 "batch_create: upload");
+  MEXCT_TRY_CUDA(cudaMemcpy(b->bp_desc.p, bd.data(), n * sizeof(BatchBp), cudaMemcpyHostToDevice),
+                 "batch_create: upload");
+  MEXCT_TRY_CUDA(cudaMemset(b->err.p, 0, 64), "batch_create: error word");
+  *out = b.release();
+  return MEXCT_OK;
+}
+
+mexct_status mexct_batch_fp(mexct_batch* b, void* stream) {
+  if (!b) return set_err(MEXCT_ERR_ARG, "batch_fp: NULL batch");
+  DevGuard dg(b->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MEXCT_TRY_CUDA(launch_pad_batch(b->fp_desc.as<BatchFp>(), b->n, b->pad_items, st),
+                 "batch_fp: padding");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(b->counters.p, 0, sizeof(unsigned long long), st),
+                 "batch_fp: counter");
+  MEXCT_TRY_CUDA(launch_fp_batch(b->fp_desc.as<BatchFp>(), b->n, b->fp_items,
+                                 b->counters.as<unsigned long long>(), b->err.as<unsigned>(),
+                                 b->sms * 3, st),
+                 "batch_fp: launch");
+  return MEXCT_OK;
+}
+
+mexct_status mexct_batch_bp(mexct_batch* b, void* stream) {
+  if (!b) return set_err(MEXCT_ERR_ARG, "batch_bp: NULL batch");
+  DevGuard dg(b->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned long long* ctr = b->counters.as<unsigned long long>() + 1;
+  MEXCT_TRY_CUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st), "batch_bp: counter");
+  MEXCT_TRY_CUDA(launch_bp_batch(b->bp_desc.as<BatchBp>(), b->n, b->bp_items, ctr, b->sms * 4, st),
+                 "batch_bp: launch");
+  return MEXCT_OK;
+}
+
+mexct_status mexct_batch_destroy(mexct_batch* b) {
+  if (!b) return MEXCT_OK;
+  DevGuard dg(b->device);
+  delete b;
+  return MEXCT_OK;
+}
+
+}  // extern "C"

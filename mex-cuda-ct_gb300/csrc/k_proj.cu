@@ -593,16 +593,24 @@ struct SmFoot {
   int u0, v0, fb;
 };
 
+// Geometry of one brick job.
+struct BrickJob {
+  int W, H, nviews, view0;
+  float v0, SR;
+  uint32_t hw;
+  long long P;
+  const Trig* trig;
+  int bx0, by0, z0;
+};
+
 template <int GEOM, typename TS, typename TV>
-__global__ void __launch_bounds__(256, 2) bp_smem_kernel(
-    const __grid_constant__ VoxArgs A, const TS* __restrict__ sino,
-    TV* __restrict__ vol, int accumulate) {
-  extern __shared__ float stage[];  // kSmVb * kSmView floats
-  __shared__ SmFoot foot[kSmVb];
+__device__ __forceinline__ void bp_brick(const BrickJob& A, const TS* __restrict__ sino,
+                                         TV* __restrict__ vol, int accumulate, float* stage,
+                                         SmFoot* foot) {
   const int tid = threadIdx.x + 32 * threadIdx.y;
-  const int bx0 = blockIdx.x * 32, by0 = blockIdx.y * 8;
+  const int bx0 = A.bx0, by0 = A.by0;
   const int ix = bx0 + threadIdx.x, iy = by0 + threadIdx.y;
-  const int z0 = blockIdx.z * kSmZc;
+  const int z0 = A.z0;
   const bool live = ix < A.W && iy < A.W && in_circle(ix, iy, A.hw);
   float acc[kSmZc];
 #pragma unroll
@@ -706,16 +714,92 @@ __global__ void __launch_bounds__(256, 2) bp_smem_kernel(
     }
     __syncthreads();
   }
+  if (ix < A.W && iy < A.W) {
+    const size_t base = (size_t)iy * A.W + ix;
+    const size_t sz = (size_t)A.W * A.W;
+#pragma unroll
+    for (int j = 0; j < kSmZc; ++j) {
+      if (z0 + j < A.H) {
+        TV* o = vol + base + (size_t)(z0 + j) * sz;
+        stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
+      }
+    }
+  }
+}
+
+template <int GEOM, typename TS, typename TV>
+__global__ void __launch_bounds__(256, 2) bp_smem_kernel(
+    const __grid_constant__ VoxArgs A, const TS* __restrict__ sino,
+    TV* __restrict__ vol, int accumulate) {
+  extern __shared__ float stage[];  // kSmVb * kSmView floats
+  __shared__ SmFoot foot[kSmVb];
+  BrickJob J{A.W, A.H, A.nviews, A.view0, A.v0, A.SR, A.hw, A.P, A.trig,
+             (int)blockIdx.x * 32, (int)blockIdx.y * 8, (int)blockIdx.z * kSmZc};
+  bp_brick<GEOM, TS, TV>(J, sino, vol, accumulate, stage, foot);
+}
+
+// One 32 x 8 x kSmZc brick through L1 (the body of bp_kernel with the view
+// geometry read from a device table): the batched BP computes exactly what the
+// single-problem BP computes.
+template <int GEOM>
+__device__ __forceinline__ void bp_l1_brick(const BrickJob& A, const float* __restrict__ sino,
+                                            float* __restrict__ vol) {
+  const int ix = A.bx0 + threadIdx.x, iy = A.by0 + threadIdx.y, z0 = A.z0;
   if (ix >= A.W || iy >= A.W) return;
+  float acc[kSmZc];
+#pragma unroll
+  for (int j = 0; j < kSmZc; ++j) acc[j] = 0.f;
+  if (in_circle(ix, iy, A.hw)) {
+    const float x = (float)ix - ((float)A.hw + 0.5f);
+    const float y = (float)iy - ((float)A.hw + 0.5f);
+    for (int v = 0; v < A.nviews; ++v) {
+      const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
+      bp_column<GEOM, false, kSmZc>(sino + (size_t)(A.view0 + v) * A.P, A.W, A.H, z0, g, acc);
+    }
+  }
   const size_t base = (size_t)iy * A.W + ix;
   const size_t sz = (size_t)A.W * A.W;
 #pragma unroll
-  for (int j = 0; j < kSmZc; ++j) {
-    if (z0 + j < A.H) {
-      TV* o = vol + base + (size_t)(z0 + j) * sz;
-      stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
+  for (int j = 0; j < kSmZc; ++j)
+    if (z0 + j < A.H) vol[base + (size_t)(z0 + j) * sz] = acc[j];
+}
+
+// Batched BP: persistent CTAs take (problem, brick) items from a counter.
+__global__ void __launch_bounds__(256) bp_batch_kernel(
+    const BatchBp* __restrict__ probs, int nprob, long long total,
+    unsigned long long* __restrict__ counter) {
+  __shared__ long long s_item;
+  for (;;) {
+    if (threadIdx.x + 32 * threadIdx.y == 0) s_item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= total) break;
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].item0 <= item) lo = mid;
+      else hi = mid - 1;
     }
+    const BatchBp& B = probs[lo];
+    const long long rr = item - B.item0;
+    const int bxi = (int)(rr % B.bx), byi = (int)((rr / B.bx) % B.by), bzi = (int)(rr / ((long long)B.bx * B.by));
+    BrickJob J{B.W, B.H, B.nviews, 0, B.v0, B.sad, B.hw, (long long)B.W * B.H, B.trig,
+               bxi * 32, byi * 8, bzi * kSmZc};
+    if (B.geom == 0) bp_l1_brick<0>(J, (const float*)B.sino, (float*)B.vol);
+    else if (B.geom == 1) bp_l1_brick<1>(J, (const float*)B.sino, (float*)B.vol);
+    else bp_l1_brick<2>(J, (const float*)B.sino, (float*)B.vol);
+    __syncthreads();  // s_item is rewritten by thread 0 at the top of the loop
   }
+}
+
+int bp_brick_z() { return kSmZc; }
+
+cudaError_t launch_bp_batch(const BatchBp* d_probs, int nprob, long long total,
+                            unsigned long long* counter, int ctas, cudaStream_t st) {
+  if (total <= 0) return cudaSuccess;
+  bp_batch_kernel<<<ctas, dim3(32, 8), 0, st>>>(d_probs, nprob, total, counter);
+  return cudaGetLastError();
 }
 
 template <int GEOM, typename TS, typename TV>

@@ -77,6 +77,56 @@ __global__ void __launch_bounds__(256) pad_transpose_kernel(
   }
 }
 
+// Batched padding: one CTA per (problem, padded z slice, 32 x 32 tile) writes
+// both padded layouts of the tile (clamp addressing).
+__global__ void __launch_bounds__(256) pad_batch_kernel(const BatchFp* __restrict__ probs,
+                                                        int nprob, long long total) {
+  __shared__ float tile[32][33];
+  const long long item = blockIdx.x;
+  if (item >= total) return;
+  int lo = 0, hi = nprob - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].pad_item0 <= item) lo = mid;
+    else hi = mid - 1;
+  }
+  const BatchFp& B = probs[lo];
+  const int W = B.W, H = B.H, Pf = B.Pf, Ps = W + 2;
+  const int nt = (Pf + 31) / 32;
+  const long long r = item - B.pad_item0;
+  const int zp = (int)(r / ((long long)nt * nt));
+  const int t = (int)(r % ((long long)nt * nt));
+  const int x0 = (t % nt) * 32, y0 = (t / nt) * 32;
+  const float* src = static_cast<const float*>(B.vol);
+  float* px = static_cast<float*>(const_cast<void*>(B.px));
+  float* py = static_cast<float*>(const_cast<void*>(B.py));
+  const size_t zoff = (size_t)zp * Pf * Ps;
+  const int z = min(max(zp - 1, 0), H - 1);
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int xp = x0 + threadIdx.x, yp = y0 + j;
+    float v = 0.f;
+    if (xp < Ps && yp < Ps) {
+      const int x = min(max(xp - 1, 0), W - 1), y = min(max(yp - 1, 0), W - 1);
+      v = __ldg(src + (size_t)x + (size_t)W * ((size_t)y + (size_t)W * z));
+    }
+    tile[j][threadIdx.x] = v;
+    if (xp < Pf && yp < Ps) px[zoff + (size_t)yp * Pf + xp] = v;
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int yp = y0 + threadIdx.x, xp = x0 + j;
+    if (yp < Pf && xp < Ps) py[zoff + (size_t)xp * Pf + yp] = tile[threadIdx.x][j];
+  }
+}
+
+cudaError_t launch_pad_batch(const BatchFp* d_probs, int nprob, long long total,
+                             cudaStream_t st) {
+  if (total <= 0) return cudaSuccess;
+  if (total > 0x7fffffffLL) return cudaErrorInvalidValue;
+  pad_batch_kernel<<<(unsigned)total, dim3(32, 8), 0, st>>>(d_probs, nprob, total);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
                               bool border, void* px, void* py, cudaStream_t st) {
   const int Ps = W + 2, Pz = H + 2;
@@ -188,52 +238,72 @@ __device__ __forceinline__ float sample_at(const T* base, int sa, int sz, float 
   return fmaf(wz, s1 - s0, s0);
 }
 
-template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
-__global__ void __launch_bounds__(256, 3) fp_slab_kernel(
-    const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
-    const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
-    const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  TV* buf0 = reinterpret_cast<TV*>(smem_raw);
-  TV* buf1 = buf0 + kBufElems;
-  __shared__ __align__(8) uint64_t bar[2];
-  __shared__ SlabPlan plan[2];
-  __shared__ float corner[4][6];
-  __shared__ int s_amin, s_amax, s_pos, s_neg, s_nslab;
+// Geometry of one slab job: a 32 x 8 detector tile of one view.
+struct SlabJob {
+  int det_w, det_h, S, Z, Pf;
+  float u0, v0, bx, by, bz, SR, RD, step;
+  Trig tr;
+  long long P;      // detector pixels per view
+  long long gview;  // sinogram / pre / post slot of the view
+  long long lview;  // residual slot (OSC epilogue)
+  int tu0, tv0;     // tile origin on the detector
+  const CUtensorMap* tmx;
+  const CUtensorMap* tmy;
+  const void* px;
+  const void* py;
+  void* out;
+};
 
+struct SlabShared {
+  uint64_t bar[2];
+  SlabPlan plan[2];
+  float corner[4][6];
+  int amin, amax, pos, neg;
+  long long item;
+};
+
+__device__ __forceinline__ void slab_init_barriers(SlabShared& S) {
+  if (threadIdx.x + 32 * threadIdx.y == 0) {
+    mbar_init(&S.bar[0], 1);
+    mbar_init(&S.bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+// One tile: sweep the volume along the view's dominant axis slab by slab.
+// Ends with a CTA barrier, so the shared state can be reused by the next job.
+template <int GEOM, int EPI, typename TV, typename TO>
+__device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, SlabShared& S,
+                                          uint32_t* phase, const SlabEpi& E) {
   constexpr bool Z2 = (GEOM == 2);  // par/fan rays sample exact z texel rows
   const int tid = threadIdx.x + 32 * threadIdx.y;
-  const int view = blockIdx.x;
-  const int tiles_u = (A.det_w + 31) >> 5;
-  const int u0 = (blockIdx.y % tiles_u) * 32, v0 = (blockIdx.y / tiles_u) * 8;
+  const int u0 = J.tu0, v0 = J.tv0;
   const int ix = u0 + threadIdx.x, iy = v0 + threadIdx.y;
-  const bool valid = ix < A.det_w && iy < A.det_h;
-  const Trig tr = A.trig[view];
+  const bool valid = ix < J.det_w && iy < J.det_h;
+  const Trig tr = J.tr;
   const bool xdom = fabsf(tr.c) >= fabsf(tr.s);  // rays run mostly along x
-  const int Ps = A.S + 2, Pz = A.Z + 2;
+  const int Ps = J.S + 2, Pz = J.Z + 2, Pf = J.Pf;
 
   float s[3], e[3];
-  std_ray<GEOM < 3 ? GEOM : 2>(min(ix, A.det_w - 1), min(iy, A.det_h - 1), A.u0, A.v0, tr.s,
-                               tr.c, A.SR, A.RD, s, e);
-  const Ray r = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], A.bx, A.by, A.bz, A.step);
+  std_ray<GEOM>(min(ix, J.det_w - 1), min(iy, J.det_h - 1), J.u0, J.v0, tr.s, tr.c, J.SR, J.RD,
+                s, e);
+  const Ray r = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], J.bx, J.by, J.bz, J.step);
   // Tap space: padded texture coordinate minus 0.5, i.e. world - b + 0.5.
-  const float ca = xdom ? r.cx - A.bx : r.cy - A.by;
-  const float cf = xdom ? r.cy - A.by : r.cx - A.bx;
-  const float ta0 = ca + 0.5f, tf0 = cf + 0.5f, tz0 = (r.cz - A.bz) + 0.5f;
+  const float ca = xdom ? r.cx - J.bx : r.cy - J.by;
+  const float cf = xdom ? r.cy - J.by : r.cx - J.bx;
+  const float ta0 = ca + 0.5f, tf0 = cf + 0.5f, tz0 = (r.cz - J.bz) + 0.5f;
   const float da = xdom ? r.dx : r.dy, df = xdom ? r.dy : r.dx, dz = r.dz;
   const int n = valid ? r.n : 0;
 
   if (tid == 0) {
-    s_amin = 0x7fffffff;
-    s_amax = -0x7fffffff;
-    s_pos = 0;
-    s_neg = 0;
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    S.amin = 0x7fffffff;
+    S.amax = -0x7fffffff;
+    S.pos = 0;
+    S.neg = 0;
   }
   // Corner rays of the valid part of the tile bound the bundle.
-  const int lx = min(31, A.det_w - 1 - u0), ly = min(7, A.det_h - 1 - v0);
+  const int lx = min(31, J.det_w - 1 - u0), ly = min(7, J.det_h - 1 - v0);
   const int cid = (threadIdx.x == 0 && threadIdx.y == 0)     ? 0
                   : (threadIdx.x == lx && threadIdx.y == 0)  ? 1
                   : (threadIdx.x == 0 && threadIdx.y == ly)  ? 2
@@ -241,27 +311,30 @@ __global__ void __launch_bounds__(256, 3) fp_slab_kernel(
                                                              : -1;
   __syncthreads();
   if (cid >= 0) {
-    corner[cid][0] = s[0]; corner[cid][1] = s[1]; corner[cid][2] = s[2];
-    corner[cid][3] = e[0]; corner[cid][4] = e[1]; corner[cid][5] = e[2];
+    S.corner[cid][0] = s[0]; S.corner[cid][1] = s[1]; S.corner[cid][2] = s[2];
+    S.corner[cid][3] = e[0]; S.corner[cid][4] = e[1]; S.corner[cid][5] = e[2];
   }
   if (n > 0) {
     const int t_first = __float2int_rd(ta0);
     const int t_last = __float2int_rd(fmaf((float)(n - 1), da, ta0));
-    atomicMin(&s_amin, min(t_first, t_last));
-    atomicMax(&s_amax, max(t_first, t_last));
-    if (da > 0.f) atomicAdd(&s_pos, 1);
-    else atomicAdd(&s_neg, 1);
+    atomicMin(&S.amin, min(t_first, t_last));
+    atomicMax(&S.amax, max(t_first, t_last));
+    if (da > 0.f) atomicAdd(&S.pos, 1);
+    else atomicAdd(&S.neg, 1);
   }
   __syncthreads();
+  const int s_amin = S.amin, s_amax = S.amax;
   const bool any = s_amax >= s_amin;
-  const int dir = s_neg == 0 ? 1 : -1;
-  const bool mixed = s_pos > 0 && s_neg > 0;
+  const int dir = S.neg == 0 ? 1 : -1;
+  const bool mixed = S.pos > 0 && S.neg > 0;
   const int nslab = any ? (s_amax - s_amin) / kSlabT + 1 : 0;
-  const TV* gv = xdom ? py : px;            // padded layout with f fastest
-  const CUtensorMap* tm = xdom ? &tmy : &tmx;
-  const float bfw = xdom ? A.by : A.bx;     // world offset of the f axis
-  const float baw = xdom ? A.bx : A.by;     // world offset of the a axis
-
+  const TV* gv = static_cast<const TV*>(xdom ? J.py : J.px);  // f-fastest padded layout
+  const CUtensorMap* tm = xdom ? J.tmy : J.tmx;
+  const float bfw = xdom ? J.by : J.bx;     // world offset of the f axis
+  const float baw = xdom ? J.bx : J.by;     // world offset of the a axis
+  auto& corner = S.corner;
+  auto& plan = S.plan;
+  uint64_t* bar = S.bar;
   // Plan slab j into slot j&1 and start its copy.  Called by all of warp 0:
   // lanes 0-7 evaluate the 4 corner rays at the 2 ends of the slab in FP32
   // (error ~1e-4 voxel, covered by the 1-voxel margin), lane 0 issues the TMA.
@@ -305,8 +378,8 @@ __global__ void __launch_bounds__(256, 3) fp_slab_kernel(
     const int align = sizeof(TV) == 4 ? 4 : 8;
     const float flo = floorf(fmn - bfw + 0.5f) - 1.0f;
     const float fhi = floorf(fmx - bfw + 0.5f) + 2.0f;
-    const float zlo = floorf(zmn - A.bz + 0.5f) - 1.0f;
-    const float zhi = floorf(zmx - A.bz + 0.5f) + 2.0f;
+    const float zlo = floorf(zmn - J.bz + 0.5f) - 1.0f;
+    const float zhi = floorf(zmx - J.bz + 0.5f) + 2.0f;
     bool fits = isfinite(flo) && isfinite(fhi) && isfinite(zlo) && isfinite(zhi) && !mixed &&
                 fhi >= 0.f && zhi >= 0.f && flo <= (float)(Pf - 1) && zlo <= (float)(Pz - 1);
     int f0 = 0, z0 = 0, nzr = 0;
@@ -338,7 +411,6 @@ __global__ void __launch_bounds__(256, 3) fp_slab_kernel(
 
   float acc0 = 0.f, acc1 = 0.f;
   int k = 0;
-  uint32_t phase[2] = {0u, 0u};
   for (int j = 0; j < nslab; ++j) {
     if (threadIdx.y == 0 && j + 1 < nslab) plan_and_issue(j + 1);
     const SlabPlan p = plan[j & 1];
@@ -398,18 +470,95 @@ __global__ void __launch_bounds__(256, 3) fp_slab_kernel(
     }
     __syncthreads();
   }
-  if (!valid) return;
-  const float l = (acc0 + acc1) * A.step;
-  const size_t pix = (size_t)iy * A.det_w + ix;
-  const size_t gi = (size_t)(A.view0 + view * A.vstride) * A.P + pix;
-  if (EPI == 0) {
-    stf(out + gi, l);
-  } else {
-    // CUDAmex_oscIter.cu:262-268: pre' = pre e^-l - post, post' = pre e^-l l.
-    const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
-    const float ehat = pv * expf(-l);
-    E.rpre[(size_t)view * A.P + pix] = ehat - qv;
-    E.rpost[(size_t)view * A.P + pix] = ehat * l;
+  if (valid) {
+    const float l = (acc0 + acc1) * J.step;
+    const size_t pix = (size_t)iy * J.det_w + ix;
+    const size_t gi = (size_t)J.gview * J.P + pix;
+    if (EPI == 0) {
+      stf(static_cast<TO*>(J.out) + gi, l);
+    } else {
+      // CUDAmex_oscIter.cu:262-268: pre' = pre e^-l - post, post' = pre e^-l l.
+      const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
+      const float ehat = pv * expf(-l);
+      E.rpre[(size_t)J.lview * J.P + pix] = ehat - qv;
+      E.rpost[(size_t)J.lview * J.P + pix] = ehat * l;
+    }
+  }
+  __syncthreads();
+}
+
+template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
+__global__ void __launch_bounds__(256, 3) fp_slab_kernel(
+    const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
+    const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
+    const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ SlabShared S;
+  TV* buf0 = reinterpret_cast<TV*>(smem_raw);
+  TV* buf1 = buf0 + kBufElems;
+  slab_init_barriers(S);
+  uint32_t phase[2] = {0u, 0u};
+  const int view = blockIdx.x;
+  const int tiles_u = (A.det_w + 31) >> 5;
+  SlabJob J;
+  J.det_w = A.det_w; J.det_h = A.det_h; J.S = A.S; J.Z = A.Z; J.Pf = Pf;
+  J.u0 = A.u0; J.v0 = A.v0; J.bx = A.bx; J.by = A.by; J.bz = A.bz;
+  J.SR = A.SR; J.RD = A.RD; J.step = A.step;
+  J.tr = A.trig[view];
+  J.P = A.P;
+  J.gview = A.view0 + (long long)view * A.vstride;
+  J.lview = view;
+  J.tu0 = (blockIdx.y % tiles_u) * 32;
+  J.tv0 = (blockIdx.y / tiles_u) * 8;
+  J.tmx = &tmx; J.tmy = &tmy; J.px = px; J.py = py; J.out = out;
+  slab_tile<GEOM, EPI, TV, TO>(J, buf0, buf1, S, phase, E);
+}
+
+// ---------------------------------------------------------------------------
+// Batched FP over many problems of different sizes and geometries in one
+// persistent launch: CTAs take (problem, view, tile) items from a global
+// counter (work stealing) and run the same tile code as above.
+// ---------------------------------------------------------------------------
+template <typename TV>
+__global__ void __launch_bounds__(256, 3) fp_batch_kernel(
+    const BatchFp* __restrict__ probs, int nprob, long long total,
+    unsigned long long* __restrict__ counter, unsigned* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ SlabShared S;
+  TV* buf0 = reinterpret_cast<TV*>(smem_raw);
+  TV* buf1 = buf0 + kBufElems;
+  slab_init_barriers(S);
+  uint32_t phase[2] = {0u, 0u};
+  const SlabEpi E{nullptr, nullptr, nullptr, nullptr, err};
+  for (;;) {
+    if (threadIdx.x + 32 * threadIdx.y == 0) S.item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const long long item = S.item;
+    if (item >= total) break;
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].item0 <= item) lo = mid;
+      else hi = mid - 1;
+    }
+    const BatchFp& B = probs[lo];
+    const long long rr = item - B.item0;
+    const int view = (int)(rr % B.nviews);
+    const int tile = (int)(rr / B.nviews);
+    SlabJob J;
+    J.det_w = B.W; J.det_h = B.H; J.S = B.W; J.Z = B.H; J.Pf = B.Pf;
+    J.u0 = B.u0; J.v0 = B.v0; J.bx = B.bx; J.by = B.by; J.bz = B.bz;
+    J.SR = B.sad; J.RD = B.sad; J.step = B.step;
+    J.tr = B.trig[view];
+    J.P = (long long)B.W * B.H;
+    J.gview = view;
+    J.lview = view;
+    J.tu0 = (tile % B.tiles_u) * 32;
+    J.tv0 = (tile / B.tiles_u) * 8;
+    J.tmx = &B.tmx; J.tmy = &B.tmy; J.px = B.px; J.py = B.py; J.out = B.out;
+    if (B.geom == 0) slab_tile<0, 0, TV, TV>(J, buf0, buf1, S, phase, E);
+    else if (B.geom == 1) slab_tile<1, 0, TV, TV>(J, buf0, buf1, S, phase, E);
+    else slab_tile<2, 0, TV, TV>(J, buf0, buf1, S, phase, E);
   }
 }
 
@@ -448,6 +597,22 @@ cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype, int Pf
 }
 
 int slab_pitch(int W) { return ((W + 2 + 7) / 8) * 8; }
+
+cudaError_t launch_fp_batch(const BatchFp* d_probs, int nprob, long long total,
+                            unsigned long long* counter, unsigned* err, int ctas,
+                            cudaStream_t st) {
+  if (total <= 0) return cudaSuccess;
+  auto k = fp_batch_kernel<float>;
+  const size_t smem = 2 * (size_t)kBufElems * sizeof(float) + 128;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  k<<<ctas, dim3(32, 8), smem, st>>>(d_probs, nprob, total, counter, err);
+  return cudaGetLastError();
+}
 
 template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
 static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtensorMap& my,

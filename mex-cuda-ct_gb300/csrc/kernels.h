@@ -56,6 +56,40 @@ struct SlabEpi {
   unsigned* err;     // set to non-zero when a bounded wait gave up
 };
 int slab_pitch(int W);
+
+// One problem of a batched FP launch (device-resident descriptor).
+struct alignas(64) BatchFp {
+  CUtensorMap tmx, tmy;       // over the problem's padded volumes
+  int W, H, geom, nviews, Pf, tiles_u;
+  float u0, v0, bx, by, bz, sad, step;
+  long long item0;            // first work item: nviews * tiles items follow
+  const void* px;
+  const void* py;
+  void* out;                  // sinogram (nviews, H, W)
+  const Trig* trig;           // nviews entries (device)
+  const void* vol;            // source volume (H, W, W) for the padding pass
+  long long pad_item0;        // first padding item: ceil(Pf/32)^2 * (H+2) tiles
+};
+
+// One problem of a batched BP launch.
+struct BatchBp {
+  int W, H, geom, nviews, bx, by, bz;  // bx/by/bz: bricks per axis
+  float v0, sad;
+  uint32_t hw;
+  long long item0;            // first work item: bx * by * bz bricks follow
+  const void* sino;
+  void* vol;
+  const Trig* trig;
+};
+
+cudaError_t launch_fp_batch(const BatchFp* d_probs, int nprob, long long total,
+                            unsigned long long* counter, unsigned* err, int ctas,
+                            cudaStream_t st);
+cudaError_t launch_pad_batch(const BatchFp* d_probs, int nprob, long long total,
+                             cudaStream_t st);
+cudaError_t launch_bp_batch(const BatchBp* d_probs, int nprob, long long total,
+                            unsigned long long* counter, int ctas, cudaStream_t st);
+int bp_brick_z();
 cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
                               bool border, void* px, void* py, cudaStream_t st);
 cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype,

@@ -30,7 +30,7 @@ cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
 mexct_status upload(Buf& b, const void* src, size_t bytes, cudaStream_t st,
                     const char* what) {
-  MEXCT_TRY_CUDA(b.ensure(bytes), what);
+  MEXCT_TRY_CUDA(b.ensure_async(bytes, st), what);
   if (bytes) MEXCT_TRY_CUDA(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, st), what);
   return MEXCT_OK;
 }
@@ -192,7 +192,7 @@ mexct_status bp_dev_impl(mexct_ctx* c, const void* d_sino, int stype, int W,
     a->nviews = std::min(kMaxViews, nP - v0);
     a->view0 = v0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-    MEXCT_TRY_CUDA(launch_bp_smem(geom, *a, d_sino, stype, d_vol, vt, v0 > 0, st), "bp: launch");
+    MEXCT_TRY_CUDA(launch_bp(geom, *a, d_sino, stype, d_vol, vt, v0 > 0, st), "bp: launch");
   }
   return MEXCT_OK;
 }
@@ -545,7 +545,7 @@ mexct_status mexct_fp(mexct_ctx* ctx, const float* vol, int W, int H,
   const size_t N = (size_t)W * W * H, M = (size_t)W * H * nP;
   mexct_status s = upload(c->in, vol, N * 4, c->stream, "fp: upload");
   if (s) return s;
-  MEXCT_TRY_CUDA(c->out.ensure(M * 4), "fp: workspace");
+  MEXCT_TRY_CUDA(c->out.ensure_async(M * 4, c->stream), "fp: workspace");
   s = fp_dev_impl(c, c->in.p, kF32, W, H, sad, angles, nP, geom, c->out.p, kF32,
                   MEXCT_FP_EXPLICIT, c->stream);
   if (s) return s;
@@ -580,7 +580,7 @@ mexct_status mexct_bp(mexct_ctx* ctx, const float* sino, int W, int H, int nP,
   const size_t N = (size_t)W * W * H, M = (size_t)W * H * nP;
   mexct_status s = upload(c->in, sino, M * 4, c->stream, "bp: upload");
   if (s) return s;
-  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "bp: workspace");
+  MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "bp: workspace");
   s = bp_dev_impl(c, c->in.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, c->stream);
   if (s) return s;
   return finish(c, vol, c->out, N * 4, "bp: download");
@@ -608,7 +608,7 @@ mexct_status mexct_g3d_fp(mexct_ctx* ctx, const float* vol, int S, int Z,
   if (s) return s;
   s = upload(c->in2, pts, npts * 4, c->stream, "g3d_fp: upload");
   if (s) return s;
-  MEXCT_TRY_CUDA(c->out.ensure(M * 4), "g3d_fp: workspace");
+  MEXCT_TRY_CUDA(c->out.ensure_async(M * 4, c->stream), "g3d_fp: workspace");
   s = g3d_fp_dev_impl(c, c->in.as<float>(), S, Z, angles, c->in2.as<float>(), W, H, nP,
                       per_view, c->out.as<float>(), c->stream);
   if (s) return s;
@@ -637,7 +637,7 @@ mexct_status mexct_g3d_bp(mexct_ctx* ctx, const float* sino, int W, int H,
   if (s) return s;
   s = upload(c->in2, pts, npts * 4, c->stream, "g3d_bp: upload");
   if (s) return s;
-  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "g3d_bp: workspace");
+  MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "g3d_bp: workspace");
   s = g3d_bp_dev_impl(c, c->in.as<float>(), W, H, nP, angles, c->in2.as<float>(), per_view,
                       S, Z, c->out.as<float>(), c->stream);
   if (s) return s;
@@ -691,7 +691,7 @@ mexct_status mexct_tvmin3d(mexct_ctx* ctx, const float* vol, int Nx, int Ny,
   const size_t N = (size_t)Nx * Ny * Nz;
   mexct_status s = upload(c->in, vol, N * 4, c->stream, "tvmin3d: upload");
   if (s) return s;
-  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "tvmin3d: workspace");
+  MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "tvmin3d: workspace");
   s = tv_dev_impl(c, c->in.p, kF32, Nx, Ny, Nz, cval, n_steps, c->out.p, c->stream);
   if (s) return s;
   return finish(c, out, c->out, N * 4, "tvmin3d: download");
@@ -723,7 +723,7 @@ mexct_status mexct_prefilter(mexct_ctx* ctx, const float* sino,
     s = upload(c->in2, pre, M * 4, c->stream, "prefilter: upload");
     if (s) return s;
   }
-  MEXCT_TRY_CUDA(c->out.ensure(M * 4), "prefilter: workspace");
+  MEXCT_TRY_CUDA(c->out.ensure_async(M * 4, c->stream), "prefilter: workspace");
   s = prefilter_dev_impl(c, c->in.as<float>(), pre ? c->in2.as<float>() : nullptr, W, H, nP,
                          angles, geom, sad, filter, cutoff, q, c->out.as<float>(), c->stream);
   if (s) return s;
@@ -743,8 +743,8 @@ mexct_status mexct_fbp(mexct_ctx* ctx, const float* pre, const float* post,
   if (s) return s;
   s = upload(c->in2, pre, M * 4, c->stream, "fbp: upload");
   if (s) return s;
-  MEXCT_TRY_CUDA(c->in3.ensure(M * 4), "fbp: workspace");
-  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "fbp: workspace");
+  MEXCT_TRY_CUDA(c->in3.ensure_async(M * 4, c->stream), "fbp: workspace");
+  MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "fbp: workspace");
   s = prefilter_dev_impl(c, c->in.as<float>(), c->in2.as<float>(), W, H, nP, angles, geom, sad,
                          filter, cutoff, q, c->in3.as<float>(), c->stream);
   if (s) return s;

@@ -56,11 +56,11 @@ struct mexct_osctv {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   ~mexct_osctv() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    for (Buf* b : {&mu, &mu_old, &pre, &post, &padx, &pady, &err, &r1, &r2, &tvbuf, &red, &cnt, &scal})
+      b->release();  // stream-ordered on `own`, after all its work
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
     if (own) cudaStreamDestroy(own);
-    for (Buf* b : {&mu, &mu_old, &pre, &post, &padx, &pady, &err, &r1, &r2, &tvbuf, &red, &cnt, &scal})
-      b->release();
   }
   size_t N() const { return (size_t)W * W * H; }
   size_t M() const { return (size_t)W * H * nP; }
@@ -215,24 +215,30 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   const size_t maxv = (size_t)nP;  // a subset holds at most nP views
   if (maxv > (size_t)kMaxViews)
     return set_err(MEXCT_ERR_UNSUPPORTED, "osctv_create: %d views (max %d)", nP, kMaxViews);
-  MEXCT_TRY_CUDA(s->mu.ensure(vb), "osctv_create: mu");
-  MEXCT_TRY_CUDA(s->mu_old.ensure(vb), "osctv_create: mu_old");
+  // Buffers are allocated stream-ordered on the solver's stream, so creating
+  // and destroying solvers never synchronises the device (other streams keep
+  // running); the caller's stream waits for the allocations.
+  cudaStream_t a = s->own;
   const size_t pb = (size_t)slab_pitch(W) * (W + 2) * (H + 2) * dsize(mu_type);
-  MEXCT_TRY_CUDA(s->padx.ensure(pb), "osctv_create: padded mu");
-  MEXCT_TRY_CUDA(s->pady.ensure(pb), "osctv_create: padded mu");
-  MEXCT_TRY_CUDA(s->err.ensure(64), "osctv_create: error word");
-  MEXCT_TRY_CUDA(cudaMemsetAsync(s->err.p, 0, 64, st), "osctv_create: error word");
-  MEXCT_TRY_CUDA(s->tvbuf.ensure(vb), "osctv_create: tv");
-  MEXCT_TRY_CUDA(s->pre.ensure(M * 4), "osctv_create: pre");
-  MEXCT_TRY_CUDA(s->post.ensure(M * 4), "osctv_create: post");
-  MEXCT_TRY_CUDA(s->r1.ensure(P * maxv * 4), "osctv_create: residual");
-  MEXCT_TRY_CUDA(s->r2.ensure(P * maxv * 4), "osctv_create: residual");
   const size_t parts = std::max<size_t>(tv_partials_needed(W, W, H), 152 * 4) + 8;
-  MEXCT_TRY_CUDA(s->red.ensure(parts * sizeof(double)), "osctv_create: reduction");
-  MEXCT_TRY_CUDA(s->cnt.ensure(64), "osctv_create: counter");
-  MEXCT_TRY_CUDA(cudaMemsetAsync(s->cnt.p, 0, 64, st), "osctv_create: counter");
-  MEXCT_TRY_CUDA(s->scal.ensure(64), "osctv_create: scalars");
-  MEXCT_TRY_CUDA(cudaMemsetAsync(s->scal.p, 0, 64, st), "osctv_create: scalars");
+  MEXCT_TRY_CUDA(s->mu.ensure_async(vb, a), "osctv_create: mu");
+  MEXCT_TRY_CUDA(s->mu_old.ensure_async(vb, a), "osctv_create: mu_old");
+  MEXCT_TRY_CUDA(s->tvbuf.ensure_async(vb, a), "osctv_create: tv");
+  MEXCT_TRY_CUDA(s->padx.ensure_async(pb, a), "osctv_create: padded mu");
+  MEXCT_TRY_CUDA(s->pady.ensure_async(pb, a), "osctv_create: padded mu");
+  MEXCT_TRY_CUDA(s->pre.ensure_async(M * 4, a), "osctv_create: pre");
+  MEXCT_TRY_CUDA(s->post.ensure_async(M * 4, a), "osctv_create: post");
+  MEXCT_TRY_CUDA(s->r1.ensure_async(P * maxv * 4, a), "osctv_create: residual");
+  MEXCT_TRY_CUDA(s->r2.ensure_async(P * maxv * 4, a), "osctv_create: residual");
+  MEXCT_TRY_CUDA(s->red.ensure_async(parts * sizeof(double), a), "osctv_create: reduction");
+  MEXCT_TRY_CUDA(s->err.ensure_async(64, a), "osctv_create: error word");
+  MEXCT_TRY_CUDA(s->cnt.ensure_async(64, a), "osctv_create: counter");
+  MEXCT_TRY_CUDA(s->scal.ensure_async(64, a), "osctv_create: scalars");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->err.p, 0, 64, a), "osctv_create: error word");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->cnt.p, 0, 64, a), "osctv_create: counter");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->scal.p, 0, 64, a), "osctv_create: scalars");
+  MEXCT_TRY_CUDA(cudaEventRecord(s->ev_in, a), "osctv_create: join");
+  MEXCT_TRY_CUDA(cudaStreamWaitEvent(st, s->ev_in, 0), "osctv_create: join");
   // OSC_TV_recon.m:33 mu = 1e-10; :35-37 pre/post clamped to >= 1e-6.
   MEXCT_TRY_CUDA(launch_fill(s->mu.p, mu_type, (long long)N, 1e-10f, st), "osctv_create: mu");
   MEXCT_TRY_CUDA(launch_clamp_copy(d_pre, s->pre.as<float>(), (long long)M, 1e-6f, st),
@@ -394,6 +400,19 @@ mexct_status mexct_osc_tv_recon(mexct_ctx* ctx, const float* pre, const float* p
                                 int H, int nP, const float* angles, float sad, int geom,
                                 int n_iter, float tv_const, int n_sub_init, int n_sub_final,
                                 float p_val, const int32_t* first_picks, float* recon) {
+  return mexct::osc_tv_recon_typed(ctx, pre, post, W, H, nP, angles, sad, geom, n_iter, tv_const,
+                                   n_sub_init, n_sub_final, p_val, first_picks, kF32, recon);
+}
+
+}  // extern "C"
+
+namespace mexct {
+
+// OSC_TV_recon with host arrays on a context's stream, mu stored as mu_type.
+mexct_status osc_tv_recon_typed(mexct_ctx* ctx, const float* pre, const float* post, int W, int H,
+                                int nP, const float* angles, float sad, int geom, int n_iter,
+                                float tv_const, int n_sub_init, int n_sub_final, float p_val,
+                                const int32_t* first_picks, int mu_type, float* recon) {
   if (!pre || !post || !angles || !recon || !first_picks)
     return set_err(MEXCT_ERR_ARG, "osc_tv_recon: NULL pointer");
   if (W <= 0 || H <= 0 || nP <= 0 || n_iter < 1)
@@ -403,16 +422,16 @@ mexct_status mexct_osc_tv_recon(mexct_ctx* ctx, const float* pre, const float* p
   std::lock_guard<std::recursive_mutex> lk(c->mu);
   DevGuard dg(c->device);
   const size_t M = (size_t)W * H * nP, N = (size_t)W * W * H;
-  MEXCT_TRY_CUDA(c->in.ensure(M * 4), "osc_tv_recon: upload");
-  MEXCT_TRY_CUDA(c->in2.ensure(M * 4), "osc_tv_recon: upload");
-  MEXCT_TRY_CUDA(c->out.ensure(N * 4), "osc_tv_recon: workspace");
+  MEXCT_TRY_CUDA(c->in.ensure_async(M * 4, c->stream), "osc_tv_recon: upload");
+  MEXCT_TRY_CUDA(c->in2.ensure_async(M * 4, c->stream), "osc_tv_recon: upload");
+  MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "osc_tv_recon: workspace");
   MEXCT_TRY_CUDA(cudaMemcpyAsync(c->in.p, pre, M * 4, cudaMemcpyHostToDevice, c->stream),
                  "osc_tv_recon: upload");
   MEXCT_TRY_CUDA(cudaMemcpyAsync(c->in2.p, post, M * 4, cudaMemcpyHostToDevice, c->stream),
                  "osc_tv_recon: upload");
   mexct_osctv* s = nullptr;
   mexct_status r = mexct_osctv_create(c, c->in.as<float>(), c->in2.as<float>(), W, H, nP, angles,
-                                      sad, geom, kF32, c->stream, &s);
+                                      sad, geom, mu_type, c->stream, &s);
   if (r) return r;
   mexct_osctv_params p{n_iter, tv_const, n_sub_init, n_sub_final, p_val, 1, 0};
   r = mexct_osctv_run(s, &p, first_picks, n_iter, c->stream);
@@ -426,4 +445,4 @@ mexct_status mexct_osc_tv_recon(mexct_ctx* ctx, const float* pre, const float* p
   return r;
 }
 
-}  // extern "C"
+}  // namespace mexct
