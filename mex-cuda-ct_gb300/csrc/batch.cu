@@ -145,7 +145,7 @@ mexct_status mexct_batch_fp(mexct_batch* b, void* stream) {
                  "batch_fp: counter");
   MEXCT_TRY_CUDA(launch_fp_batch(b->fp_desc.as<BatchFp>(), b->n, b->fp_items,
                                  b->counters.as<unsigned long long>(), b->err.as<unsigned>(),
-                                 b->sms * 3, st),
+                                 b->sms * slab_ctas_per_sm(), st),
                  "batch_fp: launch");
   return MEXCT_OK;
 }

@@ -7,13 +7,17 @@
 // enter the volume through different faces and are spread along the ray
 // direction.  Here a CTA (32 x 8 detector pixels of one view) sweeps the
 // volume along the view's dominant axis a (x or y) in slabs of kSlabT tap
-// planes.  For each slab one thread computes the bounding box of the tile's
-// ray bundle (from the 4 corner rays: the coordinates across a plane are
+// planes.  For each slab warp 0 computes the bounding box of the tile's ray
+// bundle (from the 4 corner rays: the coordinates across a plane are
 // monotone in the detector coordinates), and TMA copies that box from a
 // padded volume into shared memory ([z][a][f] with f fastest); every lane
 // then takes its samples whose a-tap lies in the slab from shared memory
 // with constant-offset loads.  Two buffers and two mbarriers overlap the copy
-// of slab j+1 with the sampling of slab j.
+// of slab j+1 with the sampling of slab j.  Shapes (measured on cone 512^3 x
+// 720): 4 taps per slab, boxes of 64 (f) x 5 (a) x <=20 (z) elements that
+// hold 99.9% of the bundles, 4 CTAs of 256 threads per SM (<=64 registers,
+// 50 KB of buffers each); 5 taps at 3 CTAs/SM and 3 taps at 4 CTAs/SM were
+// 7% and 20% slower.
 //
 // The padded volume has a one-voxel border (replicated edge for clamp
 // addressing, zeros for border addressing) and a fast-axis pitch rounded up
@@ -180,12 +184,17 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// Bounded wait: gives up after ~2^22 polls (seconds), records the failure and
-// reports it to the caller, which then samples the slab from global memory.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
-                                                  unsigned* err) {
+// Bounded wait: gives up after ~2^22 polls (seconds), records the failure in
+// err and in the CTA's abort flag, and reports it to the caller, which then
+// samples the slab from global memory.  Once a CTA has given up, its later
+// waits return at once and no further copies are issued, so a broken pipeline
+// costs one time-out per CTA, not one per slab.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned* err,
+                                                  volatile int* abort) {
+  if (*abort) return false;
   for (int i = 0; i < (1 << 22); ++i)
     if (mbar_try_wait(bar, parity)) return true;
+  *abort = 1;
   if (err) atomicOr(err, 1u);
   return false;
 }
@@ -193,14 +202,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // ---------------------------------------------------------------------------
 // Slab kernel.
 // ---------------------------------------------------------------------------
-constexpr int kSlabT = 5;                     // a-taps per slab
+constexpr int kSlabCtas = 4;                  // resident CTAs per SM (launch bounds)
+constexpr int kSlabT = 4;                     // a-taps per slab
 constexpr int kSlabA = kSlabT + 1;            // a-planes in a box
-constexpr int kBoxF = 96;                     // box extent along f (elements)
+constexpr int kBoxF = 64;                     // box extent along f (elements)
 constexpr int kBoxZ = 2;                      // z rows per TMA box
-constexpr int kBZ = 16;                       // z rows per slab buffer
+constexpr int kBZ = 20;                       // z rows per slab buffer (even)
 constexpr int kPlane = kSlabA * kBoxF;        // elements per z row of a buffer
 constexpr int kBufElems = kBZ * kPlane;       // elements per buffer
 constexpr int kMaxIdx = kBufElems - 1 - (kPlane + kBoxF + 1);
+// A TMA destination in shared memory must be 128-byte aligned: every box and
+// the second buffer start on a multiple of 128 bytes for 2- and 4-byte types.
+static_assert((kBoxZ * kPlane * 2) % 128 == 0, "box size must keep 128-byte alignment");
+static_assert((kBufElems * 2) % 128 == 0, "buffer size must keep 128-byte alignment");
+static_assert(kBZ % kBoxZ == 0, "a buffer holds whole boxes");
 
 struct SlabPlan {
   int alo, ahi;  // a-taps sampled in this slab
@@ -208,6 +223,8 @@ struct SlabPlan {
   int f0, z0;    // first f column / z row in the buffer
   int fb;        // 1: sample from global memory
 };
+
+int slab_ctas_per_sm() { return kSlabCtas; }
 
 size_t slab_smem_bytes(int dtype) {
   return 2 * (size_t)kBufElems * (dtype == kF32 ? 4 : 2) + 256;
@@ -238,6 +255,30 @@ __device__ __forceinline__ float sample_at(const T* base, int sa, int sz, float 
   return fmaf(wz, s1 - s0, s0);
 }
 
+// The same sample with the lerps of the two z rows (and, without Z2, of the
+// two a rows) paired into packed FP32x2 operations: the same IEEE operations
+// in the same order, so the result is bit-identical to sample_at.
+template <bool Z2, typename T>
+__device__ __forceinline__ float sample_at2(const T* base, int sa, int sz, float wa,
+                                            float wf, float wz) {
+  const float2 wf2 = make_float2(wf, wf);
+  if (!Z2) {
+    const float2 lo = make_float2(ld_any(base), ld_any(base + sa));
+    const float2 hi = make_float2(ld_any(base + 1), ld_any(base + sa + 1));
+    const float2 r = __ffma2_rn(wf2, __fadd2_rn(hi, make_float2(-lo.x, -lo.y)), lo);
+    return fmaf(wa, r.y - r.x, r.x);
+  }
+  const T* b = base + sz;
+  const float2 A = make_float2(ld_any(base), ld_any(b));                 // v00, u00
+  const float2 B = make_float2(ld_any(base + 1), ld_any(b + 1));         // v01, u01
+  const float2 C = make_float2(ld_any(base + sa), ld_any(b + sa));       // v10, u10
+  const float2 D = make_float2(ld_any(base + sa + 1), ld_any(b + sa + 1));
+  const float2 P = __ffma2_rn(wf2, __fadd2_rn(B, make_float2(-A.x, -A.y)), A);  // r0, q0
+  const float2 Q = __ffma2_rn(wf2, __fadd2_rn(D, make_float2(-C.x, -C.y)), C);  // r1, q1
+  const float2 S = __ffma2_rn(make_float2(wa, wa), __fadd2_rn(Q, make_float2(-P.x, -P.y)), P);
+  return fmaf(wz, S.y - S.x, S.x);
+}
+
 // Geometry of one slab job: a 32 x 8 detector tile of one view.
 struct SlabJob {
   int det_w, det_h, S, Z, Pf;
@@ -259,6 +300,7 @@ struct SlabShared {
   SlabPlan plan[2];
   float corner[4][6];
   int amin, amax, pos, neg;
+  int abort;  // set by a timed-out wait
   long long item;
 };
 
@@ -266,6 +308,7 @@ __device__ __forceinline__ void slab_init_barriers(SlabShared& S) {
   if (threadIdx.x + 32 * threadIdx.y == 0) {
     mbar_init(&S.bar[0], 1);
     mbar_init(&S.bar[1], 1);
+    S.abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -393,6 +436,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     }
     p.f0 = f0;
     p.z0 = z0;
+    if (S.abort) fits = false;
     p.fb = fits ? 0 : 1;
     plan[j & 1] = p;
     if (fits) {
@@ -409,7 +453,9 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   if (threadIdx.y == 0 && nslab > 0) plan_and_issue(0);
   __syncthreads();
 
-  float acc0 = 0.f, acc1 = 0.f;
+  // One accumulator, samples added in ray order: the sum does not depend on
+  // how the samples fall into slabs or on which path (shared / global) took them.
+  float acc = 0.f;
   int k = 0;
   for (int j = 0; j < nslab; ++j) {
     if (threadIdx.y == 0 && j + 1 < nslab) plan_and_issue(j + 1);
@@ -417,7 +463,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     const TV* b = (j & 1) ? buf1 : buf0;
     bool from_smem = !p.fb;
     if (from_smem) {
-      from_smem = mbar_wait_bounded(&bar[j & 1], phase[j & 1], E.err);
+      from_smem = mbar_wait_bounded(&bar[j & 1], phase[j & 1], E.err, &S.abort);
       phase[j & 1] ^= 1u;
     }
     // Samples of this lane whose a-tap lies in [alo, ahi], two per iteration
@@ -445,12 +491,12 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
           const float wa1 = tb - fb_, wf1 = tf1 - ff1, wz1 = tz1 - fz1;
           int i1 = __float2int_rn(fmaf(fz1, (float)kPlane, fmaf(fb_, (float)kBoxF, ff1 + off)));
           i1 = min(max(i1, 0), kMaxIdx);
-          const float v0 = sample_at<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
-          const float v1 = sample_at<Z2>(b + i1, kBoxF, kPlane, wa1, wf1, wz1);
-          acc0 += v0;
-          acc1 += v1;
+          const float v0 = sample_at2<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
+          const float v1 = sample_at2<Z2>(b + i1, kBoxF, kPlane, wa1, wf1, wz1);
+          acc += v0;
+          acc += v1;
         } else {
-          acc0 += sample_at<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
+          acc += sample_at2<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
         }
       } else {
         // Fallback: the same taps from the padded volume in global memory.
@@ -461,7 +507,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
           const float fq = floorf(tq), ffq = floorf(tfq), fzq = floorf(tzq);
           const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
           const int gz = min(max((int)fzq, 0), Pz - 2);
-          acc0 += sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
+          acc += sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
                                 Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
         }
       }
@@ -471,7 +517,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     __syncthreads();
   }
   if (valid) {
-    const float l = (acc0 + acc1) * J.step;
+    const float l = acc * J.step;
     const size_t pix = (size_t)iy * J.det_w + ix;
     const size_t gi = (size_t)J.gview * J.P + pix;
     if (EPI == 0) {
@@ -488,7 +534,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
 }
 
 template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
-__global__ void __launch_bounds__(256, 3) fp_slab_kernel(
+__global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
     const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
     const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
     const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E) {
@@ -520,7 +566,7 @@ __global__ void __launch_bounds__(256, 3) fp_slab_kernel(
 // counter (work stealing) and run the same tile code as above.
 // ---------------------------------------------------------------------------
 template <typename TV>
-__global__ void __launch_bounds__(256, 3) fp_batch_kernel(
+__global__ void __launch_bounds__(256, kSlabCtas) fp_batch_kernel(
     const BatchFp* __restrict__ probs, int nprob, long long total,
     unsigned long long* __restrict__ counter, unsigned* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem_raw[];

@@ -56,6 +56,9 @@ struct SlabEpi {
   unsigned* err;     // set to non-zero when a bounded wait gave up
 };
 int slab_pitch(int W);
+// CTAs of the slab FP kernels resident per SM (its launch bounds); persistent
+// launches size their grids by it.
+int slab_ctas_per_sm();
 
 // One problem of a batched FP launch (device-resident descriptor).
 struct alignas(64) BatchFp {

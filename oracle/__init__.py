@@ -75,11 +75,13 @@ def _load():
             "orc_filter_response": [i, i, d, D, i],
             "orc_set_threads": [i],
             "orc_get_threads": [],
+            "orc_set_tex_weights": [i],
+            "orc_get_tex_weights": [],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)
             fn.argtypes = args
-            fn.restype = None if name == "orc_set_threads" else ctypes.c_int
+            fn.restype = None if name in ("orc_set_threads", "orc_set_tex_weights") else ctypes.c_int
         cb = ctypes.CFUNCTYPE(None, ctypes.c_int, D, ctypes.c_void_p)
         lib.orc_osc_tv.argtypes = [F, F, i, i, i, F, f, i, i, d, i, i, d, I32, D, cb, ctypes.c_void_p]
         lib.orc_osc_tv.restype = ctypes.c_int
@@ -111,6 +113,35 @@ def set_threads(n: int) -> None:
 
 def get_threads() -> int:
     return int(_load().orc_get_threads())
+
+
+TEX_EXACT, TEX8_NEAREST, TEX8_TRUNC = 0, 1, 2
+
+
+def set_tex_weights(mode: int) -> None:
+    """Texture-fetch weights of every oracle operator: TEX_EXACT (default),
+    TEX8_NEAREST or TEX8_TRUNC (1/256 fixed point, the texture hardware's)."""
+    _load().orc_set_tex_weights(int(mode))
+
+
+def get_tex_weights() -> int:
+    return int(_load().orc_get_tex_weights())
+
+
+class tex_weights:
+    """Context manager: run oracle calls with the given texture-weight mode."""
+
+    def __init__(self, mode: int):
+        self.mode = mode
+
+    def __enter__(self):
+        self.prev = get_tex_weights()
+        set_tex_weights(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        set_tex_weights(self.prev)
+        return False
 
 
 def fp(vol, sad, angles, n_proj, geom):

@@ -30,6 +30,19 @@
 namespace {
 
 int g_threads = 0;
+// Interpolation weights of the texture fetches: 0 = exact, 1 = rounded to the
+// nearest 1/256, 2 = truncated to 1/256.  CUDA's linear texture filter keeps
+// the fractional weight in 9-bit fixed point with 8 fractional bits (CUDA C
+// Programming Guide, "Linear Filtering"); modes 1/2 emulate that so the
+// difference between exact trilinear output and the reference's
+// texture-filtered output can be stated.
+int g_tex_weights = 0;
+
+inline double qw(double a) {
+  if (g_tex_weights == 1) return std::floor(a * 256.0 + 0.5) / 256.0;
+  if (g_tex_weights == 2) return std::floor(a * 256.0) / 256.0;
+  return a;
+}
 
 inline int nthreads() {
 #ifdef _OPENMP
@@ -130,7 +143,7 @@ inline double tex3(const T* v, int n0, int n1, int n2, double c0, double c1,
   c1 = safe_coord(c1, n1) - 0.5;
   c2 = safe_coord(c2, n2) - 0.5;
   const double f0 = std::floor(c0), f1 = std::floor(c1), f2 = std::floor(c2);
-  const double a = c0 - f0, b = c1 - f1, g = c2 - f2;
+  const double a = qw(c0 - f0), b = qw(c1 - f1), g = qw(c2 - f2);
   const int i0 = (int)f0, j0 = (int)f1, k0 = (int)f2;
   double acc = 0.0;
   for (int dk = 0; dk < 2; ++dk) {
@@ -171,7 +184,7 @@ inline double tex2(const T* p, int n0, int n1, double c0, double c1,
   c0 = safe_coord(c0, n0) - 0.5;
   c1 = safe_coord(c1, n1) - 0.5;
   const double f0 = std::floor(c0), f1 = std::floor(c1);
-  const double a = c0 - f0, b = c1 - f1;
+  const double a = qw(c0 - f0), b = qw(c1 - f1);
   const int i0 = (int)f0, j0 = (int)f1;
   double acc = 0.0;
   for (int dj = 0; dj < 2; ++dj) {
@@ -303,6 +316,8 @@ extern "C" {
 
 void orc_set_threads(int n) { g_threads = n; }
 int orc_get_threads(void) { return nthreads(); }
+void orc_set_tex_weights(int mode) { g_tex_weights = (mode >= 0 && mode <= 2) ? mode : 0; }
+int orc_get_tex_weights(void) { return g_tex_weights; }
 
 // CUDAmex_FP.cu:350-477 (gateway) and :56-346 (kernels).
 int orc_fp(const float* vol, int W, int H, float sad, const float* angles,

@@ -104,6 +104,12 @@ int orc_filter_response(int W, int filter, double cutoff, double* H,
 void orc_set_threads(int n);
 int orc_get_threads(void);
 
+/* Texture-fetch weights: 0 exact (default), 1 nearest 1/256, 2 truncated to
+ * 1/256 -- an emulation of the 8-fractional-bit weights of CUDA's linear
+ * texture filter, which the reference's tex2D/tex3D fetches use. */
+void orc_set_tex_weights(int mode);
+int orc_get_tex_weights(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,8 @@ closed-form answers, plus the committed golden fixtures in tests/golden/.
 import numpy as np
 import pytest
 
+from conftest import rel_l2
+
 
 def _cyl(W, H, r, val=1.0):
     from mexct import phantoms
@@ -299,3 +301,33 @@ def test_osc_tv_trajectory_is_rounding_sensitive(orc):
     a, b = run(False), run(True)
     e = [np.linalg.norm(x - y) / np.linalg.norm(x) for x, y in zip(a, b)]
     assert e[0] < 1e-7 and e[3] > 1e-4 and e[3] > 100 * e[1]
+
+
+@pytest.mark.parametrize("geom", [0, 2])
+def test_texture_weight_difference_is_stated(orc, geom):
+    """The reference samples through CUDA's linear texture filter, whose weights
+    are 1/256 fixed point.  The oracle's emulation of that states how far the
+    reference's texture-filtered FP and BP sit from exact trilinear/bilinear
+    output (the form every FP32 kernel here is checked against at 1e-5)."""
+    import oracle
+    from mexct import phantoms
+
+    W, H, nP = 48, 40, 16
+    vol = phantoms.ellipsoids(W, count=6, seed=3, nz=H)
+    ang = phantoms.angles_full(nP)
+    fp = orc.fp(vol, 1000.0, ang, nP, geom)
+    bp = orc.bp(fp.astype(np.float32), 1000.0, ang, geom)
+    out = {}
+    for name, mode in [("nearest", oracle.TEX8_NEAREST), ("trunc", oracle.TEX8_TRUNC)]:
+        with oracle.tex_weights(mode):
+            fq = orc.fp(vol, 1000.0, ang, nP, geom)
+            bq = orc.bp(fp.astype(np.float32), 1000.0, ang, geom)
+        out[name] = (rel_l2(fq, fp), rel_l2(bq, bp))
+    assert oracle.get_tex_weights() == oracle.TEX_EXACT
+    print("8-bit texture weights vs exact, geom %d (FP, BP):" % geom,
+          {k: ("%.3g" % a, "%.3g" % b) for k, (a, b) in out.items()})
+    for a, b in out.values():
+        # a weight error below 1/256 of a neighbour difference: well above FP32
+        # rounding, well below 1e-3
+        assert 1e-6 < a < 1e-3
+        assert 1e-7 < b < 1e-3

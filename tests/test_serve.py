@@ -89,6 +89,8 @@ def test_served_results_equal_alone(cuda):
         kind = i % 2
         reqs.append((kind, pre, post, ang, geom, rng.integers(0, 4, 3)))
     s = serve.Server(slots=3, budget_bytes=8 << 30)
+    # a 0.5 s host-side request holds one slot, so real requests overlap it
+    hold = s.submit_simulated(0.5)
     tickets = []
     for kind, pre, post, ang, geom, picks in reqs:
         if kind == 0:
@@ -96,6 +98,7 @@ def test_served_results_equal_alone(cuda):
         else:
             tickets.append(s.submit_osctv(pre, post, ang, geom, picks, n_iter=3, n_sub=4))
     served = [s.wait(t)[0] for t in tickets]
+    s.wait(hold)
     assert s.stats()["max_concurrent"] >= 2
     s.close()
     gs = {0: "par3d", 1: "fan3d", 2: "cone3d"}
