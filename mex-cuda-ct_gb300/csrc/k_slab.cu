@@ -7,17 +7,19 @@
 // enter the volume through different faces and are spread along the ray
 // direction.  Here a CTA (32 x 8 detector pixels of one view) sweeps the
 // volume along the view's dominant axis a (x or y) in slabs of kSlabT tap
-// planes.  For each slab warp 0 computes the bounding box of the tile's ray
-// bundle (from the 4 corner rays: the coordinates across a plane are
-// monotone in the detector coordinates), and TMA copies that box from a
-// padded volume into shared memory ([z][a][f] with f fastest); every lane
-// then takes its samples whose a-tap lies in the slab from shared memory
-// with constant-offset loads.  Two buffers and two mbarriers overlap the copy
-// of slab j+1 with the sampling of slab j.  Shapes (measured on cone 512^3 x
+// planes.  Before the sweep the whole CTA plans every slab at once: the
+// bounding box of the tile's ray bundle in the slab, from the 4 corner rays
+// (the coordinates across a plane are monotone in the detector coordinates).
+// During the sweep one thread starts the TMA copy of the next slab's box from
+// a padded volume into shared memory ([z][a][f] with f fastest) and every
+// lane takes its samples whose a-tap lies in the slab from shared memory with
+// constant-offset loads.  Two buffers and two mbarriers overlap the copy of
+// slab j+1 with the sampling of slab j.  Shapes (measured on cone 512^3 x
 // 720): 4 taps per slab, boxes of 64 (f) x 5 (a) x <=20 (z) elements that
 // hold 99.9% of the bundles, 4 CTAs of 256 threads per SM (<=64 registers,
-// 50 KB of buffers each); 5 taps at 3 CTAs/SM and 3 taps at 4 CTAs/SM were
-// 7% and 20% slower.
+// 50 KB of buffers each); 3 taps (4 or 5 CTAs/SM) and 2 taps (5 CTAs/SM)
+// were 12-32% slower.  Planning all slabs up front instead of one slab ahead
+// in warp 0 took 15% off the sweep.
 //
 // The padded volume has a one-voxel border (replicated edge for clamp
 // addressing, zeros for border addressing) and a fast-axis pitch rounded up
@@ -295,9 +297,25 @@ struct SlabJob {
   void* out;
 };
 
+// Packed slab plan: f0/4 (bits 0-13), z0 (bits 14-26) and the box's z rows
+// nzr (bits 27-31) in the padded volume; nzr = 0 means "sample the slab from
+// global memory".  Plans are computed for the first kMaxPlans slabs of a tile
+// (an a-extent of 2048 taps, W <= ~2040); later slabs of larger volumes, and
+// boxes beyond f0 = 65532 or z0 = 8191, read global memory.
+constexpr int kMaxPlans = 2048 / kSlabT;
+constexpr uint32_t kPlanFallback = 0u;
+static_assert(kBZ < 32, "nzr must fit 5 bits");
+
+__device__ __forceinline__ uint32_t pack_plan(int f0, int z0, int nzr) {
+  return ((uint32_t)f0 >> 2) | ((uint32_t)z0 << 14) | ((uint32_t)nzr << 27);
+}
+__device__ __forceinline__ int plan_f0(uint32_t p) { return (int)(p & 0x3fffu) << 2; }
+__device__ __forceinline__ int plan_z0(uint32_t p) { return (int)((p >> 14) & 0x1fffu); }
+__device__ __forceinline__ int plan_nzr(uint32_t p) { return (int)(p >> 27); }
+
 struct SlabShared {
   uint64_t bar[2];
-  SlabPlan plan[2];
+  uint32_t plans[kMaxPlans];
   float corner[4][6];
   int amin, amax, pos, neg;
   int abort;  // set by a timed-out wait
@@ -373,17 +391,9 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   const int nslab = any ? (s_amax - s_amin) / kSlabT + 1 : 0;
   const TV* gv = static_cast<const TV*>(xdom ? J.py : J.px);  // f-fastest padded layout
   const CUtensorMap* tm = xdom ? J.tmy : J.tmx;
-  const float bfw = xdom ? J.by : J.bx;     // world offset of the f axis
-  const float baw = xdom ? J.bx : J.by;     // world offset of the a axis
-  auto& corner = S.corner;
-  auto& plan = S.plan;
   uint64_t* bar = S.bar;
-  // Plan slab j into slot j&1 and start its copy.  Called by all of warp 0:
-  // lanes 0-7 evaluate the 4 corner rays at the 2 ends of the slab in FP32
-  // (error ~1e-4 voxel, covered by the 1-voxel margin), lane 0 issues the TMA.
-  auto plan_and_issue = [&](int j) {
-    const int lane = threadIdx.x;
-    int alo, ahi;
+  // Tap range [alo, ahi] of slab j.
+  auto slab_range = [&](int j, int& alo, int& ahi) {
     if (dir > 0) {
       alo = s_amin + j * kSlabT;
       ahi = alo + kSlabT - 1;
@@ -391,77 +401,98 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       ahi = s_amax - j * kSlabT;
       alo = ahi - kSlabT + 1;
     }
-    float fv = 0.f, zv = 0.f;
-    if (lane < 8) {
-      const int c = lane & 3, w = lane >> 2;
-      const float aw = w ? (float)ahi + 0.5f + baw : (float)alo - 0.5f + baw;
-      const float sa = xdom ? corner[c][0] : corner[c][1];
-      const float sf = xdom ? corner[c][1] : corner[c][0];
-      const float ea = xdom ? corner[c][3] : corner[c][4];
-      const float ef = xdom ? corner[c][4] : corner[c][3];
-      const float den = ea - sa;
-      const float t = den != 0.f ? (aw - sa) / den : 0.f;
-      fv = fmaf(t, ef - sf, sf);
-      zv = fmaf(t, corner[c][5] - corner[c][2], corner[c][2]);
-    }
-    float fmn = lane < 8 ? fv : 3.0e38f, fmx = lane < 8 ? fv : -3.0e38f;
-    float zmn = lane < 8 ? zv : 3.0e38f, zmx = lane < 8 ? zv : -3.0e38f;
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) {
-      fmn = fminf(fmn, __shfl_xor_sync(0xffffffffu, fmn, o));
-      fmx = fmaxf(fmx, __shfl_xor_sync(0xffffffffu, fmx, o));
-      zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
-      zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
-    }
-    if (lane != 0) return;
-    SlabPlan p;
-    p.alo = alo;
-    p.ahi = ahi;
-    p.a0 = alo;
-    const int align = sizeof(TV) == 4 ? 4 : 8;
-    const float flo = floorf(fmn - bfw + 0.5f) - 1.0f;
-    const float fhi = floorf(fmx - bfw + 0.5f) + 2.0f;
-    const float zlo = floorf(zmn - J.bz + 0.5f) - 1.0f;
-    const float zhi = floorf(zmx - J.bz + 0.5f) + 2.0f;
-    bool fits = isfinite(flo) && isfinite(fhi) && isfinite(zlo) && isfinite(zhi) && !mixed &&
-                fhi >= 0.f && zhi >= 0.f && flo <= (float)(Pf - 1) && zlo <= (float)(Pz - 1);
-    int f0 = 0, z0 = 0, nzr = 0;
-    if (fits) {
-      const int fl = (int)fmaxf(flo, 0.f), zl = (int)fmaxf(zlo, 0.f);
-      const int fh = (int)fminf(fhi, (float)(Pf - 1)), zh = (int)fminf(zhi, (float)(Pz - 1));
-      f0 = (fl / align) * align;
-      z0 = zl;
-      nzr = zh - z0 + 1;
-      fits = (fh - f0 + 1 <= kBoxF) && (nzr <= kBZ) && nzr > 0;
-    }
-    p.f0 = f0;
-    p.z0 = z0;
-    if (S.abort) fits = false;
-    p.fb = fits ? 0 : 1;
-    plan[j & 1] = p;
-    if (fits) {
-      const int nbox = (nzr + kBoxZ - 1) / kBoxZ;
-      TV* dst = (j & 1) ? buf1 : buf0;
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_expect_tx(&bar[j & 1], (uint32_t)(nbox * kBoxZ * kPlane * sizeof(TV)));
-      for (int bx = 0; bx < nbox; ++bx)
-        tma_load_3d(dst + (size_t)bx * kBoxZ * kPlane, tm, f0, p.a0, z0 + bx * kBoxZ,
-                    &bar[j & 1]);
-    }
   };
 
-  if (threadIdx.y == 0 && nslab > 0) plan_and_issue(0);
+  // Plan every slab of the tile up front, 32 slabs per pass of the CTA: the 8
+  // lanes of a group evaluate the 4 corner rays at the 2 a-ends of their slab
+  // in FP32 (error ~1e-4 voxel, covered by the 1-voxel margin), reduce the
+  // f/z extent by shuffles, and the group's first lane stores the box.
+  {
+    const float bfw = xdom ? J.by : J.bx;  // world offset of the f axis
+    const float baw = xdom ? J.bx : J.by;  // world offset of the a axis
+    const int np = min(nslab, kMaxPlans);
+    const int c = tid & 3, w = (tid >> 2) & 1;
+    const float sa = xdom ? S.corner[c][0] : S.corner[c][1];
+    const float sf = xdom ? S.corner[c][1] : S.corner[c][0];
+    const float ea = xdom ? S.corner[c][3] : S.corner[c][4];
+    const float ef = xdom ? S.corner[c][4] : S.corner[c][3];
+    const float sz = S.corner[c][2], ez = S.corner[c][5];
+    const float den = ea - sa;
+    for (int base = 0; base < np; base += 32) {
+      const int j = base + (tid >> 3);
+      const bool act = j < np;
+      int alo, ahi;
+      slab_range(j, alo, ahi);
+      const float aw = w ? (float)ahi + 0.5f + baw : (float)alo - 0.5f + baw;
+      const float t = den != 0.f ? (aw - sa) / den : 0.f;
+      const float fv = fmaf(t, ef - sf, sf), zv = fmaf(t, ez - sz, sz);
+      float fmn = act ? fv : 3.0e38f, fmx = act ? fv : -3.0e38f;
+      float zmn = act ? zv : 3.0e38f, zmx = act ? zv : -3.0e38f;
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1) {
+        fmn = fminf(fmn, __shfl_xor_sync(0xffffffffu, fmn, o));
+        fmx = fmaxf(fmx, __shfl_xor_sync(0xffffffffu, fmx, o));
+        zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
+        zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
+      }
+      if (act && (tid & 7) == 0) {
+        const int align = sizeof(TV) == 4 ? 4 : 8;
+        const float flo = floorf(fmn - bfw + 0.5f) - 1.0f;
+        const float fhi = floorf(fmx - bfw + 0.5f) + 2.0f;
+        const float zlo = floorf(zmn - J.bz + 0.5f) - 1.0f;
+        const float zhi = floorf(zmx - J.bz + 0.5f) + 2.0f;
+        bool fits = isfinite(flo) && isfinite(fhi) && isfinite(zlo) && isfinite(zhi) &&
+                    !mixed && fhi >= 0.f && zhi >= 0.f && flo <= (float)(Pf - 1) &&
+                    zlo <= (float)(Pz - 1);
+        int f0 = 0, z0 = 0;
+        if (fits) {
+          const int fl = (int)fmaxf(flo, 0.f), zl = (int)fmaxf(zlo, 0.f);
+          const int fh = (int)fminf(fhi, (float)(Pf - 1));
+          const int zh = (int)fminf(zhi, (float)(Pz - 1));
+          f0 = (fl / align) * align;
+          z0 = zl;
+          const int nzr = zh - z0 + 1;
+          fits = (fh - f0 + 1 <= kBoxF) && (nzr <= kBZ) && nzr > 0 && f0 <= 65532 &&
+                 z0 <= 8191;
+          if (fits) S.plans[j] = pack_plan(f0, z0, nzr);
+        }
+        if (!fits) S.plans[j] = kPlanFallback;
+      }
+    }
+  }
   __syncthreads();
+
+  // Start the copy of slab j into buffer j&1 (thread 0 only).
+  auto issue = [&](int j) {
+    const uint32_t pk = j < kMaxPlans ? S.plans[j] : kPlanFallback;
+    const int nzr = plan_nzr(pk);
+    if (nzr == 0 || S.abort) return;
+    int alo, ahi;
+    slab_range(j, alo, ahi);
+    const int nbox = (nzr + kBoxZ - 1) / kBoxZ;
+    const int f0 = plan_f0(pk), z0 = plan_z0(pk);
+    TV* dst = (j & 1) ? buf1 : buf0;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bar[j & 1], (uint32_t)(nbox * kBoxZ * kPlane * sizeof(TV)));
+    for (int bx = 0; bx < nbox; ++bx)
+      tma_load_3d(dst + (size_t)bx * kBoxZ * kPlane, tm, f0, alo, z0 + bx * kBoxZ, &bar[j & 1]);
+  };
+  if (tid == 0 && nslab > 0) issue(0);
 
   // One accumulator, samples added in ray order: the sum does not depend on
   // how the samples fall into slabs or on which path (shared / global) took them.
   float acc = 0.f;
   int k = 0;
   for (int j = 0; j < nslab; ++j) {
-    if (threadIdx.y == 0 && j + 1 < nslab) plan_and_issue(j + 1);
-    const SlabPlan p = plan[j & 1];
+    // Buffer (j+1)&1 was released by the barrier that ended slab j-1.
+    if (tid == 0 && j + 1 < nslab) issue(j + 1);
+    const uint32_t pk = j < kMaxPlans ? S.plans[j] : kPlanFallback;
+    int alo, ahi;
+    slab_range(j, alo, ahi);
     const TV* b = (j & 1) ? buf1 : buf0;
-    bool from_smem = !p.fb;
+    // A copy was issued exactly when the plan has a box and no wait of this
+    // CTA had timed out; after a time-out every wait returns false at once.
+    bool from_smem = plan_nzr(pk) != 0;
     if (from_smem) {
       from_smem = mbar_wait_bounded(&bar[j & 1], phase[j & 1], E.err, &S.abort);
       phase[j & 1] ^= 1u;
@@ -469,8 +500,8 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     // Samples of this lane whose a-tap lies in [alo, ahi], two per iteration
     // where possible.  Tap indices are kept as floats (exact below 2^24) so a
     // sample costs one float->int conversion for its shared-memory index.
-    const float alo_f = (float)p.alo, ahi_f = (float)p.ahi;
-    const float off = -(float)(p.z0 * kPlane + p.a0 * kBoxF + p.f0);
+    const float alo_f = (float)alo, ahi_f = (float)ahi;
+    const float off = -(float)(plan_z0(pk) * kPlane + alo * kBoxF + plan_f0(pk));
     while (k < n) {
       const float k0 = (float)k;
       const float ta = fmaf(k0, da, ta0);
