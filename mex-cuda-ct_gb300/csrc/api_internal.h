@@ -43,6 +43,7 @@ struct mexct_ctx {
   // Padded volumes of the slab FP (x-fastest and y-fastest) and the device
   // error word of bounded waits.
   mexct::Buf padx, pady, err;
+  mexct::Buf spad;  // padded sinogram views for BP
   // Texture variant: cached 3D array + texture object.
   cudaArray_t tex_arr = nullptr;
   cudaTextureObject_t tex = 0;
@@ -54,7 +55,7 @@ struct mexct_ctx {
 
   std::vector<mexct::Buf*> all_bufs() {
     return {&in, &in2, &in3, &out, &volT, &r1, &r2, &r3, &tabs, &red, &cnt, &scal,
-            &padx, &pady, &err};
+            &padx, &pady, &err, &spad};
   }
 };
 

@@ -4,7 +4,8 @@
 // A batch is planned once (padded-volume buffers, per-problem device
 // descriptors with TMA maps and trig tables); each operator then runs as a
 // fixed, capturable sequence: one batched padding launch plus one persistent
-// FP launch, or one persistent BP launch.  Persistent CTAs take work items
+// FP launch, or one sinogram-padding launch per problem plus one persistent BP
+// launch.  Persistent CTAs take work items
 // (problem, view, tile) / (problem, brick) from a global counter, so uneven
 // problems load-balance inside one launch.
 #include <algorithm>
@@ -22,12 +23,15 @@ using namespace mexct;
 struct mexct_batch {
   int device = 0;
   int n = 0;
-  std::vector<Buf> pads;  // 2 per problem
+  std::vector<Buf> pads;   // 2 per problem: padded volume, both layouts
+  std::vector<Buf> spads;  // 1 per problem: padded sinogram for BP
+  std::vector<mexct_problem> probs;
   Buf fp_desc, bp_desc, trig, counters, err;
   long long fp_items = 0, bp_items = 0, pad_items = 0;
   int sms = 152;
   ~mexct_batch() {
     for (Buf& b : pads) b.release();
+    for (Buf& b : spads) b.release();
     for (Buf* b : {&fp_desc, &bp_desc, &trig, &counters, &err}) b->release();
   }
 };
@@ -61,6 +65,8 @@ mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int 
   std::vector<BatchFp> fd(n);
   std::vector<BatchBp> bd(n);
   b->pads.resize(2 * n);
+  b->spads.resize(n);
+  b->probs.assign(probs, probs + n);
   size_t toff = 0;
   MEXCT_TRY_CUDA(b->trig.ensure(ntrig * sizeof(Trig)), "batch_create: trig");
   const Trig* dtrig = b->trig.as<Trig>();
@@ -115,7 +121,9 @@ mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int 
     g.hw = (uint32_t)W / 2u - 1u;  // :73
     g.item0 = b->bp_items;
     b->bp_items += (long long)g.bx * g.by * g.bz;
-    g.sino = p.d_sino;
+    MEXCT_TRY_CUDA(b->spads[i].ensure(sino_pad_elems(W, H, p.nP) * sizeof(float)),
+                   "batch_create: padded sinogram");
+    g.sino = b->spads[i].p;
     g.vol = p.d_rec;
     g.trig = dtrig + toff;
     toff += p.nP;
@@ -154,6 +162,11 @@ mexct_status mexct_batch_bp(mexct_batch* b, void* stream) {
   if (!b) return set_err(MEXCT_ERR_ARG, "batch_bp: NULL batch");
   DevGuard dg(b->device);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  for (int i = 0; i < b->n; ++i) {
+    const mexct_problem& p = b->probs[i];
+    MEXCT_TRY_CUDA(launch_pad_sino(p.d_sino, kF32, p.W, p.H, p.nP, false, b->spads[i].p, st),
+                   "batch_bp: padding");
+  }
   unsigned long long* ctr = b->counters.as<unsigned long long>() + 1;
   MEXCT_TRY_CUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st), "batch_bp: counter");
   MEXCT_TRY_CUDA(launch_bp_batch(b->bp_desc.as<BatchBp>(), b->n, b->bp_items, ctr, b->sms * 4, st),

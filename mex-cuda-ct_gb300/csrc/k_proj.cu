@@ -354,6 +354,142 @@ __global__ void __launch_bounds__(256) bp_kernel(
   }
 }
 
+// ---------------------------------------------------------------------------
+// Backprojection from a padded sinogram.  Each view is copied once into
+// [H+4][W+4] with two extra rows and columns on every side: the edge value
+// replicated (clamp addressing) or zeros (border addressing).  A tap index
+// then only needs clamping into [-2, n] -- both taps of an index outside the
+// image read pad values, which is what the clamp / border texture fetch
+// returns -- instead of clamping both taps of both axes into the image.
+// ---------------------------------------------------------------------------
+constexpr int kSinoPad = 2;
+
+template <typename T, bool BORDER>
+__global__ void __launch_bounds__(256) pad_sino_kernel(const T* __restrict__ in, int W, int H,
+                                                       T* __restrict__ out, int Wp) {
+  const int x = blockIdx.x * 32 + threadIdx.x - kSinoPad;
+  const int y = blockIdx.y * 8 + threadIdx.y - kSinoPad;
+  const int Hp = H + 2 * kSinoPad;
+  if (x >= W + kSinoPad || y >= H + kSinoPad) return;
+  const size_t v = blockIdx.z;
+  T val;
+  if (BORDER && (x < 0 || x >= W || y < 0 || y >= H)) {
+    val = T(0.0f);
+  } else {
+    const int cx = min(max(x, 0), W - 1), cy = min(max(y, 0), H - 1);
+    val = in[(v * H + cy) * W + cx];
+  }
+  out[(v * Hp + (y + kSinoPad)) * Wp + (x + kSinoPad)] = val;
+}
+
+__host__ __device__ int sino_pad_pitch(int W) { return W + 2 * kSinoPad; }
+size_t sino_pad_elems(int W, int H, int nviews) {
+  return (size_t)sino_pad_pitch(W) * (H + 2 * kSinoPad) * nviews;
+}
+
+cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews, bool border,
+                            void* out, cudaStream_t st) {
+  if (nviews <= 0) return cudaSuccess;
+  const int Wp = sino_pad_pitch(W);
+  dim3 blk(32, 8), grd((W + 2 * kSinoPad + 31) / 32, (H + 2 * kSinoPad + 7) / 8, nviews);
+#define PAD_SINO(T)                                                                       \
+  do {                                                                                    \
+    if (border)                                                                           \
+      pad_sino_kernel<T, true><<<grd, blk, 0, st>>>((const T*)in, W, H, (T*)out, Wp);   \
+    else                                                                                  \
+      pad_sino_kernel<T, false><<<grd, blk, 0, st>>>((const T*)in, W, H, (T*)out, Wp);  \
+  } while (0)
+  if (dtype == kF32) PAD_SINO(float);
+  else if (dtype == kF16) PAD_SINO(__half);
+  else PAD_SINO(__nv_bfloat16);
+#undef PAD_SINO
+  return cudaGetLastError();
+}
+
+// Sample one padded projection along a voxel column: acc[j] += w * B(py, pz).
+// g.py / g.pz0 are texture coordinates (texel centres at i + 0.5).
+template <int GEOM, int ZC, typename TS>
+__device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, int H, int Wp,
+                                              int z0, const ColGeom<GEOM>& g, float* acc) {
+  // u tap, once per view and column (coordinate bounded so floor fits an int)
+  const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
+  const float fu = floorf(cu);
+  const float au = cu - fu;
+  const int iu = min(max((int)fu, -kSinoPad), W) + kSinoPad;
+  const float w0 = g.w * (1.0f - au), w1 = g.w * au;
+  const TS* col = p + iu;
+  // Two z voxels per step with packed FP32x2 arithmetic (x: z, y: z+1); each
+  // lane's operations are those of the one-voxel form, in the same order.
+  static_assert(ZC % 2 == 0, "ZC must be even");
+  const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
+  if (GEOM < 2) {
+    // par / fan: the column's z rows are texel rows (pz = iz + 0.5)
+#pragma unroll
+    for (int j = 0; j < ZC; j += 2) {
+      const TS* r0 = col + (size_t)(min(z0 + j, H - 1) + kSinoPad) * Wp;
+      const TS* r1 = col + (size_t)(min(z0 + j + 1, H - 1) + kSinoPad) * Wp;
+      const float2 v0 = make_float2(ldf(r0), ldf(r1));
+      const float2 v1 = make_float2(ldf(r0 + 1), ldf(r1 + 1));
+      const float2 t = __ffma2_rn(w02, v0, __ffma2_rn(w12, v1, make_float2(acc[j], acc[j + 1])));
+      acc[j] = t.x;
+      acc[j + 1] = t.y;
+    }
+  } else {
+    const float pz0 = g.pz0 - 0.5f;
+    const float2 dpz2 = make_float2(g.dpz, g.dpz), pz02 = make_float2(pz0, pz0);
+#pragma unroll
+    for (int j = 0; j < ZC; j += 2) {
+      const float2 zz = make_float2((float)(z0 + j), (float)(z0 + j + 1));
+      const float2 cz = __ffma2_rn(zz, dpz2, pz02);
+      const float2 fz = make_float2(floorf(cz.x), floorf(cz.y));
+      const float2 az = __fadd2_rn(cz, make_float2(-fz.x, -fz.y));
+      const int i0 = min(max(__float2int_rz(fz.x), -kSinoPad), H) + kSinoPad;
+      const int i1 = min(max(__float2int_rz(fz.y), -kSinoPad), H) + kSinoPad;
+      const TS* p0 = col + (size_t)i0 * Wp;
+      const TS* p1 = col + (size_t)i1 * Wp;
+      const float2 a = __ffma2_rn(w02, make_float2(ldf(p0), ldf(p1)),
+                                  __fmul2_rn(w12, make_float2(ldf(p0 + 1), ldf(p1 + 1))));
+      const float2 b = __ffma2_rn(w02, make_float2(ldf(p0 + Wp), ldf(p1 + Wp)),
+                                  __fmul2_rn(w12, make_float2(ldf(p0 + Wp + 1), ldf(p1 + Wp + 1))));
+      const float2 omaz = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-az.x, -az.y));
+      const float2 t = __ffma2_rn(omaz, a, __ffma2_rn(az, b, make_float2(acc[j], acc[j + 1])));
+      acc[j] = t.x;
+      acc[j + 1] = t.y;
+    }
+  }
+}
+
+template <int GEOM, int ZC, typename TS, typename TV>
+__global__ void __launch_bounds__(256) bp_pad_kernel(const __grid_constant__ VoxArgs A,
+                                                     const TS* __restrict__ sino, int Wp,
+                                                     TV* __restrict__ vol, int accumulate) {
+  const int ix = blockIdx.x * 32 + threadIdx.x;
+  const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z0 = blockIdx.z * ZC;
+  if (ix >= A.W || iy >= A.W) return;
+  float acc[ZC];
+#pragma unroll
+  for (int j = 0; j < ZC; ++j) acc[j] = 0.f;
+  if (in_circle(ix, iy, A.hw)) {
+    const float x = (float)ix - ((float)A.hw + 0.5f);
+    const float y = (float)iy - ((float)A.hw + 0.5f);
+    const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
+    for (int v = 0; v < A.nviews; ++v) {
+      const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
+      bp_column_pad<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+    }
+  }
+  const size_t base = (size_t)iy * A.W + ix;
+  const size_t sz = (size_t)A.W * A.W;
+#pragma unroll
+  for (int j = 0; j < ZC; ++j) {
+    if (z0 + j < A.H) {
+      TV* o = vol + base + (size_t)(z0 + j) * sz;
+      stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
+    }
+  }
+}
+
 constexpr int kBpZc = 16;
 
 template <int GEOM, typename TS, typename TV>
@@ -381,6 +517,43 @@ static cudaError_t bp_types(const VoxArgs& a, const void* sino, int stype,
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
+}
+
+template <int GEOM, typename TS, typename TV>
+static void bp_pad_go(const VoxArgs& a, const void* sino, int Wp, void* vol, bool accum,
+                      cudaStream_t st) {
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + kBpZc - 1) / kBpZc);
+  bp_pad_kernel<GEOM, kBpZc, TS, TV>
+      <<<grd, blk, 0, st>>>(a, (const TS*)sino, Wp, (TV*)vol, accum ? 1 : 0);
+}
+
+template <int GEOM>
+static cudaError_t bp_pad_types(const VoxArgs& a, const void* sino, int stype, int Wp, void* vol,
+                                int vtype, bool accum, cudaStream_t st) {
+  if (stype == kF32 && vtype == kF32)
+    bp_pad_go<GEOM, float, float>(a, sino, Wp, vol, accum, st);
+  else if (stype == kF16 && vtype == kF16)
+    bp_pad_go<GEOM, __half, __half>(a, sino, Wp, vol, accum, st);
+  else if (stype == kF16 && vtype == kF32)
+    bp_pad_go<GEOM, __half, float>(a, sino, Wp, vol, accum, st);
+  else if (stype == kBF16 && vtype == kBF16)
+    bp_pad_go<GEOM, __nv_bfloat16, __nv_bfloat16>(a, sino, Wp, vol, accum, st);
+  else if (stype == kBF16 && vtype == kF32)
+    bp_pad_go<GEOM, __nv_bfloat16, float>(a, sino, Wp, vol, accum, st);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, int stype,
+                             void* vol, int vtype, bool accumulate, cudaStream_t st) {
+  const int Wp = sino_pad_pitch(a.W);
+  switch (geom) {
+    case 0: return bp_pad_types<0>(a, sino_pad, stype, Wp, vol, vtype, accumulate, st);
+    case 1: return bp_pad_types<1>(a, sino_pad, stype, Wp, vol, vtype, accumulate, st);
+    case 2: return bp_pad_types<2>(a, sino_pad, stype, Wp, vol, vtype, accumulate, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_bp(int geom, const VoxArgs& a, const void* sino,
@@ -746,6 +919,9 @@ __device__ __forceinline__ void bp_l1_brick(const BrickJob& A, const float* __re
                                             float* __restrict__ vol) {
   const int ix = A.bx0 + threadIdx.x, iy = A.by0 + threadIdx.y, z0 = A.z0;
   if (ix >= A.W || iy >= A.W) return;
+  // sino: padded views ([H+4][W+4] each), as for bp_pad_kernel
+  const int Wp = sino_pad_pitch(A.W);
+  const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
   float acc[kSmZc];
 #pragma unroll
   for (int j = 0; j < kSmZc; ++j) acc[j] = 0.f;
@@ -754,7 +930,8 @@ __device__ __forceinline__ void bp_l1_brick(const BrickJob& A, const float* __re
     const float y = (float)iy - ((float)A.hw + 0.5f);
     for (int v = 0; v < A.nviews; ++v) {
       const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
-      bp_column<GEOM, false, kSmZc>(sino + (size_t)(A.view0 + v) * A.P, A.W, A.H, z0, g, acc);
+      bp_column_pad<GEOM, kSmZc>(sino + (size_t)(A.view0 + v) * vstride, A.W, A.H, Wp, z0, g,
+                                 acc);
     }
   }
   const size_t base = (size_t)iy * A.W + ix;

@@ -257,28 +257,40 @@ __device__ __forceinline__ float sample_at(const T* base, int sa, int sz, float 
   return fmaf(wz, s1 - s0, s0);
 }
 
-// The same sample with the lerps of the two z rows (and, without Z2, of the
-// two a rows) paired into packed FP32x2 operations: the same IEEE operations
-// in the same order, so the result is bit-identical to sample_at.
+// a - b on both lanes of a packed FP32x2 pair (one sub.rn.f32x2).
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+      " sub.rn.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+
+// Two samples at once (x: sample k, y: sample k+1) with every lerp a packed
+// FP32x2 subtract + fma: per sample the same IEEE operations in the same
+// order as sample_at, so each lane's result is bit-identical to it.
 template <bool Z2, typename T>
-__device__ __forceinline__ float sample_at2(const T* base, int sa, int sz, float wa,
-                                            float wf, float wz) {
-  const float2 wf2 = make_float2(wf, wf);
-  if (!Z2) {
-    const float2 lo = make_float2(ld_any(base), ld_any(base + sa));
-    const float2 hi = make_float2(ld_any(base + 1), ld_any(base + sa + 1));
-    const float2 r = __ffma2_rn(wf2, __fadd2_rn(hi, make_float2(-lo.x, -lo.y)), lo);
-    return fmaf(wa, r.y - r.x, r.x);
-  }
-  const T* b = base + sz;
-  const float2 A = make_float2(ld_any(base), ld_any(b));                 // v00, u00
-  const float2 B = make_float2(ld_any(base + 1), ld_any(b + 1));         // v01, u01
-  const float2 C = make_float2(ld_any(base + sa), ld_any(b + sa));       // v10, u10
-  const float2 D = make_float2(ld_any(base + sa + 1), ld_any(b + sa + 1));
-  const float2 P = __ffma2_rn(wf2, __fadd2_rn(B, make_float2(-A.x, -A.y)), A);  // r0, q0
-  const float2 Q = __ffma2_rn(wf2, __fadd2_rn(D, make_float2(-C.x, -C.y)), C);  // r1, q1
-  const float2 S = __ffma2_rn(make_float2(wa, wa), __fadd2_rn(Q, make_float2(-P.x, -P.y)), P);
-  return fmaf(wz, S.y - S.x, S.x);
+__device__ __forceinline__ float2 sample_pair(const T* p0, const T* p1, int sa, int sz,
+                                              float2 wa, float2 wf, float2 wz) {
+  const float2 A = make_float2(ld_any(p0), ld_any(p1));
+  const float2 B = make_float2(ld_any(p0 + 1), ld_any(p1 + 1));
+  const float2 C = make_float2(ld_any(p0 + sa), ld_any(p1 + sa));
+  const float2 D = make_float2(ld_any(p0 + sa + 1), ld_any(p1 + sa + 1));
+  const float2 r0 = __ffma2_rn(wf, sub2(B, A), A);
+  const float2 r1 = __ffma2_rn(wf, sub2(D, C), C);
+  const float2 s0 = __ffma2_rn(wa, sub2(r1, r0), r0);
+  if (!Z2) return s0;
+  const T* q0 = p0 + sz;
+  const T* q1 = p1 + sz;
+  const float2 E = make_float2(ld_any(q0), ld_any(q1));
+  const float2 F = make_float2(ld_any(q0 + 1), ld_any(q1 + 1));
+  const float2 G = make_float2(ld_any(q0 + sa), ld_any(q1 + sa));
+  const float2 H = make_float2(ld_any(q0 + sa + 1), ld_any(q1 + sa + 1));
+  const float2 u0 = __ffma2_rn(wf, sub2(F, E), E);
+  const float2 u1 = __ffma2_rn(wf, sub2(H, G), G);
+  const float2 s1 = __ffma2_rn(wa, sub2(u1, u0), u0);
+  return __ffma2_rn(wz, sub2(s1, s0), s0);
 }
 
 // Geometry of one slab job: a 32 x 8 detector tile of one view.
@@ -336,7 +348,7 @@ __device__ __forceinline__ void slab_init_barriers(SlabShared& S) {
 // Ends with a CTA barrier, so the shared state can be reused by the next job.
 template <int GEOM, int EPI, typename TV, typename TO>
 __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, SlabShared& S,
-                                          uint32_t* phase, const SlabEpi& E) {
+                                          uint32_t& phase, const SlabEpi& E) {
   constexpr bool Z2 = (GEOM == 2);  // par/fan rays sample exact z texel rows
   const int tid = threadIdx.x + 32 * threadIdx.y;
   const int u0 = J.tu0, v0 = J.tv0;
@@ -482,6 +494,12 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   // One accumulator, samples added in ray order: the sum does not depend on
   // how the samples fall into slabs or on which path (shared / global) took them.
   float acc = 0.f;
+  const float2 da2 = make_float2(da, da), df2 = make_float2(df, df), dz2 = make_float2(dz, dz);
+  const float2 ta02 = make_float2(ta0, ta0), tf02 = make_float2(tf0, tf0);
+  const float2 tz02 = make_float2(tz0, tz0);
+  // par / fan rays keep one z tap row for the whole ray
+  const float fzc = floorf(tz0);
+  const float2 fz02 = make_float2(fzc, fzc), wz02 = make_float2(tz0 - fzc, tz0 - fzc);
   int k = 0;
   for (int j = 0; j < nslab; ++j) {
     // Buffer (j+1)&1 was released by the barrier that ended slab j-1.
@@ -494,52 +512,59 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     // CTA had timed out; after a time-out every wait returns false at once.
     bool from_smem = plan_nzr(pk) != 0;
     if (from_smem) {
-      from_smem = mbar_wait_bounded(&bar[j & 1], phase[j & 1], E.err, &S.abort);
-      phase[j & 1] ^= 1u;
+      // bit b of phase: parity of buffer b's next completion
+      from_smem = mbar_wait_bounded(&bar[j & 1], (phase >> (j & 1)) & 1u, E.err, &S.abort);
+      phase ^= 1u << (j & 1);
     }
     // Samples of this lane whose a-tap lies in [alo, ahi], two per iteration
     // where possible.  Tap indices are kept as floats (exact below 2^24) so a
     // sample costs one float->int conversion for its shared-memory index.
     const float alo_f = (float)alo, ahi_f = (float)ahi;
     const float off = -(float)(plan_z0(pk) * kPlane + alo * kBoxF + plan_f0(pk));
+    const float2 off2 = make_float2(off, off);
     while (k < n) {
+      // Samples k and k+1: positions fma(k, d, t0) on both lanes of a pair.
       const float k0 = (float)k;
-      const float ta = fmaf(k0, da, ta0);
-      const float fa_ = floorf(ta);
-      if (dir > 0 ? fa_ > ahi_f : fa_ < alo_f) break;
-      const float tb = ta + da;
-      const float fb_ = floorf(tb);
-      const bool two = (k + 1 < n) && (dir > 0 ? fb_ <= ahi_f : fb_ >= alo_f);
-      const float tf0_ = fmaf(k0, df, tf0), tz0_ = Z2 ? fmaf(k0, dz, tz0) : tz0;
-      const float ff0 = floorf(tf0_), fz0 = floorf(tz0_);
+      const float2 kk = make_float2(k0, k0 + 1.0f);
+      const float2 ta2 = __ffma2_rn(kk, da2, ta02);
+      const float fa0 = floorf(ta2.x);
+      if (dir > 0 ? fa0 > ahi_f : fa0 < alo_f) break;
+      const float fa1 = floorf(ta2.y);
+      const bool two = (k + 1 < n) && (dir > 0 ? fa1 <= ahi_f : fa1 >= alo_f);
+      const float2 tf2 = __ffma2_rn(kk, df2, tf02);
+      const float2 fa2 = make_float2(fa0, fa1);
+      const float2 ff2 = make_float2(floorf(tf2.x), floorf(tf2.y));
+      float2 fz2 = fz02, wz2 = wz02;
+      if (Z2) {
+        const float2 tz2 = __ffma2_rn(kk, dz2, tz02);
+        fz2 = make_float2(floorf(tz2.x), floorf(tz2.y));
+        wz2 = sub2(tz2, fz2);
+      }
+      const float2 wa2 = sub2(ta2, fa2), wf2 = sub2(tf2, ff2);
       if (from_smem) {
-        const float wa0 = ta - fa_, wf0 = tf0_ - ff0, wz0 = tz0_ - fz0;
-        int i0 = __float2int_rn(fmaf(fz0, (float)kPlane, fmaf(fa_, (float)kBoxF, ff0 + off)));
-        i0 = min(max(i0, 0), kMaxIdx);
+        const float2 x2 = __ffma2_rn(fz2, make_float2((float)kPlane, (float)kPlane),
+                                     __ffma2_rn(fa2, make_float2((float)kBoxF, (float)kBoxF),
+                                                __fadd2_rn(ff2, off2)));
+        // Tap indices are exact in FP32 (< 2^24); a negative one wraps to a
+        // large unsigned value and is clamped like one past the end.
+        const unsigned i0 = min((unsigned)__float2int_rn(x2.x), (unsigned)kMaxIdx);
         if (two) {
-          const float tf1 = tf0_ + df, tz1 = Z2 ? tz0_ + dz : tz0;
-          const float ff1 = floorf(tf1), fz1 = floorf(tz1);
-          const float wa1 = tb - fb_, wf1 = tf1 - ff1, wz1 = tz1 - fz1;
-          int i1 = __float2int_rn(fmaf(fz1, (float)kPlane, fmaf(fb_, (float)kBoxF, ff1 + off)));
-          i1 = min(max(i1, 0), kMaxIdx);
-          const float v0 = sample_at2<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
-          const float v1 = sample_at2<Z2>(b + i1, kBoxF, kPlane, wa1, wf1, wz1);
-          acc += v0;
-          acc += v1;
+          const unsigned i1 = min((unsigned)__float2int_rn(x2.y), (unsigned)kMaxIdx);
+          const float2 v = sample_pair<Z2>(b + i0, b + i1, kBoxF, kPlane, wa2, wf2, wz2);
+          acc += v.x;
+          acc += v.y;
         } else {
-          acc += sample_at2<Z2>(b + i0, kBoxF, kPlane, wa0, wf0, wz0);
+          acc += sample_at<Z2>(b + i0, kBoxF, kPlane, wa2.x, wf2.x, wz2.x);
         }
       } else {
         // Fallback: the same taps from the padded volume in global memory.
         for (int q = 0; q < (two ? 2 : 1); ++q) {
-          const float kq = k0 + (float)q;
-          const float tq = fmaf(kq, da, ta0), tfq = fmaf(kq, df, tf0);
-          const float tzq = Z2 ? fmaf(kq, dz, tz0) : tz0;
-          const float fq = floorf(tq), ffq = floorf(tfq), fzq = floorf(tzq);
+          const float fq = q ? fa2.y : fa2.x, ffq = q ? ff2.y : ff2.x, fzq = q ? fz2.y : fz2.x;
           const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
           const int gz = min(max((int)fzq, 0), Pz - 2);
           acc += sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
-                                Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
+                               Pf * Ps, q ? wa2.y : wa2.x, q ? wf2.y : wf2.x,
+                               q ? wz2.y : wz2.x);
         }
       }
       k += two ? 2 : 1;
@@ -574,7 +599,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   TV* buf0 = reinterpret_cast<TV*>(smem_raw);
   TV* buf1 = buf0 + kBufElems;
   slab_init_barriers(S);
-  uint32_t phase[2] = {0u, 0u};
+  uint32_t phase = 0u;
   const int view = blockIdx.x;
   const int tiles_u = (A.det_w + 31) >> 5;
   SlabJob J;
@@ -605,7 +630,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_batch_kernel(
   TV* buf0 = reinterpret_cast<TV*>(smem_raw);
   TV* buf1 = buf0 + kBufElems;
   slab_init_barriers(S);
-  uint32_t phase[2] = {0u, 0u};
+  uint32_t phase = 0u;
   const SlabEpi E{nullptr, nullptr, nullptr, nullptr, err};
   for (;;) {
     if (threadIdx.x + 32 * threadIdx.y == 0) S.item = (long long)atomicAdd(counter, 1ull);

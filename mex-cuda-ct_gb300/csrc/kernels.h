@@ -107,6 +107,15 @@ cudaError_t launch_fp_tex(int geom, const RayArgs& a,
                           cudaTextureObject_t tex, float* out,
                           cudaStream_t st);
 
+// Padded sinogram for the voxel-driven BP: [nviews][H+4][W+4], edge values
+// replicated (clamp) or zero (border) in the two-texel frame.
+__host__ __device__ int sino_pad_pitch(int W);
+size_t sino_pad_elems(int W, int H, int nviews);
+cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews, bool border,
+                            void* out, cudaStream_t st);
+// BP of a.nviews views from a padded sinogram (view 0 of the launch first).
+cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, int stype,
+                             void* vol, int vtype, bool accumulate, cudaStream_t st);
 cudaError_t launch_bp(int geom, const VoxArgs& a, const void* sino,
                       int sino_type, void* vol, int vol_type, bool accumulate,
                       cudaStream_t st);

@@ -188,11 +188,20 @@ mexct_status bp_dev_impl(mexct_ctx* c, const void* d_sino, int stype, int W,
     MEXCT_TRY_CUDA(launch_fill(d_vol, vt, (long long)W * W * H, 0.f, st), "bp: zero");
     return MEXCT_OK;
   }
+  // Views go through a padded copy (clamp frame) in chunks of kMaxViews.
+  const int chunk = std::min(nP, kMaxViews);
+  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) * dsize(stype), st),
+                 "bp: workspace");
+  const size_t P = (size_t)W * H;
   for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
     a->nviews = std::min(kMaxViews, nP - v0);
-    a->view0 = v0;
+    a->view0 = 0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-    MEXCT_TRY_CUDA(launch_bp(geom, *a, d_sino, stype, d_vol, vt, v0 > 0, st), "bp: launch");
+    const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
+    MEXCT_TRY_CUDA(launch_pad_sino(src, stype, W, H, a->nviews, false, c->spad.p, st),
+                   "bp: pad");
+    MEXCT_TRY_CUDA(launch_bp_padded(geom, *a, c->spad.p, stype, d_vol, vt, v0 > 0, st),
+                   "bp: launch");
   }
   return MEXCT_OK;
 }
