@@ -49,6 +49,7 @@ typedef int mexct_status;
 #define MEXCT_FP_EXPLICIT 0 /* FP32 trilinear, TMA slab-staged (parity path) */
 #define MEXCT_FP_TEXTURE 1  /* hardware 3D texture, 8-bit filter weights */
 #define MEXCT_FP_RAY 2      /* FP32 trilinear, one ray per thread via L1 */
+#define MEXCT_FP_AUTO 3     /* EXPLICIT or RAY, from the context's shape table */
 
 typedef struct mexct_ctx mexct_ctx;
 
@@ -165,7 +166,8 @@ mexct_status mexct_prefilter_dev(mexct_ctx* ctx, const float* d_sino,
 
 /* Extended FP/BP: storage type of the volume and sinogram (MEXCT_F32,
  * MEXCT_F16, MEXCT_BF16; accumulation is always FP32) and the FP variant
- * (MEXCT_FP_EXPLICIT or MEXCT_FP_TEXTURE, FP32 storage only). */
+ * (MEXCT_FP_EXPLICIT, MEXCT_FP_RAY, MEXCT_FP_AUTO, or MEXCT_FP_TEXTURE with
+ * FP32 storage only). */
 mexct_status mexct_fp_dev_ex(mexct_ctx* ctx, const void* d_vol, int vol_type,
                              int W, int H, float sad, const float* angles,
                              int nP, int geom, void* d_out, int out_type,
@@ -174,6 +176,64 @@ mexct_status mexct_bp_dev_ex(mexct_ctx* ctx, const void* d_sino,
                              int sino_type, int W, int H, int nP, float sad,
                              const float* angles, int geom, void* d_vol,
                              int vol_type, void* stream);
+
+/* ---- launch shapes and autotuning -------------------------------------- */
+
+/* No counterpart in the reference (its kernels have one fixed launch shape).
+ *
+ * Every FP and BP call belongs to a shape class: operator, geometry, W, H,
+ * the view count rounded up to a power of two, and the input / output
+ * storage types.  A context keeps one launch shape per class.
+ * FP: variant, MEXCT_FP_EXPLICIT (TMA slab kernel) or MEXCT_FP_RAY (one ray
+ *     per thread); both compute the exact FP32 form.  Used by mexct_fp,
+ *     mexct_fp_dev and mexct_fp_dev_ex with MEXCT_FP_AUTO.
+ * BP: zc = z voxels per thread (8 or 16), rows = voxel rows per 32-column
+ *     block (4 or 8), vblocks = view blocks (1..64) whose FP32 partial sums
+ *     are added in block order; used by every BP entry point.
+ * Shapes change only the rounding of the FP32 sums (vblocks) or nothing at
+ * all (zc, rows, variant). */
+typedef struct mexct_shape {
+  int variant;               /* FP */
+  int zc, rows, vblocks;     /* BP */
+} mexct_shape;
+
+#define MEXCT_OP_FP 0
+#define MEXCT_OP_BP 1
+
+/* Modes for a class without a table entry. */
+#define MEXCT_TUNE_FIXED 0     /* FP slab kernel; BP zc 16, rows 8, 1 view block */
+#define MEXCT_TUNE_HEURISTIC 1 /* default: view blocks so small volumes fill the GPU */
+#define MEXCT_TUNE_AUTO 2      /* the first call of the class times every candidate
+                                  shape on its own data and keeps the fastest (a call
+                                  made during stream capture uses the heuristic) */
+mexct_status mexct_ctx_set_tune_mode(mexct_ctx* ctx, int mode);
+
+/* Pin (set) or read the shape of one class.  get returns the entry if there
+ * is one (ms = the tuned time in milliseconds, NaN if pinned, tuned = 1 if
+ * chosen by timing), else the shape the current mode would start from with
+ * tuned = -1. */
+mexct_status mexct_shape_set(mexct_ctx* ctx, int op, int geom, int W, int H,
+                             int nP, int in_type, int out_type,
+                             const mexct_shape* shape);
+mexct_status mexct_shape_get(mexct_ctx* ctx, int op, int geom, int W, int H,
+                             int nP, int in_type, int out_type,
+                             mexct_shape* shape, double* ms, int* tuned);
+/* Drop every table entry of the context. */
+mexct_status mexct_shape_clear(mexct_ctx* ctx);
+
+/* Tune one class now: time every candidate shape on these device buffers
+ * (the output is overwritten; on return it holds the result of the best
+ * shape), record the fastest and return it.  Must not run during stream
+ * capture. */
+mexct_status mexct_autotune_fp(mexct_ctx* ctx, const void* d_vol, int vol_type,
+                               int W, int H, float sad, const float* angles,
+                               int nP, int geom, void* d_out, int out_type,
+                               void* stream, mexct_shape* best, double* best_ms);
+mexct_status mexct_autotune_bp(mexct_ctx* ctx, const void* d_sino,
+                               int sino_type, int W, int H, int nP, float sad,
+                               const float* angles, int geom, void* d_vol,
+                               int vol_type, void* stream, mexct_shape* best,
+                               double* best_ms);
 
 /* ---- allocation-free variant ------------------------------------------ */
 

@@ -3,7 +3,9 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <initializer_list>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -29,6 +31,16 @@ struct Buf {
   }
 };
 
+// One entry of a context's launch-shape table.
+struct TuneEntry {
+  mexct_shape shape;
+  double ms;   // time of the tuned shape on its tuning call (NaN if not tuned)
+  int tuned;   // 1: chosen by timing, 0: set by the caller
+};
+// Shape class: operator, geometry, W, H, view count rounded up to a power of
+// two, input and output storage types.
+using TuneKey = std::array<int, 7>;
+
 }  // namespace mexct
 
 struct mexct_ctx {
@@ -43,7 +55,11 @@ struct mexct_ctx {
   // Padded volumes of the slab FP (x-fastest and y-fastest) and the device
   // error word of bounded waits.
   mexct::Buf padx, pady, err;
-  mexct::Buf spad;  // padded sinogram views for BP
+  mexct::Buf spad;   // padded sinogram views for BP
+  mexct::Buf bpart;  // BP view-block partial sums
+  // Launch shapes: MEXCT_TUNE_* mode and the per-class table.
+  int tune_mode = MEXCT_TUNE_HEURISTIC;
+  std::map<mexct::TuneKey, mexct::TuneEntry> tune;
   // Texture variant: cached 3D array + texture object.
   cudaArray_t tex_arr = nullptr;
   cudaTextureObject_t tex = 0;
@@ -55,7 +71,7 @@ struct mexct_ctx {
 
   std::vector<mexct::Buf*> all_bufs() {
     return {&in, &in2, &in3, &out, &volT, &r1, &r2, &r3, &tabs, &red, &cnt, &scal,
-            &padx, &pady, &err, &spad};
+            &padx, &pady, &err, &spad, &bpart};
   }
 };
 
@@ -96,6 +112,23 @@ mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
                           bool border, CUtensorMap* mx, CUtensorMap* my, int* Pf_out,
                           cudaStream_t st);
 
+// FP with a concrete variant / BP with an explicit launch shape (arguments
+// already checked; ops.cu).
+mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float sad,
+                    const float* angles, int nP, int geom, void* d_out, int ot, int variant,
+                    cudaStream_t st);
+mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, int nP, float sad,
+                    const float* angles, int geom, void* d_vol, int vt, const BpShape& shp,
+                    cudaStream_t st);
+// Shape of a call's class from the context's table, its mode's default, or
+// (MEXCT_TUNE_AUTO, outside stream capture) by timing the candidates on the
+// call's own buffers (tune.cu).
+mexct_status pick_fp_shape(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float sad,
+                           const float* angles, int nP, int geom, void* d_out, int ot,
+                           cudaStream_t st, mexct_shape* out);
+mexct_status pick_bp_shape(mexct_ctx* c, const void* d_sino, int stype, int W, int H, int nP,
+                           float sad, const float* angles, int geom, void* d_vol, int vt,
+                           cudaStream_t st, mexct_shape* out);
 }  // namespace mexct
 
 #define MEXCT_TRY_CUDA(expr, what)                         \

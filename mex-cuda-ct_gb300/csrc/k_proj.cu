@@ -16,6 +16,7 @@
 //   One thread per (x, y) voxel column and a chunk of ZC voxels along z held
 //   in registers across all views; per-view geometry comes from the kernel
 //   parameter block (constant bank), the volume is written once.
+#include <algorithm>
 #include <cstdio>
 
 #include "kernels.h"
@@ -459,14 +460,23 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
   }
 }
 
+// Launch shape (BpShape): ZC z voxels per thread, blocks of 32 x rows
+// columns, and the views split into vblocks blocks along grid z.  With
+// vblocks > 1 every view block writes FP32 partial sums to part[vb][voxel]
+// and bp_reduce_kernel adds them in block order (deterministic).
 template <int GEOM, int ZC, typename TS, typename TV>
 __global__ void __launch_bounds__(256) bp_pad_kernel(const __grid_constant__ VoxArgs A,
                                                      const TS* __restrict__ sino, int Wp,
-                                                     TV* __restrict__ vol, int accumulate) {
+                                                     TV* __restrict__ vol, int accumulate,
+                                                     int nz, int vblocks,
+                                                     float* __restrict__ part) {
   const int ix = blockIdx.x * 32 + threadIdx.x;
   const int iy = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z0 = blockIdx.z * ZC;
+  const int zb = blockIdx.z % nz, vb = blockIdx.z / nz;
+  const int z0 = zb * ZC;
   if (ix >= A.W || iy >= A.W) return;
+  const int vbeg = (int)((long long)A.nviews * vb / vblocks);
+  const int vend = (int)((long long)A.nviews * (vb + 1) / vblocks);
   float acc[ZC];
 #pragma unroll
   for (int j = 0; j < ZC; ++j) acc[j] = 0.f;
@@ -474,19 +484,37 @@ __global__ void __launch_bounds__(256) bp_pad_kernel(const __grid_constant__ Vox
     const float x = (float)ix - ((float)A.hw + 0.5f);
     const float y = (float)iy - ((float)A.hw + 0.5f);
     const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
-    for (int v = 0; v < A.nviews; ++v) {
+    for (int v = vbeg; v < vend; ++v) {
       const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
       bp_column_pad<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
     }
   }
   const size_t base = (size_t)iy * A.W + ix;
   const size_t sz = (size_t)A.W * A.W;
+  if (vblocks > 1) {
+    float* pp = part + (size_t)vb * sz * A.H + base;
+#pragma unroll
+    for (int j = 0; j < ZC; ++j)
+      if (z0 + j < A.H) pp[(size_t)(z0 + j) * sz] = acc[j];
+    return;
+  }
 #pragma unroll
   for (int j = 0; j < ZC; ++j) {
     if (z0 + j < A.H) {
       TV* o = vol + base + (size_t)(z0 + j) * sz;
       stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
     }
+  }
+}
+
+template <typename TV>
+__global__ void __launch_bounds__(256) bp_reduce_kernel(const float* __restrict__ part,
+                                                        int vblocks, long long N,
+                                                        TV* __restrict__ vol, int accumulate) {
+  for (long long i = blockIdx.x * 256ll + threadIdx.x; i < N; i += (long long)gridDim.x * 256) {
+    float s = accumulate ? ldp(vol + i) : 0.f;
+    for (int b = 0; b < vblocks; ++b) s += part[(size_t)b * N + i];
+    stf(vol + i, s);
   }
 }
 
@@ -519,39 +547,60 @@ static cudaError_t bp_types(const VoxArgs& a, const void* sino, int stype,
   return cudaGetLastError();
 }
 
+template <int GEOM, int ZC, typename TS, typename TV>
+static cudaError_t bp_pad_go(const VoxArgs& a, const void* sino, int Wp, void* vol, bool accum,
+                             const BpShape& shp, float* part, cudaStream_t st) {
+  const int nz = (a.H + ZC - 1) / ZC;
+  dim3 blk(32, shp.rows), grd((a.W + 31) / 32, (a.W + shp.rows - 1) / shp.rows,
+                              nz * shp.vblocks);
+  bp_pad_kernel<GEOM, ZC, TS, TV><<<grd, blk, 0, st>>>(a, (const TS*)sino, Wp, (TV*)vol,
+                                                       accum ? 1 : 0, nz, shp.vblocks, part);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || shp.vblocks == 1) return e;
+  const long long N = (long long)a.W * a.W * a.H;
+  const int ctas = (int)std::min<long long>((N + 255) / 256, 152ll * 16);
+  bp_reduce_kernel<TV><<<ctas, 256, 0, st>>>(part, shp.vblocks, N, (TV*)vol, accum ? 1 : 0);
+  return cudaGetLastError();
+}
+
 template <int GEOM, typename TS, typename TV>
-static void bp_pad_go(const VoxArgs& a, const void* sino, int Wp, void* vol, bool accum,
-                      cudaStream_t st) {
-  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + kBpZc - 1) / kBpZc);
-  bp_pad_kernel<GEOM, kBpZc, TS, TV>
-      <<<grd, blk, 0, st>>>(a, (const TS*)sino, Wp, (TV*)vol, accum ? 1 : 0);
+static cudaError_t bp_pad_zc(const VoxArgs& a, const void* sino, int Wp, void* vol, bool accum,
+                             const BpShape& shp, float* part, cudaStream_t st) {
+  if (shp.zc == 8) return bp_pad_go<GEOM, 8, TS, TV>(a, sino, Wp, vol, accum, shp, part, st);
+  return bp_pad_go<GEOM, 16, TS, TV>(a, sino, Wp, vol, accum, shp, part, st);
 }
 
 template <int GEOM>
 static cudaError_t bp_pad_types(const VoxArgs& a, const void* sino, int stype, int Wp, void* vol,
-                                int vtype, bool accum, cudaStream_t st) {
+                                int vtype, bool accum, const BpShape& shp, float* part,
+                                cudaStream_t st) {
   if (stype == kF32 && vtype == kF32)
-    bp_pad_go<GEOM, float, float>(a, sino, Wp, vol, accum, st);
-  else if (stype == kF16 && vtype == kF16)
-    bp_pad_go<GEOM, __half, __half>(a, sino, Wp, vol, accum, st);
-  else if (stype == kF16 && vtype == kF32)
-    bp_pad_go<GEOM, __half, float>(a, sino, Wp, vol, accum, st);
-  else if (stype == kBF16 && vtype == kBF16)
-    bp_pad_go<GEOM, __nv_bfloat16, __nv_bfloat16>(a, sino, Wp, vol, accum, st);
-  else if (stype == kBF16 && vtype == kF32)
-    bp_pad_go<GEOM, __nv_bfloat16, float>(a, sino, Wp, vol, accum, st);
-  else
-    return cudaErrorInvalidValue;
-  return cudaGetLastError();
+    return bp_pad_zc<GEOM, float, float>(a, sino, Wp, vol, accum, shp, part, st);
+  if (stype == kF16 && vtype == kF16)
+    return bp_pad_zc<GEOM, __half, __half>(a, sino, Wp, vol, accum, shp, part, st);
+  if (stype == kF16 && vtype == kF32)
+    return bp_pad_zc<GEOM, __half, float>(a, sino, Wp, vol, accum, shp, part, st);
+  if (stype == kBF16 && vtype == kBF16)
+    return bp_pad_zc<GEOM, __nv_bfloat16, __nv_bfloat16>(a, sino, Wp, vol, accum, shp, part, st);
+  if (stype == kBF16 && vtype == kF32)
+    return bp_pad_zc<GEOM, __nv_bfloat16, float>(a, sino, Wp, vol, accum, shp, part, st);
+  return cudaErrorInvalidValue;
+}
+
+bool bp_shape_valid(const BpShape& s) {
+  return (s.zc == 8 || s.zc == 16) && (s.rows == 4 || s.rows == 8) && s.vblocks >= 1 &&
+         s.vblocks <= 64;
 }
 
 cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, int stype,
-                             void* vol, int vtype, bool accumulate, cudaStream_t st) {
+                             void* vol, int vtype, bool accumulate, const BpShape& shp,
+                             float* part, cudaStream_t st) {
+  if (!bp_shape_valid(shp) || (shp.vblocks > 1 && !part)) return cudaErrorInvalidValue;
   const int Wp = sino_pad_pitch(a.W);
   switch (geom) {
-    case 0: return bp_pad_types<0>(a, sino_pad, stype, Wp, vol, vtype, accumulate, st);
-    case 1: return bp_pad_types<1>(a, sino_pad, stype, Wp, vol, vtype, accumulate, st);
-    case 2: return bp_pad_types<2>(a, sino_pad, stype, Wp, vol, vtype, accumulate, st);
+    case 0: return bp_pad_types<0>(a, sino_pad, stype, Wp, vol, vtype, accumulate, shp, part, st);
+    case 1: return bp_pad_types<1>(a, sino_pad, stype, Wp, vol, vtype, accumulate, shp, part, st);
+    case 2: return bp_pad_types<2>(a, sino_pad, stype, Wp, vol, vtype, accumulate, shp, part, st);
     default: return cudaErrorInvalidValue;
   }
 }

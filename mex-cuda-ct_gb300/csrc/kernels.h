@@ -113,9 +113,17 @@ __host__ __device__ int sino_pad_pitch(int W);
 size_t sino_pad_elems(int W, int H, int nviews);
 cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews, bool border,
                             void* out, cudaStream_t st);
+// Launch shape of the padded-sinogram BP: z voxels per thread (8 or 16),
+// column rows per block (4 or 8), view blocks along grid z (1..64; > 1 needs
+// an FP32 partial-sum workspace of vblocks * W*W*H floats).
+struct BpShape {
+  int zc, rows, vblocks;
+};
+bool bp_shape_valid(const BpShape& s);
 // BP of a.nviews views from a padded sinogram (view 0 of the launch first).
 cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, int stype,
-                             void* vol, int vtype, bool accumulate, cudaStream_t st);
+                             void* vol, int vtype, bool accumulate, const BpShape& shp,
+                             float* part, cudaStream_t st);
 cudaError_t launch_bp(int geom, const VoxArgs& a, const void* sino,
                       int sino_type, void* vol, int vol_type, bool accumulate,
                       cudaStream_t st);

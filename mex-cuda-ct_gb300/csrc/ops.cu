@@ -122,18 +122,15 @@ mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
 
 namespace {
 
-mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
-                         int H, float sad, const float* angles, int nP,
-                         int geom, void* d_out, int ot, int variant,
-                         cudaStream_t st) {
-  if (!d_vol || !d_out || !angles) return set_err(MEXCT_ERR_ARG, "fp: NULL pointer");
-  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "fp: bad volume dims %d x %d x %d", W, W, H);
-  if (nP < 0) return set_err(MEXCT_ERR_ARG, "fp: nProj must be >= 0 (got %d)", nP);
-  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "fp: invalid geometry %d", geom);
-  if (bad_type(vt) || bad_type(ot)) return set_err(MEXCT_ERR_ARG, "fp: bad storage type");
-  if (variant != MEXCT_FP_EXPLICIT && variant != MEXCT_FP_TEXTURE && variant != MEXCT_FP_RAY)
-    return set_err(MEXCT_ERR_ARG, "fp: unknown variant %d", variant);
-  if (!c || nP == 0) return MEXCT_OK;  // c == NULL: validate only
+}  // namespace
+
+namespace mexct {
+
+// FP with a concrete variant (EXPLICIT, RAY or TEXTURE); arguments checked.
+mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float sad,
+                    const float* angles, int nP, int geom, void* d_out, int ot, int variant,
+                    cudaStream_t st) {
+  if (nP == 0) return MEXCT_OK;
   std::unique_ptr<RayArgs> a(new RayArgs);
   fill_std_rays(*a, W, H, sad, geom, false);
   if (variant == MEXCT_FP_TEXTURE) {
@@ -170,6 +167,66 @@ mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
   return MEXCT_OK;
 }
 
+// BP with an explicit launch shape; arguments checked.  Views go through a
+// padded copy (clamp frame) in chunks of kMaxViews.
+mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, int nP, float sad,
+                    const float* angles, int geom, void* d_vol, int vt, const BpShape& shp,
+                    cudaStream_t st) {
+  std::unique_ptr<VoxArgs> a(new VoxArgs);
+  fill_vox(*a, W, H, sad);
+  if (nP == 0) {
+    MEXCT_TRY_CUDA(launch_fill(d_vol, vt, (long long)W * W * H, 0.f, st), "bp: zero");
+    return MEXCT_OK;
+  }
+  if (!bp_shape_valid(shp)) return set_err(MEXCT_ERR_ARG, "bp: invalid launch shape");
+  const int chunk = std::min(nP, kMaxViews);
+  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) * dsize(stype), st),
+                 "bp: workspace");
+  const size_t N = (size_t)W * W * H;
+  if (shp.vblocks > 1)
+    MEXCT_TRY_CUDA(c->bpart.ensure_async(N * shp.vblocks * sizeof(float), st), "bp: workspace");
+  const size_t P = (size_t)W * H;
+  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+    a->nviews = std::min(kMaxViews, nP - v0);
+    a->view0 = 0;
+    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+    const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
+    MEXCT_TRY_CUDA(launch_pad_sino(src, stype, W, H, a->nviews, false, c->spad.p, st),
+                   "bp: pad");
+    MEXCT_TRY_CUDA(launch_bp_padded(geom, *a, c->spad.p, stype, d_vol, vt, v0 > 0, shp,
+                                    c->bpart.as<float>(), st),
+                   "bp: launch");
+  }
+  return MEXCT_OK;
+}
+
+}  // namespace mexct
+
+namespace {
+
+mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
+                         int H, float sad, const float* angles, int nP,
+                         int geom, void* d_out, int ot, int variant,
+                         cudaStream_t st) {
+  if (!d_vol || !d_out || !angles) return set_err(MEXCT_ERR_ARG, "fp: NULL pointer");
+  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "fp: bad volume dims %d x %d x %d", W, W, H);
+  if (nP < 0) return set_err(MEXCT_ERR_ARG, "fp: nProj must be >= 0 (got %d)", nP);
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "fp: invalid geometry %d", geom);
+  if (bad_type(vt) || bad_type(ot)) return set_err(MEXCT_ERR_ARG, "fp: bad storage type");
+  if (variant != MEXCT_FP_EXPLICIT && variant != MEXCT_FP_TEXTURE && variant != MEXCT_FP_RAY &&
+      variant != MEXCT_FP_AUTO)
+    return set_err(MEXCT_ERR_ARG, "fp: unknown variant %d", variant);
+  if (!c || nP == 0) return MEXCT_OK;  // c == NULL: validate only
+  if (variant == MEXCT_FP_AUTO) {
+    mexct_shape shp;
+    mexct_status s = pick_fp_shape(c, d_vol, vt, W, H, sad, angles, nP, geom, d_out, ot, st,
+                                   &shp);
+    if (s) return s;
+    variant = shp.variant;
+  }
+  return fp_run(c, d_vol, vt, W, H, sad, angles, nP, geom, d_out, ot, variant, st);
+}
+
 // ---------------------------------------------------------------------------
 // BP
 // ---------------------------------------------------------------------------
@@ -182,28 +239,14 @@ mexct_status bp_dev_impl(mexct_ctx* c, const void* d_sino, int stype, int W,
   if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "bp: invalid geometry %d", geom);
   if (bad_type(stype) || bad_type(vt)) return set_err(MEXCT_ERR_ARG, "bp: bad storage type");
   if (!c) return MEXCT_OK;  // validate only
-  std::unique_ptr<VoxArgs> a(new VoxArgs);
-  fill_vox(*a, W, H, sad);
-  if (nP == 0) {
-    MEXCT_TRY_CUDA(launch_fill(d_vol, vt, (long long)W * W * H, 0.f, st), "bp: zero");
-    return MEXCT_OK;
+  mexct_shape shp{MEXCT_FP_EXPLICIT, 16, 8, 1};
+  if (nP > 0) {
+    mexct_status s = pick_bp_shape(c, d_sino, stype, W, H, nP, sad, angles, geom, d_vol, vt, st,
+                                   &shp);
+    if (s) return s;
   }
-  // Views go through a padded copy (clamp frame) in chunks of kMaxViews.
-  const int chunk = std::min(nP, kMaxViews);
-  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) * dsize(stype), st),
-                 "bp: workspace");
-  const size_t P = (size_t)W * H;
-  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
-    a->nviews = std::min(kMaxViews, nP - v0);
-    a->view0 = 0;
-    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-    const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
-    MEXCT_TRY_CUDA(launch_pad_sino(src, stype, W, H, a->nviews, false, c->spad.p, st),
-                   "bp: pad");
-    MEXCT_TRY_CUDA(launch_bp_padded(geom, *a, c->spad.p, stype, d_vol, vt, v0 > 0, st),
-                   "bp: launch");
-  }
-  return MEXCT_OK;
+  return bp_run(c, d_sino, stype, W, H, nP, sad, angles, geom, d_vol, vt,
+                BpShape{shp.zc, shp.rows, shp.vblocks}, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -528,10 +571,10 @@ mexct_status mexct_fp_dev(mexct_ctx* ctx, const float* d_vol, int W, int H,
                           float sad, const float* angles, int nP, int geom,
                           float* d_out, void* stream) {
   VALIDATE(fp_dev_impl(nullptr, d_vol, kF32, W, H, sad, angles, nP, geom, d_out, kF32,
-                       MEXCT_FP_EXPLICIT, nullptr));
+                       MEXCT_FP_AUTO, nullptr));
   CTX_OR_FAIL(c, "fp");
   return fp_dev_impl(c, d_vol, kF32, W, H, sad, angles, nP, geom, d_out, kF32,
-                     MEXCT_FP_EXPLICIT, as_stream(stream));
+                     MEXCT_FP_AUTO, as_stream(stream));
 }
 
 mexct_status mexct_fp_dev_ex(mexct_ctx* ctx, const void* d_vol, int vt, int W,
@@ -549,14 +592,14 @@ mexct_status mexct_fp(mexct_ctx* ctx, const float* vol, int W, int H,
                       float sad, const float* angles, int nP, int geom,
                       float* out) {
   VALIDATE(fp_dev_impl(nullptr, vol, kF32, W, H, sad, angles, nP, geom, out, kF32,
-                       MEXCT_FP_EXPLICIT, nullptr));
+                       MEXCT_FP_AUTO, nullptr));
   CTX_OR_FAIL(c, "fp");
   const size_t N = (size_t)W * W * H, M = (size_t)W * H * nP;
   mexct_status s = upload(c->in, vol, N * 4, c->stream, "fp: upload");
   if (s) return s;
   MEXCT_TRY_CUDA(c->out.ensure_async(M * 4, c->stream), "fp: workspace");
   s = fp_dev_impl(c, c->in.p, kF32, W, H, sad, angles, nP, geom, c->out.p, kF32,
-                  MEXCT_FP_EXPLICIT, c->stream);
+                  MEXCT_FP_AUTO, c->stream);
   if (s) return s;
   return finish(c, out, c->out, M * 4, "fp: download");
 }

@@ -16,7 +16,9 @@ LIB_PATH = os.path.join(PKG, "_build", "libmexct.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED, ERR_TIMEOUT, ERR_BUDGET = range(7)
 F32, F16, BF16 = 0, 1, 2
-FP_EXPLICIT, FP_TEXTURE = 0, 1
+FP_EXPLICIT, FP_TEXTURE, FP_RAY, FP_AUTO = 0, 1, 2, 3
+OP_FP, OP_BP = 0, 1
+TUNE_FIXED, TUNE_HEURISTIC, TUNE_AUTO = 0, 1, 2
 
 _lock = threading.Lock()
 _lib = None

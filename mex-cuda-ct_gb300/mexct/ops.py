@@ -250,8 +250,9 @@ def _dptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-def fp_dev(vol, sad, angles, geom, out=None, out_dtype=None, variant=_lib.FP_EXPLICIT, stream=None):
-    """FP of a device volume (H, W, W) -> sinogram (nP, H, W), stream-ordered."""
+def fp_dev(vol, sad, angles, geom, out=None, out_dtype=None, variant=_lib.FP_AUTO, stream=None):
+    """FP of a device volume (H, W, W) -> sinogram (nP, H, W), stream-ordered.  variant:
+    FP_AUTO (the context's shape table, see mexct.tune), FP_EXPLICIT, FP_RAY or FP_TEXTURE."""
     import torch
     H, W, W2 = vol.shape
     assert W == W2, "volume must be (H, W, W)"

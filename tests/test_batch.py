@@ -31,17 +31,25 @@ def test_batch_equals_single_problem_calls(cuda):
     import torch
     from mexct import batch, ops
 
+    from mexct import tune
+
     probs = _problems(1)
     b = batch.Batch(probs)
     b.fp()
     b.bp()
     torch.cuda.synchronize()
-    for p in probs:
-        s = ops.fp_dev(p["vol"], p["sad"], p["angles"], p["geom"])
-        r = ops.bp_dev(s, p["sad"], p["angles"], p["geom"])
-        torch.cuda.synchronize()
-        assert torch.equal(s, p["sino"])
-        assert torch.equal(r, p["rec"])
+    # the batch runs the fixed shapes (slab FP, BP without view blocks)
+    tune.clear()
+    tune.set_mode(tune.FIXED)
+    try:
+        for p in probs:
+            s = ops.fp_dev(p["vol"], p["sad"], p["angles"], p["geom"])
+            r = ops.bp_dev(s, p["sad"], p["angles"], p["geom"])
+            torch.cuda.synchronize()
+            assert torch.equal(s, p["sino"])
+            assert torch.equal(r, p["rec"])
+    finally:
+        tune.set_mode(tune.HEURISTIC)
     b.close()
 
 
