@@ -380,7 +380,8 @@ def main():
         del vol16, s16, r16
         # OSC-TV reconstruction latency (config: 256^3, 60 views, 20 it x 10 subsets).
         del ref_sino
-        for name, fn in (("osc_tv", lambda: osc_tv_latency(args.osc_reps)),
+        for name, fn in (("autotune", autotune_section),
+                         ("osc_tv", lambda: osc_tv_latency(args.osc_reps)),
                          ("batched", lambda: batched_uneven(args.batch_problems)),
                          ("serving", lambda: serving(args.serve_requests))):
             try:
@@ -536,6 +537,56 @@ def batched_uneven(count, seed=2026):
     out["workload"] = ("%d problems: geom 0/1/2, 64^3..256^3, 90..720 views, SAD 1000; FP, BP, "
                        "5 OSC-TV iterations x 8 subsets each" % count)
     b.close()
+    return out
+
+
+def autotune_section(classes=((64, 90, 2), (96, 180, 0), (128, 360, 2), (256, 720, 2))):
+    """FP and BP of small and mid-size classes under the three shape modes: fixed
+    (slab FP, BP without view blocks), heuristic (the default) and autotuned (every
+    candidate timed on the first call).  GUPS from CUDA events over >= 3 runs and
+    >= ~20 ms of work after warm-up."""
+    import torch
+
+    from mexct import ops, phantoms, tune
+
+    out = {}
+    for n, nv, g in classes:
+        vol = phantoms.ellipsoids(n, count=6, seed=n + nv, nz=n)
+        ang = phantoms.angles_full(nv)
+        d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+        sino = ops.fp_dev(d, 1000.0, ang, g)
+        rec = torch.empty_like(d)
+        res = {}
+        for mode, name in ((tune.FIXED, "fixed"), (tune.HEURISTIC, "heuristic"),
+                           (tune.AUTO, "autotuned")):
+            tune.clear()
+            tune.set_mode(mode)
+            row = {}
+            for op, fn in (("fp", lambda: ops.fp_dev(d, 1000.0, ang, g, out=sino)),
+                           ("bp", lambda: ops.bp_dev(sino, 1000.0, ang, g, out=rec))):
+                fn()  # tunes in auto mode
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                fn()
+                e1.record()
+                torch.cuda.synchronize()
+                reps = int(min(200, max(3, np.ceil(20.0 / max(e0.elapsed_time(e1), 1e-3)))))
+                e0.record()
+                for _ in range(reps):  # >= ~20 ms of work per measurement
+                    fn()
+                e1.record()
+                torch.cuda.synchronize()
+                t = e0.elapsed_time(e1) / reps / 1e3
+                row[op + "_gups"] = round(n ** 3 * nv / t / 1e9, 2)
+            row["bp_shape"] = tune.shape_get(tune.BP, g, n, n, nv)
+            row["fp_variant"] = tune.shape_get(tune.FP, g, n, n, nv)["variant"]
+            for k in ("ms",):
+                row["bp_shape"].pop(k, None)
+            res[name] = row
+        out["%d^3x%d_geom%d" % (n, nv, g)] = res
+    tune.clear()
+    tune.set_mode(tune.HEURISTIC)
     return out
 
 

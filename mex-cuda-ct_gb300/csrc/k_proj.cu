@@ -465,7 +465,11 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
 // vblocks > 1 every view block writes FP32 partial sums to part[vb][voxel]
 // and bp_reduce_kernel adds them in block order (deterministic).
 template <int GEOM, int ZC, typename TS, typename TV>
-__global__ void __launch_bounds__(256) bp_pad_kernel(const __grid_constant__ VoxArgs A,
+// Cone columns take 16 bilinear taps per z pair; bounding registers to 64 keeps
+// 4 CTAs (32 warps) per SM resident, 5% faster at 512^3 x 720 than the 66
+// registers / 3 CTAs the compiler picks unbounded.  Par/fan columns need no
+// bound.
+__global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __grid_constant__ VoxArgs A,
                                                      const TS* __restrict__ sino, int Wp,
                                                      TV* __restrict__ vol, int accumulate,
                                                      int nz, int vblocks,

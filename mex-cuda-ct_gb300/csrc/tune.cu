@@ -77,7 +77,9 @@ bool capturing(cudaStream_t st) {
   return cs != cudaStreamCaptureStatusNone;
 }
 
-// Best of `reps` timed runs of fn() on st after one untimed run, in ms.
+// Best of the timed runs of fn() on st after one untimed run, in ms.  Short
+// calls are repeated inside each timed run (about 2 ms of work per run) so
+// launch jitter does not pick the shape.
 template <typename F>
 mexct_status time_on(cudaStream_t st, int reps, F&& fn, double* ms) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -87,11 +89,12 @@ mexct_status time_on(cudaStream_t st, int reps, F&& fn, double* ms) {
     cudaEventDestroy(e0);
     return cuda_err(ce, "autotune: event");
   }
-  mexct_status s = fn();
   double best = std::numeric_limits<double>::infinity();
-  for (int r = 0; r < reps && s == MEXCT_OK; ++r) {
+  int inner = 1;
+  mexct_status s = MEXCT_OK;
+  for (int r = -1; r < reps && s == MEXCT_OK; ++r) {  // r = -1: warm-up and sizing
     cudaEventRecord(e0, st);
-    s = fn();
+    for (int i = 0; i < inner && s == MEXCT_OK; ++i) s = fn();
     cudaEventRecord(e1, st);
     ce = cudaEventSynchronize(e1);
     if (ce != cudaSuccess) {
@@ -100,7 +103,11 @@ mexct_status time_on(cudaStream_t st, int reps, F&& fn, double* ms) {
     }
     float t = 0.f;
     cudaEventElapsedTime(&t, e0, e1);
-    best = std::min(best, (double)t);
+    if (r < 0) {
+      inner = (int)std::min(20.0, std::max(1.0, std::ceil(2.0 / std::max((double)t, 1e-3))));
+      continue;
+    }
+    best = std::min(best, (double)t / inner);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -130,7 +137,7 @@ mexct_status tune_bp(mexct_ctx* c, const void* d_sino, int stype, int W, int H, 
   for (const mexct_shape& cand : bp_candidates(W, H, nt)) {
     const BpShape b{cand.zc, cand.rows, cand.vblocks};
     double ms = 0;
-    mexct_status s = time_on(st, 2, [&] {
+    mexct_status s = time_on(st, 3, [&] {
       return bp_run(c, d_sino, stype, W, H, nt, sad, angles, geom, d_vol, vt, b, st);
     }, &ms);
     if (s == MEXCT_ERR_OOM) continue;  // workspace of a large view split: skip it
@@ -151,7 +158,7 @@ mexct_status tune_fp(mexct_ctx* c, const void* d_vol, int vt, int W, int H, floa
   *best_ms = std::numeric_limits<double>::infinity();
   for (int variant : {MEXCT_FP_EXPLICIT, MEXCT_FP_RAY}) {
     double ms = 0;
-    mexct_status s = time_on(st, 2, [&] {
+    mexct_status s = time_on(st, 3, [&] {
       return fp_run(c, d_vol, vt, W, H, sad, angles, nt, geom, d_out, ot, variant, st);
     }, &ms);
     if (s) return s;
