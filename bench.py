@@ -401,7 +401,7 @@ def main():
         dist.destroy_process_group()
 
 
-def osc_tv_latency(reps):
+def osc_tv_latency(reps, forms=("plain_fp32", "chosen_graph_fp32", "chosen_graph_bf16")):
     """p50/p99 seconds per OSC-TV reconstruction, plain (eager, FP32) vs chosen (graphs)."""
     import torch
 
@@ -420,6 +420,8 @@ def osc_tv_latency(reps):
     out = {}
     for name, graph, dt in (("plain_fp32", False, None), ("chosen_graph_fp32", True, None),
                             ("chosen_graph_bf16", True, torch.bfloat16)):
+        if name not in forms:
+            continue
         times = []
         mu_last = None
         for r in range(reps + 1):
@@ -438,9 +440,12 @@ def osc_tv_latency(reps):
                      "p99_s": round(float(np.percentile(times, 99)), 4),
                      "volumes_per_s": round(1.0 / float(np.mean(times)), 3), "reps": reps}
         out[name]["_mu"] = mu_last
-    ref = out["plain_fp32"].pop("_mu")
+    ref = out["plain_fp32"].pop("_mu") if "plain_fp32" in out else None
     for k in ("chosen_graph_fp32", "chosen_graph_bf16"):
-        out[k]["rel_l2_vs_plain"] = rel(out[k].pop("_mu"), ref)
+        if k in out:
+            mu = out[k].pop("_mu")
+            if ref is not None:
+                out[k]["rel_l2_vs_plain"] = rel(mu, ref)
     out["workload"] = "256^3, 60 cone views, 20 iterations x 10 subsets, TV 20 steps at 0.2*d_a"
     return out
 

@@ -3,9 +3,10 @@
 // TV (CUDAmex_TVmin_3D.cu:101-234).  The reference runs three full-volume
 // passes per step (gradient kernel -> thrust norm -> thrust saxpy) and stores
 // the gradient.  Here a step is two passes and no gradient volume:
-//   tv_norm_kernel   gradient recomputed per voxel, ||g||^2 reduced in FP64
-//                    (warp shuffles, per-CTA partials, last-CTA fixed-order
-//                    sum: deterministic), step scale -c/||g|| written to HBM;
+//   tv_norm_kernel   gradient recomputed per voxel, ||g||^2 reduced (FP32 per
+//                    thread, FP64 across threads: warp shuffles, per-CTA
+//                    partials, last-CTA fixed-order sum: deterministic), step
+//                    scale -c/||g|| written to HBM;
 //   tv_update_kernel gradient recomputed, y = x + scale*g into the other
 //                    buffer of a ping-pong pair.
 // Algorithmic traffic is 12 bytes per voxel per step (read x twice, write y).
@@ -14,37 +15,6 @@
 #include "kernels.h"
 
 namespace mexct {
-
-// ---------------------------------------------------------------------------
-// TV gradient of one interior voxel (CUDAmex_TVmin_3D.cu:121-152), FP32.
-// ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ float tv_grad(const T* __restrict__ v, size_t i,
-                                         size_t sy, size_t sz) {
-  const float eps = 1.0e-6f;
-  const float x = ldf(v + i);
-  const float xm = ldf(v + i - 1), xp = ldf(v + i + 1);
-  const float ym = ldf(v + i - sy), yp = ldf(v + i + sy);
-  const float zm = ldf(v + i - sz), zp = ldf(v + i + sz);
-  const float xmyp = ldf(v + i - 1 + sy), xpym = ldf(v + i + 1 - sy);
-  const float ymzp = ldf(v + i - sy + sz), ypzm = ldf(v + i + sy - sz);
-  const float xmzp = ldf(v + i - 1 + sz), xpzm = ldf(v + i + 1 - sz);
-  const float a = x - xm, b = x - ym, c = x - zm;
-  float t = ((a + b) + c) / (eps + sqrtf(a * a + b * b + c * c));
-  const float d1 = xp - x, e1 = xp - xpym, f1 = xp - xpzm;
-  t -= d1 / (eps + sqrtf(d1 * d1 + e1 * e1 + f1 * f1));
-  const float d2 = yp - x, e2 = yp - xmyp, f2 = yp - ypzm;
-  t -= d2 / (eps + sqrtf(d2 * d2 + e2 * e2 + f2 * f2));
-  const float d3 = zp - x, e3 = zp - xmzp, f3 = zp - ymzp;
-  t -= d3 / (eps + sqrtf(d3 * d3 + e3 * e3 + f3 * f3));
-  return t;
-}
-
-__device__ __forceinline__ bool tv_interior(int ix, int iy, int iz, int Nx,
-                                            int Ny, int Nz) {
-  return ix >= 1 && iy >= 1 && iz >= 1 && ix < Nx - 1 && iy < Ny - 1 &&
-         iz < Nz - 1;
-}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -99,7 +69,87 @@ __device__ __forceinline__ bool finish_partials(double mine, double* partials,
   return tid == 0;
 }
 
-constexpr int kTvBx = 32, kTvBy = 8, kTvZ = 4;  // each thread: kTvZ voxels in z
+// ---------------------------------------------------------------------------
+// Tiled TV gradient.  With backward differences a_p = x_p - x_{p-1},
+// b_p = x_p - x_{p-sy}, c_p = x_p - x_{p-sz} and r_p = 1/(eps + |(a,b,c)_p|),
+// the four terms of the reference's gradient at voxel i are
+//   g_i = (a+b+c)_i r_i - a_{i+1} r_{i+1} - b_{i+sy} r_{i+sy} - c_{i+sz} r_{i+sz}
+// (CUDAmex_TVmin_3D.cu:121-152: the second to fourth terms are the first
+// term's components at the +x, +y and +z neighbours), so each voxel's
+// (a, b, c, r) is computed once (one sqrt, one reciprocal) instead of four
+// times.  A CTA of 32 x 8 threads sweeps a column tile along z: thread
+// (tx, ty) computes q at its column in every plane, takes the +x neighbour's
+// value by a shuffle, the +y neighbour's from shared memory (one barrier per
+// plane) and the +z neighbour's from its next plane, and writes the voxel
+// when tx < 31 and ty < 7 (tiles overlap by one column and one row).  The
+// next plane's loads are issued before the current plane is computed.
+// ---------------------------------------------------------------------------
+constexpr int kTvBx = 32, kTvBy = 8, kTvZ = 32;  // threads 32 x 8, 32 planes per CTA
+constexpr int kTvOx = kTvBx - 1, kTvOy = kTvBy - 1;  // output voxels per tile row / column
+
+// Sweep of one tile: calls visit(z, x_z, g, out) for every plane z of the
+// tile, with x_z the voxel value, g the gradient (0 on the volume border) and
+// out whether this thread owns the voxel.
+template <typename T, typename F>
+__device__ __forceinline__ void tv_sweep(const T* __restrict__ v, int Nx, int Ny, int Nz,
+                                         F&& visit) {
+  __shared__ float sqb[2][kTvBy][kTvBx];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int gx = blockIdx.x * kTvOx + tx, gy = blockIdx.y * kTvOy + ty;
+  const int z0 = blockIdx.z * kTvZ;
+  const int zend = min(z0 + kTvZ, Nz);
+  const size_t sy = (size_t)Nx, sz = (size_t)Nx * Ny;
+  const bool incol = gx < Nx && gy < Ny;
+  const bool qcol = incol && gx >= 1 && gy >= 1;  // columns where q exists
+  const bool own = incol && tx < kTvOx && ty < kTvOy;
+  const size_t ci = (size_t)gx + (size_t)gy * sy;
+  // value of the plane below the first one, and the first plane's loads
+  float xprev = (qcol && z0 >= 1) ? ldf(v + ci + (size_t)(z0 - 1) * sz) : 0.f;
+  float xcur = 0.f, xym = 0.f, xxm = 0.f;
+  auto load = [&](int p, float& xo, float& yo, float& mo) {
+    if (incol && p < Nz) {
+      const size_t i = ci + (size_t)p * sz;
+      xo = ldf(v + i);
+      yo = (gy >= 1) ? ldf(v + i - sy) : 0.f;
+      mo = (tx == 0 && gx >= 1) ? ldf(v + i - 1) : 0.f;
+    }
+  };
+  load(z0, xcur, xym, xxm);
+  float q0p = 0.f, qanp = 0.f, xz = 0.f;  // plane p-1: own q0, +x neighbour's qa, x
+  for (int p = z0; p <= zend; ++p) {
+    float xn = 0.f, yn = 0.f, mn = 0.f;
+    if (p + 1 <= zend) load(p + 1, xn, yn, mn);  // prefetch the next plane
+    // x_{p-1} of lane tx is lane tx-1's x_p; lane 0 loaded it
+    const float xl = __shfl_up_sync(0xffffffffu, xcur, 1);
+    const float xm = tx == 0 ? xxm : xl;
+    float q0 = 0.f, qa = 0.f, qb = 0.f, qc = 0.f;
+    if (qcol && p >= 1 && p < Nz) {
+      const float a = xcur - xm, b = xcur - xym, c = xcur - xprev;
+      const float r = __frcp_rn(1.0e-6f + __fsqrt_rn(fmaf(c, c, fmaf(b, b, a * a))));
+      q0 = ((a + b) + c) * r;
+      qa = a * r;
+      qb = b * r;
+      qc = c * r;
+    }
+    if (p > z0) {
+      const int z = p - 1;
+      const bool interior = gx >= 1 && gy >= 1 && z >= 1 && gx < Nx - 1 && gy < Ny - 1 &&
+                            z < Nz - 1;
+      const float g = interior ? ((q0p - qanp) - sqb[(p - 1) & 1][ty + (ty < kTvOy)][tx]) - qc
+                               : 0.f;
+      visit(z, xz, g, own && interior, own);
+    }
+    sqb[p & 1][ty][tx] = qb;
+    qanp = __shfl_down_sync(0xffffffffu, qa, 1);
+    q0p = q0;
+    xz = xcur;
+    xprev = xcur;
+    xcur = xn;
+    xym = yn;
+    xxm = mn;
+    __syncthreads();
+  }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) tv_norm_kernel(
@@ -107,18 +157,13 @@ __global__ void __launch_bounds__(256) tv_norm_kernel(
     const double* __restrict__ cmul, double* __restrict__ partials,
     unsigned* __restrict__ counter, float* __restrict__ scale,
     double* __restrict__ norm) {
-  const int ix = blockIdx.x * kTvBx + threadIdx.x;
-  const int iy = blockIdx.y * kTvBy + threadIdx.y;
-  const size_t sy = (size_t)Nx, sz = (size_t)Nx * Ny;
-  double ss = 0.0;
-  for (int j = 0; j < kTvZ; ++j) {
-    const int iz = blockIdx.z * kTvZ + j;
-    if (ix < Nx && iy < Ny && iz < Nz && tv_interior(ix, iy, iz, Nx, Ny, Nz)) {
-      const float g = tv_grad(x, (size_t)ix + iy * sy + iz * sz, sy, sz);
-      ss += (double)g * (double)g;
-    }
-  }
-  const double blk = block_sum(ss);
+  // ||g||^2: squares and the 32-voxel sum of a thread in FP32, every level
+  // above in FP64 (fixed order, deterministic).
+  float ss = 0.f;
+  tv_sweep(x, Nx, Ny, Nz, [&](int, float, float g, bool interior, bool) {
+    if (interior) ss = fmaf(g, g, ss);
+  });
+  const double blk = block_sum((double)ss);
   double total;
   if (finish_partials(blk, partials, counter, &total)) {
     const double m = sqrt(total);
@@ -134,32 +179,29 @@ template <typename T>
 __global__ void __launch_bounds__(256) tv_update_kernel(
     const T* __restrict__ x, T* __restrict__ y, int Nx, int Ny, int Nz,
     const float* __restrict__ scale) {
-  const int ix = blockIdx.x * kTvBx + threadIdx.x;
-  const int iy = blockIdx.y * kTvBy + threadIdx.y;
-  if (ix >= Nx || iy >= Ny) return;
   const float a = __ldg(scale);
   const size_t sy = (size_t)Nx, sz = (size_t)Nx * Ny;
-  for (int j = 0; j < kTvZ; ++j) {
-    const int iz = blockIdx.z * kTvZ + j;
-    if (iz >= Nz) break;
-    const size_t i = (size_t)ix + iy * sy + iz * sz;
-    const float xv = ldf(x + i);
+  const size_t ci = (size_t)(blockIdx.x * kTvOx + threadIdx.x) +
+                    (size_t)(blockIdx.y * kTvOy + threadIdx.y) * sy;
+  tv_sweep(x, Nx, Ny, Nz, [&](int z, float xv, float g, bool, bool own) {
     // x <- a*g + x (thrust saxpy, CUDAmex_TVmin_3D.cu:232); border g = 0.
-    const float g = tv_interior(ix, iy, iz, Nx, Ny, Nz) ? tv_grad(x, i, sy, sz) : 0.f;
-    stf(y + i, fmaf(a, g, xv));
-  }
+    if (own) stf(y + ci + (size_t)z * sz, fmaf(a, g, xv));
+  });
+}
+
+static dim3 tv_grid(int Nx, int Ny, int Nz) {
+  return dim3((Nx + kTvOx - 1) / kTvOx, (Ny + kTvOy - 1) / kTvOy, (Nz + kTvZ - 1) / kTvZ);
 }
 
 size_t tv_partials_needed(int Nx, int Ny, int Nz) {
-  return (size_t)((Nx + kTvBx - 1) / kTvBx) * ((Ny + kTvBy - 1) / kTvBy) *
-         ((Nz + kTvZ - 1) / kTvZ);
+  const dim3 g = tv_grid(Nx, Ny, Nz);
+  return (size_t)g.x * g.y * g.z;
 }
 
 static cudaError_t tv_norm_go(const void* x, int xt, int Nx, int Ny, int Nz, float c,
                               const double* cmul, double* partials, unsigned* counter,
                               float* scale, double* norm, cudaStream_t st) {
-  dim3 blk(kTvBx, kTvBy), grd((Nx + kTvBx - 1) / kTvBx, (Ny + kTvBy - 1) / kTvBy,
-                              (Nz + kTvZ - 1) / kTvZ);
+  dim3 blk(kTvBx, kTvBy), grd = tv_grid(Nx, Ny, Nz);
   if (xt == kF32)
     tv_norm_kernel<float><<<grd, blk, 0, st>>>((const float*)x, Nx, Ny, Nz, c, cmul,
                                                partials, counter, scale, norm);
@@ -187,8 +229,7 @@ cudaError_t launch_tv_norm_scaled(const void* x, int xt, int Nx, int Ny, int Nz,
 
 cudaError_t launch_tv_update(const void* x, void* y, int xt, int Nx, int Ny,
                              int Nz, const float* scale, cudaStream_t st) {
-  dim3 blk(kTvBx, kTvBy), grd((Nx + kTvBx - 1) / kTvBx, (Ny + kTvBy - 1) / kTvBy,
-                              (Nz + kTvZ - 1) / kTvZ);
+  dim3 blk(kTvBx, kTvBy), grd = tv_grid(Nx, Ny, Nz);
   if (xt == kF32)
     tv_update_kernel<float><<<grd, blk, 0, st>>>((const float*)x, (float*)y,
                                                  Nx, Ny, Nz, scale);
