@@ -1,9 +1,12 @@
-// k_proj.cu -- ray-driven forward projectors, voxel-driven backprojector and
-// the general3D scatter backprojector for sm_103a.
+// k_proj.cu -- ray-per-thread forward projectors (general3D FP, the
+// MEXCT_FP_RAY and MEXCT_FP_TEXTURE variants), voxel-driven backprojectors
+// (standard BP, OSC dual BP + update, batched BP) and the general3D scatter
+// backprojector for sm_103a.  The standard and OSC forward projections run
+// in the slab kernel of k_slab.cu.
 //
-// Forward projection (CUDAmex_FP.cu:56-346, CUDAmex_general3D_FP.cu:59-150)
+// Ray-per-thread FP (CUDAmex_FP.cu:56-346, CUDAmex_general3D_FP.cu:59-150)
 //   One thread per detector pixel; a warp owns 32 consecutive pixels of one
-//   detector row, a CTA an 32x8 pixel tile of one view.  blockIdx.x is the
+//   detector row, a CTA a 32x8 pixel tile of one view.  blockIdx.x is the
 //   view, so CTAs that are resident together march the same detector tile at
 //   neighbouring angles through the same part of the volume (L2 reuse).
 //   Samples are explicit FP32 trilinear fetches (the texture unit's 8-bit
@@ -14,8 +17,10 @@
 //
 // Backprojection (CUDAmex_BP.cu:44-221)
 //   One thread per (x, y) voxel column and a chunk of ZC voxels along z held
-//   in registers across all views; per-view geometry comes from the kernel
-//   parameter block (constant bank), the volume is written once.
+//   in registers across all views (or a block of views); per-view geometry
+//   comes from the kernel parameter block (constant bank); the projection taps
+//   come from a padded copy of the sinogram through L1; the volume is written
+//   once.
 #include <algorithm>
 #include <cstdio>
 
@@ -324,37 +329,6 @@ __device__ __forceinline__ void bp_column(const TS* __restrict__ p, int W,
   }
 }
 
-template <int GEOM, int ZC, typename TS, typename TV>
-__global__ void __launch_bounds__(256) bp_kernel(
-    const __grid_constant__ VoxArgs A, const TS* __restrict__ sino,
-    TV* __restrict__ vol, int accumulate) {
-  const int ix = blockIdx.x * 32 + threadIdx.x;
-  const int iy = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z0 = blockIdx.z * ZC;
-  if (ix >= A.W || iy >= A.W) return;
-  float acc[ZC];
-#pragma unroll
-  for (int j = 0; j < ZC; ++j) acc[j] = 0.f;
-  if (in_circle(ix, iy, A.hw)) {
-    const float x = (float)ix - ((float)A.hw + 0.5f);
-    const float y = (float)iy - ((float)A.hw + 0.5f);
-    for (int v = 0; v < A.nviews; ++v) {
-      const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
-      bp_column<GEOM, false, ZC>(sino + (size_t)(A.view0 + v) * A.P, A.W,
-                                 A.H, z0, g, acc);
-    }
-  }
-  const size_t base = (size_t)iy * A.W + ix;
-  const size_t sz = (size_t)A.W * A.W;
-#pragma unroll
-  for (int j = 0; j < ZC; ++j) {
-    if (z0 + j < A.H) {
-      TV* o = vol + base + (size_t)(z0 + j) * sz;
-      stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Backprojection from a padded sinogram.  Each view is copied once into
 // [H+4][W+4] with two extra rows and columns on every side: the edge value
@@ -524,33 +498,6 @@ __global__ void __launch_bounds__(256) bp_reduce_kernel(const float* __restrict_
 
 constexpr int kBpZc = 16;
 
-template <int GEOM, typename TS, typename TV>
-static void bp_go(const VoxArgs& a, const void* sino, void* vol, bool accum,
-                  cudaStream_t st) {
-  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + kBpZc - 1) / kBpZc);
-  bp_kernel<GEOM, kBpZc, TS, TV>
-      <<<grd, blk, 0, st>>>(a, (const TS*)sino, (TV*)vol, accum ? 1 : 0);
-}
-
-template <int GEOM>
-static cudaError_t bp_types(const VoxArgs& a, const void* sino, int stype,
-                            void* vol, int vtype, bool accum,
-                            cudaStream_t st) {
-  if (stype == kF32 && vtype == kF32)
-    bp_go<GEOM, float, float>(a, sino, vol, accum, st);
-  else if (stype == kF16 && vtype == kF16)
-    bp_go<GEOM, __half, __half>(a, sino, vol, accum, st);
-  else if (stype == kF16 && vtype == kF32)
-    bp_go<GEOM, __half, float>(a, sino, vol, accum, st);
-  else if (stype == kBF16 && vtype == kBF16)
-    bp_go<GEOM, __nv_bfloat16, __nv_bfloat16>(a, sino, vol, accum, st);
-  else if (stype == kBF16 && vtype == kF32)
-    bp_go<GEOM, __nv_bfloat16, float>(a, sino, vol, accum, st);
-  else
-    return cudaErrorInvalidValue;
-  return cudaGetLastError();
-}
-
 template <int GEOM, int ZC, typename TS, typename TV>
 static cudaError_t bp_pad_go(const VoxArgs& a, const void* sino, int Wp, void* vol, bool accum,
                              const BpShape& shp, float* part, cudaStream_t st) {
@@ -609,17 +556,6 @@ cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, i
   }
 }
 
-cudaError_t launch_bp(int geom, const VoxArgs& a, const void* sino,
-                      int stype, void* vol, int vtype, bool accumulate,
-                      cudaStream_t st) {
-  switch (geom) {
-    case 0: return bp_types<0>(a, sino, stype, vol, vtype, accumulate, st);
-    case 1: return bp_types<1>(a, sino, stype, vol, vtype, accumulate, st);
-    case 2: return bp_types<2>(a, sino, stype, vol, vtype, accumulate, st);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
 // ---------------------------------------------------------------------------
 // general3D BP (CUDAmex_general3D_BP.cu:61-188): ray-driven, two-corner
 // scatter with atomics.  Positions advance incrementally in binary32 and the
@@ -674,68 +610,10 @@ cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
 }
 
 // ---------------------------------------------------------------------------
-// OSC kernels.
+// OSC kernels.  The subset FP with the residual epilogue
+// (CUDAmex_oscIter.cu:140-271) is the slab kernel of k_slab.cu with border
+// addressing and step 0.5.
 // ---------------------------------------------------------------------------
-// FP of mu with border addressing and step 0.5 for every geometry
-// (CUDAmex_oscIter.cu:140-259), then pre' = pre e^-l - post and
-// post' = pre e^-l l (:262-268), written to the subset residual buffers.
-template <int GEOM, typename TM>
-__global__ void __launch_bounds__(256) osc_fp_kernel(
-    const __grid_constant__ RayArgs A, const TM* __restrict__ mx,
-    const TM* __restrict__ my, const float* __restrict__ pre,
-    const float* __restrict__ post, float* __restrict__ rpre,
-    float* __restrict__ rpost) {
-  const int view = blockIdx.x;
-  const int tiles_u = (A.det_w + 31) >> 5;
-  const int ix = (blockIdx.y % tiles_u) * 32 + threadIdx.x;
-  const int iy = (blockIdx.y / tiles_u) * blockDim.y + threadIdx.y;
-  const bool valid = ix < A.det_w && iy < A.det_h;
-  const Ray r = make_ray<GEOM>(A, view, min(ix, A.det_w - 1),
-                               min(iy, A.det_h - 1), nullptr);
-  const bool use_y = pick_y_layout<GEOM>(A, view, r, valid, my != nullptr);
-  if (!valid) return;
-  const float cx = r.cx - A.bx, cy = r.cy - A.by, cz = r.cz - A.bz;
-  float l;
-  if (use_y)
-    l = march<true>(my, A.S, A.S, A.Z, cy, cx, cz, r.dy, r.dx, r.dz, r.n);
-  else
-    l = march<true>(mx, A.S, A.S, A.Z, cx, cy, cz, r.dx, r.dy, r.dz, r.n);
-  l *= A.step;
-  const size_t pix = (size_t)iy * A.det_w + ix;
-  const size_t gi = (size_t)(A.view0 + view * A.vstride) * A.P + pix;
-  const float pv = __ldg(pre + gi), qv = __ldg(post + gi);
-  const float e = pv * expf(-l);
-  rpre[(size_t)view * A.P + pix] = e - qv;
-  rpost[(size_t)view * A.P + pix] = e * l;
-}
-
-cudaError_t launch_osc_fp(int geom, const RayArgs& a, const void* mx,
-                          const void* my, int mt, const float* pre,
-                          const float* post, float* rpre, float* rpost,
-                          cudaStream_t st) {
-  if (a.nviews <= 0) return cudaSuccess;
-  const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
-  dim3 blk(32, 8), grd(a.nviews, tiles);
-#define OSC_FP(G, T)                                                   \
-  osc_fp_kernel<G, T><<<grd, blk, 0, st>>>(a, (const T*)mx, (const T*)my, \
-                                           pre, post, rpre, rpost)
-  if (mt == kF32) {
-    if (geom == 0) OSC_FP(0, float);
-    else if (geom == 1) OSC_FP(1, float);
-    else OSC_FP(2, float);
-  } else if (mt == kF16) {
-    if (geom == 0) OSC_FP(0, __half);
-    else if (geom == 1) OSC_FP(1, __half);
-    else OSC_FP(2, __half);
-  } else {
-    if (geom == 0) OSC_FP(0, __nv_bfloat16);
-    else if (geom == 1) OSC_FP(1, __nv_bfloat16);
-    else OSC_FP(2, __nv_bfloat16);
-  }
-#undef OSC_FP
-  return cudaGetLastError();
-}
-
 // Dual BP of the residuals with border addressing (CUDAmex_oscIter.cu:305-356)
 // into register accumulators, then mu <- max(mu + mu*num/den, 0) inside the
 // circle (:119-134).  num/den never touch memory.
@@ -799,25 +677,9 @@ cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
 namespace mexct {
 
 // ---------------------------------------------------------------------------
-// Voxel-driven BP with projection footprints staged in shared memory.
-// A CTA owns a 32 x 8 x kSmZc voxel brick.  For a block of kSmVb views it
-// copies, per view, the rectangle of detector texels the brick projects onto
-// (u from the four column corners -- u is linear-fractional in (x, y), so its
-// extremes sit at the corners -- and v from the two end slices at the extreme
-// magnifications), with the reference's clamp applied at load time; the
-// threads then take all bilinear taps from shared memory.  A view whose
-// footprint exceeds the staging rectangle is sampled from global memory.
+// Batched BP (mexct_batch.h): persistent CTAs over (problem, brick) items.
 // ---------------------------------------------------------------------------
-constexpr int kSmZc = 16;        // z voxels per thread
-constexpr int kSmVb = 4;         // views per staged block
-constexpr int kSmU = 64;         // staging rectangle: columns (pitch kSmU + 1)
-constexpr int kSmV = 56;         //                    rows
-constexpr int kSmPitch = kSmU + 1;
-constexpr int kSmView = kSmV * kSmPitch;
-
-struct SmFoot {
-  int u0, v0, fb;
-};
+constexpr int kSmZc = 16;  // z voxels per thread (= kBpZc: same arithmetic)
 
 // Geometry of one brick job.
 struct BrickJob {
@@ -828,141 +690,6 @@ struct BrickJob {
   const Trig* trig;
   int bx0, by0, z0;
 };
-
-template <int GEOM, typename TS, typename TV>
-__device__ __forceinline__ void bp_brick(const BrickJob& A, const TS* __restrict__ sino,
-                                         TV* __restrict__ vol, int accumulate, float* stage,
-                                         SmFoot* foot) {
-  const int tid = threadIdx.x + 32 * threadIdx.y;
-  const int bx0 = A.bx0, by0 = A.by0;
-  const int ix = bx0 + threadIdx.x, iy = by0 + threadIdx.y;
-  const int z0 = A.z0;
-  const bool live = ix < A.W && iy < A.W && in_circle(ix, iy, A.hw);
-  float acc[kSmZc];
-#pragma unroll
-  for (int j = 0; j < kSmZc; ++j) acc[j] = 0.f;
-  const float hwf = (float)A.hw + 0.5f;
-  const float x = (float)ix - hwf, y = (float)iy - hwf;
-  const int xl = bx0, xh = min(bx0 + 31, A.W - 1), yl = by0, yh = min(by0 + 7, A.W - 1);
-  const int zl = z0, zh = min(z0 + kSmZc - 1, A.H - 1);
-  for (int vb = 0; vb < A.nviews; vb += kSmVb) {
-    const int nvb = min(kSmVb, A.nviews - vb);
-    // Footprints: warp w < nvb computes view vb + w (lanes 0-3: corners).
-    if (threadIdx.y < nvb) {
-      const Trig t = A.trig[vb + threadIdx.y];
-      const int lane = threadIdx.x;
-      float umn = 3e38f, umx = -3e38f, Umn = 3e38f, Umx = -3e38f;
-      if (lane < 4) {
-        const float cx = (float)((lane & 1) ? xh : xl) - hwf;
-        const float cy = (float)((lane & 2) ? yh : yl) - hwf;
-        const ColGeom<GEOM> g = col_geom<GEOM>(cx, cy, t, A.SR, A.v0, A.hw);
-        umn = umx = g.py;
-        Umn = Umx = (GEOM == 2) ? g.dpz : 1.f;
-      }
-#pragma unroll
-      for (int o = 2; o > 0; o >>= 1) {
-        umn = fminf(umn, __shfl_xor_sync(0xffffffffu, umn, o));
-        umx = fmaxf(umx, __shfl_xor_sync(0xffffffffu, umx, o));
-        Umn = fminf(Umn, __shfl_xor_sync(0xffffffffu, Umn, o));
-        Umx = fmaxf(Umx, __shfl_xor_sync(0xffffffffu, Umx, o));
-      }
-      if (lane == 0) {
-        float vmn, vmx;
-        if (GEOM == 2) {
-          const float a = ((float)zl - A.v0), b = ((float)zh - A.v0);
-          vmn = fminf(fminf(a * Umn, a * Umx), fminf(b * Umn, b * Umx)) + A.v0 + 0.5f;
-          vmx = fmaxf(fmaxf(a * Umn, a * Umx), fmaxf(b * Umn, b * Umx)) + A.v0 + 0.5f;
-        } else {
-          vmn = (float)zl + 0.5f;
-          vmx = (float)zh + 0.5f;
-        }
-        const float ulo = floorf(umn - 0.5f) - 1.f, uhi = floorf(umx - 0.5f) + 2.f;
-        const float vlo = floorf(vmn - 0.5f) - 1.f, vhi = floorf(vmx - 0.5f) + 2.f;
-        SmFoot f;
-        f.fb = !(isfinite(ulo) && isfinite(uhi) && isfinite(vlo) && isfinite(vhi) &&
-                 uhi - ulo + 1.f <= (float)kSmU && vhi - vlo + 1.f <= (float)kSmV &&
-                 fabsf(ulo) < 1e6f && fabsf(vlo) < 1e6f);
-        f.u0 = f.fb ? 0 : (int)ulo;
-        f.v0 = f.fb ? 0 : (int)vlo;
-        foot[threadIdx.y] = f;
-      }
-    }
-    __syncthreads();
-    // Stage: clamped texel (u, v) of view vb+q at stage[q][v - v0][u - u0].
-    for (int q = 0; q < nvb; ++q) {
-      const SmFoot f = foot[q];
-      if (f.fb) continue;
-      const TS* p = sino + (size_t)(A.view0 + vb + q) * A.P;
-      float* s = stage + q * kSmView;
-      for (int e = tid; e < kSmU * kSmV; e += 256) {
-        const int r = e / kSmU, c = e - r * kSmU;
-        const int u = min(max(f.u0 + c, 0), A.W - 1), v = min(max(f.v0 + r, 0), A.H - 1);
-        s[r * kSmPitch + c] = ldf(p + (size_t)v * A.W + u);
-      }
-    }
-    __syncthreads();
-    if (live) {
-      for (int q = 0; q < nvb; ++q) {
-        const SmFoot f = foot[q];
-        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[vb + q], A.SR, A.v0, A.hw);
-        if (f.fb) {
-          bp_column<GEOM, false, kSmZc>(sino + (size_t)(A.view0 + vb + q) * A.P, A.W, A.H, z0, g,
-                                        acc);
-          continue;
-        }
-        const float* s = stage + q * kSmView;
-        const float tu = g.py - 0.5f;
-        const float fu = floorf(tu);
-        const float au = tu - fu;
-        const float w0 = g.w * (1.f - au), w1 = g.w * au;
-        const int cu = (int)fu - f.u0;
-        if (GEOM < 2) {
-          // Par/fan rows are exact texel rows (pz = iz + 0.5).
-#pragma unroll
-          for (int j = 0; j < kSmZc; ++j) {
-            const int r = min(z0 + j, A.H - 1) - f.v0;
-            const int o = min(max(r * kSmPitch + cu, 0), kSmView - 2);
-            acc[j] = fmaf(w0, s[o], fmaf(w1, s[o + 1], acc[j]));
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < kSmZc; ++j) {
-            const float tv = fmaf((float)(z0 + j), g.dpz, g.pz0) - 0.5f;
-            const float fv = floorf(tv);
-            const float av = tv - fv;
-            const int o = min(max(((int)fv - f.v0) * kSmPitch + cu, 0), kSmView - kSmPitch - 2);
-            const float a = fmaf(w0, s[o], w1 * s[o + 1]);
-            const float b = fmaf(w0, s[o + kSmPitch], w1 * s[o + kSmPitch + 1]);
-            acc[j] = fmaf(1.f - av, a, fmaf(av, b, acc[j]));
-          }
-        }
-      }
-    }
-    __syncthreads();
-  }
-  if (ix < A.W && iy < A.W) {
-    const size_t base = (size_t)iy * A.W + ix;
-    const size_t sz = (size_t)A.W * A.W;
-#pragma unroll
-    for (int j = 0; j < kSmZc; ++j) {
-      if (z0 + j < A.H) {
-        TV* o = vol + base + (size_t)(z0 + j) * sz;
-        stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
-      }
-    }
-  }
-}
-
-template <int GEOM, typename TS, typename TV>
-__global__ void __launch_bounds__(256, 2) bp_smem_kernel(
-    const __grid_constant__ VoxArgs A, const TS* __restrict__ sino,
-    TV* __restrict__ vol, int accumulate) {
-  extern __shared__ float stage[];  // kSmVb * kSmView floats
-  __shared__ SmFoot foot[kSmVb];
-  BrickJob J{A.W, A.H, A.nviews, A.view0, A.v0, A.SR, A.hw, A.P, A.trig,
-             (int)blockIdx.x * 32, (int)blockIdx.y * 8, (int)blockIdx.z * kSmZc};
-  bp_brick<GEOM, TS, TV>(J, sino, vol, accumulate, stage, foot);
-}
 
 // One 32 x 8 x kSmZc brick through L1 (the body of bp_kernel with the view
 // geometry read from a device table): the batched BP computes exactly what the
@@ -1030,40 +757,6 @@ cudaError_t launch_bp_batch(const BatchBp* d_probs, int nprob, long long total,
   if (total <= 0) return cudaSuccess;
   bp_batch_kernel<<<ctas, dim3(32, 8), 0, st>>>(d_probs, nprob, total, counter);
   return cudaGetLastError();
-}
-
-template <int GEOM, typename TS, typename TV>
-static cudaError_t bp_smem_go(const VoxArgs& a, const void* sino, void* vol, bool accum,
-                              cudaStream_t st) {
-  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + kSmZc - 1) / kSmZc);
-  const int smem = kSmVb * kSmView * (int)sizeof(float);
-  static bool attr_set = false;  // once per instantiation
-  if (!attr_set) {
-    const cudaError_t e = cudaFuncSetAttribute(
-        bp_smem_kernel<GEOM, TS, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
-  bp_smem_kernel<GEOM, TS, TV>
-      <<<grd, blk, smem, st>>>(a, (const TS*)sino, (TV*)vol, accum ? 1 : 0);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_bp_smem(int geom, const VoxArgs& a, const void* sino, int stype,
-                           void* vol, int vtype, bool accumulate, cudaStream_t st) {
-#define BPS(G, S, T) return bp_smem_go<G, S, T>(a, sino, vol, accumulate, st)
-#define BPG(S, T)                          \
-  if (geom == 0) BPS(0, S, T);             \
-  if (geom == 1) BPS(1, S, T);             \
-  BPS(2, S, T)
-  if (stype == kF32 && vtype == kF32) { BPG(float, float); }
-  else if (stype == kF16 && vtype == kF16) { BPG(__half, __half); }
-  else if (stype == kF16 && vtype == kF32) { BPG(__half, float); }
-  else if (stype == kBF16 && vtype == kBF16) { BPG(__nv_bfloat16, __nv_bfloat16); }
-  else if (stype == kBF16 && vtype == kF32) { BPG(__nv_bfloat16, float); }
-  return cudaErrorInvalidValue;
-#undef BPG
-#undef BPS
 }
 
 }  // namespace mexct

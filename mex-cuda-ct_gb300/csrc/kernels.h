@@ -124,30 +124,19 @@ bool bp_shape_valid(const BpShape& s);
 cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, int stype,
                              void* vol, int vtype, bool accumulate, const BpShape& shp,
                              float* part, cudaStream_t st);
-cudaError_t launch_bp(int geom, const VoxArgs& a, const void* sino,
-                      int sino_type, void* vol, int vol_type, bool accumulate,
-                      cudaStream_t st);
 
-// BP with per-brick projection footprints staged in shared memory.
-cudaError_t launch_bp_smem(int geom, const VoxArgs& a, const void* sino,
-                           int sino_type, void* vol, int vol_type,
-                           bool accumulate, cudaStream_t st);
-
+// general3D ray-driven two-corner scatter BP (CUDAmex_general3D_BP.cu:61-188).
 cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
                           const float* pts, float* vol, cudaStream_t st);
 
-// OSC: FP of mu for the subset's views with the residual epilogue
-// (CUDAmex_oscIter.cu:140-271) and the dual BP + update
-// (CUDAmex_oscIter.cu:94-136,272-358).
-cudaError_t launch_osc_fp(int geom, const RayArgs& a, const void* mu_x,
-                          const void* mu_y, int mu_type, const float* pre,
-                          const float* post, float* rpre, float* rpost,
-                          cudaStream_t st);
+// OSC dual BP + update (CUDAmex_oscIter.cu:94-136,272-358); the subset FP with
+// the residual epilogue (:140-271) is launch_fp_slab with osc = true.
 cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
                                  const float* rpre, const float* rpost,
                                  void* mu, int mu_type, cudaStream_t st);
 
-// TV (CUDAmex_TVmin_3D.cu:101-234).  tv_norm computes ||g||^2 in FP64 and the
+// TV (CUDAmex_TVmin_3D.cu:101-234).  tv_norm computes ||g||^2 (FP64 above the
+// per-thread level) and the
 // step scale -c/||g|| into *scale; tv_update writes y = x + scale*g(x).
 size_t tv_partials_needed(int Nx, int Ny, int Nz);
 cudaError_t launch_tv_norm(const void* x, int x_type, int Nx, int Ny, int Nz,
