@@ -337,8 +337,6 @@ __device__ __forceinline__ void bp_column(const TS* __restrict__ p, int W,
 // image read pad values, which is what the clamp / border texture fetch
 // returns -- instead of clamping both taps of both axes into the image.
 // ---------------------------------------------------------------------------
-constexpr int kSinoPad = 2;
-
 template <typename T, bool BORDER>
 __global__ void __launch_bounds__(256) pad_sino_kernel(const T* __restrict__ in, int W, int H,
                                                        T* __restrict__ out, int Wp) {
@@ -357,7 +355,6 @@ __global__ void __launch_bounds__(256) pad_sino_kernel(const T* __restrict__ in,
   out[(v * Hp + (y + kSinoPad)) * Wp + (x + kSinoPad)] = val;
 }
 
-__host__ __device__ int sino_pad_pitch(int W) { return W + 2 * kSinoPad; }
 size_t sino_pad_elems(int W, int H, int nviews) {
   return (size_t)sino_pad_pitch(W) * (H + 2 * kSinoPad) * nviews;
 }
@@ -620,7 +617,8 @@ cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
 template <int GEOM, int ZC, typename TM>
 __global__ void __launch_bounds__(256) osc_bp_update_kernel(
     const __grid_constant__ VoxArgs A, const float* __restrict__ rpre,
-    const float* __restrict__ rpost, TM* __restrict__ mu) {
+    const float* __restrict__ rpost, TM* __restrict__ mu, TM* __restrict__ padx,
+    TM* __restrict__ pady, int Pf) {
   const int ix = blockIdx.x * 32 + threadIdx.x;
   const int iy = blockIdx.y * blockDim.y + threadIdx.y;
   const int z0 = blockIdx.z * ZC;
@@ -631,30 +629,44 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
   for (int j = 0; j < ZC; ++j) num[j] = den[j] = 0.f;
   const float x = (float)ix - ((float)A.hw + 0.5f);
   const float y = (float)iy - ((float)A.hw + 0.5f);
+  const int Wp = sino_pad_pitch(A.W);
+  const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
   for (int v = 0; v < A.nviews; ++v) {
     const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
-    bp_column<GEOM, true, ZC>(rpre + (size_t)v * A.P, A.W, A.H, z0, g, num);
-    bp_column<GEOM, true, ZC>(rpost + (size_t)v * A.P, A.W, A.H, z0, g, den);
+    // zero frame = border addressing (CUDAmex_oscIter.cu:419-425)
+    bp_column_pad<GEOM, ZC>(rpre + (size_t)v * vstride, A.W, A.H, Wp, z0, g, num);
+    bp_column_pad<GEOM, ZC>(rpost + (size_t)v * vstride, A.W, A.H, Wp, z0, g, den);
   }
   const size_t base = (size_t)iy * A.W + ix;
   const size_t sz = (size_t)A.W * A.W;
+  const size_t Ps = (size_t)A.W + 2;
 #pragma unroll
   for (int j = 0; j < ZC; ++j) {
-    if (z0 + j < A.H) {
-      TM* o = mu + base + (size_t)(z0 + j) * sz;
+    const int z = z0 + j;
+    if (z < A.H) {
+      TM* o = mu + base + (size_t)z * sz;
       const float f = ldp(o);
-      stf(o, fmaxf(f + (f * num[j] / den[j]), 0.f));
+      const float m = fmaxf(f + (f * num[j] / den[j]), 0.f);
+      stf(o, m);
+      if (padx) {
+        // the slab FP's padded layouts: x-fastest and y-fastest, frame of one
+        const size_t zp = (size_t)(z + 1) * Ps;
+        stf(padx + (size_t)(ix + 1) + (size_t)Pf * ((size_t)(iy + 1) + zp), m);
+        stf(pady + (size_t)(iy + 1) + (size_t)Pf * ((size_t)(ix + 1) + zp), m);
+      }
     }
   }
 }
 
 cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
                                  const float* rpre, const float* rpost,
-                                 void* mu, int mt, cudaStream_t st) {
+                                 void* mu, int mt, void* padx, void* pady, int Pf,
+                                 cudaStream_t st) {
   constexpr int ZC = 8;
   dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + ZC - 1) / ZC);
-#define OSC_BP(G, T) \
-  osc_bp_update_kernel<G, ZC, T><<<grd, blk, 0, st>>>(a, rpre, rpost, (T*)mu)
+#define OSC_BP(G, T)                                                                 \
+  osc_bp_update_kernel<G, ZC, T><<<grd, blk, 0, st>>>(a, rpre, rpost, (T*)mu, (T*)padx, \
+                                                      (T*)pady, Pf)
   if (mt == kF32) {
     if (geom == 0) OSC_BP(0, float);
     else if (geom == 1) OSC_BP(1, float);

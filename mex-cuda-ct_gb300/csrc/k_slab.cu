@@ -582,8 +582,12 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       // CUDAmex_oscIter.cu:262-268: pre' = pre e^-l - post, post' = pre e^-l l.
       const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
       const float ehat = pv * expf(-l);
-      E.rpre[(size_t)J.lview * J.P + pix] = ehat - qv;
-      E.rpost[(size_t)J.lview * J.P + pix] = ehat * l;
+      // padded residual view [H+4][W+4] (zero frame kept by the caller)
+      const int Wp = sino_pad_pitch(J.det_w);
+      const size_t ri = ((size_t)J.lview * (J.det_h + 2 * kSinoPad) + (iy + kSinoPad)) * Wp +
+                        (ix + kSinoPad);
+      E.rpre[ri] = ehat - qv;
+      E.rpost[ri] = ehat * l;
     }
   }
   __syncthreads();

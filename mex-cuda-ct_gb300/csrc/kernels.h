@@ -51,8 +51,8 @@ cudaError_t launch_fp(int geom, bool border, const RayArgs& a,
 struct SlabEpi {
   const float* pre;  // OSC: pre/post counts and residual outputs
   const float* post;
-  float* rpre;
-  float* rpost;
+  float* rpre;       // residuals in the padded-sinogram layout of each view:
+  float* rpost;      // [H+4][W+4] with a zero frame (border addressing)
   unsigned* err;     // set to non-zero when a bounded wait gave up
 };
 int slab_pitch(int W);
@@ -109,7 +109,8 @@ cudaError_t launch_fp_tex(int geom, const RayArgs& a,
 
 // Padded sinogram for the voxel-driven BP: [nviews][H+4][W+4], edge values
 // replicated (clamp) or zero (border) in the two-texel frame.
-__host__ __device__ int sino_pad_pitch(int W);
+constexpr int kSinoPad = 2;  // frame width of padded sinogram views
+__host__ __device__ inline int sino_pad_pitch(int W) { return W + 2 * kSinoPad; }
 size_t sino_pad_elems(int W, int H, int nviews);
 cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews, bool border,
                             void* out, cudaStream_t st);
@@ -131,9 +132,13 @@ cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
 
 // OSC dual BP + update (CUDAmex_oscIter.cu:94-136,272-358); the subset FP with
 // the residual epilogue (:140-271) is launch_fp_slab with osc = true.
+// rpre/rpost: padded residual views (sino_pad_pitch layout, zero frame).
+// With padx/pady non-null the updated mu is also written into the padded
+// volumes of the slab FP (pitch Pf), so the next subset needs no padding pass.
 cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
                                  const float* rpre, const float* rpost,
-                                 void* mu, int mu_type, cudaStream_t st);
+                                 void* mu, int mu_type, void* padx, void* pady, int Pf,
+                                 cudaStream_t st);
 
 // TV (CUDAmex_TVmin_3D.cu:101-234).  tv_norm computes ||g||^2 (FP64 above the
 // per-thread level) and the

@@ -339,10 +339,19 @@ mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
     return set_err(MEXCT_ERR_UNSUPPORTED, "osc_iter: %d views in one subset (max %d)", maxv, kMaxViews);
   if (!c) return MEXCT_OK;  // validate only
   (void)N;
-  if (maxv > 0) {
-    MEXCT_TRY_CUDA(c->r1.ensure(P * maxv * sizeof(float)), "osc_iter: workspace");
-    MEXCT_TRY_CUDA(c->r2.ensure(P * maxv * sizeof(float)), "osc_iter: workspace");
-  }
+  (void)P;
+  // Residual views in the padded layout with a zero frame (border addressing).
+  const size_t rbytes = sino_pad_elems(W, H, std::max(maxv, 1)) * sizeof(float);
+  MEXCT_TRY_CUDA(c->r1.ensure(rbytes), "osc_iter: workspace");
+  MEXCT_TRY_CUDA(c->r2.ensure(rbytes), "osc_iter: workspace");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(c->r1.p, 0, rbytes, st), "osc_iter: workspace");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(c->r2.p, 0, rbytes, st), "osc_iter: workspace");
+  // mu is padded (zero frame) once; every subset update rewrites the padded
+  // copies along with mu.
+  CUtensorMap mx, my;
+  int Pf = 0;
+  mexct_status ps = prepare_slab(c, d_mu, mu_type, W, H, /*border=*/true, &mx, &my, &Pf, st);
+  if (ps) return ps;
   std::unique_ptr<RayArgs> ra(new RayArgs);
   std::unique_ptr<VoxArgs> va(new VoxArgs);
   fill_std_rays(*ra, W, H, sad, geom, /*osc=*/true);
@@ -359,10 +368,6 @@ mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
       va->trig[i] = ra->trig[i];
     }
     if (nv > 0) {
-      CUtensorMap mx, my;
-      int Pf = 0;
-      mexct_status ps = prepare_slab(c, d_mu, mu_type, W, H, /*border=*/true, &mx, &my, &Pf, st);
-      if (ps) return ps;
       SlabEpi e{d_pre, d_post, c->r1.as<float>(), c->r2.as<float>(), c->err.as<unsigned>()};
       MEXCT_TRY_CUDA(launch_fp_slab(geom, true, true, *ra, mx, my, c->padx.p, c->pady.p, Pf,
                                     mu_type, nullptr, kF32, e, st),
@@ -371,7 +376,7 @@ mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
     // An empty subset still runs the update: num = den = 0 gives
     // max(mu + mu*0/0, 0) = 0 inside the circle, as in the reference.
     MEXCT_TRY_CUDA(launch_osc_bp_update(geom, *va, c->r1.as<float>(), c->r2.as<float>(),
-                                        d_mu, mu_type, st),
+                                        d_mu, mu_type, c->padx.p, c->pady.p, Pf, st),
                    "osc_iter: bp/update");
   }
   return MEXCT_OK;

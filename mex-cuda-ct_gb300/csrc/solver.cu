@@ -118,6 +118,13 @@ mexct_status enqueue_iteration(mexct_osctv* s, bool k_gt1, int nsub,
   std::unique_ptr<VoxArgs> va(new VoxArgs);
   fill_std_rays(*ra, s->W, s->H, s->sad, s->geom, /*osc=*/true);
   fill_vox(*va, s->W, s->H, s->sad);
+  // mu is padded (zero frame) once per iteration; every subset update
+  // rewrites the padded copies along with mu.
+  CUtensorMap mx, my;
+  int Pf = 0;
+  mexct_status ps = prepare_slab_bufs(s->padx, s->pady, s->err, s->mu.p, s->mu_type, s->W, s->H,
+                                      /*border=*/true, &mx, &my, &Pf, st);
+  if (ps) return ps;
   for (int si = 0; si < nsub; ++si) {
     const int sel = picks[si];
     const int nv = (sel < 0 || sel >= s->nP) ? 0 : (s->nP - 1 - sel) / nsub + 1;
@@ -130,11 +137,6 @@ mexct_status enqueue_iteration(mexct_osctv* s, bool k_gt1, int nsub,
       va->trig[i] = ra->trig[i];
     }
     if (nv > 0) {
-      CUtensorMap mx, my;
-      int Pf = 0;
-      mexct_status ps = prepare_slab_bufs(s->padx, s->pady, s->err, s->mu.p, s->mu_type, s->W,
-                                          s->H, /*border=*/true, &mx, &my, &Pf, st);
-      if (ps) return ps;
       SlabEpi e{s->pre.as<float>(), s->post.as<float>(), s->r1.as<float>(), s->r2.as<float>(),
                 s->err.as<unsigned>()};
       MEXCT_TRY_CUDA(launch_fp_slab(s->geom, true, true, *ra, mx, my, s->padx.p, s->pady.p, Pf,
@@ -142,7 +144,7 @@ mexct_status enqueue_iteration(mexct_osctv* s, bool k_gt1, int nsub,
                      "osctv: fp");
     }
     MEXCT_TRY_CUDA(launch_osc_bp_update(s->geom, *va, s->r1.as<float>(), s->r2.as<float>(),
-                                        s->mu.p, s->mu_type, st),
+                                        s->mu.p, s->mu_type, s->padx.p, s->pady.p, Pf, st),
                    "osctv: bp/update");
   }
   (void)P;
@@ -228,8 +230,14 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   MEXCT_TRY_CUDA(s->pady.ensure_async(pb, a), "osctv_create: padded mu");
   MEXCT_TRY_CUDA(s->pre.ensure_async(M * 4, a), "osctv_create: pre");
   MEXCT_TRY_CUDA(s->post.ensure_async(M * 4, a), "osctv_create: post");
-  MEXCT_TRY_CUDA(s->r1.ensure_async(P * maxv * 4, a), "osctv_create: residual");
-  MEXCT_TRY_CUDA(s->r2.ensure_async(P * maxv * 4, a), "osctv_create: residual");
+  // residual views in the padded layout; their zero frame (border addressing)
+  // is written once here and never touched again
+  const size_t rb = sino_pad_elems(W, H, (int)maxv) * 4;
+  (void)P;
+  MEXCT_TRY_CUDA(s->r1.ensure_async(rb, a), "osctv_create: residual");
+  MEXCT_TRY_CUDA(s->r2.ensure_async(rb, a), "osctv_create: residual");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->r1.p, 0, rb, a), "osctv_create: residual");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->r2.p, 0, rb, a), "osctv_create: residual");
   MEXCT_TRY_CUDA(s->red.ensure_async(parts * sizeof(double), a), "osctv_create: reduction");
   MEXCT_TRY_CUDA(s->err.ensure_async(64, a), "osctv_create: error word");
   MEXCT_TRY_CUDA(s->cnt.ensure_async(64, a), "osctv_create: counter");
