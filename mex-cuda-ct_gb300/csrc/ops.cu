@@ -208,7 +208,9 @@ mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
                          int H, float sad, const float* angles, int nP,
                          int geom, void* d_out, int ot, int variant,
                          cudaStream_t st) {
-  if (!d_vol || !d_out || !angles) return set_err(MEXCT_ERR_ARG, "fp: NULL pointer");
+  // With nP == 0 there is no output and no angle to read (an empty MATLAB array
+  // may come with a NULL data pointer).
+  if (!d_vol || (nP > 0 && (!d_out || !angles))) return set_err(MEXCT_ERR_ARG, "fp: NULL pointer");
   if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "fp: bad volume dims %d x %d x %d", W, W, H);
   if (nP < 0) return set_err(MEXCT_ERR_ARG, "fp: nProj must be >= 0 (got %d)", nP);
   if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "fp: invalid geometry %d", geom);
@@ -233,7 +235,7 @@ mexct_status fp_dev_impl(mexct_ctx* c, const void* d_vol, int vt, int W,
 mexct_status bp_dev_impl(mexct_ctx* c, const void* d_sino, int stype, int W,
                          int H, int nP, float sad, const float* angles,
                          int geom, void* d_vol, int vt, cudaStream_t st) {
-  if (!d_sino || !d_vol || (!angles && nP > 0)) return set_err(MEXCT_ERR_ARG, "bp: NULL pointer");
+  if (!d_vol || (nP > 0 && (!d_sino || !angles))) return set_err(MEXCT_ERR_ARG, "bp: NULL pointer");
   if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "bp: bad sinogram dims %d x %d", W, H);
   if (nP < 0) return set_err(MEXCT_ERR_ARG, "bp: bad view count %d", nP);
   if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "bp: invalid geometry %d", geom);
