@@ -35,6 +35,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include "kernels.h"
 
@@ -522,26 +523,30 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     const float alo_f = (float)alo, ahi_f = (float)ahi;
     const float off = -(float)(plan_z0(pk) * kPlane + alo * kBoxF + plan_f0(pk));
     const float2 off2 = make_float2(off, off);
-    while (k < n) {
-      // Samples k and k+1: positions fma(k, d, t0) on both lanes of a pair.
-      const float k0 = (float)k;
-      const float2 kk = make_float2(k0, k0 + 1.0f);
-      const float2 ta2 = __ffma2_rn(kk, da2, ta02);
-      const float fa0 = floorf(ta2.x);
-      if (dir > 0 ? fa0 > ahi_f : fa0 < alo_f) break;
-      const float fa1 = floorf(ta2.y);
-      const bool two = (k + 1 < n) && (dir > 0 ? fa1 <= ahi_f : fa1 >= alo_f);
-      const float2 tf2 = __ffma2_rn(kk, df2, tf02);
-      const float2 fa2 = make_float2(fa0, fa1);
-      const float2 ff2 = make_float2(floorf(tf2.x), floorf(tf2.y));
-      float2 fz2 = fz02, wz2 = wz02;
-      if (Z2) {
-        const float2 tz2 = __ffma2_rn(kk, dz2, tz02);
-        fz2 = make_float2(floorf(tz2.x), floorf(tz2.y));
-        wz2 = sub2(tz2, fz2);
-      }
-      const float2 wa2 = sub2(ta2, fa2), wf2 = sub2(tf2, ff2);
-      if (from_smem) {
+    // The sweep direction and the sample source are uniform over a slab, so
+    // each gets its own loop: the shared-memory loops compare against one
+    // bound with no per-sample selects or source branch.
+    auto smem_loop = [&](auto dirc) {
+      constexpr int D = decltype(dirc)::value;
+      while (k < n) {
+        // Samples k and k+1: positions fma(k, d, t0) on both lanes of a pair.
+        const float k0 = (float)k;
+        const float2 kk = make_float2(k0, k0 + 1.0f);
+        const float2 ta2 = __ffma2_rn(kk, da2, ta02);
+        const float fa0 = floorf(ta2.x);
+        if (D > 0 ? fa0 > ahi_f : fa0 < alo_f) break;
+        const float fa1 = floorf(ta2.y);
+        const bool two = (k + 1 < n) && (D > 0 ? fa1 <= ahi_f : fa1 >= alo_f);
+        const float2 tf2 = __ffma2_rn(kk, df2, tf02);
+        const float2 fa2 = make_float2(fa0, fa1);
+        const float2 ff2 = make_float2(floorf(tf2.x), floorf(tf2.y));
+        float2 fz2 = fz02, wz2 = wz02;
+        if (Z2) {
+          const float2 tz2 = __ffma2_rn(kk, dz2, tz02);
+          fz2 = make_float2(floorf(tz2.x), floorf(tz2.y));
+          wz2 = sub2(tz2, fz2);
+        }
+        const float2 wa2 = sub2(ta2, fa2), wf2 = sub2(tf2, ff2);
         const float2 x2 = __ffma2_rn(fz2, make_float2((float)kPlane, (float)kPlane),
                                      __ffma2_rn(fa2, make_float2((float)kBoxF, (float)kBoxF),
                                                 __fadd2_rn(ff2, off2)));
@@ -553,22 +558,33 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
           const float2 v = sample_pair<Z2>(b + i0, b + i1, kBoxF, kPlane, wa2, wf2, wz2);
           acc += v.x;
           acc += v.y;
+          k += 2;
         } else {
           acc += sample_at<Z2>(b + i0, kBoxF, kPlane, wa2.x, wf2.x, wz2.x);
-        }
-      } else {
-        // Fallback: the same taps from the padded volume in global memory.
-        for (int q = 0; q < (two ? 2 : 1); ++q) {
-          const float fq = q ? fa2.y : fa2.x, ffq = q ? ff2.y : ff2.x, fzq = q ? fz2.y : fz2.x;
-          const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
-          const int gz = min(max((int)fzq, 0), Pz - 2);
-          acc += sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
-                               Pf * Ps, q ? wa2.y : wa2.x, q ? wf2.y : wf2.x,
-                               q ? wz2.y : wz2.x);
+          k += 1;
+          break;
         }
       }
-      k += two ? 2 : 1;
-      if (!two) break;
+    };
+    if (from_smem) {
+      if (dir > 0) smem_loop(std::integral_constant<int, 1>{});
+      else smem_loop(std::integral_constant<int, -1>{});
+    } else {
+      // Fallback: the same samples, taps from the padded volume in global memory.
+      while (k < n) {
+        const float kq = (float)k;
+        const float tq = fmaf(kq, da, ta0);
+        const float fq = floorf(tq);
+        if (dir > 0 ? fq > ahi_f : fq < alo_f) break;
+        const float tfq = fmaf(kq, df, tf0);
+        const float tzq = Z2 ? fmaf(kq, dz, tz0) : tz0;
+        const float ffq = floorf(tfq), fzq = floorf(tzq);
+        const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
+        const int gz = min(max((int)fzq, 0), Pz - 2);
+        acc += sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
+                             Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
+        ++k;
+      }
     }
     __syncthreads();
   }
