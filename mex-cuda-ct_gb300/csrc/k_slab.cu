@@ -16,10 +16,12 @@
 // constant-offset loads.  Two buffers and two mbarriers overlap the copy of
 // slab j+1 with the sampling of slab j.  Shapes (measured on cone 512^3 x
 // 720): 4 taps per slab, boxes of 64 (f) x 5 (a) x <=20 (z) elements that
-// hold 99.9% of the bundles, 4 CTAs of 256 threads per SM (<=64 registers,
-// 50 KB of buffers each); 3 taps (4 or 5 CTAs/SM) and 2 taps (5 CTAs/SM)
-// were 12-32% slower.  Planning all slabs up front instead of one slab ahead
-// in warp 0 took 15% off the sweep.
+// hold 99.9% of the bundles, copied as one 20-row box per slab (2-, 4-, 5-
+// and 10-row boxes for the rows the bundle needs were 1-5% slower: the
+// issuing thread stalls its warp), 4 CTAs of 256 threads per SM (<=64
+// registers, 50 KB of buffers each); 3 taps (4 or 5 CTAs/SM) and 2 taps
+// (5 CTAs/SM) were 12-32% slower.  Planning all slabs up front instead of one
+// slab ahead in warp 0 took 15% off the sweep.
 //
 // The padded volume has a one-voxel border (replicated edge for clamp
 // addressing, zeros for border addressing) and a fast-axis pitch rounded up
@@ -209,7 +211,7 @@ constexpr int kSlabCtas = 4;                  // resident CTAs per SM (launch bo
 constexpr int kSlabT = 4;                     // a-taps per slab
 constexpr int kSlabA = kSlabT + 1;            // a-planes in a box
 constexpr int kBoxF = 64;                     // box extent along f (elements)
-constexpr int kBoxZ = 2;                      // z rows per TMA box
+constexpr int kBoxZ = 20;                     // z rows per TMA box: one copy per slab
 constexpr int kBZ = 20;                       // z rows per slab buffer (even)
 constexpr int kPlane = kSlabA * kBoxF;        // elements per z row of a buffer
 constexpr int kBufElems = kBZ * kPlane;       // elements per buffer
