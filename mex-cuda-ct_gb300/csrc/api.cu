@@ -45,16 +45,30 @@ mexct_status cuda_err(cudaError_t e, const char* what) {
 
 void Buf::release() {
   if (p) {
-    if (ast) cudaFreeAsync(p, ast);
+    // Memory from cudaMallocAsync is freed in the order of its stream, after
+    // the work queued there (cudaFree would not wait for it).
+    if (is_async) cudaFreeAsync(p, ast);
     else cudaFree(p);
   }
   p = nullptr;
   n = 0;
   ast = nullptr;
+  is_async = false;
 }
 
 cudaError_t Buf::ensure_async(size_t bytes, cudaStream_t st) {
   if (bytes <= n && p) return cudaSuccess;
+  if (p && is_async && ast != st) {
+    // The old block is freed on st once the work queued on its own stream
+    // is done.
+    cudaEvent_t ev = nullptr;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess) {
+      cudaEventRecord(ev, ast);
+      cudaStreamWaitEvent(st, ev, 0);
+      cudaEventDestroy(ev);
+    }
+    ast = st;
+  }
   release();
   if (bytes == 0) bytes = 16;
   cudaError_t e = cudaMallocAsync(&p, bytes, st);
@@ -66,6 +80,7 @@ cudaError_t Buf::ensure_async(size_t bytes, cudaStream_t st) {
   }
   n = bytes;
   ast = st;
+  is_async = true;
   return cudaSuccess;
 }
 

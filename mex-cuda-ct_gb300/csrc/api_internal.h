@@ -18,7 +18,11 @@ namespace mexct {
 struct Buf {
   void* p = nullptr;
   size_t n = 0;
-  cudaStream_t ast = nullptr;  // set when allocated stream-ordered
+  // Stream-ordered allocation: the stream it was allocated on (may be the
+  // legacy default stream, handle 0) and whether it was.  Such memory must be
+  // released with cudaFreeAsync: cudaFree does not wait for queued work.
+  cudaStream_t ast = nullptr;
+  bool is_async = false;
   cudaError_t ensure(size_t bytes);
   // Stream-ordered allocation (cudaMallocAsync): no device-wide
   // synchronisation on allocation or release, so work on other streams keeps

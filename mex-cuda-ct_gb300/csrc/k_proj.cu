@@ -691,7 +691,7 @@ namespace mexct {
 // ---------------------------------------------------------------------------
 // Batched BP (mexct_batch.h): persistent CTAs over (problem, brick) items.
 // ---------------------------------------------------------------------------
-constexpr int kSmZc = 16;  // z voxels per thread (= kBpZc: same arithmetic)
+constexpr int kSmZc = 8;  // z voxels per thread (any ZC gives the same per-voxel arithmetic)
 
 // Geometry of one brick job.
 struct BrickJob {
