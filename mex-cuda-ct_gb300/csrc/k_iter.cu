@@ -76,8 +76,8 @@ __device__ __forceinline__ bool finish_partials(double mine, double* partials,
 //   g_i = (a+b+c)_i r_i - a_{i+1} r_{i+1} - b_{i+sy} r_{i+sy} - c_{i+sz} r_{i+sz}
 // (CUDAmex_TVmin_3D.cu:121-152: the second to fourth terms are the first
 // term's components at the +x, +y and +z neighbours), so each voxel's
-// (a, b, c, r) is computed once (one sqrt, one reciprocal) instead of four
-// times.  A CTA of 32 x 8 threads sweeps a column tile along z: thread
+// (a, b, c, r) is computed once (one reciprocal square root, one reciprocal)
+// instead of four times.  A CTA of 32 x 8 threads sweeps a column tile along z: thread
 // (tx, ty) computes q at its column in every plane, takes the +x neighbour's
 // value by a shuffle, the +y neighbour's from shared memory (one barrier per
 // plane) and the +z neighbour's from its next plane, and writes the voxel
@@ -125,7 +125,13 @@ __device__ __forceinline__ void tv_sweep(const T* __restrict__ v, int Nx, int Ny
     float q0 = 0.f, qa = 0.f, qb = 0.f, qc = 0.f;
     if (qcol && p >= 1 && p < Nz) {
       const float a = xcur - xm, b = xcur - xym, c = xcur - xprev;
-      const float r = __frcp_rn(1.0e-6f + __fsqrt_rn(fmaf(c, c, fmaf(b, b, a * a))));
+      // |(a,b,c)| from the hardware reciprocal square root and 1/(eps + |.|)
+      // from the hardware reciprocal (a few ulp each, far inside the 1e-5
+      // bound; the IEEE-rounded forms cost ~4x the instructions of the whole
+      // stencil).  s = 0 (flat region) gives |.| = 0 as it must.
+      const float s2 = fmaf(c, c, fmaf(b, b, a * a));
+      const float nrm = s2 > 0.f ? s2 * rsqrtf(s2) : 0.f;
+      const float r = __fdividef(1.0f, 1.0e-6f + nrm);
       q0 = ((a + b) + c) * r;
       qa = a * r;
       qb = b * r;
