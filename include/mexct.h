@@ -64,6 +64,19 @@ mexct_status mexct_ctx_destroy(mexct_ctx* ctx);
 /* Release the context's workspaces (they are re-created on demand). */
 mexct_status mexct_ctx_trim(mexct_ctx* ctx);
 
+/* Bounded waits (no counterpart in the reference).  The slab forward projector
+ * waits on its shared-memory copies with a wall-clock limit; a wait that runs
+ * out records a flag in the context's device error word and the CTA samples
+ * from global memory instead, so the result is unchanged and nothing hangs.
+ * set_wait_limit: us > 0 limit per wait in microseconds, 0 give up at once
+ * (diagnostics: every wait that is not already satisfied falls back), < 0 the
+ * default (2 s).  device_errors: the error word's flags (bit 0: a wait gave
+ * up; bit 1: a copy issued before that did not land within 2 s either), read
+ * with a blocking copy once the covered work has finished (e.g. after
+ * synchronising its stream); clear != 0 zeroes it. */
+mexct_status mexct_ctx_set_wait_limit(mexct_ctx* ctx, int us);
+mexct_status mexct_ctx_device_errors(mexct_ctx* ctx, unsigned* flags, int clear);
+
 /* ---- MEX-equivalent host entry points --------------------------------- */
 
 /* fp = CUDAmex_FP(vol, SAD, angles, nProj, geomFlag)

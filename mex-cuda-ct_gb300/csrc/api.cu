@@ -214,6 +214,31 @@ mexct_status mexct_ctx_trim(mexct_ctx* c) {
   return MEXCT_OK;
 }
 
+mexct_status mexct_ctx_set_wait_limit(mexct_ctx* ctx, int us) {
+  mexct_ctx* c = resolve(ctx);
+  if (!c) return set_err(MEXCT_ERR_CUDA, "set_wait_limit: no CUDA device / context");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  c->wait_us = us < 0 ? 0 : (us == 0 ? -1 : us);
+  return MEXCT_OK;
+}
+
+mexct_status mexct_ctx_device_errors(mexct_ctx* ctx, unsigned* flags, int clear) {
+  if (!flags) return set_err(MEXCT_ERR_ARG, "device_errors: flags is NULL");
+  mexct_ctx* c = resolve(ctx);
+  if (!c) return set_err(MEXCT_ERR_CUDA, "device_errors: no CUDA device / context");
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  *flags = 0;
+  if (!c->err.p) return MEXCT_OK;  // no slab launch yet
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaMemcpy(flags, c->err.p, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && clear) e = cudaMemset(c->err.p, 0, sizeof(unsigned));
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return cuda_err(e, "device_errors");
+  return MEXCT_OK;
+}
+
 mexct_status mexct_ctx_destroy(mexct_ctx* c) {
   if (!c) return MEXCT_OK;
   {

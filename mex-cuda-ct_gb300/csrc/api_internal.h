@@ -63,6 +63,8 @@ struct mexct_ctx {
   mexct::Buf bpart;  // BP view-block partial sums
   // Launch shapes: MEXCT_TUNE_* mode and the per-class table.
   int tune_mode = MEXCT_TUNE_HEURISTIC;
+  // Limit of one bounded wait in the slab FP (SlabEpi::wait_us encoding).
+  int wait_us = 0;
   std::map<mexct::TuneKey, mexct::TuneEntry> tune;
   // Texture variant: cached 3D array + texture object.
   cudaArray_t tex_arr = nullptr;

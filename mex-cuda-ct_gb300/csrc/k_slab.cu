@@ -189,16 +189,62 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// Bounded wait: gives up after ~2^22 polls (seconds), records the failure in
-// err and in the CTA's abort flag, and reports it to the caller, which then
-// samples the slab from global memory.  Once a CTA has given up, its later
-// waits return at once and no further copies are issued, so a broken pipeline
-// costs one time-out per CTA, not one per slab.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Non-blocking test of a phase (try_wait may suspend the thread for a while).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// After a CTA gave up waiting: copies issued before still land in its
+// buffers, so wait (at most 2 s each) until the last copy issued into each
+// buffer has completed.  Copies into one buffer complete in order, so the
+// last one's phase parity is (count - 1) & 1.  issued: 16-bit counts per
+// buffer.  Kept out of line: it only runs after a failure.
+__device__ __noinline__ void slab_drain(uint64_t* bar, uint32_t issued, unsigned* err) {
+  for (int b = 0; b < 2; ++b) {
+    const uint32_t n = (issued >> (16 * b)) & 0xffffu;
+    if (n == 0) continue;
+    const uint64_t t0 = global_ns();
+    bool done = false;
+    do {
+      done = mbar_try_wait(&bar[b], (n - 1u) & 1u);
+    } while (!done && global_ns() - t0 < 2000000000ull);
+    if (!done && err) atomicOr(err, 2u);
+  }
+}
+
+// Bounded wait: after one attempt, keeps trying for at most wait_us
+// microseconds of wall time (default 2 s; < 0: one non-blocking test only), then records the
+// failure in err and in the CTA's abort flag and reports it to the caller,
+// which samples the slab from global memory instead (the result is the same).
+// Once a CTA has given up, its later waits return at once and no further
+// copies are issued, so a broken pipeline costs one time-out per CTA.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, unsigned* err,
-                                                  volatile int* abort) {
+                                                  volatile int* abort, int wait_us) {
   if (*abort) return false;
-  for (int i = 0; i < (1 << 22); ++i)
-    if (mbar_try_wait(bar, parity)) return true;
+  if (wait_us < 0) {
+    if (mbar_test_wait(bar, parity)) return true;
+  } else {
+    // the usual short waits end here, without reading the clock
+    for (int i = 0; i < 64; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t limit = wait_us > 0 ? (uint64_t)wait_us * 1000ull : 2000000000ull;
+    const uint64_t t0 = global_ns();
+    while (global_ns() - t0 < limit)
+      if (mbar_try_wait(bar, parity)) return true;
+  }
   *abort = 1;
   if (err) atomicOr(err, 1u);
   return false;
@@ -333,7 +379,7 @@ struct SlabShared {
   uint32_t plans[kMaxPlans];
   float corner[4][6];
   int amin, amax, pos, neg;
-  int abort;  // set by a timed-out wait
+  int abort;          // set by a timed-out wait
   long long item;
 };
 
@@ -351,7 +397,8 @@ __device__ __forceinline__ void slab_init_barriers(SlabShared& S) {
 // Ends with a CTA barrier, so the shared state can be reused by the next job.
 template <int GEOM, int EPI, typename TV, typename TO>
 __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, SlabShared& S,
-                                          uint32_t& phase, const SlabEpi& E) {
+                                          uint32_t& phase, uint32_t& issued,
+                                          const SlabEpi& E) {
   constexpr bool Z2 = (GEOM == 2);  // par/fan rays sample exact z texel rows
   const int tid = threadIdx.x + 32 * threadIdx.y;
   const int u0 = J.tu0, v0 = J.tv0;
@@ -491,6 +538,8 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     mbar_expect_tx(&bar[j & 1], (uint32_t)(nbox * kBoxZ * kPlane * sizeof(TV)));
     for (int bx = 0; bx < nbox; ++bx)
       tma_load_3d(dst + (size_t)bx * kBoxZ * kPlane, tm, f0, alo, z0 + bx * kBoxZ, &bar[j & 1]);
+    // thread 0 counts the copies issued into each buffer (16 bits each)
+    issued += 1u << (16 * (j & 1));
   };
   if (tid == 0 && nslab > 0) issue(0);
 
@@ -516,7 +565,8 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     bool from_smem = plan_nzr(pk) != 0;
     if (from_smem) {
       // bit b of phase: parity of buffer b's next completion
-      from_smem = mbar_wait_bounded(&bar[j & 1], (phase >> (j & 1)) & 1u, E.err, &S.abort);
+      from_smem = mbar_wait_bounded(&bar[j & 1], (phase >> (j & 1)) & 1u, E.err, &S.abort,
+                                    E.wait_us);
       phase ^= 1u << (j & 1);
     }
     // Samples of this lane whose a-tap lies in [alo, ahi], two per iteration
@@ -590,6 +640,11 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     }
     __syncthreads();
   }
+  if (tid == 0 && S.abort) {
+    // Copies issued before a wait gave up still land in this CTA's buffers:
+    // wait for them (bounded) before the buffers are reused or the CTA exits.
+    slab_drain(bar, issued, E.err);
+  }
   if (valid) {
     const float l = acc * J.step;
     const size_t pix = (size_t)iy * J.det_w + ix;
@@ -621,7 +676,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   TV* buf0 = reinterpret_cast<TV*>(smem_raw);
   TV* buf1 = buf0 + kBufElems;
   slab_init_barriers(S);
-  uint32_t phase = 0u;
+  uint32_t phase = 0u, issued = 0u;  // issued: copies per buffer (thread 0)
   const int view = blockIdx.x;
   const int tiles_u = (A.det_w + 31) >> 5;
   SlabJob J;
@@ -635,7 +690,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   J.tu0 = (blockIdx.y % tiles_u) * 32;
   J.tv0 = (blockIdx.y / tiles_u) * 8;
   J.tmx = &tmx; J.tmy = &tmy; J.px = px; J.py = py; J.out = out;
-  slab_tile<GEOM, EPI, TV, TO>(J, buf0, buf1, S, phase, E);
+  slab_tile<GEOM, EPI, TV, TO>(J, buf0, buf1, S, phase, issued, E);
 }
 
 // ---------------------------------------------------------------------------
@@ -652,7 +707,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_batch_kernel(
   TV* buf0 = reinterpret_cast<TV*>(smem_raw);
   TV* buf1 = buf0 + kBufElems;
   slab_init_barriers(S);
-  uint32_t phase = 0u;
+  uint32_t phase = 0u, issued = 0u;  // issued: copies per buffer (thread 0)
   const SlabEpi E{nullptr, nullptr, nullptr, nullptr, err};
   for (;;) {
     if (threadIdx.x + 32 * threadIdx.y == 0) S.item = (long long)atomicAdd(counter, 1ull);
@@ -680,9 +735,9 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_batch_kernel(
     J.tu0 = (tile % B.tiles_u) * 32;
     J.tv0 = (tile / B.tiles_u) * 8;
     J.tmx = &B.tmx; J.tmy = &B.tmy; J.px = B.px; J.py = B.py; J.out = B.out;
-    if (B.geom == 0) slab_tile<0, 0, TV, TV>(J, buf0, buf1, S, phase, E);
-    else if (B.geom == 1) slab_tile<1, 0, TV, TV>(J, buf0, buf1, S, phase, E);
-    else slab_tile<2, 0, TV, TV>(J, buf0, buf1, S, phase, E);
+    if (B.geom == 0) slab_tile<0, 0, TV, TV>(J, buf0, buf1, S, phase, issued, E);
+    else if (B.geom == 1) slab_tile<1, 0, TV, TV>(J, buf0, buf1, S, phase, issued, E);
+    else slab_tile<2, 0, TV, TV>(J, buf0, buf1, S, phase, issued, E);
   }
 }
 

@@ -54,6 +54,7 @@ struct SlabEpi {
   float* rpre;       // residuals in the padded-sinogram layout of each view:
   float* rpost;      // [H+4][W+4] with a zero frame (border addressing)
   unsigned* err;     // set to non-zero when a bounded wait gave up
+  int wait_us;       // limit of one wait: 0 = default (2 s), < 0 = give up at once
 };
 int slab_pitch(int W);
 // CTAs of the slab FP kernels resident per SM (its launch bounds); persistent

@@ -143,7 +143,7 @@ mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float
     int Pf = 0;
     mexct_status s = prepare_slab(c, d_vol, vt, W, H, false, &mx, &my, &Pf, st);
     if (s) return s;
-    SlabEpi e{nullptr, nullptr, nullptr, nullptr, c->err.as<unsigned>()};
+    SlabEpi e{nullptr, nullptr, nullptr, nullptr, c->err.as<unsigned>(), c->wait_us};
     for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
       a->nviews = std::min(kMaxViews, nP - v0);
       a->view0 = v0;
@@ -370,7 +370,8 @@ mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
       va->trig[i] = ra->trig[i];
     }
     if (nv > 0) {
-      SlabEpi e{d_pre, d_post, c->r1.as<float>(), c->r2.as<float>(), c->err.as<unsigned>()};
+      SlabEpi e{d_pre, d_post, c->r1.as<float>(), c->r2.as<float>(), c->err.as<unsigned>(),
+                c->wait_us};
       MEXCT_TRY_CUDA(launch_fp_slab(geom, true, true, *ra, mx, my, c->padx.p, c->pady.p, Pf,
                                     mu_type, nullptr, kF32, e, st),
                      "osc_iter: fp");

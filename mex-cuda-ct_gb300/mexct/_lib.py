@@ -62,6 +62,8 @@ SIGNATURES = {
     "mexct_prefilter_dev": [_P, _P, _P, _i, _i, _i, _P, _i, _f, _i, _f, _f, _P, _P],
     "mexct_fp_dev_ex": [_P, _P, _i, _i, _i, _f, _P, _i, _i, _P, _i, _i, _P],
     "mexct_bp_dev_ex": [_P, _P, _i, _i, _i, _i, _f, _P, _i, _P, _i, _P],
+    "mexct_ctx_set_wait_limit": [_P, _i],
+    "mexct_ctx_device_errors": [_P, _c.POINTER(_c.c_uint), _i],
 }
 _RESTYPES = {"mexct_last_error": _c.c_char_p, "mexct_version": _c.c_char_p}
 OPTIONAL = {}  # symbols declared later in the header are added by their modules

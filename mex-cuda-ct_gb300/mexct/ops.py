@@ -336,3 +336,20 @@ def prefilter_dev(sino, angles, geom, sad, filt="ramp", cutoff=1.0, q=1.0, pre=N
               nP, _ptr(ang), _geom_flag(geom), float(sad), FILTERS[filt.lower()], float(cutoff),
               float(q), _dptr(out), _stream(stream))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Bounded waits of the default context (include/mexct.h).
+# ---------------------------------------------------------------------------
+def set_wait_limit(us: int) -> None:
+    """Limit of one bounded wait of the slab FP in microseconds (0: give up at once,
+    < 0: the 2 s default)."""
+    _lib.call("mexct_ctx_set_wait_limit", None, int(us))
+
+
+def device_errors(clear: bool = False) -> int:
+    """Flags of the default context's device error word (bit 0: a bounded wait gave up);
+    call after the covered work has finished."""
+    f = ctypes.c_uint(0)
+    _lib.call("mexct_ctx_device_errors", None, ctypes.byref(f), 1 if clear else 0)
+    return int(f.value)
