@@ -9,6 +9,8 @@
 #include <mutex>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/mexct.h"
 #include "kernels.h"
 
@@ -33,6 +35,15 @@ struct Buf {
   T* as() const {
     return static_cast<T*>(p);
   }
+};
+
+// NVTX range over one library call ("mexct:fp", ...), visible in Nsight
+// timelines; costs nothing when no tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 // One entry of a context's launch-shape table.

@@ -146,6 +146,7 @@ mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int 
 mexct_status mexct_batch_fp(mexct_batch* b, void* stream) {
   if (!b) return set_err(MEXCT_ERR_ARG, "batch_fp: NULL batch");
   DevGuard dg(b->device);
+  NvtxRange nvtx("mexct:batch_fp");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   MEXCT_TRY_CUDA(launch_pad_batch(b->fp_desc.as<BatchFp>(), b->n, b->pad_items, st),
                  "batch_fp: padding");
@@ -161,6 +162,7 @@ mexct_status mexct_batch_fp(mexct_batch* b, void* stream) {
 mexct_status mexct_batch_bp(mexct_batch* b, void* stream) {
   if (!b) return set_err(MEXCT_ERR_ARG, "batch_bp: NULL batch");
   DevGuard dg(b->device);
+  NvtxRange nvtx("mexct:batch_bp");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   for (int i = 0; i < b->n; ++i) {
     const mexct_problem& p = b->probs[i];

@@ -570,6 +570,7 @@ extern "C" {
   } while (0)
 
 #define CTX_OR_FAIL(c, name)                                                \
+  NvtxRange _nvtx("mexct:" name);                                           \
   mexct_ctx* c = resolve(ctx);                                              \
   if (!c) return set_err(MEXCT_ERR_CUDA, name ": no CUDA device / context"); \
   std::lock_guard<std::recursive_mutex> _lk(c->mu);                         \

@@ -279,6 +279,7 @@ mexct_status mexct_osctv_run(mexct_osctv* s, const mexct_osctv_params* p,
   if (!s || !p || (!first_picks && n > 0)) return set_err(MEXCT_ERR_ARG, "osctv_run: NULL pointer");
   if (n < 0 || p->n_iter < 1) return set_err(MEXCT_ERR_ARG, "osctv_run: bad iteration count");
   DevGuard dg(s->device);
+  NvtxRange nvtx("mexct:osctv_run");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   for (int i = 0; i < n; ++i) {
     const int k = s->k_done + 1;  // 1-based iteration number
