@@ -103,16 +103,21 @@ __device__ __forceinline__ void tv_sweep(const T* __restrict__ v, int Nx, int Ny
   const bool qcol = incol && gx >= 1 && gy >= 1;  // columns where q exists
   const bool own = incol && tx < kTvOx && ty < kTvOy;
   const size_t ci = (size_t)gx + (size_t)gy * sy;
+  // column-invariant parts of the interior test and of the loads
+  const bool col_int = gx >= 1 && gy >= 1 && gx < Nx - 1 && gy < Ny - 1;
+  const bool ld_y = gy >= 1, ld_m = tx == 0 && gx >= 1;
+  const int srow = ty + (ty < kTvOy);  // row of the +y neighbour in sqb
   // value of the plane below the first one, and the first plane's loads
   float xprev = (qcol && z0 >= 1) ? ldf(v + ci + (size_t)(z0 - 1) * sz) : 0.f;
   float xcur = 0.f, xym = 0.f, xxm = 0.f;
+  const T* pl = v + ci + (size_t)z0 * sz;  // column at the plane being loaded
   auto load = [&](int p, float& xo, float& yo, float& mo) {
     if (incol && p < Nz) {
-      const size_t i = ci + (size_t)p * sz;
-      xo = ldf(v + i);
-      yo = (gy >= 1) ? ldf(v + i - sy) : 0.f;
-      mo = (tx == 0 && gx >= 1) ? ldf(v + i - 1) : 0.f;
+      xo = ldf(pl);
+      yo = ld_y ? ldf(pl - sy) : 0.f;
+      mo = ld_m ? ldf(pl - 1) : 0.f;
     }
+    pl += sz;
   };
   load(z0, xcur, xym, xxm);
   float q0p = 0.f, qanp = 0.f, xz = 0.f;  // plane p-1: own q0, +x neighbour's qa, x
@@ -139,10 +144,8 @@ __device__ __forceinline__ void tv_sweep(const T* __restrict__ v, int Nx, int Ny
     }
     if (p > z0) {
       const int z = p - 1;
-      const bool interior = gx >= 1 && gy >= 1 && z >= 1 && gx < Nx - 1 && gy < Ny - 1 &&
-                            z < Nz - 1;
-      const float g = interior ? ((q0p - qanp) - sqb[(p - 1) & 1][ty + (ty < kTvOy)][tx]) - qc
-                               : 0.f;
+      const bool interior = col_int && z >= 1 && z < Nz - 1;
+      const float g = interior ? ((q0p - qanp) - sqb[(p - 1) & 1][srow][tx]) - qc : 0.f;
       visit(z, xz, g, own && interior, own);
     }
     sqb[p & 1][ty][tx] = qb;

@@ -662,7 +662,7 @@ cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
                                  const float* rpre, const float* rpost,
                                  void* mu, int mt, void* padx, void* pady, int Pf,
                                  cudaStream_t st) {
-  constexpr int ZC = 8;
+  constexpr int ZC = 4;
   dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + ZC - 1) / ZC);
 #define OSC_BP(G, T)                                                                 \
   osc_bp_update_kernel<G, ZC, T><<<grd, blk, 0, st>>>(a, rpre, rpost, (T*)mu, (T*)padx, \
