@@ -64,6 +64,8 @@ def _load():
         sig = {
             "orc_fp": [F, i, i, f, F, i, i, D],
             "orc_bp": [F, i, i, i, f, F, i, D],
+            "orc_fp_det": [F, i, i, f, F, i, i, i, i, f, f, i, D],
+            "orc_bp_det": [F, i, i, i, f, F, i, i, i, f, f, D],
             "orc_g3d_fp": [F, i, i, F, F, i, i, i, i, D],
             "orc_g3d_bp": [F, i, i, i, F, F, i, i, i, D],
             "orc_osc_iter": [D, F, F, i, i, i, i, I32, F, f, i],
@@ -167,6 +169,33 @@ def bp(sino, sad, angles, geom):
     out = np.zeros((W, W, H), dtype=np.float64, order="F")
     _check(lib.orc_bp(_p(sino, ctypes.c_float), W, H, nP, float(sad), _p(ang, ctypes.c_float),
                       int(geom), _p(out, ctypes.c_double)), "bp")
+    return out
+
+
+def fp_det(vol, sad, angles, geom, det_w, det_h, du=1.0, dv=1.0, ss=1):
+    """FP onto a Wd x Hd detector of pitch du, dv with ss x ss rays per pixel:
+    vol [W,W,H] -> [Wd,Hd,nP] (float64)."""
+    lib = _load()
+    vol = _f32(vol)
+    W, _, H = vol.shape
+    ang = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).ravel())
+    out = np.zeros((int(det_w), int(det_h), ang.size), dtype=np.float64, order="F")
+    _check(lib.orc_fp_det(_p(vol, ctypes.c_float), W, H, float(sad), _p(ang, ctypes.c_float),
+                          ang.size, int(geom), int(det_w), int(det_h), float(du), float(dv),
+                          int(ss), _p(out, ctypes.c_double)), "fp_det")
+    return out
+
+
+def bp_det(sino, sad, angles, geom, W, H, du=1.0, dv=1.0):
+    """BP of a Wd x Hd x nP sinogram of pitch du, dv into a W x W x H volume."""
+    lib = _load()
+    sino = _f32(sino)
+    Wd, Hd, nP = sino.shape
+    ang = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).ravel())
+    out = np.zeros((int(W), int(W), int(H)), dtype=np.float64, order="F")
+    _check(lib.orc_bp_det(_p(sino, ctypes.c_float), Wd, Hd, nP, float(sad),
+                          _p(ang, ctypes.c_float), int(geom), int(W), int(H), float(du),
+                          float(dv), _p(out, ctypes.c_double)), "bp_det")
     return out
 
 

@@ -220,27 +220,33 @@ inline void trig(float beta, float* s, float* c) {
 // Ray end points of the standard geometries in binary32.
 // par: CUDAmex_FP.cu:64-77; cone: :162-175; fan: :259-272 (and the switch in
 // CUDAmex_oscIter.cu:152-187).
+// Detector generalisation (no counterpart in the reference, whose detector is
+// the volume's W x H with one voxel per pixel at the isocentre): pixel pitch
+// du, dv at the isocentre and a sub-pixel offset ou, ov.  du = dv = 1,
+// ou = ov = 0 give the reference's binary32 operations exactly.
 inline void std_ray(int geom, int ix, int iy, float u0, float v0, float sb,
-                    float cb, float SR, float RD, float* s, float* e) {
+                    float cb, float SR, float RD, float* s, float* e,
+                    float du = 1.0f, float dv = 1.0f, float ou = 0.0f,
+                    float ov = 0.0f) {
   float u, v;
   switch (geom) {
     case 0:
-      u = ((float)ix - u0);
-      v = ((float)iy - v0);
+      u = (((float)ix + ou) - u0) * du;
+      v = (((float)iy + ov) - v0) * dv;
       s[0] = (SR * cb) - u * sb;
       s[1] = (SR * sb) + u * cb;
       s[2] = v;
       break;
     case 1:
-      u = ((float)ix - u0) * (SR + RD) / SR;
-      v = ((float)iy - v0);
+      u = ((((float)ix + ou) - u0) * du) * (SR + RD) / SR;
+      v = (((float)iy + ov) - v0) * dv;
       s[0] = (SR * cb);
       s[1] = (SR * sb);
       s[2] = v;
       break;
     default:
-      u = ((float)ix - u0) * (SR + RD) / SR;
-      v = ((float)iy - v0) * (SR + RD) / SR;
+      u = ((((float)ix + ou) - u0) * du) * (SR + RD) / SR;
+      v = ((((float)iy + ov) - v0) * dv) * (SR + RD) / SR;
       s[0] = (SR * cb);
       s[1] = (SR * sb);
       s[2] = 0.0f;
@@ -283,28 +289,35 @@ struct BpCol {
   double dpz;   // increment per iz
 };
 
+// Projection coordinates of voxel column (ix, iy) for one view.  The
+// detector generalisation: the u centre is Wd/2 (integer division, the
+// reference's hw + 1), the v centre (Hd - 1)/2 + 0.5, pixel pitches du, dv at
+// the isocentre; Wd = W, Hd = H, du = dv = 1 are the reference's formulas.
 inline BpCol bp_column(int geom, int ix, int iy, uint32_t hw, float v0,
-                       float sb, float cb, float SR) {
+                       float sb, float cb, float SR, int Wd = -1, int Hd = -1,
+                       double du = 1.0, double dv = 1.0) {
   const float x = ix - (hw + 0.5f);
   const float y = iy - (hw + 0.5f);
   const double s = (double)x * cb + (double)y * sb;
   const double t = -(double)x * sb + (double)y * cb;
+  const double uc = Wd < 0 ? (double)hw + 1.0 : (double)((uint32_t)Wd / 2u);
+  const double v0d = Hd < 0 ? (double)v0 : (double)(Hd - 1) / 2.0;
   BpCol c;
   if (geom == 0) {
     c.wgt = 1.0;
-    c.py = t + (double)hw + 1.0;
-    c.pz0 = 0.5;
-    c.dpz = 1.0;
+    c.py = t / du + uc;
+    c.pz0 = -(double)v0 / dv + v0d + 0.5;
+    c.dpz = 1.0 / dv;
   } else {
     const double U = (double)SR / ((double)SR - s);
     c.wgt = U * U;
-    c.py = t * U + (double)hw + 1.0;
+    c.py = t * U / du + uc;
     if (geom == 1) {
-      c.pz0 = 0.5;
-      c.dpz = 1.0;
+      c.pz0 = -(double)v0 / dv + v0d + 0.5;
+      c.dpz = 1.0 / dv;
     } else {
-      c.pz0 = -(double)v0 * U + (double)v0 + 0.5;
-      c.dpz = U;
+      c.pz0 = -(double)v0 * U / dv + v0d + 0.5;
+      c.dpz = U / dv;
     }
   }
   return c;
@@ -319,63 +332,86 @@ int orc_get_threads(void) { return nthreads(); }
 void orc_set_tex_weights(int mode) { g_tex_weights = (mode >= 0 && mode <= 2) ? mode : 0; }
 int orc_get_tex_weights(void) { return g_tex_weights; }
 
-// CUDAmex_FP.cu:350-477 (gateway) and :56-346 (kernels).
-int orc_fp(const float* vol, int W, int H, float sad, const float* angles,
-           int nP, int geom, double* out) {
+// CUDAmex_FP.cu:350-477 (gateway) and :56-346 (kernels), with the detector
+// generalisation: Wd x Hd pixels of pitch du, dv at the isocentre, ss x ss
+// rays per pixel at sub-pixel offsets (k + 0.5)/ss - 0.5, averaged.
+int orc_fp_det(const float* vol, int W, int H, float sad, const float* angles,
+               int nP, int geom, int Wd, int Hd, float du, float dv, int ss,
+               double* out) {
   if (!vol || !angles || !out || W <= 0 || H <= 0 || nP < 0) return 1;
-  if (geom < 0 || geom > 2) return 1;
-  const float u0 = float(W - 1) / 2;
-  const float v0 = float(H - 1) / 2;
+  if (geom < 0 || geom > 2 || Wd <= 0 || Hd <= 0 || ss < 1 || !(du > 0.f) || !(dv > 0.f))
+    return 1;
+  const float u0 = float(Wd - 1) / 2;
+  const float v0 = float(Hd - 1) / 2;
   const float bx = -(float)W / 2.0f, by = -(float)W / 2.0f,
               bz = -(float)H / 2.0f;
   const float step = (geom == 2) ? 1.0f : 0.5f;  // :231 vs :133,:328
   const float SR = sad, RD = sad;
-  const long long P = (long long)W * H;
+  const long long P = (long long)Wd * Hd;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
   for (long long r = 0; r < P * nP; ++r) {
     const int view = (int)(r / P);
     const int pix = (int)(r % P);
-    const int ix = pix % W, iy = pix / W;
+    const int ix = pix % Wd, iy = pix / Wd;
     float sb, cb;
     trig(angles[view], &sb, &cb);
-    float s[3], e[3];
-    std_ray(geom, ix, iy, u0, v0, sb, cb, SR, RD, s, e);
-    const Ray ray = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], bx, by, bz,
-                             step);
-    out[r] = march(ray, step, vol, W, W, H, bx, by, bz, /*border=*/false);
+    double acc = 0.0;
+    for (int a = 0; a < ss; ++a)
+      for (int b = 0; b < ss; ++b) {
+        const float ou = ss == 1 ? 0.0f : ((float)b + 0.5f) / (float)ss - 0.5f;
+        const float ov = ss == 1 ? 0.0f : ((float)a + 0.5f) / (float)ss - 0.5f;
+        float s[3], e[3];
+        std_ray(geom, ix, iy, u0, v0, sb, cb, SR, RD, s, e, du, dv, ou, ov);
+        const Ray ray = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], bx, by, bz,
+                                 step);
+        acc += march(ray, step, vol, W, W, H, bx, by, bz, /*border=*/false);
+      }
+    out[r] = acc / ((double)ss * ss);
   }
   return 0;
 }
 
-// CUDAmex_BP.cu:223-324 (gateway) and :44-221 (kernels).
-int orc_bp(const float* sino, int W, int H, int nP, float sad,
-           const float* angles, int geom, double* vol) {
-  if (!sino || !angles || !vol || W <= 0 || H <= 0 || nP < 0) return 1;
-  if (geom < 0 || geom > 2) return 1;
+int orc_fp(const float* vol, int W, int H, float sad, const float* angles,
+           int nP, int geom, double* out) {
+  return orc_fp_det(vol, W, H, sad, angles, nP, geom, W, H, 1.0f, 1.0f, 1, out);
+}
+
+// CUDAmex_BP.cu:223-324 (gateway) and :44-221 (kernels), with the detector
+// generalisation (sinogram Wd x Hd x nP, pitch du, dv; volume W x W x H).
+int orc_bp_det(const float* sino, int Wd, int Hd, int nP, float sad,
+               const float* angles, int geom, int W, int H, float du, float dv,
+               double* vol) {
+  if (!sino || !angles || !vol || W <= 0 || H <= 0 || Wd <= 0 || Hd <= 0 || nP < 0) return 1;
+  if (geom < 0 || geom > 2 || !(du > 0.f) || !(dv > 0.f)) return 1;
   const float v0 = float(H - 1) / 2;
   const uint32_t hw = (uint32_t)W / 2u - 1u;
   const size_t N = (size_t)W * W * H;
   std::memset(vol, 0, N * sizeof(double));
   std::vector<float> sbv(nP), cbv(nP);
   for (int j = 0; j < nP; ++j) trig(angles[j], &sbv[j], &cbv[j]);
-  const size_t P = (size_t)W * H;
+  const size_t P = (size_t)Wd * Hd;
 #pragma omp parallel for schedule(dynamic, 8) num_threads(nthreads())
   for (long long col = 0; col < (long long)W * W; ++col) {
     const int ix = (int)(col % W), iy = (int)(col / W);
     if (!in_circle(ix, iy, hw)) continue;
     std::vector<double> acc(H, 0.0);
     for (int j = 0; j < nP; ++j) {
-      const BpCol c = bp_column(geom, ix, iy, hw, v0, sbv[j], cbv[j], sad);
+      const BpCol c = bp_column(geom, ix, iy, hw, v0, sbv[j], cbv[j], sad, Wd, Hd, du, dv);
       const float* proj = sino + P * j;
       for (int iz = 0; iz < H; ++iz) {
         const double pz = c.pz0 + c.dpz * iz;
-        acc[iz] += c.wgt * tex2(proj, W, H, c.py, pz, /*border=*/false);
+        acc[iz] += c.wgt * tex2(proj, Wd, Hd, c.py, pz, /*border=*/false);
       }
     }
     for (int iz = 0; iz < H; ++iz)
       vol[(size_t)ix + (size_t)W * iy + (size_t)W * W * iz] = acc[iz];
   }
   return 0;
+}
+
+int orc_bp(const float* sino, int W, int H, int nP, float sad,
+           const float* angles, int geom, double* vol) {
+  return orc_bp_det(sino, W, H, nP, sad, angles, geom, W, H, 1.0f, 1.0f, vol);
 }
 
 // CUDAmex_general3D_FP.cu:154-252 (gateway) and :59-150 (kernel).

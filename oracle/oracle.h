@@ -44,6 +44,17 @@ int orc_fp(const float* vol, int W, int H, float sad, const float* angles,
 int orc_bp(const float* sino, int W, int H, int nP, float sad,
            const float* angles, int geom, double* vol);
 
+/* Detector generalisation of orc_fp / orc_bp (no counterpart in the
+ * reference): detector Wd x Hd pixels of pitch du, dv (voxels, at the
+ * isocentre), FP with ss x ss rays per pixel averaged.  Wd = W, Hd = H,
+ * du = dv = 1, ss = 1 are orc_fp / orc_bp exactly. */
+int orc_fp_det(const float* vol, int W, int H, float sad, const float* angles,
+               int nP, int geom, int Wd, int Hd, float du, float dv, int ss,
+               double* out);
+int orc_bp_det(const float* sino, int Wd, int Hd, int nP, float sad,
+               const float* angles, int geom, int W, int H, float du, float dv,
+               double* vol);
+
 /* general3D forward projection (CUDAmex_general3D_FP.cu:59-150, border
  * address mode, step 0.5).  pts: [W,H,6] shared by every view
  * (pts_per_view=0) or [W,H,6,nP] (pts_per_view=1). out: [W,H,nP]. */

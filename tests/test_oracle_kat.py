@@ -331,3 +331,48 @@ def test_texture_weight_difference_is_stated(orc, geom):
         # rounding, well below 1e-3
         assert 1e-6 < a < 1e-3
         assert 1e-7 < b < 1e-3
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+def test_detector_generalisation_defaults_are_the_reference_form(orc, geom):
+    """fp_det / bp_det with the volume's detector (pitch 1, one ray per pixel) are
+    fp / bp bit for bit."""
+    from mexct import phantoms
+
+    W, H, nP = 24, 16, 6
+    vol = phantoms.ellipsoids(W, count=3, seed=1, nz=H)
+    ang = phantoms.angles_full(nP)
+    fp = orc.fp(vol, 1000.0, ang, nP, geom)
+    assert np.array_equal(orc.fp_det(vol, 1000.0, ang, geom, W, H), fp)
+    sino = fp.astype(np.float32)
+    assert np.array_equal(orc.bp_det(sino, 1000.0, ang, geom, W, H), orc.bp(sino, 1000.0, ang, geom))
+
+
+def test_detector_half_pitch_samples_the_cylinder_chord(orc):
+    """A parallel detector with twice the pixels at half the pitch, along a grid
+    axis: each ray sums its interpolated row, so a row of the detector integrates
+    (times the pitch) to the slice's mass exactly, and the flat middle of the
+    profile is the cylinder's longest chord, as with the full-pitch detector."""
+    W, H, r = 40, 4, 15.0
+    vol = _cyl(W, H, r, 1.0)
+    ang = np.array([0.0], np.float32)
+    full = orc.fp(vol, 1000.0, ang, 1, 0)
+    half = orc.fp_det(vol, 1000.0, ang, 0, 2 * W, H, du=0.5)
+    for iy in range(H):
+        np.testing.assert_allclose(0.5 * half[:, iy, 0].sum(), full[:, iy, 0].sum(), rtol=1e-12)
+        assert half[:, iy, 0].max() == full[:, iy, 0].max() == _row_counts(W, r).max()
+
+
+def test_supersampling_averages_sub_rays(orc):
+    """ss = 2: each pixel is the mean of four rays at (+-1/4, +-1/4) pixel, i.e. the
+    mean of a 2 x 2 finer detector's pixels."""
+    from mexct import phantoms
+
+    W, H = 20, 12
+    vol = phantoms.ellipsoids(W, count=3, seed=4, nz=H)
+    ang = np.array([0.4, 1.9], np.float32)
+    for geom in (0, 2):
+        ss = orc.fp_det(vol, 1000.0, ang, geom, W, H, ss=2)
+        fine = orc.fp_det(vol, 1000.0, ang, geom, 2 * W, 2 * H, du=0.5, dv=0.5)
+        coarse = 0.25 * (fine[0::2, 0::2] + fine[1::2, 0::2] + fine[0::2, 1::2] + fine[1::2, 1::2])
+        np.testing.assert_allclose(ss, coarse, rtol=1e-5, atol=1e-6)
