@@ -190,6 +190,36 @@ mexct_status mexct_bp_dev_ex(mexct_ctx* ctx, const void* d_sino,
                              const float* angles, int geom, void* d_vol,
                              int vol_type, void* stream);
 
+/* ---- decoupled detector ----------------------------------------------- */
+
+/* No counterpart in the reference, whose detector is always the volume's
+ * face: W x H pixels of unit pitch, one ray through each pixel centre
+ * (CUDAmex_FP.cu:378-379, CUDAmex_BP.cu:73,249).  Here the detector is
+ * det_w x det_h pixels of pitch du x dv (voxel units at the isocentre), with
+ * its centre where the reference puts it: u0 = (det_w - 1)/2 for the rays,
+ * det_w/2 (integer division) for BP's u coordinate, (det_h - 1)/2 in v.
+ * ss >= 1: FP traces ss x ss rays per pixel at sub-pixel offsets
+ * (k + 0.5)/ss - 0.5 and returns their mean.  det_w = W, det_h = H,
+ * du = dv = 1, ss = 1 gives what mexct_fp_dev / mexct_bp_dev give. */
+typedef struct mexct_detector {
+  int det_w, det_h;  /* pixels, >= 1 each */
+  float du, dv;      /* pitch, > 0 */
+  int ss;            /* FP rays per pixel side, 1..8 */
+} mexct_detector;
+
+/* FP32 volume W x W x H (x fastest) to an FP32 sinogram det_w x det_h x nP
+ * (the slab kernel; ss x ss launches for ss > 1). */
+mexct_status mexct_fp_det_dev(mexct_ctx* ctx, const float* d_vol, int W, int H,
+                              float sad, const float* angles, int nP,
+                              int geom, const mexct_detector* det,
+                              float* d_out, void* stream);
+/* FP32 sinogram det_w x det_h x nP to an FP32 volume W x W x H (voxel-driven,
+ * bilinear in u and v for every geometry; ss is ignored). */
+mexct_status mexct_bp_det_dev(mexct_ctx* ctx, const float* d_sino,
+                              const mexct_detector* det, int nP, float sad,
+                              const float* angles, int geom, int W, int H,
+                              float* d_vol, void* stream);
+
 /* ---- launch shapes and autotuning -------------------------------------- */
 
 /* No counterpart in the reference (its kernels have one fixed launch shape).

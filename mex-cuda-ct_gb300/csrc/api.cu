@@ -152,6 +152,8 @@ void fill_std_rays(RayArgs& a, int W, int H, float sad, int geom,
   a.step = (geom == 2 && !osc) ? 1.0f : 0.5f;
   a.P = (long long)W * H;
   a.vstride = 1;
+  a.du = 1.0f;                      // the reference's detector: unit pitch,
+  a.dv = 1.0f;                      // rays through the pixel centres
 }
 
 void fill_vox(VoxArgs& a, int W, int H, float sad) {
@@ -162,6 +164,12 @@ void fill_vox(VoxArgs& a, int W, int H, float sad) {
   a.SR = sad;
   a.hw = (uint32_t)W / 2u - 1u;     // :73
   a.P = (long long)W * H;
+  a.det_w = W;                      // the volume's face, unit pitch
+  a.det_h = H;
+  a.hwd = (float)a.hw;
+  a.v0d = a.v0;
+  a.inv_du = 1.0f;
+  a.inv_dv = 1.0f;
 }
 
 }  // namespace mexct

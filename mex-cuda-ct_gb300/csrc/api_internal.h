@@ -72,6 +72,7 @@ struct mexct_ctx {
   mexct::Buf padx, pady, err;
   mexct::Buf spad;   // padded sinogram views for BP
   mexct::Buf bpart;  // BP view-block partial sums
+  mexct::Buf subs;   // one sub-ray sinogram of a super-sampled FP
   // Launch shapes: MEXCT_TUNE_* mode and the per-class table.
   int tune_mode = MEXCT_TUNE_HEURISTIC;
   // Limit of one bounded wait in the slab FP (SlabEpi::wait_us encoding).
@@ -88,7 +89,7 @@ struct mexct_ctx {
 
   std::vector<mexct::Buf*> all_bufs() {
     return {&in, &in2, &in3, &out, &volT, &r1, &r2, &r3, &tabs, &red, &cnt, &scal,
-            &padx, &pady, &err, &spad, &bpart};
+            &padx, &pady, &err, &spad, &bpart, &subs};
   }
 };
 

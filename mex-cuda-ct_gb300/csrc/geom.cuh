@@ -108,28 +108,59 @@ __device__ __forceinline__ Ray clip_ray(float sx, float sy, float sz, float ex,
   return r;
 }
 
+// Whether the segment s -> e meets the volume box [b, -b] per axis (no
+// counterpart in the reference, whose rays all pass through the box: each
+// crosses the isocentre plane at a point 0.5 voxel or more inside it).  The
+// clip above leaves an axis the ray runs parallel to open and marches a ray
+// that misses the box between two points outside it; the decoupled detector
+// drops such rays instead.  The per-axis alphas are the clip's own.
+__device__ __forceinline__ bool hits_box(const float* s, const float* e, float bx, float by,
+                                         float bz) {
+  const float b[3] = {bx, by, bz};
+  float amin = 0.f, amax = 1.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    float lo, hi;
+    slab(s[i], e[i], b[i], lo, hi);
+    if (lo != lo) {  // parallel to the axis' planes: inside or not at all
+      if (fabsf(s[i]) > -b[i]) return false;
+    } else {
+      amin = fmaxf(amin, lo);
+      amax = fminf(amax, hi);
+    }
+  }
+  return amin <= amax;
+}
+
 // Standard-geometry ray end points (CUDAmex_FP.cu:64-77 par, :162-175 cone,
-// :259-272 fan; CUDAmex_oscIter.cu:152-187).
+// :259-272 fan; CUDAmex_oscIter.cu:152-187).  Detector generalisation (no
+// counterpart in the reference): pixel pitch du, dv at the isocentre and a
+// sub-pixel offset ou, ov; du = dv = 1, ou = ov = 0 give the reference's
+// binary32 operations exactly (adding 0 and multiplying by 1 are exact).
 template <int GEOM>
 __device__ __forceinline__ void std_ray(int ix, int iy, float u0, float v0,
                                         float sb, float cb, float SR, float RD,
-                                        float* s, float* e) {
+                                        float* s, float* e, float du = 1.0f,
+                                        float dv = 1.0f, float ou = 0.0f,
+                                        float ov = 0.0f) {
   float u, v;
+  const float du0 = fmul(fsub(fadd((float)ix, ou), u0), du);
+  const float dv0 = fmul(fsub(fadd((float)iy, ov), v0), dv);
   if (GEOM == 0) {
-    u = fsub((float)ix, u0);
-    v = fsub((float)iy, v0);
+    u = du0;
+    v = dv0;
     s[0] = fsub(fmul(SR, cb), fmul(u, sb));
     s[1] = fadd(fmul(SR, sb), fmul(u, cb));
     s[2] = v;
   } else if (GEOM == 1) {
-    u = fdiv(fmul(fsub((float)ix, u0), fadd(SR, RD)), SR);
-    v = fsub((float)iy, v0);
+    u = fdiv(fmul(du0, fadd(SR, RD)), SR);
+    v = dv0;
     s[0] = fmul(SR, cb);
     s[1] = fmul(SR, sb);
     s[2] = v;
   } else {
-    u = fdiv(fmul(fsub((float)ix, u0), fadd(SR, RD)), SR);
-    v = fdiv(fmul(fsub((float)iy, v0), fadd(SR, RD)), SR);
+    u = fdiv(fmul(du0, fadd(SR, RD)), SR);
+    v = fdiv(fmul(dv0, fadd(SR, RD)), SR);
     s[0] = fmul(SR, cb);
     s[1] = fmul(SR, sb);
     s[2] = 0.0f;

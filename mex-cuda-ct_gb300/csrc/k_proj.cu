@@ -116,7 +116,7 @@ __device__ __forceinline__ Ray make_ray(const RayArgs& A, int view, int ix,
   const Trig t = A.trig[view];
   float s[3], e[3];
   if (GEOM < 3) {
-    std_ray<GEOM>(ix, iy, A.u0, A.v0, t.s, t.c, A.SR, A.RD, s, e);
+    std_ray<GEOM>(ix, iy, A.u0, A.v0, t.s, t.c, A.SR, A.RD, s, e, A.du, A.dv, A.ou, A.ov);
   } else {
     const long long pix = (long long)iy * A.det_w + ix;
     const float* p =
@@ -271,28 +271,34 @@ struct ColGeom {
   float w, py, pz0, dpz;
 };
 
+// Projection coordinates of column (x, y) for one view (CUDAmex_BP.cu:
+// 88-190).  Detector generalisation: u centre hwd + 1, v centre v0d,
+// reciprocal pitches inv_du, inv_dv; the defaults (hwd = hw, v0d = v0,
+// inv_du = inv_dv = 1) are the reference's operations exactly.
 template <int GEOM>
 __device__ __forceinline__ ColGeom<GEOM> col_geom(float x, float y, Trig t,
                                                   float SR, float v0,
-                                                  uint32_t hw) {
+                                                  float hwd, float v0d, float inv_du,
+                                                  float inv_dv) {
   ColGeom<GEOM> g;
   const float s = fmaf(x, t.c, y * t.s);
   const float tt = fmaf(-x, t.s, y * t.c);
   if (GEOM == 0) {
     g.w = 1.f;
-    g.py = tt + (float)hw + 1.f;
-    g.pz0 = 0.5f;
-    g.dpz = 1.f;
+    g.py = fmaf(tt, inv_du, hwd) + 1.f;
+    g.pz0 = fmaf(-v0, inv_dv, v0d) + 0.5f;
+    g.dpz = inv_dv;
   } else {
     const float U = SR / (SR - s);
     g.w = U * U;
-    g.py = fmaf(tt, U, (float)hw) + 1.f;
+    g.py = fmaf(tt, U * inv_du, hwd) + 1.f;
     if (GEOM == 1) {
-      g.pz0 = 0.5f;
-      g.dpz = 1.f;
+      g.pz0 = fmaf(-v0, inv_dv, v0d) + 0.5f;
+      g.dpz = inv_dv;
     } else {
-      g.pz0 = fmaf(-v0, U, v0) + 0.5f;
-      g.dpz = U;
+      const float Uv = U * inv_dv;
+      g.pz0 = fmaf(-v0, Uv, v0d) + 0.5f;
+      g.dpz = Uv;
     }
   }
   return g;
@@ -380,7 +386,9 @@ cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews,
 
 // Sample one padded projection along a voxel column: acc[j] += w * B(py, pz).
 // g.py / g.pz0 are texture coordinates (texel centres at i + 0.5).
-template <int GEOM, int ZC, typename TS>
+// W x H is the detector; ROWS: the column's z rows are texel rows (par / fan
+// with the volume's own detector), otherwise pz is interpolated.
+template <int GEOM, int ZC, typename TS, bool ROWS = (GEOM < 2)>
 __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, int H, int Wp,
                                               int z0, const ColGeom<GEOM>& g, float* acc) {
   // u tap, once per view and column (coordinate bounded so floor fits an int)
@@ -394,7 +402,7 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
   // lane's operations are those of the one-voxel form, in the same order.
   static_assert(ZC % 2 == 0, "ZC must be even");
   const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
-  if (GEOM < 2) {
+  if (ROWS) {
     // par / fan: the column's z rows are texel rows (pz = iz + 0.5)
 #pragma unroll
     for (int j = 0; j < ZC; j += 2) {
@@ -435,7 +443,7 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
 // columns, and the views split into vblocks blocks along grid z.  With
 // vblocks > 1 every view block writes FP32 partial sums to part[vb][voxel]
 // and bp_reduce_kernel adds them in block order (deterministic).
-template <int GEOM, int ZC, typename TS, typename TV>
+template <int GEOM, int ZC, typename TS, typename TV, bool DET = false>
 // Cone columns take 16 bilinear taps per z pair; bounding registers to 64 keeps
 // 4 CTAs (32 warps) per SM resident, 5% faster at 512^3 x 720 than the 66
 // registers / 3 CTAs the compiler picks unbounded.  Par/fan columns need no
@@ -458,10 +466,22 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
   if (in_circle(ix, iy, A.hw)) {
     const float x = (float)ix - ((float)A.hw + 0.5f);
     const float y = (float)iy - ((float)A.hw + 0.5f);
-    const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
-    for (int v = vbeg; v < vend; ++v) {
-      const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
-      bp_column_pad<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+    if (DET) {
+      // decoupled detector (launch_bp_det): its own size, centre and pitch
+      const size_t vstride = (size_t)Wp * (A.det_h + 2 * kSinoPad);
+      for (int v = vbeg; v < vend; ++v) {
+        const ColGeom<GEOM> g =
+            col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hwd, A.v0d, A.inv_du, A.inv_dv);
+        bp_column_pad<GEOM, ZC, TS, false>(sino + (size_t)v * vstride, A.det_w, A.det_h, Wp, z0,
+                                           g, acc);
+      }
+    } else {
+      const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
+      for (int v = vbeg; v < vend; ++v) {
+        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
+                                               1.f, 1.f);
+        bp_column_pad<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+      }
     }
   }
   const size_t base = (size_t)iy * A.W + ix;
@@ -553,6 +573,54 @@ cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, i
   }
 }
 
+// Decoupled-detector BP: FP32 sinogram of det_w x det_h views padded with
+// sino_pad_pitch(det_w), one launch shape (8 z voxels per thread, 32 x 8
+// columns), every geometry interpolating in v.
+cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
+                          bool accumulate, cudaStream_t st) {
+  if (a.nviews <= 0) return cudaSuccess;
+  constexpr int ZC = 8;
+  const int Wp = sino_pad_pitch(a.det_w);
+  const int nz = (a.H + ZC - 1) / ZC;
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, nz);
+  const int acc = accumulate ? 1 : 0;
+  switch (geom) {
+    case 0:
+      bp_pad_kernel<0, ZC, float, float, true><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
+                                                                    nz, 1, nullptr);
+      break;
+    case 1:
+      bp_pad_kernel<1, ZC, float, float, true><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
+                                                                    nz, 1, nullptr);
+      break;
+    case 2:
+      bp_pad_kernel<2, ZC, float, float, true><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
+                                                                    nz, 1, nullptr);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// dst = w * src (first) or dst + w * src: the sub-ray average of a
+// super-sampled FP, one sub-ray sinogram at a time.
+__global__ void __launch_bounds__(256) add_scaled_kernel(const float* __restrict__ src,
+                                                         float* __restrict__ dst, long long n,
+                                                         float w, int first) {
+  for (long long i = blockIdx.x * 256ll + threadIdx.x; i < n; i += (long long)gridDim.x * 256) {
+    const float t = w * src[i];
+    dst[i] = first ? t : dst[i] + t;
+  }
+}
+
+cudaError_t launch_add_scaled(const float* src, float* dst, long long n, float w, bool first,
+                              cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int ctas = (int)std::min<long long>((n + 255) / 256, 152ll * 16);
+  add_scaled_kernel<<<ctas, 256, 0, st>>>(src, dst, n, w, first ? 1 : 0);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // general3D BP (CUDAmex_general3D_BP.cu:61-188): ray-driven, two-corner
 // scatter with atomics.  Positions advance incrementally in binary32 and the
@@ -632,7 +700,7 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
   const int Wp = sino_pad_pitch(A.W);
   const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
   for (int v = 0; v < A.nviews; ++v) {
-    const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
+    const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
     // zero frame = border addressing (CUDAmex_oscIter.cu:419-425)
     bp_column_pad<GEOM, ZC>(rpre + (size_t)v * vstride, A.W, A.H, Wp, z0, g, num);
     bp_column_pad<GEOM, ZC>(rpost + (size_t)v * vstride, A.W, A.H, Wp, z0, g, den);
@@ -721,7 +789,7 @@ __device__ __forceinline__ void bp_l1_brick(const BrickJob& A, const float* __re
     const float x = (float)ix - ((float)A.hw + 0.5f);
     const float y = (float)iy - ((float)A.hw + 0.5f);
     for (int v = 0; v < A.nviews; ++v) {
-      const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hw);
+      const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
       bp_column_pad<GEOM, kSmZc>(sino + (size_t)(A.view0 + v) * vstride, A.W, A.H, Wp, z0, g,
                                  acc);
     }

@@ -346,6 +346,7 @@ __device__ __forceinline__ float2 sample_pair(const T* p0, const T* p1, int sa, 
 struct SlabJob {
   int det_w, det_h, S, Z, Pf;
   float u0, v0, bx, by, bz, SR, RD, step;
+  float du, dv, ou, ov;  // detector pitch and sub-pixel ray offset
   Trig tr;
   long long P;      // detector pixels per view
   long long gview;  // sinogram / pre / post slot of the view
@@ -395,11 +396,16 @@ __device__ __forceinline__ void slab_init_barriers(SlabShared& S) {
 
 // One tile: sweep the volume along the view's dominant axis slab by slab.
 // Ends with a CTA barrier, so the shared state can be reused by the next job.
-template <int GEOM, int EPI, typename TV, typename TO>
+// ZL (decoupled detector): par / fan rays whose constant z falls between
+// texel rows interpolate in z as well, and rays that miss the volume sample
+// nothing.
+template <int GEOM, int EPI, typename TV, typename TO, bool ZL = false>
 __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, SlabShared& S,
                                           uint32_t& phase, uint32_t& issued,
                                           const SlabEpi& E) {
-  constexpr bool Z2 = (GEOM == 2);  // par/fan rays sample exact z texel rows
+  constexpr bool Z2 = (GEOM == 2);  // z changes along the ray
+  // trilinear samples; otherwise par/fan rays sample exact z texel rows
+  constexpr bool ZW = Z2 || ZL;
   const int tid = threadIdx.x + 32 * threadIdx.y;
   const int u0 = J.tu0, v0 = J.tv0;
   const int ix = u0 + threadIdx.x, iy = v0 + threadIdx.y;
@@ -410,14 +416,16 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
 
   float s[3], e[3];
   std_ray<GEOM>(min(ix, J.det_w - 1), min(iy, J.det_h - 1), J.u0, J.v0, tr.s, tr.c, J.SR, J.RD,
-                s, e);
+                s, e, J.du, J.dv, J.ou, J.ov);
   const Ray r = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], J.bx, J.by, J.bz, J.step);
   // Tap space: padded texture coordinate minus 0.5, i.e. world - b + 0.5.
   const float ca = xdom ? r.cx - J.bx : r.cy - J.by;
   const float cf = xdom ? r.cy - J.by : r.cx - J.bx;
   const float ta0 = ca + 0.5f, tf0 = cf + 0.5f, tz0 = (r.cz - J.bz) + 0.5f;
   const float da = xdom ? r.dx : r.dy, df = xdom ? r.dy : r.dx, dz = r.dz;
-  const int n = valid ? r.n : 0;
+  // On a decoupled detector (ZL) a ray that misses the volume samples nothing.
+  const bool miss = ZL && !hits_box(s, e, J.bx, J.by, J.bz);
+  const int n = (valid && !miss) ? r.n : 0;
 
   if (tid == 0) {
     S.amin = 0x7fffffff;
@@ -607,12 +615,12 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
         const unsigned i0 = min((unsigned)__float2int_rn(x2.x), (unsigned)kMaxIdx);
         if (two) {
           const unsigned i1 = min((unsigned)__float2int_rn(x2.y), (unsigned)kMaxIdx);
-          const float2 v = sample_pair<Z2>(b + i0, b + i1, kBoxF, kPlane, wa2, wf2, wz2);
+          const float2 v = sample_pair<ZW>(b + i0, b + i1, kBoxF, kPlane, wa2, wf2, wz2);
           acc += v.x;
           acc += v.y;
           k += 2;
         } else {
-          acc += sample_at<Z2>(b + i0, kBoxF, kPlane, wa2.x, wf2.x, wz2.x);
+          acc += sample_at<ZW>(b + i0, kBoxF, kPlane, wa2.x, wf2.x, wz2.x);
           k += 1;
           break;
         }
@@ -633,7 +641,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
         const float ffq = floorf(tfq), fzq = floorf(tzq);
         const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
         const int gz = min(max((int)fzq, 0), Pz - 2);
-        acc += sample_at<Z2>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
+        acc += sample_at<ZW>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
                              Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
         ++k;
       }
@@ -666,7 +674,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   __syncthreads();
 }
 
-template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
+template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = false>
 __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
     const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
     const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
@@ -683,6 +691,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   J.det_w = A.det_w; J.det_h = A.det_h; J.S = A.S; J.Z = A.Z; J.Pf = Pf;
   J.u0 = A.u0; J.v0 = A.v0; J.bx = A.bx; J.by = A.by; J.bz = A.bz;
   J.SR = A.SR; J.RD = A.RD; J.step = A.step;
+  J.du = A.du; J.dv = A.dv; J.ou = A.ou; J.ov = A.ov;
   J.tr = A.trig[view];
   J.P = A.P;
   J.gview = A.view0 + (long long)view * A.vstride;
@@ -690,7 +699,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   J.tu0 = (blockIdx.y % tiles_u) * 32;
   J.tv0 = (blockIdx.y / tiles_u) * 8;
   J.tmx = &tmx; J.tmy = &tmy; J.px = px; J.py = py; J.out = out;
-  slab_tile<GEOM, EPI, TV, TO>(J, buf0, buf1, S, phase, issued, E);
+  slab_tile<GEOM, EPI, TV, TO, ZL>(J, buf0, buf1, S, phase, issued, E);
 }
 
 // ---------------------------------------------------------------------------
@@ -728,6 +737,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_batch_kernel(
     J.det_w = B.W; J.det_h = B.H; J.S = B.W; J.Z = B.H; J.Pf = B.Pf;
     J.u0 = B.u0; J.v0 = B.v0; J.bx = B.bx; J.by = B.by; J.bz = B.bz;
     J.SR = B.sad; J.RD = B.sad; J.step = B.step;
+    J.du = 1.0f; J.dv = 1.0f; J.ou = 0.0f; J.ov = 0.0f;
     J.tr = B.trig[view];
     J.P = (long long)B.W * B.H;
     J.gview = view;
@@ -793,11 +803,11 @@ cudaError_t launch_fp_batch(const BatchFp* d_probs, int nprob, long long total,
   return cudaGetLastError();
 }
 
-template <int GEOM, bool BORDER, int EPI, typename TV, typename TO>
+template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = false>
 static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtensorMap& my,
                            const void* px, const void* py, int Pf, void* out,
                            const SlabEpi& e, cudaStream_t st) {
-  auto k = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO>;
+  auto k = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO, ZL>;
   const size_t smem = 2 * (size_t)kBufElems * sizeof(TV) + 128;
   static bool attr_set = false;  // once per instantiation (before any capture)
   if (!attr_set) {
@@ -811,6 +821,15 @@ static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtens
   dim3 blk(32, 8), grd(a.nviews, tiles);
   k<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e);
   return cudaGetLastError();
+}
+
+cudaError_t launch_fp_slab_det(int geom, const RayArgs& a, const CUtensorMap& mx,
+                               const CUtensorMap& my, const void* px, const void* py, int Pf,
+                               float* out, const SlabEpi& e, cudaStream_t st) {
+  if (geom == 0) return slab_go<0, false, 0, float, float, true>(a, mx, my, px, py, Pf, out, e, st);
+  if (geom == 1) return slab_go<1, false, 0, float, float, true>(a, mx, my, px, py, Pf, out, e, st);
+  if (geom == 2) return slab_go<2, false, 0, float, float, true>(a, mx, my, px, py, Pf, out, e, st);
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,

@@ -20,17 +20,25 @@ struct RayArgs {
   int view0, vstride;      // launch view i is global view view0 + i*vstride
   long long P;             // det_w * det_h
   int pts_per_view;        // general3D: per-view points
+  float du, dv;            // pixel pitch at the isocentre (1: the reference's)
+  float ou, ov;            // sub-pixel ray offset (0: the reference's)
   Trig trig[kMaxViews];
 };
 
 // Voxel-driven BP launch (standard BP, OSC dual BP).
 struct VoxArgs {
-  int W, H;       // volume W x W x H, detector W x H
+  int W, H;       // volume W x W x H
   int nviews;
   float v0, SR;
   uint32_t hw;    // circle half width W/2 - 1 (unsigned, as the reference)
   int view0;      // launch view i reads sinogram slot view0 + i
-  long long P;
+  long long P;    // det_w * det_h
+  // Detector of the decoupled-geometry BP (launch_bp_det): det_w x det_h
+  // pixels, u centre hwd + 1 = det_w/2 (integer division), v centre
+  // v0d = (det_h - 1)/2, reciprocal pitches inv_du, inv_dv.  The standard
+  // launches ignore these fields: their detector is the volume's face.
+  int det_w, det_h;
+  float hwd, v0d, inv_du, inv_dv;
   Trig trig[kMaxViews];
 };
 
@@ -104,6 +112,13 @@ cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
                            void* out, int ot, const SlabEpi& e,
                            cudaStream_t st);
 
+// Slab FP (FP32) onto a decoupled detector (a.det_w, a.det_h, a.du, a.dv,
+// a.ou, a.ov): par / fan rays interpolate in z, rays that miss the volume
+// add nothing.
+cudaError_t launch_fp_slab_det(int geom, const RayArgs& a, const CUtensorMap& mx,
+                               const CUtensorMap& my, const void* px, const void* py, int Pf,
+                               float* out, const SlabEpi& e, cudaStream_t st);
+
 cudaError_t launch_fp_tex(int geom, const RayArgs& a,
                           cudaTextureObject_t tex, float* out,
                           cudaStream_t st);
@@ -126,6 +141,14 @@ bool bp_shape_valid(const BpShape& s);
 cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, int stype,
                              void* vol, int vtype, bool accumulate, const BpShape& shp,
                              float* part, cudaStream_t st);
+
+// Decoupled-detector BP (FP32 padded sinogram of a.det_w x a.det_h views).
+cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
+                          bool accumulate, cudaStream_t st);
+
+// dst = w * src (first) or dst += w * src over n elements.
+cudaError_t launch_add_scaled(const float* src, float* dst, long long n, float w, bool first,
+                              cudaStream_t st);
 
 // general3D ray-driven two-corner scatter BP (CUDAmex_general3D_BP.cu:61-188).
 cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,

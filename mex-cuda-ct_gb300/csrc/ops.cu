@@ -252,6 +252,113 @@ mexct_status bp_dev_impl(mexct_ctx* c, const void* d_sino, int stype, int W,
 }
 
 // ---------------------------------------------------------------------------
+// Decoupled detector
+// ---------------------------------------------------------------------------
+mexct_status bad_detector(const mexct_detector* d, const char* op) {
+  if (!d) return set_err(MEXCT_ERR_ARG, "%s: NULL detector", op);
+  if (d->det_w < 1 || d->det_h < 1 || d->det_w > 32768 || d->det_h > 32768)
+    return set_err(MEXCT_ERR_ARG, "%s: bad detector size %d x %d", op, d->det_w, d->det_h);
+  if (!(d->du > 0.f) || !(d->dv > 0.f) || !std::isfinite(d->du) || !std::isfinite(d->dv))
+    return set_err(MEXCT_ERR_ARG, "%s: detector pitch must be finite and > 0", op);
+  if (d->ss < 1 || d->ss > 8)
+    return set_err(MEXCT_ERR_ARG, "%s: rays per pixel side must be 1..8 (got %d)", op, d->ss);
+  return MEXCT_OK;
+}
+
+// FP onto a det_w x det_h detector of pitch du x dv: the slab kernel with the
+// rays through the pixel centres, or (ss > 1) once per sub-ray offset into a
+// scratch sinogram whose views are averaged into the output.
+mexct_status fp_det_impl(mexct_ctx* c, const float* d_vol, int W, int H, float sad,
+                         const float* angles, int nP, int geom, const mexct_detector* det,
+                         float* d_out, cudaStream_t st) {
+  if (!d_vol || (nP > 0 && (!d_out || !angles))) return set_err(MEXCT_ERR_ARG, "fp: NULL pointer");
+  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "fp: bad volume dims %d x %d x %d", W, W, H);
+  if (nP < 0) return set_err(MEXCT_ERR_ARG, "fp: nProj must be >= 0 (got %d)", nP);
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "fp: invalid geometry %d", geom);
+  if (mexct_status s = bad_detector(det, "fp")) return s;
+  if (!c || nP == 0) return MEXCT_OK;
+  std::unique_ptr<RayArgs> a(new RayArgs);
+  fill_std_rays(*a, W, H, sad, geom, false);
+  a->det_w = det->det_w;
+  a->det_h = det->det_h;
+  a->u0 = float(det->det_w - 1) / 2;
+  a->v0 = float(det->det_h - 1) / 2;
+  a->P = (long long)det->det_w * det->det_h;
+  a->du = det->du;
+  a->dv = det->dv;
+  CUtensorMap mx, my;
+  int Pf = 0;
+  mexct_status s = prepare_slab(c, d_vol, kF32, W, H, false, &mx, &my, &Pf, st);
+  if (s) return s;
+  const int ss = det->ss;
+  const long long M = a->P * nP;
+  float* dst = d_out;
+  if (ss > 1) {
+    MEXCT_TRY_CUDA(c->subs.ensure_async((size_t)M * sizeof(float), st), "fp: workspace");
+    dst = c->subs.as<float>();
+  }
+  SlabEpi e{nullptr, nullptr, nullptr, nullptr, c->err.as<unsigned>(), c->wait_us};
+  const float wsub = 1.0f / (float)(ss * ss);
+  for (int sa = 0; sa < ss; ++sa) {
+    for (int sb = 0; sb < ss; ++sb) {
+      a->ou = ss == 1 ? 0.0f : ((float)sb + 0.5f) / (float)ss - 0.5f;
+      a->ov = ss == 1 ? 0.0f : ((float)sa + 0.5f) / (float)ss - 0.5f;
+      for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+        a->nviews = std::min(kMaxViews, nP - v0);
+        a->view0 = v0;
+        for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+        MEXCT_TRY_CUDA(launch_fp_slab_det(geom, *a, mx, my, c->padx.p, c->pady.p, Pf, dst, e, st),
+                       "fp: launch");
+      }
+      if (ss > 1)
+        MEXCT_TRY_CUDA(launch_add_scaled(dst, d_out, M, wsub, sa == 0 && sb == 0, st),
+                       "fp: sub-ray mean");
+    }
+  }
+  return MEXCT_OK;
+}
+
+// BP from a det_w x det_h detector of pitch du x dv.
+mexct_status bp_det_impl(mexct_ctx* c, const float* d_sino, const mexct_detector* det, int nP,
+                         float sad, const float* angles, int geom, int W, int H, float* d_vol,
+                         cudaStream_t st) {
+  if (!d_vol || (nP > 0 && (!d_sino || !angles))) return set_err(MEXCT_ERR_ARG, "bp: NULL pointer");
+  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "bp: bad volume dims %d x %d x %d", W, W, H);
+  if (nP < 0) return set_err(MEXCT_ERR_ARG, "bp: bad view count %d", nP);
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "bp: invalid geometry %d", geom);
+  if (mexct_status s = bad_detector(det, "bp")) return s;
+  if (!c) return MEXCT_OK;
+  std::unique_ptr<VoxArgs> a(new VoxArgs);
+  fill_vox(*a, W, H, sad);
+  if (nP == 0) {
+    MEXCT_TRY_CUDA(launch_fill(d_vol, kF32, (long long)W * W * H, 0.f, st), "bp: zero");
+    return MEXCT_OK;
+  }
+  const int Wd = det->det_w, Hd = det->det_h;
+  a->det_w = Wd;
+  a->det_h = Hd;
+  a->hwd = (float)(Wd / 2) - 1.0f;
+  a->v0d = float(Hd - 1) / 2;
+  a->inv_du = 1.0f / det->du;
+  a->inv_dv = 1.0f / det->dv;
+  a->P = (long long)Wd * Hd;
+  const int chunk = std::min(nP, kMaxViews);
+  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(Wd, Hd, chunk) * sizeof(float), st),
+                 "bp: workspace");
+  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+    a->nviews = std::min(kMaxViews, nP - v0);
+    a->view0 = 0;
+    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+    MEXCT_TRY_CUDA(launch_pad_sino(d_sino + (size_t)v0 * a->P, kF32, Wd, Hd, a->nviews, false,
+                                   c->spad.p, st),
+                   "bp: pad");
+    MEXCT_TRY_CUDA(launch_bp_det(geom, *a, c->spad.as<float>(), d_vol, v0 > 0, st),
+                   "bp: launch");
+  }
+  return MEXCT_OK;
+}
+
+// ---------------------------------------------------------------------------
 // general3D
 // ---------------------------------------------------------------------------
 void fill_g3d(RayArgs& a, int S, int Z, int W, int H, int per_view) {
@@ -267,6 +374,8 @@ void fill_g3d(RayArgs& a, int S, int Z, int W, int H, int per_view) {
   a.P = (long long)W * H;
   a.pts_per_view = per_view;
   a.vstride = 1;
+  a.du = 1.0f;
+  a.dv = 1.0f;
 }
 
 mexct_status g3d_fp_dev_impl(mexct_ctx* c, const float* d_vol, int S, int Z,
@@ -632,6 +741,22 @@ mexct_status mexct_bp_dev_ex(mexct_ctx* ctx, const void* d_sino, int stype,
   CTX_OR_FAIL(c, "bp");
   return bp_dev_impl(c, d_sino, stype, W, H, nP, sad, angles, geom, d_vol, vt,
                      as_stream(stream));
+}
+
+mexct_status mexct_fp_det_dev(mexct_ctx* ctx, const float* d_vol, int W, int H,
+                              float sad, const float* angles, int nP, int geom,
+                              const mexct_detector* det, float* d_out, void* stream) {
+  VALIDATE(fp_det_impl(nullptr, d_vol, W, H, sad, angles, nP, geom, det, d_out, nullptr));
+  CTX_OR_FAIL(c, "fp_det");
+  return fp_det_impl(c, d_vol, W, H, sad, angles, nP, geom, det, d_out, as_stream(stream));
+}
+
+mexct_status mexct_bp_det_dev(mexct_ctx* ctx, const float* d_sino, const mexct_detector* det,
+                              int nP, float sad, const float* angles, int geom, int W, int H,
+                              float* d_vol, void* stream) {
+  VALIDATE(bp_det_impl(nullptr, d_sino, det, nP, sad, angles, geom, W, H, d_vol, nullptr));
+  CTX_OR_FAIL(c, "bp_det");
+  return bp_det_impl(c, d_sino, det, nP, sad, angles, geom, W, H, d_vol, as_stream(stream));
 }
 
 mexct_status mexct_bp(mexct_ctx* ctx, const float* sino, int W, int H, int nP,

@@ -24,6 +24,13 @@ _lock = threading.Lock()
 _lib = None
 
 
+class Detector(ctypes.Structure):
+    """struct mexct_detector: det_w x det_h pixels of pitch du x dv, ss x ss FP rays per pixel."""
+
+    _fields_ = [("det_w", ctypes.c_int), ("det_h", ctypes.c_int), ("du", ctypes.c_float),
+                ("dv", ctypes.c_float), ("ss", ctypes.c_int)]
+
+
 class MexctError(RuntimeError):
     """A libmexct call returned a non-zero status."""
 
@@ -62,6 +69,8 @@ SIGNATURES = {
     "mexct_prefilter_dev": [_P, _P, _P, _i, _i, _i, _P, _i, _f, _i, _f, _f, _P, _P],
     "mexct_fp_dev_ex": [_P, _P, _i, _i, _i, _f, _P, _i, _i, _P, _i, _i, _P],
     "mexct_bp_dev_ex": [_P, _P, _i, _i, _i, _i, _f, _P, _i, _P, _i, _P],
+    "mexct_fp_det_dev": [_P, _P, _i, _i, _f, _P, _i, _i, _P, _P, _P],
+    "mexct_bp_det_dev": [_P, _P, _P, _i, _f, _P, _i, _i, _i, _P, _P],
     "mexct_ctx_set_wait_limit": [_P, _i],
     "mexct_ctx_device_errors": [_P, _c.POINTER(_c.c_uint), _i],
 }

@@ -277,6 +277,36 @@ def bp_dev(sino, sad, angles, geom, out=None, out_dtype=None, stream=None):
     return out
 
 
+def fp_det_dev(vol, sad, angles, geom, det_w, det_h, du=1.0, dv=1.0, ss=1, out=None,
+               stream=None):
+    """FP of an FP32 device volume (H, W, W) onto a det_w x det_h detector of pitch du x dv
+    with ss x ss rays per pixel -> sinogram (nP, det_h, det_w), stream-ordered."""
+    import torch
+    H, W, W2 = vol.shape
+    assert W == W2, "volume must be (H, W, W)"
+    ang = _angles(angles, 0)
+    nP = ang.size
+    det = _lib.Detector(int(det_w), int(det_h), float(du), float(dv), int(ss))
+    if out is None:
+        out = torch.empty((nP, int(det_h), int(det_w)), dtype=torch.float32, device=vol.device)
+    _lib.call("mexct_fp_det_dev", None, _dptr(vol), W, H, float(sad), _ptr(ang), nP,
+              _geom_flag(geom), ctypes.addressof(det), _dptr(out), _stream(stream))
+    return out
+
+
+def bp_det_dev(sino, sad, angles, geom, W, H, du=1.0, dv=1.0, out=None, stream=None):
+    """BP of an FP32 device sinogram (nP, det_h, det_w) of pitch du x dv -> volume (H, W, W)."""
+    import torch
+    nP, det_h, det_w = sino.shape
+    ang = _angles(angles, nP)
+    det = _lib.Detector(int(det_w), int(det_h), float(du), float(dv), 1)
+    if out is None:
+        out = torch.empty((int(H), int(W), int(W)), dtype=torch.float32, device=sino.device)
+    _lib.call("mexct_bp_det_dev", None, _dptr(sino), ctypes.addressof(det), nP, float(sad),
+              _ptr(ang), _geom_flag(geom), int(W), int(H), _dptr(out), _stream(stream))
+    return out
+
+
 def g3d_fp_dev(vol, angles, pts, out=None, stream=None):
     """general3D FP: vol (Z, S, S); pts (6, H, W) or (nP, 6, H, W) -> (nP, H, W)."""
     import torch

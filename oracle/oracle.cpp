@@ -121,6 +121,27 @@ Ray clip_ray(float sx, float sy, float sz, float ex, float ey, float ez,
   return r;
 }
 
+// Whether the segment s -> e meets the volume box [b, -b] per axis, with the
+// clip's own per-axis alphas.  The reference's rays always do (each crosses
+// the isocentre plane at least 0.5 voxel inside the box); on a decoupled
+// detector a ray can miss, and then adds nothing (the clip above would march
+// it between two points outside the box, an axis it runs parallel to open).
+bool hits_box(const float* s, const float* e, float bx, float by, float bz) {
+  const float b[3] = {bx, by, bz};
+  float amin = 0.f, amax = 1.f;
+  for (int i = 0; i < 3; ++i) {
+    const float d = e[i] - s[i];
+    if ((double)std::fabs(d) >= 1e-5) {
+      const float a1 = (b[i] - s[i]) / d, a2 = (-b[i] - s[i]) / d;
+      amin = std::fmax(amin, std::fmin(a1, a2));
+      amax = std::fmin(amax, std::fmax(a1, a2));
+    } else if (std::fabs(s[i]) > -b[i]) {
+      return false;
+    }
+  }
+  return amin <= amax;
+}
+
 // ---------------------------------------------------------------------------
 // Texture fetch semantics (unnormalised coordinates, texel centre at i+0.5,
 // linear filter), with exact FP64 weights.  Clamp = clamp index to the edge,
@@ -362,6 +383,7 @@ int orc_fp_det(const float* vol, int W, int H, float sad, const float* angles,
         const float ov = ss == 1 ? 0.0f : ((float)a + 0.5f) / (float)ss - 0.5f;
         float s[3], e[3];
         std_ray(geom, ix, iy, u0, v0, sb, cb, SR, RD, s, e, du, dv, ou, ov);
+        if (!hits_box(s, e, bx, by, bz)) continue;  // misses the volume: adds nothing
         const Ray ray = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], bx, by, bz,
                                  step);
         acc += march(ray, step, vol, W, W, H, bx, by, bz, /*border=*/false);

@@ -129,3 +129,25 @@ def test_python_mirror_validates_types(lib):
     with pytest.raises(TypeError):
         mexct.CUDAmex_oscIter(mu, np.zeros((4, 4, 2), F), np.zeros((4, 4, 2), F), 1,
                               np.zeros(1, np.int32), np.zeros(2, F), 1000, 0)
+
+
+def test_detector_entry_points_validate_the_detector(lib):
+    """mexct_fp_det_dev / mexct_bp_det_dev reject a NULL or malformed detector
+    before any device work."""
+    from mexct import _lib
+
+    buf = np.zeros(64, F)
+    ang = np.zeros(2, F)
+    for det in [(0, 4, 1.0, 1.0, 1), (8, 4, 0.0, 1.0, 1), (8, 4, 1.0, float("nan"), 1),
+                (8, 4, 1.0, 1.0, 0), (8, 4, 1.0, 1.0, 9)]:
+        d = _lib.Detector(*det)
+        rc = lib.mexct_fp_det_dev(None, _p(buf), 8, 4, 1000.0, _p(ang), 2, 0,
+                                  ctypes.addressof(d), _p(buf), None)
+        assert rc == _lib.ERR_ARG, det
+    assert lib.mexct_fp_det_dev(None, _p(buf), 8, 4, 1000.0, _p(ang), 2, 0, None, _p(buf),
+                                None) == _lib.ERR_ARG
+    assert "NULL detector" in _lib.last_error()
+    d = _lib.Detector(8, 4, 1.0, 1.0, 1)
+    assert lib.mexct_bp_det_dev(None, _p(buf), ctypes.addressof(d), 2, 1000.0, _p(ang), 5, 8, 4,
+                                _p(buf), None) == _lib.ERR_ARG
+    assert "invalid geometry 5" in _lib.last_error()

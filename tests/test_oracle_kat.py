@@ -376,3 +376,20 @@ def test_supersampling_averages_sub_rays(orc):
         fine = orc.fp_det(vol, 1000.0, ang, geom, 2 * W, 2 * H, du=0.5, dv=0.5)
         coarse = 0.25 * (fine[0::2, 0::2] + fine[1::2, 0::2] + fine[0::2, 1::2] + fine[1::2, 1::2])
         np.testing.assert_allclose(ss, coarse, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("geom", [0, 1])
+def test_taller_detector_rows_outside_the_volume_are_zero(orc, geom):
+    """Par / fan rays are parallel to the z planes.  On a detector 4 rows taller
+    than the volume (pitch 1) rows 2..H+1 are the volume's own rows, bit for bit,
+    and the two rows beyond each end miss the volume and are exactly zero."""
+    from mexct import phantoms
+
+    W, H = 20, 12
+    vol = phantoms.ellipsoids(W, count=3, seed=6, nz=H)
+    vol[:, :, 0] += 1.0  # non-zero edge slices: a clamped sample would show
+    vol[:, :, -1] += 1.0
+    ang = np.array([0.3, 2.2], np.float32)
+    tall = orc.fp_det(vol, 1000.0, ang, geom, W, H + 4)
+    assert np.array_equal(tall[:, 2:H + 2], orc.fp(vol, 1000.0, ang, 2, geom))
+    assert np.count_nonzero(tall[:, :2]) == 0 and np.count_nonzero(tall[:, H + 2:]) == 0
