@@ -411,7 +411,9 @@ def main():
         for name, fn in (("autotune", autotune_section),
                          ("osc_tv", lambda: osc_tv_latency(args.osc_reps)),
                          ("batched", lambda: batched_uneven(args.batch_problems)),
-                         ("serving", lambda: serving(args.serve_requests))):
+                         ("serving", lambda: serving(args.serve_requests)),
+                         ("detector", detector_section),
+                         ("out_of_core", out_of_core)):
             try:
                 extra[name] = fn()
             except Exception as ex:  # reported, never fatal
@@ -571,6 +573,83 @@ def batched_uneven(count, seed=2026):
                        "5 OSC-TV iterations x 8 subsets each" % count)
     b.close()
     return out
+
+
+def detector_section(n=512, views=180, geom=2):
+    """Decoupled detector at 512^3 cone, 180 views: FP onto a 1.5x finer detector
+    (768 x 768, pitch 2/3) with one and with 2 x 2 rays per pixel, BP from it,
+    against the volume's own detector (512 x 512, pitch 1)."""
+    import torch
+
+    from mexct import _lib, ops, phantoms
+
+    vol = phantoms.ellipsoids(n, count=12, seed=2024, nz=n)
+    d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    ang = phantoms.angles_full(views)
+    N = float(n) ** 3
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    out = {"workload": "cone %d^3, %d views, SAD 1000; GUPS = voxels x views / s" % (n, views)}
+    sino = ops.fp_dev(d, 1000.0, ang, geom, variant=_lib.FP_EXPLICIT)
+    t = timed(lambda: ops.fp_dev(d, 1000.0, ang, geom, out=sino, variant=_lib.FP_EXPLICIT))
+    out["fp_own_detector_512"] = {"s": round(t, 4), "gups": round(N * views / t / 1e9, 3)}
+    m = n * 3 // 2
+    fine = torch.empty((views, m, m), device="cuda")
+    for ss in (1, 2):
+        t = timed(lambda: ops.fp_det_dev(d, 1000.0, ang, geom, m, m, 2 / 3, 2 / 3, ss, out=fine))
+        out["fp_det_%d_ss%d" % (m, ss)] = {"s": round(t, 4), "gups": round(N * views / t / 1e9, 3)}
+    rec = torch.empty_like(d)
+    t = timed(lambda: ops.bp_dev(sino, 1000.0, ang, geom, out=rec))
+    out["bp_own_detector_512"] = {"s": round(t, 4), "gups": round(N * views / t / 1e9, 3)}
+    t = timed(lambda: ops.bp_det_dev(fine, 1000.0, ang, geom, n, n, 2 / 3, 2 / 3, out=rec))
+    out["bp_det_%d" % m] = {"s": round(t, 4), "gups": round(N * views / t / 1e9, 3)}
+    return out
+
+
+def out_of_core(n=768, views=360, geom=2, budget=1 << 30):
+    """Host volume 768^3 (1.7 GiB) and sinogram (0.8 GiB), cone, 360 views: FP and BP
+    through the host entry points with the whole problem on the device, against the
+    out-of-core drivers held to a 1 GiB device working set (slabs / view chunks /
+    row bands streamed from host memory)."""
+    import mexct
+    from mexct import ops, phantoms
+
+    vol = phantoms.ellipsoids(n, count=12, seed=77, nz=n)
+    ang = phantoms.angles_full(views)
+    N = float(n) ** 3
+    out = {"workload": "cone %d^3 x %d views, SAD 1000, host arrays; budget %d MiB"
+                       % (n, views, budget >> 20)}
+    mexct.CUDAmex_FP(vol[:, :, :8].copy(order="F"), 1000.0, ang, 4, geom)  # warm-up
+    t0 = time.perf_counter()
+    fp_in = mexct.CUDAmex_FP(vol, 1000.0, ang, views, geom)
+    t1 = time.perf_counter()
+    fp_oc = ops.fp_ooc(vol, 1000.0, ang, geom, budget)
+    t2 = time.perf_counter()
+    bp_in = mexct.CUDAmex_BP(fp_in, 1000.0, ang, geom)
+    t3 = time.perf_counter()
+    bp_oc = ops.bp_ooc(fp_in, 1000.0, ang, geom, budget)
+    t4 = time.perf_counter()
+    out["fp_in_core"] = {"s": round(t1 - t0, 3), "gups": round(N * views / (t1 - t0) / 1e9, 3)}
+    out["fp_out_of_core"] = {"s": round(t2 - t1, 3), "gups": round(N * views / (t2 - t1) / 1e9, 3),
+                             "rel_l2_vs_in_core": rel_np(fp_oc, fp_in)}
+    out["bp_in_core"] = {"s": round(t3 - t2, 3), "gups": round(N * views / (t3 - t2) / 1e9, 3)}
+    out["bp_out_of_core"] = {"s": round(t4 - t3, 3), "gups": round(N * views / (t4 - t3) / 1e9, 3),
+                             "rel_l2_vs_in_core": rel_np(bp_oc, bp_in)}
+    return out
+
+
+def rel_np(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
 def autotune_section(classes=((64, 90, 2), (96, 180, 0), (128, 360, 2), (256, 720, 2))):

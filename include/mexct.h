@@ -220,6 +220,48 @@ mexct_status mexct_bp_det_dev(mexct_ctx* ctx, const float* d_sino,
                               const float* angles, int geom, int W, int H,
                               float* d_vol, void* stream);
 
+/* ---- sub-volumes and out-of-core FP / BP --------------------------------- */
+
+/* No counterpart in the reference (its oscIter keeps whole volumes on the
+ * device; sub-volume reconstruction of larger images is a TODO at
+ * iterative_reconstruction/CUDAmex_oscIter.cu:28-29).  A slab is slices
+ * z0 .. z0 + nz - 1 of a W x W x H volume (x fastest), standard detector
+ * (W x H, pitch 1).
+ *
+ * mexct_sub_rows: the detector rows row0 .. row0 + nrows - 1 that the BP of a
+ * slab reads (par / fan: the slab's own rows; cone: a wider band).
+ * mexct_fp_sub_dev: FP of a device slab (W x W x nz) into the device sinogram
+ * (W x H x nP): the FP of the volume with every other slice zero, the clamp
+ * frame kept at the volume's own faces; accumulate != 0 adds to d_sino, so
+ * the FPs of the slabs of a volume add up to its FP (FP32 rounding apart).
+ * mexct_bp_sub_dev: BP into a device slab from detector rows row0 .. row0 +
+ * nrows - 1 of every view (device array W x nrows x nP; the rows must hold
+ * those mexct_sub_rows names); each voxel gets the operations of the
+ * whole-volume BP, so the slabs of a volume are its BP (with one view block,
+ * MEXCT_TUNE_FIXED, bit for bit). */
+mexct_status mexct_sub_rows(int W, int H, float sad, int geom, int z0, int nz,
+                            int* row0, int* nrows);
+mexct_status mexct_fp_sub_dev(mexct_ctx* ctx, const float* d_slab, int W, int H,
+                              int z0, int nz, float sad, const float* angles,
+                              int nP, int geom, float* d_sino, int accumulate,
+                              void* stream);
+mexct_status mexct_bp_sub_dev(mexct_ctx* ctx, const float* d_rows, int row0,
+                              int nrows, int W, int H, int nP, float sad,
+                              const float* angles, int geom, int z0, int nz,
+                              float* d_slab, int accumulate, void* stream);
+
+/* FP / BP of host arrays (the layouts of mexct_fp / mexct_bp) whose device
+ * working set is kept within budget_bytes: the volume passes through the
+ * device in slabs, the sinogram in view chunks (FP) or row bands (BP).
+ * MEXCT_ERR_BUDGET if not even one slice and one view fit.  The context's
+ * workspaces grow to the working set and are kept (mexct_ctx_trim frees them). */
+mexct_status mexct_fp_ooc(mexct_ctx* ctx, const float* vol, int W, int H,
+                          float sad, const float* angles, int nP, int geom,
+                          size_t budget_bytes, float* sino);
+mexct_status mexct_bp_ooc(mexct_ctx* ctx, const float* sino, int W, int H,
+                          int nP, float sad, const float* angles, int geom,
+                          size_t budget_bytes, float* vol);
+
 /* ---- launch shapes and autotuning -------------------------------------- */
 
 /* No counterpart in the reference (its kernels have one fixed launch shape).

@@ -170,6 +170,10 @@ void fill_vox(VoxArgs& a, int W, int H, float sad) {
   a.v0d = a.v0;
   a.inv_du = 1.0f;
   a.inv_dv = 1.0f;
+  a.zoff = 0;                       // the whole volume, every detector row
+  a.nzs = H;
+  a.row0 = 0;
+  a.nrows = H;
 }
 
 }  // namespace mexct

@@ -387,10 +387,13 @@ cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews,
 // Sample one padded projection along a voxel column: acc[j] += w * B(py, pz).
 // g.py / g.pz0 are texture coordinates (texel centres at i + 0.5).
 // W x H is the detector; ROWS: the column's z rows are texel rows (par / fan
-// with the volume's own detector), otherwise pz is interpolated.
+// with the volume's own detector), otherwise pz is interpolated.  roff: the
+// projection holds detector rows roff .. roff + H - 1 (a band of a taller
+// detector, launch_bp_sub); taps are computed in full-detector coordinates.
 template <int GEOM, int ZC, typename TS, bool ROWS = (GEOM < 2)>
 __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, int H, int Wp,
-                                              int z0, const ColGeom<GEOM>& g, float* acc) {
+                                              int z0, const ColGeom<GEOM>& g, float* acc,
+                                              int roff = 0) {
   // u tap, once per view and column (coordinate bounded so floor fits an int)
   const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
   const float fu = floorf(cu);
@@ -406,8 +409,8 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
     // par / fan: the column's z rows are texel rows (pz = iz + 0.5)
 #pragma unroll
     for (int j = 0; j < ZC; j += 2) {
-      const TS* r0 = col + (size_t)(min(z0 + j, H - 1) + kSinoPad) * Wp;
-      const TS* r1 = col + (size_t)(min(z0 + j + 1, H - 1) + kSinoPad) * Wp;
+      const TS* r0 = col + (size_t)(min(z0 + j - roff, H - 1) + kSinoPad) * Wp;
+      const TS* r1 = col + (size_t)(min(z0 + j + 1 - roff, H - 1) + kSinoPad) * Wp;
       const float2 v0 = make_float2(ldf(r0), ldf(r1));
       const float2 v1 = make_float2(ldf(r0 + 1), ldf(r1 + 1));
       const float2 t = __ffma2_rn(w02, v0, __ffma2_rn(w12, v1, make_float2(acc[j], acc[j + 1])));
@@ -423,8 +426,8 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
       const float2 cz = __ffma2_rn(zz, dpz2, pz02);
       const float2 fz = make_float2(floorf(cz.x), floorf(cz.y));
       const float2 az = __fadd2_rn(cz, make_float2(-fz.x, -fz.y));
-      const int i0 = min(max(__float2int_rz(fz.x), -kSinoPad), H) + kSinoPad;
-      const int i1 = min(max(__float2int_rz(fz.y), -kSinoPad), H) + kSinoPad;
+      const int i0 = min(max(__float2int_rz(fz.x) - roff, -kSinoPad), H) + kSinoPad;
+      const int i1 = min(max(__float2int_rz(fz.y) - roff, -kSinoPad), H) + kSinoPad;
       const TS* p0 = col + (size_t)i0 * Wp;
       const TS* p1 = col + (size_t)i1 * Wp;
       const float2 a = __ffma2_rn(w02, make_float2(ldf(p0), ldf(p1)),
@@ -443,7 +446,9 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
 // columns, and the views split into vblocks blocks along grid z.  With
 // vblocks > 1 every view block writes FP32 partial sums to part[vb][voxel]
 // and bp_reduce_kernel adds them in block order (deterministic).
-template <int GEOM, int ZC, typename TS, typename TV, bool DET = false>
+// MODE 0: the reference's detector; 1: decoupled detector (launch_bp_det);
+// 2: a z-slab of the volume from a band of detector rows (launch_bp_sub).
+template <int GEOM, int ZC, typename TS, typename TV, int MODE = 0>
 // Cone columns take 16 bilinear taps per z pair; bounding registers to 64 keeps
 // 4 CTAs (32 warps) per SM resident, 5% faster at 512^3 x 720 than the 66
 // registers / 3 CTAs the compiler picks unbounded.  Par/fan columns need no
@@ -466,7 +471,7 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
   if (in_circle(ix, iy, A.hw)) {
     const float x = (float)ix - ((float)A.hw + 0.5f);
     const float y = (float)iy - ((float)A.hw + 0.5f);
-    if (DET) {
+    if (MODE == 1) {
       // decoupled detector (launch_bp_det): its own size, centre and pitch
       const size_t vstride = (size_t)Wp * (A.det_h + 2 * kSinoPad);
       for (int v = vbeg; v < vend; ++v) {
@@ -474,6 +479,15 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
             col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hwd, A.v0d, A.inv_du, A.inv_dv);
         bp_column_pad<GEOM, ZC, TS, false>(sino + (size_t)v * vstride, A.det_w, A.det_h, Wp, z0,
                                            g, acc);
+      }
+    } else if (MODE == 2) {
+      // z-slab: voxel z = zoff + local z, taps in full-detector rows minus row0
+      const size_t vstride = (size_t)Wp * (A.nrows + 2 * kSinoPad);
+      for (int v = vbeg; v < vend; ++v) {
+        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
+                                               1.f, 1.f);
+        bp_column_pad<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.nrows, Wp, A.zoff + z0, g,
+                                acc, A.row0);
       }
     } else {
       const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
@@ -486,6 +500,7 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
   }
   const size_t base = (size_t)iy * A.W + ix;
   const size_t sz = (size_t)A.W * A.W;
+  const int nzo = MODE == 2 ? A.nzs : A.H;  // output slices
   if (vblocks > 1) {
     float* pp = part + (size_t)vb * sz * A.H + base;
 #pragma unroll
@@ -495,7 +510,7 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
   }
 #pragma unroll
   for (int j = 0; j < ZC; ++j) {
-    if (z0 + j < A.H) {
+    if (z0 + j < nzo) {
       TV* o = vol + base + (size_t)(z0 + j) * sz;
       stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
     }
@@ -586,16 +601,42 @@ cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, flo
   const int acc = accumulate ? 1 : 0;
   switch (geom) {
     case 0:
-      bp_pad_kernel<0, ZC, float, float, true><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
+      bp_pad_kernel<0, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
                                                                     nz, 1, nullptr);
       break;
     case 1:
-      bp_pad_kernel<1, ZC, float, float, true><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
+      bp_pad_kernel<1, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
                                                                     nz, 1, nullptr);
       break;
     case 2:
-      bp_pad_kernel<2, ZC, float, float, true><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
+      bp_pad_kernel<2, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
                                                                     nz, 1, nullptr);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
+                          bool accumulate, cudaStream_t st) {
+  if (a.nviews <= 0) return cudaSuccess;
+  constexpr int ZC = 8;
+  const int Wp = sino_pad_pitch(a.W);
+  const int nz = (a.nzs + ZC - 1) / ZC;
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, nz);
+  const int acc = accumulate ? 1 : 0;
+  switch (geom) {
+    case 0:
+      bp_pad_kernel<0, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
+                                                                 1, nullptr);
+      break;
+    case 1:
+      bp_pad_kernel<1, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
+                                                                 1, nullptr);
+      break;
+    case 2:
+      bp_pad_kernel<2, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
+                                                                 1, nullptr);
       break;
     default: return cudaErrorInvalidValue;
   }

@@ -47,6 +47,8 @@ namespace mexct {
 // Padded volumes.
 // ---------------------------------------------------------------------------
 template <typename T>
+// border: bit 0 zero frame everywhere (border addressing), bit 1 / bit 2 zero
+// frame below / above the z range only (inner faces of a sub-volume slab).
 __global__ void __launch_bounds__(256) pad_x_kernel(const T* __restrict__ src,
                                                     T* __restrict__ dst, int W,
                                                     int H, int Pf, int border) {
@@ -59,7 +61,8 @@ __global__ void __launch_bounds__(256) pad_x_kernel(const T* __restrict__ src,
   if (xp < Ps) {
     int x = xp - 1, y = yp - 1, z = zp - 1;
     const bool out = x < 0 || x >= W || y < 0 || y >= W || z < 0 || z >= H;
-    if (!(border && out)) {
+    const bool zero = ((border & 1) && out) || ((border & 2) && z < 0) || ((border & 4) && z >= H);
+    if (!zero) {
       x = min(max(x, 0), W - 1);
       y = min(max(y, 0), W - 1);
       z = min(max(z, 0), H - 1);
@@ -152,6 +155,17 @@ cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
     PAD(__nv_bfloat16);
   }
 #undef PAD
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pad_volume_sub(const float* src, int W, int nz, int Pf, bool zero_lo,
+                                  bool zero_hi, float* px, float* py, cudaStream_t st) {
+  const int Ps = W + 2, Pz = nz + 2;
+  dim3 blk(32, 8), g1((Pf + 31) / 32, (Ps + 7) / 8, Pz);
+  dim3 g2((Pf + 31) / 32, (Pf + 31) / 32, Pz);
+  const int mode = (zero_lo ? 2 : 0) | (zero_hi ? 4 : 0);
+  pad_x_kernel<float><<<g1, blk, 0, st>>>(src, px, W, nz, Pf, mode);
+  pad_transpose_kernel<float><<<g2, blk, 0, st>>>(px, py, Ps, Pf);
   return cudaGetLastError();
 }
 
@@ -306,6 +320,33 @@ __device__ __forceinline__ float sample_at(const T* base, int sa, int sz, float 
   return fmaf(wz, s1 - s0, s0);
 }
 
+// sample_at for a sub-volume slab from global memory: z rows r and r + 1 of
+// a tensor of zrows rows, a row outside it reading as zeros (what a TMA copy
+// fills there), with sample_at's operations.
+template <bool Z2, typename T>
+__device__ __forceinline__ float sample_rows(const T* col, int r, int zrows, int sa, int sz,
+                                             float wa, float wf, float wz) {
+  float s0 = 0.f, s1 = 0.f;
+  if (r >= 0 && r < zrows) {
+    const T* b = col + (size_t)r * sz;
+    const float v00 = ld_any(b), v01 = ld_any(b + 1);
+    const float v10 = ld_any(b + sa), v11 = ld_any(b + sa + 1);
+    const float r0 = fmaf(wf, v01 - v00, v00);
+    const float r1 = fmaf(wf, v11 - v10, v10);
+    s0 = fmaf(wa, r1 - r0, r0);
+  }
+  if (!Z2) return s0;
+  if (r + 1 >= 0 && r + 1 < zrows) {
+    const T* b = col + (size_t)(r + 1) * sz;
+    const float u00 = ld_any(b), u01 = ld_any(b + 1);
+    const float u10 = ld_any(b + sa), u11 = ld_any(b + sa + 1);
+    const float q0 = fmaf(wf, u01 - u00, u00);
+    const float q1 = fmaf(wf, u11 - u10, u10);
+    s1 = fmaf(wa, q1 - q0, q0);
+  }
+  return fmaf(wz, s1 - s0, s0);
+}
+
 // a - b on both lanes of a packed FP32x2 pair (one sub.rn.f32x2).
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
   float2 d;
@@ -347,6 +388,8 @@ struct SlabJob {
   int det_w, det_h, S, Z, Pf;
   float u0, v0, bx, by, bz, SR, RD, step;
   float du, dv, ou, ov;  // detector pitch and sub-pixel ray offset
+  int zoff, zrows, accum;  // sub-volume slab (RayArgs)
+  float zlo, zhi;
   Trig tr;
   long long P;      // detector pixels per view
   long long gview;  // sinogram / pre / post slot of the view
@@ -399,7 +442,9 @@ __device__ __forceinline__ void slab_init_barriers(SlabShared& S) {
 // ZL (decoupled detector): par / fan rays whose constant z falls between
 // texel rows interpolate in z as well, and rays that miss the volume sample
 // nothing.
-template <int GEOM, int EPI, typename TV, typename TO, bool ZL = false>
+// SUB: a z-slab of the volume (launch_fp_slab_sub); each ray samples only
+// the k whose z taps can reach the slab's rows.
+template <int GEOM, int EPI, typename TV, typename TO, bool ZL = false, bool SUB = false>
 __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, SlabShared& S,
                                           uint32_t& phase, uint32_t& issued,
                                           const SlabEpi& E) {
@@ -425,7 +470,27 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   const float da = xdom ? r.dx : r.dy, df = xdom ? r.dy : r.dx, dz = r.dz;
   // On a decoupled detector (ZL) a ray that misses the volume samples nothing.
   const bool miss = ZL && !hits_box(s, e, J.bx, J.by, J.bz);
-  const int n = (valid && !miss) ? r.n : 0;
+  int n = (valid && !miss) ? r.n : 0;
+  int k0 = 0;  // first sample
+  if (SUB && n > 0) {
+    // Samples with tz in [zlo, zhi) can touch the slab's rows; the others
+    // read zeros only.  The range is widened by one sample each way, so
+    // rounding can only add samples that contribute exact zeros.
+    if (dz == 0.f) {
+      if (!(tz0 >= J.zlo && tz0 < J.zhi)) n = 0;
+    } else {
+      const float ka = (J.zlo - tz0) / dz, kb = (J.zhi - tz0) / dz;
+      const float lim = (float)n + 2.0f;
+      const float kmin = fminf(fmaxf(fminf(ka, kb), -2.0f), lim);
+      const float kmax = fminf(fmaxf(fmaxf(ka, kb), -2.0f), lim);
+      k0 = max((int)floorf(kmin) - 1, 0);
+      n = min((int)ceilf(kmax) + 2, n);
+      if (k0 >= n) {
+        k0 = 0;
+        n = 0;
+      }
+    }
+  }
 
   if (tid == 0) {
     S.amin = 0x7fffffff;
@@ -446,7 +511,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     S.corner[cid][3] = e[0]; S.corner[cid][4] = e[1]; S.corner[cid][5] = e[2];
   }
   if (n > 0) {
-    const int t_first = __float2int_rd(ta0);
+    const int t_first = __float2int_rd(SUB ? fmaf((float)k0, da, ta0) : ta0);
     const int t_last = __float2int_rd(fmaf((float)(n - 1), da, ta0));
     atomicMin(&S.amin, min(t_first, t_last));
     atomicMax(&S.amax, max(t_first, t_last));
@@ -545,7 +610,8 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_expect_tx(&bar[j & 1], (uint32_t)(nbox * kBoxZ * kPlane * sizeof(TV)));
     for (int bx = 0; bx < nbox; ++bx)
-      tma_load_3d(dst + (size_t)bx * kBoxZ * kPlane, tm, f0, alo, z0 + bx * kBoxZ, &bar[j & 1]);
+      tma_load_3d(dst + (size_t)bx * kBoxZ * kPlane, tm, f0, alo,
+                  z0 + bx * kBoxZ - (SUB ? J.zoff : 0), &bar[j & 1]);
     // thread 0 counts the copies issued into each buffer (16 bits each)
     issued += 1u << (16 * (j & 1));
   };
@@ -560,7 +626,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   // par / fan rays keep one z tap row for the whole ray
   const float fzc = floorf(tz0);
   const float2 fz02 = make_float2(fzc, fzc), wz02 = make_float2(tz0 - fzc, tz0 - fzc);
-  int k = 0;
+  int k = k0;
   for (int j = 0; j < nslab; ++j) {
     // Buffer (j+1)&1 was released by the barrier that ended slab j-1.
     if (tid == 0 && j + 1 < nslab) issue(j + 1);
@@ -641,8 +707,12 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
         const float ffq = floorf(tfq), fzq = floorf(tzq);
         const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
         const int gz = min(max((int)fzq, 0), Pz - 2);
-        acc += sample_at<ZW>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
-                             Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
+        if (SUB)
+          acc += sample_rows<ZW>(gv + (size_t)gf + (size_t)Pf * (size_t)ga, gz - J.zoff,
+                                 J.zrows, Pf, Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
+        else
+          acc += sample_at<ZW>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz),
+                               Pf, Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
         ++k;
       }
     }
@@ -658,7 +728,8 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     const size_t pix = (size_t)iy * J.det_w + ix;
     const size_t gi = (size_t)J.gview * J.P + pix;
     if (EPI == 0) {
-      stf(static_cast<TO*>(J.out) + gi, l);
+      TO* o = static_cast<TO*>(J.out) + gi;
+      stf(o, (SUB && J.accum) ? ldp(o) + l : l);
     } else {
       // CUDAmex_oscIter.cu:262-268: pre' = pre e^-l - post, post' = pre e^-l l.
       const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
@@ -674,7 +745,8 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   __syncthreads();
 }
 
-template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = false>
+template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = false,
+          bool SUB = false>
 __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
     const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
     const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
@@ -692,6 +764,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   J.u0 = A.u0; J.v0 = A.v0; J.bx = A.bx; J.by = A.by; J.bz = A.bz;
   J.SR = A.SR; J.RD = A.RD; J.step = A.step;
   J.du = A.du; J.dv = A.dv; J.ou = A.ou; J.ov = A.ov;
+  J.zoff = A.zoff; J.zrows = A.zrows; J.accum = A.accum; J.zlo = A.zlo; J.zhi = A.zhi;
   J.tr = A.trig[view];
   J.P = A.P;
   J.gview = A.view0 + (long long)view * A.vstride;
@@ -699,7 +772,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   J.tu0 = (blockIdx.y % tiles_u) * 32;
   J.tv0 = (blockIdx.y / tiles_u) * 8;
   J.tmx = &tmx; J.tmy = &tmy; J.px = px; J.py = py; J.out = out;
-  slab_tile<GEOM, EPI, TV, TO, ZL>(J, buf0, buf1, S, phase, issued, E);
+  slab_tile<GEOM, EPI, TV, TO, ZL, SUB>(J, buf0, buf1, S, phase, issued, E);
 }
 
 // ---------------------------------------------------------------------------
@@ -738,6 +811,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_batch_kernel(
     J.u0 = B.u0; J.v0 = B.v0; J.bx = B.bx; J.by = B.by; J.bz = B.bz;
     J.SR = B.sad; J.RD = B.sad; J.step = B.step;
     J.du = 1.0f; J.dv = 1.0f; J.ou = 0.0f; J.ov = 0.0f;
+    J.zoff = 0; J.zrows = B.H + 2; J.accum = 0; J.zlo = 0.f; J.zhi = 0.f;
     J.tr = B.trig[view];
     J.P = (long long)B.W * B.H;
     J.gview = view;
@@ -803,11 +877,12 @@ cudaError_t launch_fp_batch(const BatchFp* d_probs, int nprob, long long total,
   return cudaGetLastError();
 }
 
-template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = false>
+template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = false,
+          bool SUB = false>
 static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtensorMap& my,
                            const void* px, const void* py, int Pf, void* out,
                            const SlabEpi& e, cudaStream_t st) {
-  auto k = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO, ZL>;
+  auto k = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO, ZL, SUB>;
   const size_t smem = 2 * (size_t)kBufElems * sizeof(TV) + 128;
   static bool attr_set = false;  // once per instantiation (before any capture)
   if (!attr_set) {
@@ -829,6 +904,18 @@ cudaError_t launch_fp_slab_det(int geom, const RayArgs& a, const CUtensorMap& mx
   if (geom == 0) return slab_go<0, false, 0, float, float, true>(a, mx, my, px, py, Pf, out, e, st);
   if (geom == 1) return slab_go<1, false, 0, float, float, true>(a, mx, my, px, py, Pf, out, e, st);
   if (geom == 2) return slab_go<2, false, 0, float, float, true>(a, mx, my, px, py, Pf, out, e, st);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fp_slab_sub(int geom, const RayArgs& a, const CUtensorMap& mx,
+                               const CUtensorMap& my, const void* px, const void* py, int Pf,
+                               float* out, const SlabEpi& e, cudaStream_t st) {
+  if (geom == 0)
+    return slab_go<0, false, 0, float, float, false, true>(a, mx, my, px, py, Pf, out, e, st);
+  if (geom == 1)
+    return slab_go<1, false, 0, float, float, false, true>(a, mx, my, px, py, Pf, out, e, st);
+  if (geom == 2)
+    return slab_go<2, false, 0, float, float, false, true>(a, mx, my, px, py, Pf, out, e, st);
   return cudaErrorInvalidValue;
 }
 

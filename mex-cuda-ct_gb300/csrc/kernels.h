@@ -22,6 +22,12 @@ struct RayArgs {
   int pts_per_view;        // general3D: per-view points
   float du, dv;            // pixel pitch at the isocentre (1: the reference's)
   float ou, ov;            // sub-pixel ray offset (0: the reference's)
+  // Sub-volume FP (launch_fp_slab_sub): the padded tensors hold zrows padded
+  // rows starting at full padded row zoff; samples whose z taps lie outside
+  // [zlo, zhi) (tap space) read only zero rows and are skipped; accum: add to
+  // the output instead of storing.
+  int zoff, zrows, accum;
+  float zlo, zhi;
   Trig trig[kMaxViews];
 };
 
@@ -39,6 +45,9 @@ struct VoxArgs {
   // launches ignore these fields: their detector is the volume's face.
   int det_w, det_h;
   float hwd, v0d, inv_du, inv_dv;
+  // Sub-volume BP (launch_bp_sub): output slices zoff .. zoff + nzs - 1 of
+  // the H-slice volume, from detector rows row0 .. row0 + nrows - 1.
+  int zoff, nzs, row0, nrows;
   Trig trig[kMaxViews];
 };
 
@@ -119,6 +128,20 @@ cudaError_t launch_fp_slab_det(int geom, const RayArgs& a, const CUtensorMap& mx
                                const CUtensorMap& my, const void* px, const void* py, int Pf,
                                float* out, const SlabEpi& e, cudaStream_t st);
 
+// Slab FP (FP32) of a z-slab of the volume (a.zoff, a.zrows, a.zlo, a.zhi,
+// a.accum): the slab's padded tensors hold its slices with a clamp frame at
+// the volume's own faces and zeros elsewhere, so the FPs of the slabs add up
+// to the FP of the whole volume.
+cudaError_t launch_fp_slab_sub(int geom, const RayArgs& a, const CUtensorMap& mx,
+                               const CUtensorMap& my, const void* px, const void* py, int Pf,
+                               float* out, const SlabEpi& e, cudaStream_t st);
+
+// Padded layouts of a z-slab of nz slices (FP32): frame rows below / above
+// the slab are zero where zero_lo / zero_hi (an inner slab face), else edge
+// copies (the volume's own face, clamp addressing).
+cudaError_t launch_pad_volume_sub(const float* src, int W, int nz, int Pf, bool zero_lo,
+                                  bool zero_hi, float* px, float* py, cudaStream_t st);
+
 cudaError_t launch_fp_tex(int geom, const RayArgs& a,
                           cudaTextureObject_t tex, float* out,
                           cudaStream_t st);
@@ -144,6 +167,13 @@ cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, i
 
 // Decoupled-detector BP (FP32 padded sinogram of a.det_w x a.det_h views).
 cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
+                          bool accumulate, cudaStream_t st);
+
+// Sub-volume BP: slices a.zoff .. a.zoff + a.nzs - 1 (a W x W x a.nzs FP32
+// slab) from a padded FP32 sinogram of detector rows a.row0 .. + a.nrows - 1
+// (which must hold every row the slab's columns reach: mexct_sub_rows).
+// Per voxel the same operations as launch_bp_padded with one view block.
+cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
                           bool accumulate, cudaStream_t st);
 
 // dst = w * src (first) or dst += w * src over n elements.

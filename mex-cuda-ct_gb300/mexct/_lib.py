@@ -71,6 +71,11 @@ SIGNATURES = {
     "mexct_bp_dev_ex": [_P, _P, _i, _i, _i, _i, _f, _P, _i, _P, _i, _P],
     "mexct_fp_det_dev": [_P, _P, _i, _i, _f, _P, _i, _i, _P, _P, _P],
     "mexct_bp_det_dev": [_P, _P, _P, _i, _f, _P, _i, _i, _i, _P, _P],
+    "mexct_sub_rows": [_i, _i, _f, _i, _i, _i, _c.POINTER(_i), _c.POINTER(_i)],
+    "mexct_fp_sub_dev": [_P, _P, _i, _i, _i, _i, _f, _P, _i, _i, _P, _i, _P],
+    "mexct_bp_sub_dev": [_P, _P, _i, _i, _i, _i, _i, _f, _P, _i, _i, _i, _P, _i, _P],
+    "mexct_fp_ooc": [_P, _P, _i, _i, _f, _P, _i, _i, _c.c_size_t, _P],
+    "mexct_bp_ooc": [_P, _P, _i, _i, _i, _f, _P, _i, _c.c_size_t, _P],
     "mexct_ctx_set_wait_limit": [_P, _i],
     "mexct_ctx_device_errors": [_P, _c.POINTER(_c.c_uint), _i],
 }

@@ -307,6 +307,66 @@ def bp_det_dev(sino, sad, angles, geom, W, H, du=1.0, dv=1.0, out=None, stream=N
     return out
 
 
+def sub_rows(W, H, sad, geom, z0, nz):
+    """Detector rows (row0, nrows) that the BP of slab z0 .. z0 + nz - 1 reads."""
+    r0, nr = ctypes.c_int(), ctypes.c_int()
+    _lib.call("mexct_sub_rows", int(W), int(H), float(sad), _geom_flag(geom), int(z0), int(nz),
+              ctypes.byref(r0), ctypes.byref(nr))
+    return r0.value, nr.value
+
+
+def fp_sub_dev(slab, H, z0, sad, angles, geom, out=None, accumulate=False, stream=None):
+    """FP of a device slab (nz, W, W) = slices z0 .. z0 + nz - 1 of an H-slice volume into a
+    sinogram (nP, H, W): stores, or adds to `out` with accumulate."""
+    import torch
+    nz, W, W2 = slab.shape
+    assert W == W2, "slab must be (nz, W, W)"
+    ang = _angles(angles, 0)
+    nP = ang.size
+    if out is None:
+        out = torch.zeros((nP, int(H), W), dtype=torch.float32, device=slab.device)
+    _lib.call("mexct_fp_sub_dev", None, _dptr(slab), W, int(H), int(z0), nz, float(sad), _ptr(ang),
+              nP, _geom_flag(geom), _dptr(out), 1 if accumulate else 0, _stream(stream))
+    return out
+
+
+def bp_sub_dev(rows, row0, H, sad, angles, geom, z0, nz, out=None, accumulate=False,
+               stream=None):
+    """BP into slab z0 .. z0 + nz - 1 (nz, W, W) from detector rows row0 .. of every view
+    (device array (nP, nrows, W))."""
+    import torch
+    nP, nrows, W = rows.shape
+    ang = _angles(angles, nP)
+    if out is None:
+        out = torch.empty((int(nz), W, W), dtype=torch.float32, device=rows.device)
+    _lib.call("mexct_bp_sub_dev", None, _dptr(rows), int(row0), nrows, W, int(H), nP, float(sad),
+              _ptr(ang), _geom_flag(geom), int(z0), int(nz), _dptr(out),
+              1 if accumulate else 0, _stream(stream))
+    return out
+
+
+def fp_ooc(vol, sad, angles, geom, budget_bytes):
+    """CUDAmex_FP of a host volume [W, W, H] with at most budget_bytes of device memory."""
+    vol = _f32F(vol, "vol")
+    W, _, H = vol.shape
+    ang = _angles(angles, 0)
+    out = np.empty((W, H, ang.size), dtype=np.float32, order="F")
+    _lib.call("mexct_fp_ooc", None, _ptr(vol), W, H, float(sad), _ptr(ang), ang.size,
+              _geom_flag(geom), int(budget_bytes), _ptr(out))
+    return out
+
+
+def bp_ooc(sino, sad, angles, geom, budget_bytes):
+    """CUDAmex_BP of a host sinogram [W, H, nP] with at most budget_bytes of device memory."""
+    sino = _f32F(sino, "projections")
+    W, H, nP = sino.shape
+    ang = _angles(angles, nP)
+    out = np.empty((W, W, H), dtype=np.float32, order="F")
+    _lib.call("mexct_bp_ooc", None, _ptr(sino), W, H, nP, float(sad), _ptr(ang),
+              _geom_flag(geom), int(budget_bytes), _ptr(out))
+    return out
+
+
 def g3d_fp_dev(vol, angles, pts, out=None, stream=None):
     """general3D FP: vol (Z, S, S); pts (6, H, W) or (nP, 6, H, W) -> (nP, H, W)."""
     import torch
