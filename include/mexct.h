@@ -39,6 +39,7 @@ typedef int mexct_status;
 #define MEXCT_ERR_UNSUPPORTED 4 /* valid in the reference but not supported */
 #define MEXCT_ERR_TIMEOUT 5     /* a bounded device-side wait gave up */
 #define MEXCT_ERR_BUDGET 6      /* request exceeds the admission budget */
+#define MEXCT_ERR_IO 7          /* a file cannot be read, written or parsed */
 
 /* Storage types for the _ex entry points. */
 #define MEXCT_F32 0
@@ -261,6 +262,38 @@ mexct_status mexct_fp_ooc(mexct_ctx* ctx, const float* vol, int W, int H,
 mexct_status mexct_bp_ooc(mexct_ctx* ctx, const float* sino, int W, int H,
                           int nP, float sad, const float* angles, int geom,
                           size_t budget_bytes, float* vol);
+
+/* ---- scanner data files -------------------------------------------------- */
+
+/* No counterpart in the reference (its .vff / .mat data are read in MATLAB and
+ * kept out of the repository, .gitignore:14-16).  Arrays are float32,
+ * column-major, as the entry points take them.
+ *
+ * MAT-file Level 5 (MATLAB save up to -v7, compressed or not, either byte
+ * order): mexct_mat_list writes the variable names, '\n'-separated;
+ * mexct_mat_info gives a variable's dimensions (name NULL or "": the first
+ * numeric one); mexct_mat_read converts its real part (any numeric class) to
+ * float32, count = the product of the dimensions.  -v7.3 (HDF5) files:
+ * MEXCT_ERR_UNSUPPORTED.  mexct_mat_write writes one single-precision
+ * variable, creating the file or (append != 0) adding to it.
+ *
+ * VFF ("ncaa" header, single-band raster slices, big-endian data; bits 8
+ * unsigned, 16 signed, 32 float): mexct_vff_info gives the size X, Y, Z (Z = 1
+ * for rank 2), spacing and bits; mexct_vff_read converts to float32 (x
+ * fastest); mexct_vff_write writes bits 16 (rounded, saturated) or 32. */
+mexct_status mexct_mat_list(const char* path, char* names, size_t capacity);
+mexct_status mexct_mat_info(const char* path, const char* name, int* ndims,
+                            long long* dims);
+mexct_status mexct_mat_read(const char* path, const char* name, float* out,
+                            long long count);
+mexct_status mexct_mat_write(const char* path, const char* name,
+                             const float* data, int ndims,
+                             const long long* dims, int append);
+mexct_status mexct_vff_info(const char* path, int* dims, float* spacing,
+                            int* bits);
+mexct_status mexct_vff_read(const char* path, float* out, long long count);
+mexct_status mexct_vff_write(const char* path, const float* data,
+                             const int* dims, const float* spacing, int bits);
 
 /* ---- launch shapes and autotuning -------------------------------------- */
 

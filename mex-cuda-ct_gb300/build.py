@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmexct.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["k_proj.cu", "k_slab.cu", "k_iter.cu", "batch.cu", "api.cu", "ops.cu", "solver.cu",
-           "serve.cu", "noalloc.cu", "tune.cu", "subvol.cu"]
+           "serve.cu", "noalloc.cu", "tune.cu", "subvol.cu", "fileio.cpp"]
 
 
 def nvcc() -> str:
@@ -38,7 +38,7 @@ def _deps(src: str) -> list[str]:
 
 def _compile(src: str, verbose: bool) -> str:
     path = os.path.join(CSRC, src)
-    obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in _deps(path)):
         return obj
     cmd = [nvcc(), "-c", path, "-o", obj + ".tmp", *ARCH, "-O3", "-lineinfo", "-std=c++17",

@@ -14,7 +14,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(_HERE)
 LIB_PATH = os.path.join(PKG, "_build", "libmexct.so")
 
-OK, ERR_ARG, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED, ERR_TIMEOUT, ERR_BUDGET = range(7)
+OK, ERR_ARG, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED, ERR_TIMEOUT, ERR_BUDGET, ERR_IO = range(8)
 F32, F16, BF16 = 0, 1, 2
 FP_EXPLICIT, FP_TEXTURE, FP_RAY, FP_AUTO = 0, 1, 2, 3
 OP_FP, OP_BP = 0, 1
@@ -76,6 +76,13 @@ SIGNATURES = {
     "mexct_bp_sub_dev": [_P, _P, _i, _i, _i, _i, _i, _f, _P, _i, _i, _i, _P, _i, _P],
     "mexct_fp_ooc": [_P, _P, _i, _i, _f, _P, _i, _i, _c.c_size_t, _P],
     "mexct_bp_ooc": [_P, _P, _i, _i, _i, _f, _P, _i, _c.c_size_t, _P],
+    "mexct_mat_list": [_c.c_char_p, _c.c_char_p, _c.c_size_t],
+    "mexct_mat_info": [_c.c_char_p, _c.c_char_p, _c.POINTER(_i), _c.POINTER(_c.c_longlong)],
+    "mexct_mat_read": [_c.c_char_p, _c.c_char_p, _P, _c.c_longlong],
+    "mexct_mat_write": [_c.c_char_p, _c.c_char_p, _P, _i, _c.POINTER(_c.c_longlong), _i],
+    "mexct_vff_info": [_c.c_char_p, _c.POINTER(_i), _F, _c.POINTER(_i)],
+    "mexct_vff_read": [_c.c_char_p, _P, _c.c_longlong],
+    "mexct_vff_write": [_c.c_char_p, _P, _c.POINTER(_i), _F, _i],
     "mexct_ctx_set_wait_limit": [_P, _i],
     "mexct_ctx_device_errors": [_P, _c.POINTER(_c.c_uint), _i],
 }
