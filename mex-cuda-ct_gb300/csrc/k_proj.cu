@@ -22,6 +22,7 @@
 //   come from a padded copy of the sinogram through L1; the volume is written
 //   once.
 #include <algorithm>
+#include <type_traits>
 #include <cstdio>
 
 #include "kernels.h"
@@ -384,6 +385,34 @@ cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews,
   return cudaGetLastError();
 }
 
+// Quad layout of the clamp-padded views (BP, FP32): padded texel (r, c) of
+// view v -> {P(r,c), P(r,c+1), P(r+1,c), P(r+1,c+1)} with P(r, c) = the view's
+// pixel (clamp(c - kSinoPad), clamp(r - kSinoPad)), as in pad_sino_kernel.
+__global__ void __launch_bounds__(256) pad_sino_quad_kernel(const float* __restrict__ in, int W,
+                                                            int H, float4* __restrict__ out,
+                                                            int Wp) {
+  const int c = blockIdx.x * 32 + threadIdx.x;
+  const int r = blockIdx.y * 8 + threadIdx.y;
+  const int v = blockIdx.z;
+  const int Hp = H + 2 * kSinoPad;
+  if (c >= Wp || r >= Hp) return;
+  const float* view = in + (size_t)v * W * H;
+  const int x0 = min(max(c - kSinoPad, 0), W - 1), x1 = min(max(c + 1 - kSinoPad, 0), W - 1);
+  const int y0 = min(max(r - kSinoPad, 0), H - 1), y1 = min(max(r + 1 - kSinoPad, 0), H - 1);
+  out[((size_t)v * Hp + r) * Wp + c] =
+      make_float4(__ldg(view + (size_t)y0 * W + x0), __ldg(view + (size_t)y0 * W + x1),
+                  __ldg(view + (size_t)y1 * W + x0), __ldg(view + (size_t)y1 * W + x1));
+}
+
+cudaError_t launch_pad_sino_quad(const float* in, int W, int H, int nviews, float4* out,
+                                 cudaStream_t st) {
+  if (nviews <= 0) return cudaSuccess;
+  const int Wp = sino_pad_pitch(W);
+  dim3 blk(32, 8), grd((Wp + 31) / 32, (H + 2 * kSinoPad + 7) / 8, nviews);
+  pad_sino_quad_kernel<<<grd, blk, 0, st>>>(in, W, H, out, Wp);
+  return cudaGetLastError();
+}
+
 // Sample one padded projection along a voxel column: acc[j] += w * B(py, pz).
 // g.py / g.pz0 are texture coordinates (texel centres at i + 0.5).
 // W x H is the detector; ROWS: the column's z rows are texel rows (par / fan
@@ -442,6 +471,42 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
   }
 }
 
+// Cone column over a quad-layout view (launch_pad_sino_quad): texel (r, c)
+// holds the bilinear footprint {P(r,c), P(r,c+1), P(r+1,c), P(r+1,c+1)} of
+// the padded view P, so each voxel's four taps are one 16-byte load.  The
+// arithmetic is bp_column_pad's (GEOM 2), operation for operation.
+template <int ZC>
+__device__ __forceinline__ void bp_column_quad(const float4* __restrict__ p, int W, int H, int Wp,
+                                               int z0, const ColGeom<2>& g, float* acc) {
+  const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
+  const float fu = floorf(cu);
+  const float au = cu - fu;
+  const int iu = min(max((int)fu, -kSinoPad), W) + kSinoPad;
+  const float w0 = g.w * (1.0f - au), w1 = g.w * au;
+  const float4* col = p + iu;
+  static_assert(ZC % 2 == 0, "ZC must be even");
+  const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
+  const float pz0 = g.pz0 - 0.5f;
+  const float2 dpz2 = make_float2(g.dpz, g.dpz), pz02 = make_float2(pz0, pz0);
+#pragma unroll
+  for (int j = 0; j < ZC; j += 2) {
+    const float2 zz = make_float2((float)(z0 + j), (float)(z0 + j + 1));
+    const float2 cz = __ffma2_rn(zz, dpz2, pz02);
+    const float2 fz = make_float2(floorf(cz.x), floorf(cz.y));
+    const float2 az = __fadd2_rn(cz, make_float2(-fz.x, -fz.y));
+    const int i0 = min(max(__float2int_rz(fz.x), -kSinoPad), H) + kSinoPad;
+    const int i1 = min(max(__float2int_rz(fz.y), -kSinoPad), H) + kSinoPad;
+    const float4 q0 = __ldg(col + (size_t)i0 * Wp);
+    const float4 q1 = __ldg(col + (size_t)i1 * Wp);
+    const float2 a = __ffma2_rn(w02, make_float2(q0.x, q1.x), __fmul2_rn(w12, make_float2(q0.y, q1.y)));
+    const float2 b = __ffma2_rn(w02, make_float2(q0.z, q1.z), __fmul2_rn(w12, make_float2(q0.w, q1.w)));
+    const float2 omaz = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-az.x, -az.y));
+    const float2 t = __ffma2_rn(omaz, a, __ffma2_rn(az, b, make_float2(acc[j], acc[j + 1])));
+    acc[j] = t.x;
+    acc[j + 1] = t.y;
+  }
+}
+
 // Launch shape (BpShape): ZC z voxels per thread, blocks of 32 x rows
 // columns, and the views split into vblocks blocks along grid z.  With
 // vblocks > 1 every view block writes FP32 partial sums to part[vb][voxel]
@@ -471,7 +536,14 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
   if (in_circle(ix, iy, A.hw)) {
     const float x = (float)ix - ((float)A.hw + 0.5f);
     const float y = (float)iy - ((float)A.hw + 0.5f);
-    if (MODE == 1) {
+    if constexpr (std::is_same<TS, float4>::value) {
+      // cone, FP32 quad-layout views (launch_bp_quad)
+      const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
+      for (int v = vbeg; v < vend; ++v) {
+        const ColGeom<2> g = col_geom<2>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
+        bp_column_quad<ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+      }
+    } else if constexpr (MODE == 1) {
       // decoupled detector (launch_bp_det): its own size, centre and pitch
       const size_t vstride = (size_t)Wp * (A.det_h + 2 * kSinoPad);
       for (int v = vbeg; v < vend; ++v) {
@@ -480,7 +552,7 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
         bp_column_pad<GEOM, ZC, TS, false>(sino + (size_t)v * vstride, A.det_w, A.det_h, Wp, z0,
                                            g, acc);
       }
-    } else if (MODE == 2) {
+    } else if constexpr (MODE == 2) {
       // z-slab: voxel z = zoff + local z, taps in full-detector rows minus row0
       const size_t vstride = (size_t)Wp * (A.nrows + 2 * kSinoPad);
       for (int v = vbeg; v < vend; ++v) {
@@ -586,6 +658,17 @@ cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, i
     case 2: return bp_pad_types<2>(a, sino_pad, stype, Wp, vol, vtype, accumulate, shp, part, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_bp_quad(const VoxArgs& a, const float4* sino_quad, void* vol, int vtype,
+                           bool accumulate, const BpShape& shp, float* part, cudaStream_t st) {
+  if (!bp_shape_valid(shp) || (shp.vblocks > 1 && !part)) return cudaErrorInvalidValue;
+  const int Wp = sino_pad_pitch(a.W);
+  if (vtype == kF32) return bp_pad_zc<2, float4, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  if (vtype == kF16) return bp_pad_zc<2, float4, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  if (vtype == kBF16)
+    return bp_pad_zc<2, float4, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  return cudaErrorInvalidValue;
 }
 
 // Decoupled-detector BP: FP32 sinogram of det_w x det_h views padded with

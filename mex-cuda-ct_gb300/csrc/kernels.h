@@ -165,6 +165,13 @@ cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, i
                              void* vol, int vtype, bool accumulate, const BpShape& shp,
                              float* part, cudaStream_t st);
 
+// Cone BP (FP32 views) from the quad layout of launch_pad_sino_quad: the same
+// result as launch_bp_padded on the clamp-padded views, bit for bit.
+cudaError_t launch_pad_sino_quad(const float* in, int W, int H, int nviews, float4* out,
+                                 cudaStream_t st);
+cudaError_t launch_bp_quad(const VoxArgs& a, const float4* sino_quad, void* vol, int vtype,
+                           bool accumulate, const BpShape& shp, float* part, cudaStream_t st);
+
 // Decoupled-detector BP (FP32 padded sinogram of a.det_w x a.det_h views).
 cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
                           bool accumulate, cudaStream_t st);

@@ -180,7 +180,10 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
   }
   if (!bp_shape_valid(shp)) return set_err(MEXCT_ERR_ARG, "bp: invalid launch shape");
   const int chunk = std::min(nP, kMaxViews);
-  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) * dsize(stype), st),
+  // cone, FP32 views: quad layout (one 16-byte load per voxel and view)
+  const bool quad = geom == 2 && stype == kF32;
+  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) *
+                                          (quad ? sizeof(float4) : dsize(stype)), st),
                  "bp: workspace");
   const size_t N = (size_t)W * W * H;
   if (shp.vblocks > 1)
@@ -191,6 +194,15 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
     a->view0 = 0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
     const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
+    if (quad) {
+      MEXCT_TRY_CUDA(launch_pad_sino_quad(static_cast<const float*>(static_cast<const void*>(src)),
+                                          W, H, a->nviews, c->spad.as<float4>(), st),
+                     "bp: pad");
+      MEXCT_TRY_CUDA(launch_bp_quad(*a, c->spad.as<float4>(), d_vol, vt, v0 > 0, shp,
+                                    c->bpart.as<float>(), st),
+                     "bp: launch");
+      continue;
+    }
     MEXCT_TRY_CUDA(launch_pad_sino(src, stype, W, H, a->nviews, false, c->spad.p, st),
                    "bp: pad");
     MEXCT_TRY_CUDA(launch_bp_padded(geom, *a, c->spad.p, stype, d_vol, vt, v0 > 0, shp,
