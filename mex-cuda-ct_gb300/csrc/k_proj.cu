@@ -404,6 +404,30 @@ __global__ void __launch_bounds__(256) pad_sino_quad_kernel(const float* __restr
                   __ldg(view + (size_t)y1 * W + x0), __ldg(view + (size_t)y1 * W + x1));
 }
 
+// Pair layout of the clamp-padded views (par / fan BP, FP32): padded texel
+// (r, c) -> {P(r,c), P(r,c+1)}.
+__global__ void __launch_bounds__(256) pad_sino_pair_kernel(const float* __restrict__ in, int W,
+                                                            int H, float2* __restrict__ out,
+                                                            int Wp) {
+  const int c = blockIdx.x * 32 + threadIdx.x;
+  const int r = blockIdx.y * 8 + threadIdx.y;
+  const int v = blockIdx.z;
+  const int Hp = H + 2 * kSinoPad;
+  if (c >= Wp || r >= Hp) return;
+  const float* row = in + ((size_t)v * H + min(max(r - kSinoPad, 0), H - 1)) * W;
+  const int x0 = min(max(c - kSinoPad, 0), W - 1), x1 = min(max(c + 1 - kSinoPad, 0), W - 1);
+  out[((size_t)v * Hp + r) * Wp + c] = make_float2(__ldg(row + x0), __ldg(row + x1));
+}
+
+cudaError_t launch_pad_sino_pair(const float* in, int W, int H, int nviews, float2* out,
+                                 cudaStream_t st) {
+  if (nviews <= 0) return cudaSuccess;
+  const int Wp = sino_pad_pitch(W);
+  dim3 blk(32, 8), grd((Wp + 31) / 32, (H + 2 * kSinoPad + 7) / 8, nviews);
+  pad_sino_pair_kernel<<<grd, blk, 0, st>>>(in, W, H, out, Wp);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pad_sino_quad(const float* in, int W, int H, int nviews, float4* out,
                                  cudaStream_t st) {
   if (nviews <= 0) return cudaSuccess;
@@ -507,6 +531,32 @@ __device__ __forceinline__ void bp_column_quad(const float4* __restrict__ p, int
   }
 }
 
+// Par / fan column over a pair-layout view (launch_pad_sino_pair): texel
+// (r, c) holds {P(r,c), P(r,c+1)}, so each voxel's two taps (its z row is a
+// texel row) are one 8-byte load.  bp_column_pad's arithmetic (ROWS path).
+template <int GEOM, int ZC>
+__device__ __forceinline__ void bp_column_pair(const float2* __restrict__ p, int W, int H, int Wp,
+                                               int z0, const ColGeom<GEOM>& g, float* acc) {
+  const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
+  const float fu = floorf(cu);
+  const float au = cu - fu;
+  const int iu = min(max((int)fu, -kSinoPad), W) + kSinoPad;
+  const float w0 = g.w * (1.0f - au), w1 = g.w * au;
+  const float2* col = p + iu;
+  static_assert(ZC % 2 == 0, "ZC must be even");
+  const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
+#pragma unroll
+  for (int j = 0; j < ZC; j += 2) {
+    const float2 q0 = __ldg(col + (size_t)(min(z0 + j, H - 1) + kSinoPad) * Wp);
+    const float2 q1 = __ldg(col + (size_t)(min(z0 + j + 1, H - 1) + kSinoPad) * Wp);
+    const float2 t = __ffma2_rn(w02, make_float2(q0.x, q1.x),
+                                __ffma2_rn(w12, make_float2(q0.y, q1.y),
+                                           make_float2(acc[j], acc[j + 1])));
+    acc[j] = t.x;
+    acc[j + 1] = t.y;
+  }
+}
+
 // Launch shape (BpShape): ZC z voxels per thread, blocks of 32 x rows
 // columns, and the views split into vblocks blocks along grid z.  With
 // vblocks > 1 every view block writes FP32 partial sums to part[vb][voxel]
@@ -542,6 +592,14 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
       for (int v = vbeg; v < vend; ++v) {
         const ColGeom<2> g = col_geom<2>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
         bp_column_quad<ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+      }
+    } else if constexpr (std::is_same<TS, float2>::value) {
+      // par / fan, FP32 pair-layout views (launch_bp_pair)
+      const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
+      for (int v = vbeg; v < vend; ++v) {
+        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
+                                               1.f, 1.f);
+        bp_column_pair<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
       }
     } else if constexpr (MODE == 1) {
       // decoupled detector (launch_bp_det): its own size, centre and pitch
@@ -668,6 +726,27 @@ cudaError_t launch_bp_quad(const VoxArgs& a, const float4* sino_quad, void* vol,
   if (vtype == kF16) return bp_pad_zc<2, float4, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   if (vtype == kBF16)
     return bp_pad_zc<2, float4, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_bp_pair(int geom, const VoxArgs& a, const float2* sino_pair, void* vol,
+                           int vtype, bool accumulate, const BpShape& shp, float* part,
+                           cudaStream_t st) {
+  if (!bp_shape_valid(shp) || (shp.vblocks > 1 && !part)) return cudaErrorInvalidValue;
+  const int Wp = sino_pad_pitch(a.W);
+#define PAIR(G)                                                                              \
+  do {                                                                                       \
+    if (vtype == kF32)                                                                       \
+      return bp_pad_zc<G, float2, float>(a, sino_pair, Wp, vol, accumulate, shp, part, st);  \
+    if (vtype == kF16)                                                                       \
+      return bp_pad_zc<G, float2, __half>(a, sino_pair, Wp, vol, accumulate, shp, part, st); \
+    if (vtype == kBF16)                                                                      \
+      return bp_pad_zc<G, float2, __nv_bfloat16>(a, sino_pair, Wp, vol, accumulate, shp,    \
+                                                 part, st);                                  \
+  } while (0)
+  if (geom == 0) PAIR(0);
+  else if (geom == 1) PAIR(1);
+#undef PAIR
   return cudaErrorInvalidValue;
 }
 

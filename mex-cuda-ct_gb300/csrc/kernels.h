@@ -172,6 +172,14 @@ cudaError_t launch_pad_sino_quad(const float* in, int W, int H, int nviews, floa
 cudaError_t launch_bp_quad(const VoxArgs& a, const float4* sino_quad, void* vol, int vtype,
                            bool accumulate, const BpShape& shp, float* part, cudaStream_t st);
 
+// Par / fan BP (FP32 views) from the pair layout of launch_pad_sino_pair: the
+// same result as launch_bp_padded, bit for bit.
+cudaError_t launch_pad_sino_pair(const float* in, int W, int H, int nviews, float2* out,
+                                 cudaStream_t st);
+cudaError_t launch_bp_pair(int geom, const VoxArgs& a, const float2* sino_pair, void* vol,
+                           int vtype, bool accumulate, const BpShape& shp, float* part,
+                           cudaStream_t st);
+
 // Decoupled-detector BP (FP32 padded sinogram of a.det_w x a.det_h views).
 cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
                           bool accumulate, cudaStream_t st);

@@ -180,11 +180,11 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
   }
   if (!bp_shape_valid(shp)) return set_err(MEXCT_ERR_ARG, "bp: invalid launch shape");
   const int chunk = std::min(nP, kMaxViews);
-  // cone, FP32 views: quad layout (one 16-byte load per voxel and view)
-  const bool quad = geom == 2 && stype == kF32;
-  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) *
-                                          (quad ? sizeof(float4) : dsize(stype)), st),
-                 "bp: workspace");
+  // FP32 views: quad layout for cone (one 16-byte load per voxel and view),
+  // pair layout for par / fan (one 8-byte load)
+  const bool quad = geom == 2 && stype == kF32, pair = geom < 2 && stype == kF32;
+  const size_t es = quad ? sizeof(float4) : pair ? sizeof(float2) : dsize(stype);
+  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) * es, st), "bp: workspace");
   const size_t N = (size_t)W * W * H;
   if (shp.vblocks > 1)
     MEXCT_TRY_CUDA(c->bpart.ensure_async(N * shp.vblocks * sizeof(float), st), "bp: workspace");
@@ -199,6 +199,15 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
                                           W, H, a->nviews, c->spad.as<float4>(), st),
                      "bp: pad");
       MEXCT_TRY_CUDA(launch_bp_quad(*a, c->spad.as<float4>(), d_vol, vt, v0 > 0, shp,
+                                    c->bpart.as<float>(), st),
+                     "bp: launch");
+      continue;
+    }
+    if (pair) {
+      MEXCT_TRY_CUDA(launch_pad_sino_pair(static_cast<const float*>(static_cast<const void*>(src)),
+                                          W, H, a->nviews, c->spad.as<float2>(), st),
+                     "bp: pad");
+      MEXCT_TRY_CUDA(launch_bp_pair(geom, *a, c->spad.as<float2>(), d_vol, vt, v0 > 0, shp,
                                     c->bpart.as<float>(), st),
                      "bp: launch");
       continue;
