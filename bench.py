@@ -344,7 +344,8 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded 12-ellipsoid phantom)",
         "config": dict(workload_config(args),
-                       parallelism="replicas" if world > 1 else "single"),
+                       parallelism="replicas" if world > 1 else "single",
+                       fp_slab_ctas_per_sm=ops.fp_slab_occupancy()),
         "fp_gups": round(N * views / fp_t / 1e9, 3), "bp_gups": round(N * views / bp_t / 1e9, 3),
         "fp_ms": round(fp_t * 1e3, 3), "bp_ms": round(bp_t * 1e3, 3),
         "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": round(achieved, 2),
@@ -354,7 +355,7 @@ def main():
                      "traffic": dom[3],
                      "note": "gather-bound projector: compulsory bytes 4(N+P*nP) over the launch"},
         "clocks": clk,
-        # per step: pad_x, pad_transpose, fp_slab, pad_sino, bp_pad
+        # per step: pad_x, pad_transpose, fp_slab, pad_sino_quad, bp_pad
         "gpu_launches": 5 * args.steps,
         "e2e": e2e,
     }
@@ -413,6 +414,7 @@ def main():
                          ("batched", lambda: batched_uneven(args.batch_problems)),
                          ("serving", lambda: serving(args.serve_requests)),
                          ("detector", detector_section),
+                         ("other_operators", other_operators),
                          ("out_of_core", out_of_core)):
             try:
                 extra[name] = fn()
@@ -572,6 +574,65 @@ def batched_uneven(count, seed=2026):
     out["workload"] = ("%d problems: geom 0/1/2, 64^3..256^3, 90..720 views, SAD 1000; FP, BP, "
                        "5 OSC-TV iterations x 8 subsets each" % count)
     b.close()
+    return out
+
+
+def other_operators():
+    """The remaining operators at representative sizes, device-resident inputs, CUDA-synchronised
+    wall time (3 runs after a warm-up): general3D FP / BP on a cone helix (256^3, 256 x 256
+    detector, 360 views, per-view points), TV descent (512^3, 20 steps), FDK pre-filter
+    (512 x 512 x 720 cone views, ramp), OSC iteration (256^3, 60 cone views, 10 subsets)."""
+    import torch
+
+    from mexct import ops, phantoms
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    out = {}
+    n, nv = 256, 360
+    vol = phantoms.ellipsoids(n, count=10, seed=5, nz=n)
+    d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    pts, ang = phantoms.helix_pts(n, n, nv, n, sad=1000.0, turns=1.0, pitch=0.5)
+    dp = torch.from_numpy(np.ascontiguousarray(pts.transpose(3, 2, 1, 0))).cuda()
+    sino = ops.g3d_fp_dev(d, ang, dp)
+    tf = timed(lambda: ops.g3d_fp_dev(d, ang, dp, out=sino))
+    rec = torch.empty_like(d)
+    tb = timed(lambda: ops.g3d_bp_dev(sino, ang, dp, n, n, out=rec))
+    vu = float(n) ** 3 * nv
+    out["general3d_helix_256cube_360views"] = {"fp_s": round(tf, 4), "bp_s": round(tb, 4),
+                                               "fp_gups": round(vu / tf / 1e9, 3),
+                                               "bp_gups": round(vu / tb / 1e9, 3)}
+    del sino, rec, dp
+    m = 512
+    v5 = torch.from_numpy(np.ascontiguousarray(
+        phantoms.ellipsoids(m, count=12, seed=2024, nz=m).transpose(2, 1, 0))).cuda()
+    tv_out = torch.empty_like(v5)
+    t = timed(lambda: ops.tvmin3d_dev(v5, 0.2, 20, out=tv_out))
+    N = float(m) ** 3
+    out["tv_512cube_20steps"] = {"s": round(t, 4), "ms_per_step": round(t / 20 * 1e3, 3),
+                                 "gbs_per_step": round(4 * 3 * N / (t / 20) / 1e9, 1)}
+    ang7 = phantoms.angles_full(720)
+    s7 = ops.fp_dev(v5, 1000.0, ang7, 2)
+    f7 = torch.empty_like(s7)
+    t = timed(lambda: ops.prefilter_dev(s7, ang7, 2, 1000.0, "ramp", out=f7))
+    out["prefilter_cone_512x512x720_ramp"] = {"s": round(t, 4),
+                                              "gbs": round(2 * 4 * s7.numel() / t / 1e9, 1)}
+    del s7, f7, v5, tv_out
+    ang6 = phantoms.angles_full(60)
+    s6 = ops.fp_dev(d, 1000.0, ang6, 2)
+    pre = torch.full_like(s6, 1e5)
+    post = 1e5 * torch.exp(-s6)
+    mu = torch.zeros_like(d)
+    picks = np.arange(10, dtype=np.int32)
+    t = timed(lambda: ops.osc_iter_dev(mu, pre, post, 10, picks, ang6, 1000.0, 2))
+    out["osc_iteration_256cube_60views_10subsets"] = {"s": round(t, 4)}
     return out
 
 

@@ -191,6 +191,11 @@ mexct_status mexct_bp_dev_ex(mexct_ctx* ctx, const void* d_sino,
                              const float* angles, int geom, void* d_vol,
                              int vol_type, void* stream);
 
+/* Resident CTAs per SM of the cone FP32 slab kernel (256 threads, 57 KB of
+ * shared memory each) on the current device, by the occupancy calculator:
+ * 4 on a GB300. */
+mexct_status mexct_fp_slab_occupancy(int* ctas_per_sm);
+
 /* ---- decoupled detector ----------------------------------------------- */
 
 /* No counterpart in the reference, whose detector is always the volume's

@@ -80,9 +80,9 @@ mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int 
     for (int v = 0; v < p.nP; ++v) trig_of(p.angles[v], &trig[toff + v]);
     BatchFp& f = fd[i];
     std::memset(&f, 0, sizeof f);
-    MEXCT_TRY_CUDA(make_slab_tmap(&f.tmx, b->pads[2 * i].p, kF32, Pf, W + 2, H + 2),
+    MEXCT_TRY_CUDA(make_slab_tmap(&f.tmx, b->pads[2 * i].p, kF32, Pf, W + 2, H + 2, p.geom),
                    "batch_create: tensor map");
-    MEXCT_TRY_CUDA(make_slab_tmap(&f.tmy, b->pads[2 * i + 1].p, kF32, Pf, W + 2, H + 2),
+    MEXCT_TRY_CUDA(make_slab_tmap(&f.tmy, b->pads[2 * i + 1].p, kF32, Pf, W + 2, H + 2, p.geom),
                    "batch_create: tensor map");
     f.W = W;
     f.H = H;

@@ -6,7 +6,7 @@
 // issues ~28 L1 wavefronts per warp-sample, because the 32 rays of a warp
 // enter the volume through different faces and are spread along the ray
 // direction.  Here a CTA (32 x 8 detector pixels of one view) sweeps the
-// volume along the view's dominant axis a (x or y) in slabs of kSlabT tap
+// volume along the view's dominant axis a (x or y) in slabs of SlabCfg::T tap
 // planes.  Before the sweep the whole CTA plans every slab at once: the
 // bounding box of the tile's ray bundle in the slab, from the 4 corner rays
 // (the coordinates across a plane are monotone in the detector coordinates).
@@ -268,19 +268,34 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // Slab kernel.
 // ---------------------------------------------------------------------------
 constexpr int kSlabCtas = 4;                  // resident CTAs per SM (launch bounds)
-constexpr int kSlabT = 4;                     // a-taps per slab
-constexpr int kSlabA = kSlabT + 1;            // a-planes in a box
 constexpr int kBoxF = 64;                     // box extent along f (elements)
-constexpr int kBoxZ = 20;                     // z rows per TMA box: one copy per slab
-constexpr int kBZ = 20;                       // z rows per slab buffer (even)
-constexpr int kPlane = kSlabA * kBoxF;        // elements per z row of a buffer
-constexpr int kBufElems = kBZ * kPlane;       // elements per buffer
-constexpr int kMaxIdx = kBufElems - 1 - (kPlane + kBoxF + 1);
-// A TMA destination in shared memory must be 128-byte aligned: every box and
-// the second buffer start on a multiple of 128 bytes for 2- and 4-byte types.
-static_assert((kBoxZ * kPlane * 2) % 128 == 0, "box size must keep 128-byte alignment");
-static_assert((kBufElems * 2) % 128 == 0, "buffer size must keep 128-byte alignment");
-static_assert(kBZ % kBoxZ == 0, "a buffer holds whole boxes");
+// Slab shape per projection geometry.  Cone rays spread in z along a slab, so
+// cone slabs are 5 taps thick in 18-row boxes; par / fan rays keep their z
+// (an 8-row tile spans 8 rows), so their slabs are 8 taps thick in 12-row
+// boxes: fewer slabs per ray, less per-slab work.  Measured at 512^3 x 720:
+// cone 187.0 -> 180.8 ms, par 202.6 -> 173.9 ms against 4 taps in 20 rows for
+// both.  One box fills a buffer; both shapes use 6912-element buffers, so the
+// batched kernel has one shared-memory size for every geometry.
+template <int GEOM>
+struct SlabCfg {
+  static constexpr int T = GEOM == 2 ? 5 : 8;      // a-taps per slab
+  static constexpr int A = T + 1;                  // a-planes in a box
+  static constexpr int Z = GEOM == 2 ? 18 : 12;    // z rows per box (and buffer)
+  static constexpr int Plane = A * kBoxF;          // elements per z row of a buffer
+  static constexpr int BufElems = Z * Plane;       // elements per buffer
+  static constexpr int MaxIdx = BufElems - 1 - (Plane + kBoxF + 1);
+  static constexpr int MaxPlans = 2048 / T;        // planned slabs per tile
+  // A TMA destination in shared memory must be 128-byte aligned: every box
+  // and the second buffer start on a multiple of 128 bytes for 2- and 4-byte
+  // types; nzr is packed in 5 bits.
+  static_assert((Z * Plane * 2) % 128 == 0, "box size must keep 128-byte alignment");
+  static_assert(Z < 32, "nzr must fit 5 bits");
+};
+constexpr int kBufElems = SlabCfg<2>::BufElems;   // elements per buffer
+static_assert(SlabCfg<0>::BufElems == kBufElems && SlabCfg<1>::BufElems == kBufElems,
+              "every geometry uses the same buffer size");
+constexpr int kMaxPlans = SlabCfg<2>::MaxPlans > SlabCfg<0>::MaxPlans ? SlabCfg<2>::MaxPlans
+                                                                      : SlabCfg<0>::MaxPlans;
 
 struct SlabPlan {
   int alo, ahi;  // a-taps sampled in this slab
@@ -407,9 +422,7 @@ struct SlabJob {
 // global memory".  Plans are computed for the first kMaxPlans slabs of a tile
 // (an a-extent of 2048 taps, W <= ~2040); later slabs of larger volumes, and
 // boxes beyond f0 = 65532 or z0 = 8191, read global memory.
-constexpr int kMaxPlans = 2048 / kSlabT;
 constexpr uint32_t kPlanFallback = 0u;
-static_assert(kBZ < 32, "nzr must fit 5 bits");
 
 __device__ __forceinline__ uint32_t pack_plan(int f0, int z0, int nzr) {
   return ((uint32_t)f0 >> 2) | ((uint32_t)z0 << 14) | ((uint32_t)nzr << 27);
@@ -448,6 +461,7 @@ template <int GEOM, int EPI, typename TV, typename TO, bool ZL = false, bool SUB
 __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, SlabShared& S,
                                           uint32_t& phase, uint32_t& issued,
                                           const SlabEpi& E) {
+  using C = SlabCfg<GEOM>;
   constexpr bool Z2 = (GEOM == 2);  // z changes along the ray
   // trilinear samples; otherwise par/fan rays sample exact z texel rows
   constexpr bool ZW = Z2 || ZL;
@@ -523,18 +537,18 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   const bool any = s_amax >= s_amin;
   const int dir = S.neg == 0 ? 1 : -1;
   const bool mixed = S.pos > 0 && S.neg > 0;
-  const int nslab = any ? (s_amax - s_amin) / kSlabT + 1 : 0;
+  const int nslab = any ? (s_amax - s_amin) / C::T + 1 : 0;
   const TV* gv = static_cast<const TV*>(xdom ? J.py : J.px);  // f-fastest padded layout
   const CUtensorMap* tm = xdom ? J.tmy : J.tmx;
   uint64_t* bar = S.bar;
   // Tap range [alo, ahi] of slab j.
   auto slab_range = [&](int j, int& alo, int& ahi) {
     if (dir > 0) {
-      alo = s_amin + j * kSlabT;
-      ahi = alo + kSlabT - 1;
+      alo = s_amin + j * C::T;
+      ahi = alo + C::T - 1;
     } else {
-      ahi = s_amax - j * kSlabT;
-      alo = ahi - kSlabT + 1;
+      ahi = s_amax - j * C::T;
+      alo = ahi - C::T + 1;
     }
   };
 
@@ -545,7 +559,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   {
     const float bfw = xdom ? J.by : J.bx;  // world offset of the f axis
     const float baw = xdom ? J.bx : J.by;  // world offset of the a axis
-    const int np = min(nslab, kMaxPlans);
+    const int np = min(nslab, C::MaxPlans);
     const int c = tid & 3, w = (tid >> 2) & 1;
     const float sa = xdom ? S.corner[c][0] : S.corner[c][1];
     const float sf = xdom ? S.corner[c][1] : S.corner[c][0];
@@ -587,7 +601,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
           f0 = (fl / align) * align;
           z0 = zl;
           const int nzr = zh - z0 + 1;
-          fits = (fh - f0 + 1 <= kBoxF) && (nzr <= kBZ) && nzr > 0 && f0 <= 65532 &&
+          fits = (fh - f0 + 1 <= kBoxF) && (nzr <= C::Z) && nzr > 0 && f0 <= 65532 &&
                  z0 <= 8191;
           if (fits) S.plans[j] = pack_plan(f0, z0, nzr);
         }
@@ -599,19 +613,19 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
 
   // Start the copy of slab j into buffer j&1 (thread 0 only).
   auto issue = [&](int j) {
-    const uint32_t pk = j < kMaxPlans ? S.plans[j] : kPlanFallback;
+    const uint32_t pk = j < C::MaxPlans ? S.plans[j] : kPlanFallback;
     const int nzr = plan_nzr(pk);
     if (nzr == 0 || S.abort) return;
     int alo, ahi;
     slab_range(j, alo, ahi);
-    const int nbox = (nzr + kBoxZ - 1) / kBoxZ;
+    const int nbox = (nzr + C::Z - 1) / C::Z;
     const int f0 = plan_f0(pk), z0 = plan_z0(pk);
     TV* dst = (j & 1) ? buf1 : buf0;
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_expect_tx(&bar[j & 1], (uint32_t)(nbox * kBoxZ * kPlane * sizeof(TV)));
+    mbar_expect_tx(&bar[j & 1], (uint32_t)(nbox * C::Z * C::Plane * sizeof(TV)));
     for (int bx = 0; bx < nbox; ++bx)
-      tma_load_3d(dst + (size_t)bx * kBoxZ * kPlane, tm, f0, alo,
-                  z0 + bx * kBoxZ - (SUB ? J.zoff : 0), &bar[j & 1]);
+      tma_load_3d(dst + (size_t)bx * C::Z * C::Plane, tm, f0, alo,
+                  z0 + bx * C::Z - (SUB ? J.zoff : 0), &bar[j & 1]);
     // thread 0 counts the copies issued into each buffer (16 bits each)
     issued += 1u << (16 * (j & 1));
   };
@@ -630,7 +644,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   for (int j = 0; j < nslab; ++j) {
     // Buffer (j+1)&1 was released by the barrier that ended slab j-1.
     if (tid == 0 && j + 1 < nslab) issue(j + 1);
-    const uint32_t pk = j < kMaxPlans ? S.plans[j] : kPlanFallback;
+    const uint32_t pk = j < C::MaxPlans ? S.plans[j] : kPlanFallback;
     int alo, ahi;
     slab_range(j, alo, ahi);
     const TV* b = (j & 1) ? buf1 : buf0;
@@ -647,7 +661,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     // where possible.  Tap indices are kept as floats (exact below 2^24) so a
     // sample costs one float->int conversion for its shared-memory index.
     const float alo_f = (float)alo, ahi_f = (float)ahi;
-    const float off = -(float)(plan_z0(pk) * kPlane + alo * kBoxF + plan_f0(pk));
+    const float off = -(float)(plan_z0(pk) * C::Plane + alo * kBoxF + plan_f0(pk));
     const float2 off2 = make_float2(off, off);
     // The sweep direction and the sample source are uniform over a slab, so
     // each gets its own loop: the shared-memory loops compare against one
@@ -673,20 +687,20 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
           wz2 = sub2(tz2, fz2);
         }
         const float2 wa2 = sub2(ta2, fa2), wf2 = sub2(tf2, ff2);
-        const float2 x2 = __ffma2_rn(fz2, make_float2((float)kPlane, (float)kPlane),
+        const float2 x2 = __ffma2_rn(fz2, make_float2((float)C::Plane, (float)C::Plane),
                                      __ffma2_rn(fa2, make_float2((float)kBoxF, (float)kBoxF),
                                                 __fadd2_rn(ff2, off2)));
         // Tap indices are exact in FP32 (< 2^24); a negative one wraps to a
         // large unsigned value and is clamped like one past the end.
-        const unsigned i0 = min((unsigned)__float2int_rn(x2.x), (unsigned)kMaxIdx);
+        const unsigned i0 = min((unsigned)__float2int_rn(x2.x), (unsigned)C::MaxIdx);
         if (two) {
-          const unsigned i1 = min((unsigned)__float2int_rn(x2.y), (unsigned)kMaxIdx);
-          const float2 v = sample_pair<ZW>(b + i0, b + i1, kBoxF, kPlane, wa2, wf2, wz2);
+          const unsigned i1 = min((unsigned)__float2int_rn(x2.y), (unsigned)C::MaxIdx);
+          const float2 v = sample_pair<ZW>(b + i0, b + i1, kBoxF, C::Plane, wa2, wf2, wz2);
           acc += v.x;
           acc += v.y;
           k += 2;
         } else {
-          acc += sample_at<ZW>(b + i0, kBoxF, kPlane, wa2.x, wf2.x, wz2.x);
+          acc += sample_at<ZW>(b + i0, kBoxF, C::Plane, wa2.x, wf2.x, wz2.x);
           k += 1;
           break;
         }
@@ -842,13 +856,15 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype, int Pf, int Ps,
-                           int Pz) {
+                           int Pz, int geom) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
   const size_t es = dtype == kF32 ? 4 : 2;
   cuuint64_t dims[3] = {(cuuint64_t)Pf, (cuuint64_t)Ps, (cuuint64_t)Pz};
   cuuint64_t strides[2] = {(cuuint64_t)Pf * es, (cuuint64_t)Pf * Ps * es};
-  cuuint32_t box[3] = {(cuuint32_t)kBoxF, (cuuint32_t)kSlabA, (cuuint32_t)kBoxZ};
+  const int A = geom == 2 ? SlabCfg<2>::A : SlabCfg<0>::A;
+  const int Z = geom == 2 ? SlabCfg<2>::Z : SlabCfg<0>::Z;
+  cuuint32_t box[3] = {(cuuint32_t)kBoxF, (cuuint32_t)A, (cuuint32_t)Z};
   cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt = dtype == kF32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                  : dtype == kF16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
@@ -861,6 +877,26 @@ cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype, int Pf
 
 int slab_pitch(int W) { return ((W + 2 + 7) / 8) * 8; }
 
+// Dynamic shared memory of the slab kernels and the largest shared-memory
+// carveout: kSlabCtas CTAs of 57 KB each need nearly all of an SM's 228 KB.
+template <typename K>
+static cudaError_t set_slab_attrs(K k, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                              cudaSharedmemCarveoutMaxShared);
+}
+
+// Resident CTAs per SM of the cone FP32 slab kernel (occupancy calculator).
+int slab_resident_ctas() {
+  auto k = fp_slab_kernel<2, false, 0, float, float>;
+  const size_t smem = 2 * (size_t)kBufElems * sizeof(float) + 128;
+  if (set_slab_attrs(k, smem) != cudaSuccess) return -1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, smem) != cudaSuccess) return -1;
+  return n;
+}
+
 cudaError_t launch_fp_batch(const BatchFp* d_probs, int nprob, long long total,
                             unsigned long long* counter, unsigned* err, int ctas,
                             cudaStream_t st) {
@@ -869,7 +905,7 @@ cudaError_t launch_fp_batch(const BatchFp* d_probs, int nprob, long long total,
   const size_t smem = 2 * (size_t)kBufElems * sizeof(float) + 128;
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = set_slab_attrs(k, smem);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
@@ -886,8 +922,7 @@ static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtens
   const size_t smem = 2 * (size_t)kBufElems * sizeof(TV) + 128;
   static bool attr_set = false;  // once per instantiation (before any capture)
   if (!attr_set) {
-    cudaError_t err =
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t err = set_slab_attrs(k, smem);
     if (err != cudaSuccess) return err;
     attr_set = true;
   }

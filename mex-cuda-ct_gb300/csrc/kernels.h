@@ -77,6 +77,9 @@ int slab_pitch(int W);
 // CTAs of the slab FP kernels resident per SM (its launch bounds); persistent
 // launches size their grids by it.
 int slab_ctas_per_sm();
+// Resident CTAs per SM of the cone FP32 slab kernel by the occupancy
+// calculator (-1 on error).
+int slab_resident_ctas();
 
 // One problem of a batched FP launch (device-resident descriptor).
 struct alignas(64) BatchFp {
@@ -113,8 +116,10 @@ cudaError_t launch_bp_batch(const BatchBp* d_probs, int nprob, long long total,
 int bp_brick_z();
 cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
                               bool border, void* px, void* py, cudaStream_t st);
+// TMA map over a padded volume (Pf x Ps x Pz) with the box shape of the slab
+// kernel for projection geometry geom.
 cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype,
-                           int Pf, int Ps, int Pz);
+                           int Pf, int Ps, int Pz, int geom);
 cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
                            const CUtensorMap& mx, const CUtensorMap& my,
                            const void* px, const void* py, int Pf, int vt,

@@ -94,7 +94,7 @@ namespace mexct {
 // Padded copies of a W x W x H volume in both layouts (clamp: replicated edge;
 // border: zeros) in the given buffers, and TMA maps over them.
 mexct_status prepare_slab_bufs(Buf& px, Buf& py, Buf& err, const void* d_vol, int vt, int W,
-                               int H, bool border, CUtensorMap* mx, CUtensorMap* my,
+                               int H, bool border, int geom, CUtensorMap* mx, CUtensorMap* my,
                                int* Pf_out, cudaStream_t st) {
   const int Pf = slab_pitch(W);
   const size_t bytes = (size_t)Pf * (W + 2) * (H + 2) * dsize(vt);
@@ -106,17 +106,17 @@ mexct_status prepare_slab_bufs(Buf& px, Buf& py, Buf& err, const void* d_vol, in
   }
   MEXCT_TRY_CUDA(launch_pad_volume(d_vol, vt, W, H, Pf, border, px.p, py.p, st),
                  "fp: pad volume");
-  MEXCT_TRY_CUDA(make_slab_tmap(mx, px.p, vt, Pf, W + 2, H + 2), "fp: tensor map");
-  MEXCT_TRY_CUDA(make_slab_tmap(my, py.p, vt, Pf, W + 2, H + 2), "fp: tensor map");
+  MEXCT_TRY_CUDA(make_slab_tmap(mx, px.p, vt, Pf, W + 2, H + 2, geom), "fp: tensor map");
+  MEXCT_TRY_CUDA(make_slab_tmap(my, py.p, vt, Pf, W + 2, H + 2, geom), "fp: tensor map");
   *Pf_out = Pf;
   return MEXCT_OK;
 }
 
 mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
-                          bool border, CUtensorMap* mx, CUtensorMap* my, int* Pf_out,
+                          bool border, int geom, CUtensorMap* mx, CUtensorMap* my, int* Pf_out,
                           cudaStream_t st) {
-  return prepare_slab_bufs(c->padx, c->pady, c->err, d_vol, vt, W, H, border, mx, my, Pf_out,
-                           st);
+  return prepare_slab_bufs(c->padx, c->pady, c->err, d_vol, vt, W, H, border, geom, mx, my,
+                           Pf_out, st);
 }
 }  // namespace mexct
 
@@ -141,7 +141,7 @@ mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float
   if (variant == MEXCT_FP_EXPLICIT) {
     CUtensorMap mx, my;
     int Pf = 0;
-    mexct_status s = prepare_slab(c, d_vol, vt, W, H, false, &mx, &my, &Pf, st);
+    mexct_status s = prepare_slab(c, d_vol, vt, W, H, false, geom, &mx, &my, &Pf, st);
     if (s) return s;
     SlabEpi e{nullptr, nullptr, nullptr, nullptr, c->err.as<unsigned>(), c->wait_us};
     for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
@@ -309,7 +309,7 @@ mexct_status fp_det_impl(mexct_ctx* c, const float* d_vol, int W, int H, float s
   a->dv = det->dv;
   CUtensorMap mx, my;
   int Pf = 0;
-  mexct_status s = prepare_slab(c, d_vol, kF32, W, H, false, &mx, &my, &Pf, st);
+  mexct_status s = prepare_slab(c, d_vol, kF32, W, H, false, geom, &mx, &my, &Pf, st);
   if (s) return s;
   const int ss = det->ss;
   const long long M = a->P * nP;
@@ -482,7 +482,7 @@ mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
   // copies along with mu.
   CUtensorMap mx, my;
   int Pf = 0;
-  mexct_status ps = prepare_slab(c, d_mu, mu_type, W, H, /*border=*/true, &mx, &my, &Pf, st);
+  mexct_status ps = prepare_slab(c, d_mu, mu_type, W, H, /*border=*/true, geom, &mx, &my, &Pf, st);
   if (ps) return ps;
   std::unique_ptr<RayArgs> ra(new RayArgs);
   std::unique_ptr<VoxArgs> va(new VoxArgs);
@@ -762,6 +762,17 @@ mexct_status mexct_bp_dev_ex(mexct_ctx* ctx, const void* d_sino, int stype,
   CTX_OR_FAIL(c, "bp");
   return bp_dev_impl(c, d_sino, stype, W, H, nP, sad, angles, geom, d_vol, vt,
                      as_stream(stream));
+}
+
+mexct_status mexct_fp_slab_occupancy(int* ctas_per_sm) {
+  if (!ctas_per_sm) return set_err(MEXCT_ERR_ARG, "fp_slab_occupancy: NULL pointer");
+  mexct_ctx* c = resolve(nullptr);
+  if (!c) return set_err(MEXCT_ERR_CUDA, "fp_slab_occupancy: no CUDA device / context");
+  DevGuard dg(c->device);
+  const int n = slab_resident_ctas();
+  if (n < 0) return set_err(MEXCT_ERR_CUDA, "fp_slab_occupancy: occupancy query failed");
+  *ctas_per_sm = n;
+  return MEXCT_OK;
 }
 
 mexct_status mexct_fp_det_dev(mexct_ctx* ctx, const float* d_vol, int W, int H,

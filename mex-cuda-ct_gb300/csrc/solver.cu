@@ -123,7 +123,7 @@ mexct_status enqueue_iteration(mexct_osctv* s, bool k_gt1, int nsub,
   CUtensorMap mx, my;
   int Pf = 0;
   mexct_status ps = prepare_slab_bufs(s->padx, s->pady, s->err, s->mu.p, s->mu_type, s->W, s->H,
-                                      /*border=*/true, &mx, &my, &Pf, st);
+                                      /*border=*/true, s->geom, &mx, &my, &Pf, st);
   if (ps) return ps;
   for (int si = 0; si < nsub; ++si) {
     const int sel = picks[si];
@@ -259,7 +259,7 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
     CUtensorMap mx, my;
     int Pf = 0;
     mexct_status ps = prepare_slab_bufs(s->padx, s->pady, s->err, s->mu.p, mu_type, W, H, true,
-                                        &mx, &my, &Pf, st);
+                                        geom, &mx, &my, &Pf, st);
     if (ps) return ps;
     std::unique_ptr<RayArgs> ra(new RayArgs);
     fill_std_rays(*ra, W, H, sad, geom, true);

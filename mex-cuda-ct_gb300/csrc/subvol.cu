@@ -113,8 +113,8 @@ mexct_status fp_sub_impl(mexct_ctx* c, const float* d_slab, int W, int H, int z0
                                        c->padx.as<float>(), c->pady.as<float>(), st),
                  "fp_sub: pad");
   CUtensorMap mx, my;
-  MEXCT_TRY_CUDA(make_slab_tmap(&mx, c->padx.p, kF32, Pf, W + 2, nz + 2), "fp_sub: tensor map");
-  MEXCT_TRY_CUDA(make_slab_tmap(&my, c->pady.p, kF32, Pf, W + 2, nz + 2), "fp_sub: tensor map");
+  MEXCT_TRY_CUDA(make_slab_tmap(&mx, c->padx.p, kF32, Pf, W + 2, nz + 2, geom), "fp_sub: tensor map");
+  MEXCT_TRY_CUDA(make_slab_tmap(&my, c->pady.p, kF32, Pf, W + 2, nz + 2, geom), "fp_sub: tensor map");
   SlabEpi e{nullptr, nullptr, nullptr, nullptr, c->err.as<unsigned>(), c->wait_us};
   for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
     a->nviews = std::min(kMaxViews, nP - v0);

@@ -83,6 +83,7 @@ SIGNATURES = {
     "mexct_vff_info": [_c.c_char_p, _c.POINTER(_i), _F, _c.POINTER(_i)],
     "mexct_vff_read": [_c.c_char_p, _P, _c.c_longlong],
     "mexct_vff_write": [_c.c_char_p, _P, _c.POINTER(_i), _F, _i],
+    "mexct_fp_slab_occupancy": [_c.POINTER(_i)],
     "mexct_ctx_set_wait_limit": [_P, _i],
     "mexct_ctx_device_errors": [_P, _c.POINTER(_c.c_uint), _i],
 }

@@ -431,6 +431,13 @@ def prefilter_dev(sino, angles, geom, sad, filt="ramp", cutoff=1.0, q=1.0, pre=N
 # ---------------------------------------------------------------------------
 # Bounded waits of the default context (include/mexct.h).
 # ---------------------------------------------------------------------------
+def fp_slab_occupancy() -> int:
+    """Resident CTAs per SM of the cone FP32 slab kernel (occupancy calculator)."""
+    n = ctypes.c_int()
+    _lib.call("mexct_fp_slab_occupancy", ctypes.byref(n))
+    return n.value
+
+
 def set_wait_limit(us: int) -> None:
     """Limit of one bounded wait of the slab FP in microseconds (0: give up at once,
     < 0: the 2 s default)."""

@@ -290,3 +290,12 @@ def test_fp_bp_low_precision_storage(cuda, orc, dt, tol):
         refb = orc.bp(sino.float().cpu().numpy().transpose(2, 1, 0).copy(order="F"), 1000.0, ang,
                       geom)
         assert rel_l2(bp.cpu().numpy().transpose(2, 1, 0), refb) <= tol
+
+
+@pytest.mark.gpu
+def test_fp_slab_kernel_keeps_four_ctas_per_sm(cuda):
+    """The slab FP's shared memory (two 27 KB buffers per CTA) and the largest
+    carveout leave room for the 4 resident CTAs its launch bounds assume."""
+    from mexct import ops
+
+    assert ops.fp_slab_occupancy() == 4
