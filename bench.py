@@ -47,7 +47,7 @@ FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (read + write) per launch of the slab FP kernel, cone 512^3, from the
 # ncu capture summarised in profiles/fp_slab_kernel_cone_512cube_32views.md (32 views),
 # scaled to 720 views (traffic grows with the number of views).
-FP_SLAB_DRAM_BYTES_PER_VIEW = (13.689240e9 + 36.76e6) / 32
+FP_SLAB_DRAM_BYTES_PER_VIEW = (11.672490e9 + 36.73e6) / 32
 
 
 def parse():
