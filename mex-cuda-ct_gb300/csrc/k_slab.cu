@@ -268,34 +268,36 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // Slab kernel.
 // ---------------------------------------------------------------------------
 constexpr int kSlabCtas = 4;                  // resident CTAs per SM (launch bounds)
-constexpr int kBoxF = 64;                     // box extent along f (elements)
-// Slab shape per projection geometry.  Cone rays spread in z along a slab, so
-// cone slabs are 5 taps thick in 18-row boxes; par / fan rays keep their z
-// (an 8-row tile spans 8 rows), so their slabs are 8 taps thick in 12-row
-// boxes: fewer slabs per ray, less per-slab work.  Measured at 512^3 x 720:
-// cone 187.0 -> 180.8 ms, par 202.6 -> 173.9 ms against 4 taps in 20 rows for
-// both.  One box fills a buffer; both shapes use 6912-element buffers, so the
-// batched kernel has one shared-memory size for every geometry.
+// Slab shape per projection geometry: F x A x Z boxes (f extent, a-planes =
+// taps + 1, z rows).  Cone rays spread in z along a slab, so cone slabs are 5
+// taps thick in 18-row boxes; par / fan rays keep their z (an 8-row tile spans
+// 8 rows), so their slabs are 8 taps thick in 12-row boxes: fewer slabs per
+// ray, less per-slab work.  Measured at 512^3 x 720: cone 187.0 -> 180.8 ms,
+// par 202.6 -> 173.9 ms against 4 taps in 20 rows for both.  One box fills a
+// buffer; the buffers are sized for the larger shape, so the batched kernel
+// has one shared-memory size for every geometry.
+constexpr int kConeF = 64, kConeT = 5, kConeZ = 18;
+constexpr int kParF = 64, kParT = 8, kParZ = 12;
 template <int GEOM>
 struct SlabCfg {
-  static constexpr int T = GEOM == 2 ? 5 : 8;      // a-taps per slab
-  static constexpr int A = T + 1;                  // a-planes in a box
-  static constexpr int Z = GEOM == 2 ? 18 : 12;    // z rows per box (and buffer)
-  static constexpr int Plane = A * kBoxF;          // elements per z row of a buffer
-  static constexpr int BufElems = Z * Plane;       // elements per buffer
-  static constexpr int MaxIdx = BufElems - 1 - (Plane + kBoxF + 1);
-  static constexpr int MaxPlans = 2048 / T;        // planned slabs per tile
-  // A TMA destination in shared memory must be 128-byte aligned: every box
-  // and the second buffer start on a multiple of 128 bytes for 2- and 4-byte
-  // types; nzr is packed in 5 bits.
-  static_assert((Z * Plane * 2) % 128 == 0, "box size must keep 128-byte alignment");
+  static constexpr int F = GEOM == 2 ? kConeF : kParF;   // box extent along f
+  static constexpr int T = GEOM == 2 ? kConeT : kParT;   // a-taps per slab
+  static constexpr int A = T + 1;                        // a-planes in a box
+  static constexpr int Z = GEOM == 2 ? kConeZ : kParZ;   // z rows per box (and buffer)
+  static constexpr int Plane = A * F;                    // elements per z row of a buffer
+  static constexpr int BufElems = Z * Plane;             // elements of a box
+  static constexpr int MaxIdx = BufElems - 1 - (Plane + F + 1);
+  static constexpr int MaxPlans = 2048 / T;              // planned slabs per tile
+  // A TMA box row must be whole 16-byte units and a TMA destination in shared
+  // memory 128-byte aligned (both buffers start on a multiple of 128 bytes for
+  // 2- and 4-byte types); nzr is packed in 5 bits.
+  static_assert((F * 2) % 16 == 0, "box rows must be whole 16-byte units");
   static_assert(Z < 32, "nzr must fit 5 bits");
 };
-constexpr int kBufElems = SlabCfg<2>::BufElems;   // elements per buffer
-static_assert(SlabCfg<0>::BufElems == kBufElems && SlabCfg<1>::BufElems == kBufElems,
-              "every geometry uses the same buffer size");
-constexpr int kMaxPlans = SlabCfg<2>::MaxPlans > SlabCfg<0>::MaxPlans ? SlabCfg<2>::MaxPlans
-                                                                      : SlabCfg<0>::MaxPlans;
+constexpr int cmax(int a, int b) { return a > b ? a : b; }
+// elements per buffer: the larger box, rounded to 64 elements (128 bytes)
+constexpr int kBufElems = (cmax(SlabCfg<2>::BufElems, SlabCfg<0>::BufElems) + 63) / 64 * 64;
+constexpr int kMaxPlans = cmax(SlabCfg<2>::MaxPlans, SlabCfg<0>::MaxPlans);
 
 struct SlabPlan {
   int alo, ahi;  // a-taps sampled in this slab
@@ -601,7 +603,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
           f0 = (fl / align) * align;
           z0 = zl;
           const int nzr = zh - z0 + 1;
-          fits = (fh - f0 + 1 <= kBoxF) && (nzr <= C::Z) && nzr > 0 && f0 <= 65532 &&
+          fits = (fh - f0 + 1 <= C::F) && (nzr <= C::Z) && nzr > 0 && f0 <= 65532 &&
                  z0 <= 8191;
           if (fits) S.plans[j] = pack_plan(f0, z0, nzr);
         }
@@ -661,7 +663,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     // where possible.  Tap indices are kept as floats (exact below 2^24) so a
     // sample costs one float->int conversion for its shared-memory index.
     const float alo_f = (float)alo, ahi_f = (float)ahi;
-    const float off = -(float)(plan_z0(pk) * C::Plane + alo * kBoxF + plan_f0(pk));
+    const float off = -(float)(plan_z0(pk) * C::Plane + alo * C::F + plan_f0(pk));
     const float2 off2 = make_float2(off, off);
     // The sweep direction and the sample source are uniform over a slab, so
     // each gets its own loop: the shared-memory loops compare against one
@@ -688,19 +690,19 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
         }
         const float2 wa2 = sub2(ta2, fa2), wf2 = sub2(tf2, ff2);
         const float2 x2 = __ffma2_rn(fz2, make_float2((float)C::Plane, (float)C::Plane),
-                                     __ffma2_rn(fa2, make_float2((float)kBoxF, (float)kBoxF),
+                                     __ffma2_rn(fa2, make_float2((float)C::F, (float)C::F),
                                                 __fadd2_rn(ff2, off2)));
         // Tap indices are exact in FP32 (< 2^24); a negative one wraps to a
         // large unsigned value and is clamped like one past the end.
         const unsigned i0 = min((unsigned)__float2int_rn(x2.x), (unsigned)C::MaxIdx);
         if (two) {
           const unsigned i1 = min((unsigned)__float2int_rn(x2.y), (unsigned)C::MaxIdx);
-          const float2 v = sample_pair<ZW>(b + i0, b + i1, kBoxF, C::Plane, wa2, wf2, wz2);
+          const float2 v = sample_pair<ZW>(b + i0, b + i1, C::F, C::Plane, wa2, wf2, wz2);
           acc += v.x;
           acc += v.y;
           k += 2;
         } else {
-          acc += sample_at<ZW>(b + i0, kBoxF, C::Plane, wa2.x, wf2.x, wz2.x);
+          acc += sample_at<ZW>(b + i0, C::F, C::Plane, wa2.x, wf2.x, wz2.x);
           k += 1;
           break;
         }
@@ -862,9 +864,10 @@ cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype, int Pf
   const size_t es = dtype == kF32 ? 4 : 2;
   cuuint64_t dims[3] = {(cuuint64_t)Pf, (cuuint64_t)Ps, (cuuint64_t)Pz};
   cuuint64_t strides[2] = {(cuuint64_t)Pf * es, (cuuint64_t)Pf * Ps * es};
+  const int F = geom == 2 ? SlabCfg<2>::F : SlabCfg<0>::F;
   const int A = geom == 2 ? SlabCfg<2>::A : SlabCfg<0>::A;
   const int Z = geom == 2 ? SlabCfg<2>::Z : SlabCfg<0>::Z;
-  cuuint32_t box[3] = {(cuuint32_t)kBoxF, (cuuint32_t)A, (cuuint32_t)Z};
+  cuuint32_t box[3] = {(cuuint32_t)F, (cuuint32_t)A, (cuuint32_t)Z};
   cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt = dtype == kF32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                  : dtype == kF16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
