@@ -904,9 +904,17 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
   const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
   for (int v = 0; v < A.nviews; ++v) {
     const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
-    // zero frame = border addressing (CUDAmex_oscIter.cu:419-425)
-    bp_column_pad<GEOM, ZC>(rpre + (size_t)v * vstride, A.W, A.H, Wp, z0, g, num);
-    bp_column_pad<GEOM, ZC>(rpost + (size_t)v * vstride, A.W, A.H, Wp, z0, g, den);
+    // zero frame = border addressing (CUDAmex_oscIter.cu:419-425); cone
+    // residuals in the quad layout written by the FP epilogue
+    if constexpr (GEOM == 2) {
+      bp_column_quad<ZC>(reinterpret_cast<const float4*>(rpre) + (size_t)v * vstride, A.W, A.H,
+                         Wp, z0, g, num);
+      bp_column_quad<ZC>(reinterpret_cast<const float4*>(rpost) + (size_t)v * vstride, A.W, A.H,
+                         Wp, z0, g, den);
+    } else {
+      bp_column_pad<GEOM, ZC>(rpre + (size_t)v * vstride, A.W, A.H, Wp, z0, g, num);
+      bp_column_pad<GEOM, ZC>(rpost + (size_t)v * vstride, A.W, A.H, Wp, z0, g, den);
+    }
   }
   const size_t base = (size_t)iy * A.W + ix;
   const size_t sz = (size_t)A.W * A.W;
