@@ -86,6 +86,20 @@ struct mexct_ctx {
   int filt_w = -1, filt_type = -1;
   float filt_cut = -1.f;
   std::vector<float> filt_kern;
+  // The pre-filter tables in `tabs` (kernel, Parker weights, dbeta) and the
+  // arguments they were built for: a call with the same scan geometry reuses
+  // them (tab_buf: tabs.p when they were written; a trim or a reallocation
+  // invalidates them).
+  struct TabKey {
+    int W = -1, H = -1, nP = -1, geom = -1, filter = -1;
+    float sad = 0.f, cutoff = 0.f, q = 0.f;
+    std::vector<float> angles;
+    bool operator==(const TabKey& o) const {
+      return W == o.W && H == o.H && nP == o.nP && geom == o.geom && filter == o.filter &&
+             sad == o.sad && cutoff == o.cutoff && q == o.q && angles == o.angles;
+    }
+  } tab_key;
+  const void* tab_buf = nullptr;
 
   std::vector<mexct::Buf*> all_bufs() {
     return {&in, &in2, &in3, &out, &volT, &r1, &r2, &r3, &tabs, &red, &cnt, &scal,

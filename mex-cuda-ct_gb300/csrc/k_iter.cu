@@ -428,10 +428,115 @@ __global__ void __launch_bounds__(256) prefilter_kernel(
   }
 }
 
+// Weighted input sample of the pre-filter (log transform, cosine weight,
+// Parker weight), as prefilter_kernel stages it.
+__device__ __forceinline__ float prefilter_input(const FiltArgs& A, const float* __restrict__ sino,
+                                                 const float* __restrict__ pre,
+                                                 const float* __restrict__ parker, int view,
+                                                 int v, int u) {
+  const size_t gi = ((size_t)view * A.H + v) * A.W + u;
+  float s = __ldg(sino + gi);
+  if (A.log_input) {
+    s = -logf(s / __ldg(pre + gi));
+    if (!isfinite(s)) s = 0.f;
+  }
+  const float U = (float)(u + 1) - (float)(A.W - 1) * 0.5f;
+  const float V = (float)(v + 1) - (float)(A.H - 1) * 0.5f;
+  if (A.geom == 1) s *= A.sad / sqrtf(A.sad * A.sad + U * U);
+  if (A.geom == 2) s *= A.sad / sqrtf(A.sad * A.sad + U * U + V * V);
+  return s * __ldg(parker + (size_t)view * A.W + u);
+}
+
+// Register-blocked form of prefilter_kernel: a block filters 8*RG detector
+// rows of one view, each thread 8 rows x 8 consecutive columns.  The rows are
+// staged in shared memory (zero-padded to a multiple of 8 columns); the
+// thread keeps the 15 kernel taps k[(u0 - j0 - 7 + m) & mask] its 8 columns
+// need for 8 consecutive j in registers, so 64 FMAs take 8 row loads
+// (broadcasts) and 15/8 tap loads.  Each output is the same FMA chain over
+// j = 0 .. W-1 as in prefilter_kernel: the results are bit-identical.
+template <int RG>
+__global__ void __launch_bounds__(256) prefilter_tiled_kernel(
+    const FiltArgs A, const float* __restrict__ sino, const float* __restrict__ pre,
+    const float* __restrict__ parker, const float* __restrict__ dbeta,
+    const float* __restrict__ kern, float* __restrict__ out) {
+  constexpr int ROWS = 8 * RG, UG = 256 / RG;  // rows per block, column groups
+  extern __shared__ float sm[];
+  const int W = A.W, H = A.H, Wj = (W + 7) & ~7;
+  float* ks = sm;            // order (circular kernel)
+  float* xs = sm + A.order;  // ROWS x Wj, row-major
+  const int view = blockIdx.y;
+  const int v0 = blockIdx.x * ROWS;
+  for (int i = threadIdx.x; i < A.order; i += 256) ks[i] = __ldg(kern + i);
+  for (int i = threadIdx.x; i < ROWS * Wj; i += 256) {
+    const int r = i / Wj, j = i - r * Wj, v = v0 + r;
+    xs[i] = (v < H && j < W) ? prefilter_input(A, sino, pre, parker, view, v, j) : 0.f;
+  }
+  __syncthreads();
+  const int mask = A.order - 1;
+  const int ug = threadIdx.x % UG, rg = threadIdx.x / UG;
+  const float* xr = xs + (size_t)rg * 8 * Wj;
+  const float db = __ldg(dbeta + view);
+  for (int u0 = 8 * ug; u0 < W; u0 += 8 * UG) {
+    float acc[8][8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) acc[r][i] = 0.f;
+    for (int j0 = 0; j0 < Wj; j0 += 8) {
+      float kw[15];
+#pragma unroll
+      for (int m = 0; m < 15; ++m) kw[m] = ks[(u0 - j0 - 7 + m) & mask];
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) {
+        float x[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) x[r] = xr[r * Wj + j0 + jj];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const float k = kw[i - jj + 7];  // k[(u0 + i - j) & mask]
+#pragma unroll
+          for (int r = 0; r < 8; ++r) acc[r][i] = fmaf(x[r], k, acc[r][i]);
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int v = v0 + rg * 8 + r;
+      if (v >= H) continue;
+      float* o = out + ((size_t)view * H + v) * W;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (u0 + i < W) o[u0 + i] = acc[r][i] * db;
+    }
+  }
+}
+
+template <int RG>
+static cudaError_t prefilter_tiled_go(const FiltArgs& a, size_t smem, const float* sino,
+                                      const float* pre, const float* parker, const float* dbeta,
+                                      const float* kern, float* out, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(prefilter_tiled_kernel<RG>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grd((a.H + 8 * RG - 1) / (8 * RG), a.nP);
+  prefilter_tiled_kernel<RG><<<grd, 256, smem, st>>>(a, sino, pre, parker, dbeta, kern, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_prefilter(const FiltArgs& a, const float* sino,
                              const float* pre, const float* parker,
                              const float* dbeta, const float* kern, float* out,
                              cudaStream_t st) {
+  // register-blocked form with the most rows per block whose rows and kernel
+  // fit 200 KB of shared memory
+  const size_t Wj = (size_t)((a.W + 7) & ~7);
+  for (int rg : {4, 2, 1}) {
+    const size_t smem = sizeof(float) * ((size_t)a.order + (size_t)8 * rg * Wj);
+    if (smem > 200 * 1024) continue;
+    if (rg == 4) return prefilter_tiled_go<4>(a, smem, sino, pre, parker, dbeta, kern, out, st);
+    if (rg == 2) return prefilter_tiled_go<2>(a, smem, sino, pre, parker, dbeta, kern, out, st);
+    return prefilter_tiled_go<1>(a, smem, sino, pre, parker, dbeta, kern, out, st);
+  }
   dim3 grd((a.H + kFiltRows - 1) / kFiltRows, a.nP);
   const size_t smem = sizeof(float) * ((size_t)a.order + (size_t)kFiltRows * a.W);
   if (smem > 48 * 1024) {

@@ -614,6 +614,10 @@ double s_window(double b) {
   return 0.0;
 }
 
+mexct_status prefilter_tables(mexct_ctx* c, int W, int H, int nP, const float* angles, int geom,
+                              float sad, int filter, float cutoff, float q, int order,
+                              cudaStream_t st);
+
 mexct_status prefilter_dev_impl(mexct_ctx* c, const float* d_sino,
                                 const float* d_pre, int W, int H, int nP,
                                 const float* angles, int geom, float sad,
@@ -629,8 +633,45 @@ mexct_status prefilter_dev_impl(mexct_ctx* c, const float* d_sino,
                    "prefilter: W (%d) != H (%d); the Parker weighting of the reference "
                    "(parker_weight.m:225) needs a square detector", W, H);
   if (!c) return MEXCT_OK;  // validate only
-  const double pi = 3.14159265358979323846;
   const int order = filter_order(W);
+  mexct_ctx::TabKey key;
+  key.W = W;
+  key.H = H;
+  key.nP = nP;
+  key.geom = geom;
+  key.filter = filter;
+  key.sad = sad;
+  key.cutoff = cutoff;
+  key.q = q;
+  key.angles.assign(angles, angles + nP);
+  if (!(c->tab_buf && c->tab_buf == c->tabs.p && c->tab_key == key)) {
+    mexct_status s = prefilter_tables(c, W, H, nP, angles, geom, sad, filter, cutoff, q, order,
+                                      st);
+    if (s) return s;
+    c->tab_key = std::move(key);
+    c->tab_buf = c->tabs.p;
+  }
+  FiltArgs fa;
+  fa.W = W;
+  fa.H = H;
+  fa.nP = nP;
+  fa.order = order;
+  fa.geom = geom;
+  fa.log_input = d_pre ? 1 : 0;
+  fa.sad = sad;
+  const float* dt = c->tabs.as<float>();
+  MEXCT_TRY_CUDA(launch_prefilter(fa, d_sino, d_pre, dt + order, dt + order + (size_t)nP * W, dt,
+                                  d_out, st),
+                 "prefilter: launch");
+  return MEXCT_OK;
+}
+
+// Filter kernel, Parker window per (view, row element) and dbeta/2 per view,
+// computed on the host in FP64 and copied to the context's tables.
+mexct_status prefilter_tables(mexct_ctx* c, int W, int H, int nP, const float* angles, int geom,
+                              float sad, int filter, float cutoff, float q, int order,
+                              cudaStream_t st) {
+  const double pi = 3.14159265358979323846;
   if (c->filt_w != W || c->filt_type != filter || c->filt_cut != cutoff) {
     filter_kernel(W, filter, cutoff, c->filt_kern);
     c->filt_w = W;
@@ -667,24 +708,11 @@ mexct_status prefilter_dev_impl(mexct_ctx* c, const float* d_sino,
     dbeta[i] = (i > 0) ? (angles[i] - angles[i - 1]) / 2 : (angles[1] - angles[0]) / 2;
   }
   MEXCT_TRY_CUDA(c->tabs.ensure(tab.size() * sizeof(float)), "prefilter: workspace");
+  // from a pageable host vector: cudaMemcpyAsync returns once the bytes are
+  // staged, so the vector may go out of scope
   MEXCT_TRY_CUDA(cudaMemcpyAsync(c->tabs.p, tab.data(), tab.size() * sizeof(float),
                                  cudaMemcpyHostToDevice, st),
                  "prefilter: tables");
-  FiltArgs fa;
-  fa.W = W;
-  fa.H = H;
-  fa.nP = nP;
-  fa.order = order;
-  fa.geom = geom;
-  fa.log_input = d_pre ? 1 : 0;
-  fa.sad = sad;
-  const float* dt = c->tabs.as<float>();
-  MEXCT_TRY_CUDA(launch_prefilter(fa, d_sino, d_pre, dt + order, dt + order + (size_t)nP * W, dt,
-                                  d_out, st),
-                 "prefilter: launch");
-  // The tables are read from a pageable host vector: keep it alive until the
-  // copy has been staged (cudaMemcpyAsync from pageable memory returns after
-  // staging), nothing more to wait for.
   return MEXCT_OK;
 }
 

@@ -299,3 +299,24 @@ def test_fp_slab_kernel_keeps_four_ctas_per_sm(cuda):
     from mexct import ops
 
     assert ops.fp_slab_occupancy() == 4
+
+
+@pytest.mark.gpu
+def test_prefilter_tables_follow_the_scan_geometry(cuda, orc):
+    """The context keeps the pre-filter tables of the last scan geometry: a repeat
+    call reuses them (identical output), and changed angles, Parker q or SAD
+    rebuild them (each result matches the oracle)."""
+    import mexct
+
+    rng = np.random.default_rng(9)
+    W, nP = 32, 24
+    sino = np.asfortranarray(rng.uniform(0, 1, (W, W, nP)).astype(np.float32))
+    ang = np.linspace(0, 1.3 * np.pi, nP).astype(np.float32)
+    a = mexct.preFilterSinogram(sino, {"type": "cone3d", "SAD": 1000.0}, ang, "ramp", 1.0, 1.0)
+    b = mexct.preFilterSinogram(sino, {"type": "cone3d", "SAD": 1000.0}, ang, "ramp", 1.0, 1.0)
+    assert np.array_equal(a, b)
+    for ang2, q, sad in ((ang * np.float32(0.9), 1.0, 1000.0), (ang, 0.5, 1000.0),
+                         (ang, 1.0, 400.0)):
+        got = mexct.preFilterSinogram(sino, {"type": "cone3d", "SAD": sad}, ang2, "ramp", 1.0, q)
+        ref = orc.prefilter(sino, 2, ang2, "ramp", 1.0, q, sad=sad)
+        assert rel_l2(got, ref) <= 1e-5
