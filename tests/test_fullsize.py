@@ -124,3 +124,20 @@ def test_tiny_volumes(cuda, orc, W, H, geom):
         assert np.count_nonzero(bp) == 0  # W <= 3: the circle mask is empty
     else:
         assert rel_l2(bp, rb) <= TOL
+
+
+@pytest.mark.parametrize("geom", [0, 2])
+def test_wide_volume_uses_every_plan_and_the_fallback(cuda, orc, geom):
+    """A 2048 x 2048 x 4 volume: the slab plan limits are exercised (f0 up to ~2000
+    in the packed plans, more slabs per tile than are planned, so the last slabs of
+    a ray are sampled from global memory) and the results still match the oracle."""
+    import mexct
+    from mexct import phantoms
+
+    W, H, nP = 2048, 4, 3
+    vol = phantoms.ellipsoids(W, count=6, seed=17, nz=H)
+    ang = np.array([0.05, 0.8, 2.3], np.float32)
+    fp = mexct.CUDAmex_FP(vol, 4000.0, ang, nP, geom)
+    assert rel_l2(fp, orc.fp(vol, 4000.0, ang, nP, geom)) <= TOL
+    bp = mexct.CUDAmex_BP(fp, 4000.0, ang, geom)
+    assert rel_l2(bp, orc.bp(fp, 4000.0, ang, geom)) <= TOL
