@@ -385,23 +385,67 @@ cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews,
   return cudaGetLastError();
 }
 
-// Quad layout of the clamp-padded views (BP, FP32): padded texel (r, c) of
+// Quad layout of the clamp-padded views (cone BP): padded texel (r, c) of
 // view v -> {P(r,c), P(r,c+1), P(r+1,c), P(r+1,c+1)} with P(r, c) = the view's
 // pixel (clamp(c - kSinoPad), clamp(r - kSinoPad)), as in pad_sino_kernel.
-__global__ void __launch_bounds__(256) pad_sino_quad_kernel(const float* __restrict__ in, int W,
-                                                            int H, float4* __restrict__ out,
+// FP32 views: a float4 per texel; FP16 / BF16 views: the four 16-bit values
+// in a uint2 (x: P(r,c) | P(r,c+1) << 16, y: the next row), read and
+// converted exactly as the gather form reads them.
+template <typename S> struct QuadT;
+template <> struct QuadT<float> {
+  using T = float4;
+  static __device__ __forceinline__ T make(float a, float b, float c, float d) {
+    return make_float4(a, b, c, d);
+  }
+  static __device__ __forceinline__ float4 get(const T* p) { return __ldg(p); }
+};
+// 16-bit values as bits and back to float in registers (the conversions
+// ldf applies to a loaded value: exact for both types)
+__device__ __forceinline__ uint32_t bits16(__half h) { return __half_as_ushort(h); }
+__device__ __forceinline__ uint32_t bits16(__nv_bfloat16 h) { return __bfloat16_as_ushort(h); }
+template <typename H16> __device__ __forceinline__ float from_bits16(uint32_t u);
+template <> __device__ __forceinline__ float from_bits16<__half>(uint32_t u) {
+  return __half2float(__ushort_as_half((unsigned short)u));
+}
+template <> __device__ __forceinline__ float from_bits16<__nv_bfloat16>(uint32_t u) {
+  return __bfloat162float(__ushort_as_bfloat16((unsigned short)u));
+}
+template <typename H16> struct QuadT16 {
+  using T = uint2;
+  static __device__ __forceinline__ T make(H16 a, H16 b, H16 c, H16 d) {
+    return make_uint2(bits16(a) | (bits16(b) << 16), bits16(c) | (bits16(d) << 16));
+  }
+  static __device__ __forceinline__ float4 get(const T* p) {
+    const uint2 q = __ldg(p);
+    return make_float4(from_bits16<H16>(q.x & 0xffffu), from_bits16<H16>(q.x >> 16),
+                       from_bits16<H16>(q.y & 0xffffu), from_bits16<H16>(q.y >> 16));
+  }
+};
+template <> struct QuadT<__half> : QuadT16<__half> {};
+template <> struct QuadT<__nv_bfloat16> : QuadT16<__nv_bfloat16> {};
+
+// Marker type of the BP kernels' view pointer: views in the quad layout of
+// storage type S.
+template <typename S> struct QuadLayout {};
+template <typename T> struct IsQuad : std::false_type {};
+template <typename S> struct IsQuad<QuadLayout<S>> : std::true_type { using Storage = S; };
+
+template <typename S>
+__global__ void __launch_bounds__(256) pad_sino_quad_kernel(const S* __restrict__ in, int W,
+                                                            int H,
+                                                            typename QuadT<S>::T* __restrict__ out,
                                                             int Wp) {
   const int c = blockIdx.x * 32 + threadIdx.x;
   const int r = blockIdx.y * 8 + threadIdx.y;
   const int v = blockIdx.z;
   const int Hp = H + 2 * kSinoPad;
   if (c >= Wp || r >= Hp) return;
-  const float* view = in + (size_t)v * W * H;
+  const S* view = in + (size_t)v * W * H;
   const int x0 = min(max(c - kSinoPad, 0), W - 1), x1 = min(max(c + 1 - kSinoPad, 0), W - 1);
   const int y0 = min(max(r - kSinoPad, 0), H - 1), y1 = min(max(r + 1 - kSinoPad, 0), H - 1);
   out[((size_t)v * Hp + r) * Wp + c] =
-      make_float4(__ldg(view + (size_t)y0 * W + x0), __ldg(view + (size_t)y0 * W + x1),
-                  __ldg(view + (size_t)y1 * W + x0), __ldg(view + (size_t)y1 * W + x1));
+      QuadT<S>::make(view[(size_t)y0 * W + x0], view[(size_t)y0 * W + x1],
+                     view[(size_t)y1 * W + x0], view[(size_t)y1 * W + x1]);
 }
 
 // Pair layout of the clamp-padded views (par / fan BP, FP32): padded texel
@@ -428,12 +472,19 @@ cudaError_t launch_pad_sino_pair(const float* in, int W, int H, int nviews, floa
   return cudaGetLastError();
 }
 
-cudaError_t launch_pad_sino_quad(const float* in, int W, int H, int nviews, float4* out,
+cudaError_t launch_pad_sino_quad(const void* in, int stype, int W, int H, int nviews, void* out,
                                  cudaStream_t st) {
   if (nviews <= 0) return cudaSuccess;
   const int Wp = sino_pad_pitch(W);
   dim3 blk(32, 8), grd((Wp + 31) / 32, (H + 2 * kSinoPad + 7) / 8, nviews);
-  pad_sino_quad_kernel<<<grd, blk, 0, st>>>(in, W, H, out, Wp);
+#define QPAD(S)                                                                           \
+  pad_sino_quad_kernel<S><<<grd, blk, 0, st>>>(static_cast<const S*>(in), W, H,           \
+                                               static_cast<typename QuadT<S>::T*>(out), Wp)
+  if (stype == kF32) QPAD(float);
+  else if (stype == kF16) QPAD(__half);
+  else if (stype == kBF16) QPAD(__nv_bfloat16);
+  else return cudaErrorInvalidValue;
+#undef QPAD
   return cudaGetLastError();
 }
 
@@ -499,15 +550,16 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
 // holds the bilinear footprint {P(r,c), P(r,c+1), P(r+1,c), P(r+1,c+1)} of
 // the padded view P, so each voxel's four taps are one 16-byte load.  The
 // arithmetic is bp_column_pad's (GEOM 2), operation for operation.
-template <int ZC>
-__device__ __forceinline__ void bp_column_quad(const float4* __restrict__ p, int W, int H, int Wp,
-                                               int z0, const ColGeom<2>& g, float* acc) {
+template <int ZC, typename S = float>
+__device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __restrict__ p, int W,
+                                               int H, int Wp, int z0, const ColGeom<2>& g,
+                                               float* acc) {
   const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
   const float fu = floorf(cu);
   const float au = cu - fu;
   const int iu = min(max((int)fu, -kSinoPad), W) + kSinoPad;
   const float w0 = g.w * (1.0f - au), w1 = g.w * au;
-  const float4* col = p + iu;
+  const typename QuadT<S>::T* col = p + iu;
   static_assert(ZC % 2 == 0, "ZC must be even");
   const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
   const float pz0 = g.pz0 - 0.5f;
@@ -520,8 +572,8 @@ __device__ __forceinline__ void bp_column_quad(const float4* __restrict__ p, int
     const float2 az = __fadd2_rn(cz, make_float2(-fz.x, -fz.y));
     const int i0 = min(max(__float2int_rz(fz.x), -kSinoPad), H) + kSinoPad;
     const int i1 = min(max(__float2int_rz(fz.y), -kSinoPad), H) + kSinoPad;
-    const float4 q0 = __ldg(col + (size_t)i0 * Wp);
-    const float4 q1 = __ldg(col + (size_t)i1 * Wp);
+    const float4 q0 = QuadT<S>::get(col + (size_t)i0 * Wp);
+    const float4 q1 = QuadT<S>::get(col + (size_t)i1 * Wp);
     const float2 a = __ffma2_rn(w02, make_float2(q0.x, q1.x), __fmul2_rn(w12, make_float2(q0.y, q1.y)));
     const float2 b = __ffma2_rn(w02, make_float2(q0.z, q1.z), __fmul2_rn(w12, make_float2(q0.w, q1.w)));
     const float2 omaz = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-az.x, -az.y));
@@ -586,12 +638,14 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
   if (in_circle(ix, iy, A.hw)) {
     const float x = (float)ix - ((float)A.hw + 0.5f);
     const float y = (float)iy - ((float)A.hw + 0.5f);
-    if constexpr (std::is_same<TS, float4>::value) {
-      // cone, FP32 quad-layout views (launch_bp_quad)
+    if constexpr (IsQuad<TS>::value) {
+      // cone, quad-layout views (launch_bp_quad)
+      using S = typename IsQuad<TS>::Storage;
+      const auto* q = reinterpret_cast<const typename QuadT<S>::T*>(sino);
       const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
       for (int v = vbeg; v < vend; ++v) {
         const ColGeom<2> g = col_geom<2>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
-        bp_column_quad<ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+        bp_column_quad<ZC, S>(q + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
       }
     } else if constexpr (std::is_same<TS, float2>::value) {
       // par / fan, FP32 pair-layout views (launch_bp_pair)
@@ -718,14 +772,28 @@ cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, i
   }
 }
 
-cudaError_t launch_bp_quad(const VoxArgs& a, const float4* sino_quad, void* vol, int vtype,
-                           bool accumulate, const BpShape& shp, float* part, cudaStream_t st) {
+cudaError_t launch_bp_quad(const VoxArgs& a, const void* sino_quad, int stype, void* vol,
+                           int vtype, bool accumulate, const BpShape& shp, float* part,
+                           cudaStream_t st) {
   if (!bp_shape_valid(shp) || (shp.vblocks > 1 && !part)) return cudaErrorInvalidValue;
   const int Wp = sino_pad_pitch(a.W);
-  if (vtype == kF32) return bp_pad_zc<2, float4, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
-  if (vtype == kF16) return bp_pad_zc<2, float4, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
-  if (vtype == kBF16)
-    return bp_pad_zc<2, float4, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  using QF = QuadLayout<float>;
+  using QH = QuadLayout<__half>;
+  using QB = QuadLayout<__nv_bfloat16>;
+  if (stype == kF32 && vtype == kF32)
+    return bp_pad_zc<2, QF, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  if (stype == kF32 && vtype == kF16)
+    return bp_pad_zc<2, QF, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  if (stype == kF32 && vtype == kBF16)
+    return bp_pad_zc<2, QF, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  if (stype == kF16 && vtype == kF16)
+    return bp_pad_zc<2, QH, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  if (stype == kF16 && vtype == kF32)
+    return bp_pad_zc<2, QH, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  if (stype == kBF16 && vtype == kBF16)
+    return bp_pad_zc<2, QB, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+  if (stype == kBF16 && vtype == kF32)
+    return bp_pad_zc<2, QB, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   return cudaErrorInvalidValue;
 }
 
@@ -907,9 +975,9 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
     // zero frame = border addressing (CUDAmex_oscIter.cu:419-425); cone
     // residuals in the quad layout written by the FP epilogue
     if constexpr (GEOM == 2) {
-      bp_column_quad<ZC>(reinterpret_cast<const float4*>(rpre) + (size_t)v * vstride, A.W, A.H,
+      bp_column_quad<ZC, float>(reinterpret_cast<const float4*>(rpre) + (size_t)v * vstride, A.W, A.H,
                          Wp, z0, g, num);
-      bp_column_quad<ZC>(reinterpret_cast<const float4*>(rpost) + (size_t)v * vstride, A.W, A.H,
+      bp_column_quad<ZC, float>(reinterpret_cast<const float4*>(rpost) + (size_t)v * vstride, A.W, A.H,
                          Wp, z0, g, den);
     } else {
       bp_column_pad<GEOM, ZC>(rpre + (size_t)v * vstride, A.W, A.H, Wp, z0, g, num);

@@ -170,12 +170,14 @@ cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, i
                              void* vol, int vtype, bool accumulate, const BpShape& shp,
                              float* part, cudaStream_t st);
 
-// Cone BP (FP32 views) from the quad layout of launch_pad_sino_quad: the same
+// Cone BP from the quad layout of launch_pad_sino_quad (views of storage
+// type stype: FP32 in 16-byte texels, FP16 / BF16 in 8-byte texels): the same
 // result as launch_bp_padded on the clamp-padded views, bit for bit.
-cudaError_t launch_pad_sino_quad(const float* in, int W, int H, int nviews, float4* out,
+cudaError_t launch_pad_sino_quad(const void* in, int stype, int W, int H, int nviews, void* out,
                                  cudaStream_t st);
-cudaError_t launch_bp_quad(const VoxArgs& a, const float4* sino_quad, void* vol, int vtype,
-                           bool accumulate, const BpShape& shp, float* part, cudaStream_t st);
+cudaError_t launch_bp_quad(const VoxArgs& a, const void* sino_quad, int stype, void* vol,
+                           int vtype, bool accumulate, const BpShape& shp, float* part,
+                           cudaStream_t st);
 
 // Par / fan BP (FP32 views) from the pair layout of launch_pad_sino_pair: the
 // same result as launch_bp_padded, bit for bit.

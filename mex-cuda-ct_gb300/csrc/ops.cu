@@ -180,10 +180,10 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
   }
   if (!bp_shape_valid(shp)) return set_err(MEXCT_ERR_ARG, "bp: invalid launch shape");
   const int chunk = std::min(nP, kMaxViews);
-  // FP32 views: quad layout for cone (one 16-byte load per voxel and view),
-  // pair layout for par / fan (one 8-byte load)
-  const bool quad = geom == 2 && stype == kF32, pair = geom < 2 && stype == kF32;
-  const size_t es = quad ? sizeof(float4) : pair ? sizeof(float2) : dsize(stype);
+  // cone: quad layout (one 16-byte load per voxel and view for FP32 views,
+  // 8 bytes for FP16 / BF16); par / fan FP32: pair layout (one 8-byte load)
+  const bool quad = geom == 2, pair = geom < 2 && stype == kF32;
+  const size_t es = quad ? 4 * dsize(stype) : pair ? sizeof(float2) : dsize(stype);
   MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) * es, st), "bp: workspace");
   const size_t N = (size_t)W * W * H;
   if (shp.vblocks > 1)
@@ -195,10 +195,8 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
     const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
     if (quad) {
-      MEXCT_TRY_CUDA(launch_pad_sino_quad(static_cast<const float*>(static_cast<const void*>(src)),
-                                          W, H, a->nviews, c->spad.as<float4>(), st),
-                     "bp: pad");
-      MEXCT_TRY_CUDA(launch_bp_quad(*a, c->spad.as<float4>(), d_vol, vt, v0 > 0, shp,
+      MEXCT_TRY_CUDA(launch_pad_sino_quad(src, stype, W, H, a->nviews, c->spad.p, st), "bp: pad");
+      MEXCT_TRY_CUDA(launch_bp_quad(*a, c->spad.p, stype, d_vol, vt, v0 > 0, shp,
                                     c->bpart.as<float>(), st),
                      "bp: launch");
       continue;
