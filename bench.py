@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--osc-reps", type=int, default=5)
     ap.add_argument("--batch-problems", type=int, default=48)
     ap.add_argument("--serve-requests", type=int, default=60)
+    ap.add_argument("--ops-once", action="store_true",
+                    help="run one call of each secondary operator on 256^3 and exit "
+                         "(the workload of the secondary-kernel profiles)")
     return ap.parse_args()
 
 
@@ -243,6 +246,9 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     lib = _lib.load()
     V = ctypes.c_void_p
+    if args.ops_once:
+        ops_once()
+        return
 
     n, views, geom = args.size, args.views, args.geom
     N = n * n * n
@@ -575,6 +581,33 @@ def batched_uneven(count, seed=2026):
                        "5 OSC-TV iterations x 8 subsets each" % count)
     b.close()
     return out
+
+
+def ops_once(n=256, nv=90):
+    """One call of each secondary operator on a small case: general3D FP and BP (helix,
+    per-view points), one TV step, one OSC iteration (60 cone views, 10 subsets), the
+    FDK pre-filter of those views."""
+    import torch
+
+    from mexct import ops, phantoms
+
+    vol = phantoms.ellipsoids(n, count=10, seed=5, nz=n)
+    d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    pts, ang = phantoms.helix_pts(n, n, nv, n, sad=1000.0, turns=1.0, pitch=0.5)
+    dp = torch.from_numpy(np.ascontiguousarray(pts.transpose(3, 2, 1, 0))).cuda()
+    sino = ops.g3d_fp_dev(d, ang, dp)
+    rec = ops.g3d_bp_dev(sino, ang, dp, n, n)
+    tv = ops.tvmin3d_dev(d, 0.2, 1)
+    ang6 = phantoms.angles_full(60)
+    s6 = ops.fp_dev(d, 1000.0, ang6, 2)
+    pre = torch.full_like(s6, 1e5)
+    post = 1e5 * torch.exp(-s6)
+    mu = torch.full_like(d, 1e-3)
+    ops.osc_iter_dev(mu, pre, post, 10, np.arange(10, dtype=np.int32), ang6, 1000.0, 2)
+    f = ops.prefilter_dev(s6, ang6, 2, 1000.0, "ramp")
+    torch.cuda.synchronize()
+    print(json.dumps({"ops_once": "ok", "checksums": [float(t.double().sum()) for t in
+                                                      (sino, rec, tv, mu, f)]}))
 
 
 def other_operators():
