@@ -280,10 +280,10 @@ constexpr int kConeF = 64, kConeT = 5, kConeZ = 18;
 constexpr int kParF = 64, kParT = 8, kParZ = 12;
 template <int GEOM>
 struct SlabCfg {
-  static constexpr int F = GEOM == 2 ? kConeF : kParF;   // box extent along f
-  static constexpr int T = GEOM == 2 ? kConeT : kParT;   // a-taps per slab
+  static constexpr int F = GEOM >= 2 ? kConeF : kParF;   // box extent along f
+  static constexpr int T = GEOM >= 2 ? kConeT : kParT;   // a-taps per slab
   static constexpr int A = T + 1;                        // a-planes in a box
-  static constexpr int Z = GEOM == 2 ? kConeZ : kParZ;   // z rows per box (and buffer)
+  static constexpr int Z = GEOM >= 2 ? kConeZ : kParZ;   // z rows per box (and buffer)
   static constexpr int Plane = A * F;                    // elements per z row of a buffer
   static constexpr int BufElems = Z * Plane;             // elements of a box
   static constexpr int MaxIdx = BufElems - 1 - (Plane + F + 1);
@@ -407,6 +407,7 @@ struct SlabJob {
   float du, dv, ou, ov;  // detector pitch and sub-pixel ray offset
   int zoff, zrows, accum;  // sub-volume slab (RayArgs)
   float zlo, zhi;
+  const float* pts;        // general3D: ray end points of this view (6 planes of P)
   Trig tr;
   long long P;      // detector pixels per view
   long long gview;  // sinogram / pre / post slot of the view
@@ -437,6 +438,7 @@ struct SlabShared {
   uint64_t bar[2];
   uint32_t plans[kMaxPlans];
   float corner[4][6];
+  int gbi[8];         // general3D: ray bounds over the tile, order-preserving int keys
   int amin, amax, pos, neg;
   int abort;          // set by a timed-out wait
   long long item;
@@ -464,7 +466,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
                                           uint32_t& phase, uint32_t& issued,
                                           const SlabEpi& E) {
   using C = SlabCfg<GEOM>;
-  constexpr bool Z2 = (GEOM == 2);  // z changes along the ray
+  constexpr bool Z2 = (GEOM >= 2);  // z changes along the ray
   // trilinear samples; otherwise par/fan rays sample exact z texel rows
   constexpr bool ZW = Z2 || ZL;
   const int tid = threadIdx.x + 32 * threadIdx.y;
@@ -476,8 +478,13 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   const int Ps = J.S + 2, Pz = J.Z + 2, Pf = J.Pf;
 
   float s[3], e[3];
-  std_ray<GEOM>(min(ix, J.det_w - 1), min(iy, J.det_h - 1), J.u0, J.v0, tr.s, tr.c, J.SR, J.RD,
-                s, e, J.du, J.dv, J.ou, J.ov);
+  if constexpr (GEOM == 3) {
+    const long long pix = (long long)min(iy, J.det_h - 1) * J.det_w + min(ix, J.det_w - 1);
+    g3d_ray(J.pts, pix, J.P, tr.s, tr.c, s, e);
+  } else {
+    std_ray<GEOM>(min(ix, J.det_w - 1), min(iy, J.det_h - 1), J.u0, J.v0, tr.s, tr.c, J.SR,
+                  J.RD, s, e, J.du, J.dv, J.ou, J.ov);
+  }
   const Ray r = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], J.bx, J.by, J.bz, J.step);
   // Tap space: padded texture coordinate minus 0.5, i.e. world - b + 0.5.
   const float ca = xdom ? r.cx - J.bx : r.cy - J.by;
@@ -508,11 +515,57 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     }
   }
 
+  if (GEOM == 3 && n > 0) {
+    // general3D rays are not clipped when they miss the volume (the
+    // reference marches them between two points outside it): keep the
+    // samples whose taps can touch the padded volume, floor(t) in [0, P-2]
+    // on every axis.  With border addressing (zero frame) every other sample
+    // reads only zeros, so the sum is unchanged.  The samples kept are an
+    // interval of k; the estimates are settled with the loop's own positions.
+    const float Pa = (float)(Ps - 1), Pff = (float)(Ps - 1), Pzz = (float)(Pz - 1);
+    auto inside = [&](int k) {
+      const float kf = (float)k;
+      const float ta = fmaf(kf, da, ta0), tf = fmaf(kf, df, tf0), tz = fmaf(kf, dz, tz0);
+      return ta >= 0.f && ta < Pa && tf >= 0.f && tf < Pff && tz >= 0.f && tz < Pzz;
+    };
+    float klo = 0.f, khi = (float)n;
+    auto clampk = [&](float t0, float d, float hi) {
+      if (d == 0.f) {
+        if (!(t0 >= 0.f && t0 < hi)) khi = -1.f;
+      } else {
+        const float k1 = (0.f - t0) / d, k2 = (hi - t0) / d;
+        klo = fmaxf(klo, fminf(k1, k2));
+        khi = fminf(khi, fmaxf(k1, k2));
+      }
+    };
+    clampk(ta0, da, Pa);
+    clampk(tf0, df, Pff);
+    clampk(tz0, dz, Pzz);
+    // estimate [a0, a1), then settle both ends on the exact test (an empty
+    // estimate starts from one point next to where the interval would be)
+    const bool some = khi >= klo;
+    int a0 = (int)fminf(fmaxf(ceilf(some ? klo : fminf(klo, khi)), 0.f), (float)n);
+    int a1 = some ? (int)fminf(fmaxf(ceilf(khi), 0.f), (float)n) : a0;
+    while (a0 > 0 && inside(a0 - 1)) --a0;
+    while (a0 < a1 && !inside(a0)) ++a0;
+    while (a1 < n && inside(a1)) ++a1;
+    while (a1 > a0 && !inside(a1 - 1)) --a1;
+    k0 = a0;
+    n = a1;
+    if (k0 >= n) {
+      k0 = 0;
+      n = 0;
+    }
+  }
+
   if (tid == 0) {
     S.amin = 0x7fffffff;
     S.amax = -0x7fffffff;
     S.pos = 0;
     S.neg = 0;
+    if (GEOM == 3)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) S.gbi[i] = (i & 1) ? (int)0x80000000 : 0x7fffffff;
   }
   // Corner rays of the valid part of the tile bound the bundle.
   const int lx = min(31, J.det_w - 1 - u0), ly = min(7, J.det_h - 1 - v0);
@@ -527,7 +580,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     S.corner[cid][3] = e[0]; S.corner[cid][4] = e[1]; S.corner[cid][5] = e[2];
   }
   if (n > 0) {
-    const int t_first = __float2int_rd(SUB ? fmaf((float)k0, da, ta0) : ta0);
+    const int t_first = __float2int_rd((SUB || GEOM == 3) ? fmaf((float)k0, da, ta0) : ta0);
     const int t_last = __float2int_rd(fmaf((float)(n - 1), da, ta0));
     atomicMin(&S.amin, min(t_first, t_last));
     atomicMax(&S.amax, max(t_first, t_last));
@@ -540,6 +593,56 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   const int dir = S.neg == 0 ? 1 : -1;
   const bool mixed = S.pos > 0 && S.neg > 0;
   const int nslab = any ? (s_amax - s_amin) / C::T + 1 : 0;
+  // general3D: a tile's rays need not lie in the hull of its corner rays, so
+  // the slab boxes come from bounds over all its rays.  Along the sweep axis
+  // a ray's f and z are linear in a: f = F + mf (a - aref) with F its f at
+  // aref, so over the tile f >= Fmin + (a >= aref ? mfmin : mfmax)(a - aref),
+  // f <= Fmax + (a >= aref ? mfmax : mfmin)(a - aref), and the same for z.
+  float gb[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // Fmin Fmax mfmin mfmax, z: same
+  bool gunb = false;  // a ray nearly parallel to the a-planes: no box
+  const float aref = 0.5f * (float)(s_amin + s_amax + 1);
+  if constexpr (GEOM == 3) {
+    float v[8];
+    bool bad = false;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = (i & 1) ? -3.0e38f : 3.0e38f;
+    if (n > 0) {
+      if (!(fabsf(da) >= 1e-3f)) {
+        bad = true;
+      } else {
+        const float mf = df / da, mz = dz / da;
+        const float Fr = fmaf(aref - ta0, mf, tf0), Zr = fmaf(aref - ta0, mz, tz0);
+        v[0] = v[1] = Fr;
+        v[2] = v[3] = mf;
+        v[4] = v[5] = Zr;
+        v[6] = v[7] = mz;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const float t = __shfl_xor_sync(0xffffffffu, v[i], o);
+        v[i] = (i & 1) ? fmaxf(v[i], t) : fminf(v[i], t);
+      }
+    // floats as order-preserving ints for the shared-memory atomics
+    auto key = [](float f) {
+      const int i = __float_as_int(f);
+      return i >= 0 ? i : i ^ 0x7fffffff;
+    };
+    if ((tid & 31) == 0)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if (i & 1) atomicMax(&S.gbi[i], key(v[i]));
+        else atomicMin(&S.gbi[i], key(v[i]));
+      }
+    gunb = __syncthreads_or(bad) != 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int k = S.gbi[i];
+      gb[i] = __int_as_float(k >= 0 ? k : k ^ 0x7fffffff);
+    }
+  }
   const TV* gv = static_cast<const TV*>(xdom ? J.py : J.px);  // f-fastest padded layout
   const CUtensorMap* tm = xdom ? J.tmy : J.tmx;
   uint64_t* bar = S.bar;
@@ -574,11 +677,28 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       const bool act = j < np;
       int alo, ahi;
       slab_range(j, alo, ahi);
-      const float aw = w ? (float)ahi + 0.5f + baw : (float)alo - 0.5f + baw;
-      const float t = den != 0.f ? (aw - sa) / den : 0.f;
-      const float fv = fmaf(t, ef - sf, sf), zv = fmaf(t, ez - sz, sz);
-      float fmn = act ? fv : 3.0e38f, fmx = act ? fv : -3.0e38f;
-      float zmn = act ? zv : 3.0e38f, zmx = act ? zv : -3.0e38f;
+      float fmn, fmx, zmn, zmx;  // world f / z extent at this lane's slab end
+      if constexpr (GEOM == 3) {
+        // bounds over the tile's rays at tap-space a = alo or ahi + 1
+        const float dT = (w ? (float)ahi + 1.0f : (float)alo) - aref;
+        const bool up = dT >= 0.f;
+        fmn = fmaf(dT, up ? gb[2] : gb[3], gb[0]) + bfw - 0.5f;
+        fmx = fmaf(dT, up ? gb[3] : gb[2], gb[1]) + bfw - 0.5f;
+        zmn = fmaf(dT, up ? gb[6] : gb[7], gb[4]) + J.bz - 0.5f;
+        zmx = fmaf(dT, up ? gb[7] : gb[6], gb[5]) + J.bz - 0.5f;
+        if (!act || gunb) {
+          fmn = zmn = 3.0e38f;
+          fmx = zmx = -3.0e38f;
+        }
+      } else {
+        const float aw = w ? (float)ahi + 0.5f + baw : (float)alo - 0.5f + baw;
+        const float t = den != 0.f ? (aw - sa) / den : 0.f;
+        const float fv = fmaf(t, ef - sf, sf), zv = fmaf(t, ez - sz, sz);
+        fmn = act ? fv : 3.0e38f;
+        fmx = act ? fv : -3.0e38f;
+        zmn = act ? zv : 3.0e38f;
+        zmx = act ? zv : -3.0e38f;
+      }
 #pragma unroll
       for (int o = 4; o > 0; o >>= 1) {
         fmn = fminf(fmn, __shfl_xor_sync(0xffffffffu, fmn, o));
@@ -593,7 +713,7 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
         const float zlo = floorf(zmn - J.bz + 0.5f) - 1.0f;
         const float zhi = floorf(zmx - J.bz + 0.5f) + 2.0f;
         bool fits = isfinite(flo) && isfinite(fhi) && isfinite(zlo) && isfinite(zhi) &&
-                    !mixed && fhi >= 0.f && zhi >= 0.f && flo <= (float)(Pf - 1) &&
+                    !mixed && !gunb && fhi >= 0.f && zhi >= 0.f && flo <= (float)(Pf - 1) &&
                     zlo <= (float)(Pz - 1);
         int f0 = 0, z0 = 0;
         if (fits) {
@@ -797,6 +917,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   J.tr = A.trig[view];
   J.P = A.P;
   J.gview = A.view0 + (long long)view * A.vstride;
+  J.pts = GEOM == 3 ? A.pts + (A.pts_per_view ? (size_t)6 * A.P * J.gview : 0) : nullptr;
   J.lview = view;
   J.tu0 = (blockIdx.y % tiles_u) * 32;
   J.tv0 = (blockIdx.y / tiles_u) * 8;
@@ -840,7 +961,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_batch_kernel(
     J.u0 = B.u0; J.v0 = B.v0; J.bx = B.bx; J.by = B.by; J.bz = B.bz;
     J.SR = B.sad; J.RD = B.sad; J.step = B.step;
     J.du = 1.0f; J.dv = 1.0f; J.ou = 0.0f; J.ov = 0.0f;
-    J.zoff = 0; J.zrows = B.H + 2; J.accum = 0; J.zlo = 0.f; J.zhi = 0.f;
+    J.zoff = 0; J.zrows = B.H + 2; J.accum = 0; J.zlo = 0.f; J.zhi = 0.f; J.pts = nullptr;
     J.tr = B.trig[view];
     J.P = (long long)B.W * B.H;
     J.gview = view;
@@ -877,9 +998,9 @@ cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype, int Pf
   const size_t es = dtype == kF32 ? 4 : 2;
   cuuint64_t dims[3] = {(cuuint64_t)Pf, (cuuint64_t)Ps, (cuuint64_t)Pz};
   cuuint64_t strides[2] = {(cuuint64_t)Pf * es, (cuuint64_t)Pf * Ps * es};
-  const int F = geom == 2 ? SlabCfg<2>::F : SlabCfg<0>::F;
-  const int A = geom == 2 ? SlabCfg<2>::A : SlabCfg<0>::A;
-  const int Z = geom == 2 ? SlabCfg<2>::Z : SlabCfg<0>::Z;
+  const int F = geom >= 2 ? SlabCfg<2>::F : SlabCfg<0>::F;
+  const int A = geom >= 2 ? SlabCfg<2>::A : SlabCfg<0>::A;
+  const int Z = geom >= 2 ? SlabCfg<2>::Z : SlabCfg<0>::Z;
   cuuint32_t box[3] = {(cuuint32_t)F, (cuuint32_t)A, (cuuint32_t)Z};
   cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt = dtype == kF32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
@@ -956,6 +1077,12 @@ cudaError_t launch_fp_slab_det(int geom, const RayArgs& a, const CUtensorMap& mx
   if (geom == 1) return slab_go<1, false, 0, float, float, true>(a, mx, my, px, py, Pf, out, e, st);
   if (geom == 2) return slab_go<2, false, 0, float, float, true>(a, mx, my, px, py, Pf, out, e, st);
   return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fp_slab_g3d(const RayArgs& a, const CUtensorMap& mx, const CUtensorMap& my,
+                               const void* px, const void* py, int Pf, float* out,
+                               const SlabEpi& e, cudaStream_t st) {
+  return slab_go<3, true, 0, float, float>(a, mx, my, px, py, Pf, out, e, st);
 }
 
 cudaError_t launch_fp_slab_sub(int geom, const RayArgs& a, const CUtensorMap& mx,

@@ -28,6 +28,7 @@ struct RayArgs {
   // the output instead of storing.
   int zoff, zrows, accum;
   float zlo, zhi;
+  const float* pts;        // general3D slab FP: end points (launch_fp_slab_g3d)
   Trig trig[kMaxViews];
 };
 
@@ -129,6 +130,13 @@ cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
 // Slab FP (FP32) onto a decoupled detector (a.det_w, a.det_h, a.du, a.dv,
 // a.ou, a.ov): par / fan rays interpolate in z, rays that miss the volume
 // add nothing.
+// general3D FP on the slab kernel (border addressing, FP32): rays from a.pts
+// (6 planes of a.P points, per view when a.pts_per_view), per-tile boxes from
+// bounds over all rays of the tile.
+cudaError_t launch_fp_slab_g3d(const RayArgs& a, const CUtensorMap& mx, const CUtensorMap& my,
+                               const void* px, const void* py, int Pf, float* out,
+                               const SlabEpi& e, cudaStream_t st);
+
 cudaError_t launch_fp_slab_det(int geom, const RayArgs& a, const CUtensorMap& mx,
                                const CUtensorMap& my, const void* px, const void* py, int Pf,
                                float* out, const SlabEpi& e, cudaStream_t st);

@@ -406,16 +406,21 @@ mexct_status g3d_fp_dev_impl(mexct_ctx* c, const float* d_vol, int S, int Z,
   if (bad_dims(S, Z) || bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "g3d_fp: bad dims");
   if (nP < 0) return set_err(MEXCT_ERR_ARG, "g3d_fp: bad view count %d", nP);
   if (!c || nP == 0) return MEXCT_OK;  // c == NULL: validate only
-  const size_t N = (size_t)S * S * Z;
-  MEXCT_TRY_CUDA(c->volT.ensure(N * sizeof(float)), "g3d_fp: workspace");
-  MEXCT_TRY_CUDA(launch_transpose_xy(d_vol, c->volT.p, S, Z, kF32, st), "g3d_fp: transpose");
+  // the slab kernel over the zero-framed padded volume (border addressing)
   std::unique_ptr<RayArgs> a(new RayArgs);
   fill_g3d(*a, S, Z, W, H, per_view ? 1 : 0);
+  a->pts = d_pts;
+  CUtensorMap mx, my;
+  int Pf = 0;
+  mexct_status s = prepare_slab(c, d_vol, kF32, S, Z, /*border=*/true, /*geom=*/3, &mx, &my,
+                                &Pf, st);
+  if (s) return s;
+  SlabEpi e{nullptr, nullptr, nullptr, nullptr, c->err.as<unsigned>(), c->wait_us};
   for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
     a->nviews = std::min(kMaxViews, nP - v0);
     a->view0 = v0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-    MEXCT_TRY_CUDA(launch_fp(3, true, *a, d_vol, c->volT.p, kF32, d_pts, d_out, kF32, st),
+    MEXCT_TRY_CUDA(launch_fp_slab_g3d(*a, mx, my, c->padx.p, c->pady.p, Pf, d_out, e, st),
                    "g3d_fp: launch");
   }
   return MEXCT_OK;

@@ -320,3 +320,35 @@ def test_prefilter_tables_follow_the_scan_geometry(cuda, orc):
         got = mexct.preFilterSinogram(sino, {"type": "cone3d", "SAD": sad}, ang2, "ramp", 1.0, q)
         ref = orc.prefilter(sino, 2, ang2, "ramp", 1.0, q, sad=sad)
         assert rel_l2(got, ref) <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["random", "wide_helix"])
+def test_general3d_fp_hard_rays_match_oracle(cuda, orc, kind):
+    """general3D rays the slab kernel cannot box: random end points (mixed
+    directions in a tile, rays parallel to a face, rays missing the volume and
+    marched between two outside points as the reference does), and a helix whose
+    detector is much wider and taller than the volume's shadow.  The volume's
+    faces are non-zero, so the border (zero) frame around them matters."""
+    import mexct
+    from mexct import phantoms
+
+    S, Z = 24, 20
+    vol = _phantom(S, Z, seed=8)
+    vol[0, :, :] += 0.5
+    vol[:, -1, :] += 0.25
+    vol[:, :, 0] += 0.75
+    if kind == "random":
+        rng = np.random.default_rng(12)
+        W, H, nP = 40, 16, 5
+        pts = rng.uniform(-30, 30, (W, H, 6, nP)).astype(np.float32)
+        pts[:4, :, 2, :] = pts[:4, :, 5, :]  # some rays parallel to the z planes
+        pts[4:8, :, 0, :] = pts[4:8, :, 3, :]  # some parallel to the x planes
+        pts = np.asfortranarray(pts)
+        ang = np.linspace(0, 2 * np.pi, nP, endpoint=False).astype(np.float32)
+    else:
+        W, H, nP = 64, 48, 6
+        pts, ang = phantoms.helix_pts(W, H, nP, Z, sad=300.0, seed=3)
+    got = mexct.CUDAmex_general3D_FP(vol, ang, pts, nP)
+    ref = orc.g3d_fp(vol, ang, pts, nP)
+    assert rel_l2(got, ref) <= TOL
