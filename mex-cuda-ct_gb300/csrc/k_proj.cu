@@ -914,6 +914,13 @@ __global__ void __launch_bounds__(256) g3d_bp_kernel(
   const size_t SS = (size_t)S * S;
   const float ps = fmul(p, A.step);
   float cx = r.cx, cy = r.cy, cz = r.cz;
+  // Consecutive samples (step 0.5) mostly deposit into the same two voxels:
+  // the deposits of a run of samples with the same targets are summed in
+  // registers and reach memory in one atomic per voxel (the deposits
+  // themselves are the reference's binary32 values; only their grouping
+  // changes, as the order of the atomics already does).
+  size_t qL = ~(size_t)0, qU = 0;
+  float aL = 0.f, aU = 0.f;
   for (int k = 0; k < r.n; ++k) {
     const float fx = fsub(cx, A.bx), fy = fsub(cy, A.by), fz = fsub(cz, A.bz);
     const float flx = floorf(fx), fly = floorf(fy), flz = floorf(fz);
@@ -927,12 +934,29 @@ __global__ void __launch_bounds__(256) g3d_bp_kernel(
       const float wzz = fsub(1.0f, wz);
       const float pxy = fmul(fmul(ps, wxx), wyy);
       const size_t base = (size_t)jL * S + (size_t)iL;
-      atomicAdd(vol + base + (size_t)kL * SS, fmul(pxy, wzz));
-      atomicAdd(vol + base + (size_t)kU * SS, fmul(pxy, wz));
+      const size_t tL = base + (size_t)kL * SS, tU = base + (size_t)kU * SS;
+      const float dL = fmul(pxy, wzz), dU = fmul(pxy, wz);
+      if (tL == qL && tU == qU) {
+        aL = fadd(aL, dL);
+        aU = fadd(aU, dU);
+      } else {
+        if (qL != ~(size_t)0) {
+          atomicAdd(vol + qL, aL);
+          atomicAdd(vol + qU, aU);
+        }
+        qL = tL;
+        qU = tU;
+        aL = dL;
+        aU = dU;
+      }
     }
     cx = fadd(cx, r.dx);
     cy = fadd(cy, r.dy);
     cz = fadd(cz, r.dz);
+  }
+  if (qL != ~(size_t)0) {
+    atomicAdd(vol + qL, aL);
+    atomicAdd(vol + qU, aU);
   }
 }
 
