@@ -262,6 +262,12 @@ mexct_status mexct_ctx_destroy(mexct_ctx* c) {
   cudaGetDevice(&prev);
   cudaSetDevice(c->device);
   mexct_ctx_trim(c);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    for (cudaEvent_t ev : c->chunk_ev)
+      if (ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(c->copy_stream);
+  }
   cudaStreamDestroy(c->stream);
   cudaSetDevice(prev);
   delete c;

@@ -5,6 +5,7 @@
 
 #include <array>
 #include <initializer_list>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -61,6 +62,10 @@ using TuneKey = std::array<int, 7>;
 struct mexct_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;     // stream of the host entry points
+  // Output copies of the host entry points, overlapped with the launches
+  // still running on `stream` (created on first use), and one event per chunk.
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t chunk_ev[8] = {};
   std::recursive_mutex mu;           // serialises calls on this context
   // Host entry points: staged inputs / outputs.
   mexct::Buf in, in2, in3, out;
@@ -144,14 +149,22 @@ mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
                           bool border, int geom, CUtensorMap* mx, CUtensorMap* my, int* Pf_out,
                           cudaStream_t st);
 
+// Called after the launch of each chunk of an FP (views first .. first +
+// count - 1) or BP (slices first .. first + count - 1) split into `chunks`
+// launches; the results of each launch are bit-identical to the unsplit one.
+struct ChunkHook {
+  int chunks;
+  std::function<mexct_status(int index, int first, int count)> fn;
+};
+
 // FP with a concrete variant / BP with an explicit launch shape (arguments
 // already checked; ops.cu).
 mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float sad,
                     const float* angles, int nP, int geom, void* d_out, int ot, int variant,
-                    cudaStream_t st);
+                    cudaStream_t st, const ChunkHook* hook = nullptr);
 mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, int nP, float sad,
                     const float* angles, int geom, void* d_vol, int vt, const BpShape& shp,
-                    cudaStream_t st);
+                    cudaStream_t st, const ChunkHook* hook = nullptr);
 // Shape of a call's class from the context's table, its mode's default, or
 // (MEXCT_TUNE_AUTO, outside stream capture) by timing the candidates on the
 // call's own buffers (tune.cu).

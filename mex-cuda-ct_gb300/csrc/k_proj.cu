@@ -624,10 +624,10 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
                                                      const TS* __restrict__ sino, int Wp,
                                                      TV* __restrict__ vol, int accumulate,
                                                      int nz, int vblocks,
-                                                     float* __restrict__ part) {
+                                                     float* __restrict__ part, int zb0) {
   const int ix = blockIdx.x * 32 + threadIdx.x;
   const int iy = blockIdx.y * blockDim.y + threadIdx.y;
-  const int zb = blockIdx.z % nz, vb = blockIdx.z / nz;
+  const int zb = zb0 + blockIdx.z % nz, vb = blockIdx.z / nz;  // nz: z-blocks of the launch
   const int z0 = zb * ZC;
   if (ix >= A.W || iy >= A.W) return;
   const int vbeg = (int)((long long)A.nviews * vb / vblocks);
@@ -717,11 +717,15 @@ constexpr int kBpZc = 16;
 template <int GEOM, int ZC, typename TS, typename TV>
 static cudaError_t bp_pad_go(const VoxArgs& a, const void* sino, int Wp, void* vol, bool accum,
                              const BpShape& shp, float* part, cudaStream_t st) {
-  const int nz = (a.H + ZC - 1) / ZC;
+  const int nzall = (a.H + ZC - 1) / ZC;
+  if (shp.zb0 < 0 || shp.zb0 >= nzall || (shp.vblocks > 1 && (shp.zb0 > 0 || shp.nzb > 0)))
+    return cudaErrorInvalidValue;
+  const int nz = shp.nzb > 0 ? std::min(shp.nzb, nzall - shp.zb0) : nzall - shp.zb0;
   dim3 blk(32, shp.rows), grd((a.W + 31) / 32, (a.W + shp.rows - 1) / shp.rows,
                               nz * shp.vblocks);
   bp_pad_kernel<GEOM, ZC, TS, TV><<<grd, blk, 0, st>>>(a, (const TS*)sino, Wp, (TV*)vol,
-                                                       accum ? 1 : 0, nz, shp.vblocks, part);
+                                                       accum ? 1 : 0, nz, shp.vblocks, part,
+                                                       shp.zb0);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || shp.vblocks == 1) return e;
   const long long N = (long long)a.W * a.W * a.H;
@@ -832,15 +836,15 @@ cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, flo
   switch (geom) {
     case 0:
       bp_pad_kernel<0, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
-                                                                    nz, 1, nullptr);
+                                                                    nz, 1, nullptr, 0);
       break;
     case 1:
       bp_pad_kernel<1, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
-                                                                    nz, 1, nullptr);
+                                                                    nz, 1, nullptr, 0);
       break;
     case 2:
       bp_pad_kernel<2, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
-                                                                    nz, 1, nullptr);
+                                                                    nz, 1, nullptr, 0);
       break;
     default: return cudaErrorInvalidValue;
   }
@@ -858,15 +862,15 @@ cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const float* sino_pad, flo
   switch (geom) {
     case 0:
       bp_pad_kernel<0, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
-                                                                 1, nullptr);
+                                                                 1, nullptr, 0);
       break;
     case 1:
       bp_pad_kernel<1, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
-                                                                 1, nullptr);
+                                                                 1, nullptr, 0);
       break;
     case 2:
       bp_pad_kernel<2, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
-                                                                 1, nullptr);
+                                                                 1, nullptr, 0);
       break;
     default: return cudaErrorInvalidValue;
   }

@@ -171,6 +171,10 @@ cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews,
 // an FP32 partial-sum workspace of vblocks * W*W*H floats).
 struct BpShape {
   int zc, rows, vblocks;
+  // z-blocks (of zc slices) zb0 .. zb0 + nzb - 1 only (nzb = 0: all); with
+  // one view block, a z range gets exactly the per-voxel operations of the
+  // whole launch.
+  int zb0 = 0, nzb = 0;
 };
 bool bp_shape_valid(const BpShape& s);
 // BP of a.nviews views from a padded sinogram (view 0 of the launch first).

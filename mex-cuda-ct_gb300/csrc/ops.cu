@@ -129,7 +129,7 @@ namespace mexct {
 // FP with a concrete variant (EXPLICIT, RAY or TEXTURE); arguments checked.
 mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float sad,
                     const float* angles, int nP, int geom, void* d_out, int ot, int variant,
-                    cudaStream_t st) {
+                    cudaStream_t st, const ChunkHook* hook) {
   if (nP == 0) return MEXCT_OK;
   std::unique_ptr<RayArgs> a(new RayArgs);
   fill_std_rays(*a, W, H, sad, geom, false);
@@ -144,13 +144,18 @@ mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float
     mexct_status s = prepare_slab(c, d_vol, vt, W, H, false, geom, &mx, &my, &Pf, st);
     if (s) return s;
     SlabEpi e{nullptr, nullptr, nullptr, nullptr, c->err.as<unsigned>(), c->wait_us};
-    for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
-      a->nviews = std::min(kMaxViews, nP - v0);
+    // launches of at most kMaxViews views, or hook->chunks launches
+    const int step = hook ? std::min(kMaxViews, (nP + hook->chunks - 1) / hook->chunks)
+                          : kMaxViews;
+    for (int v0 = 0, ci = 0; v0 < nP; v0 += step, ++ci) {
+      a->nviews = std::min(step, nP - v0);
       a->view0 = v0;
       for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
       MEXCT_TRY_CUDA(launch_fp_slab(geom, false, false, *a, mx, my, c->padx.p, c->pady.p, Pf, vt,
                                     d_out, ot, e, st),
                      "fp: launch");
+      if (hook)
+        if (mexct_status s2 = hook->fn(ci, v0, a->nviews)) return s2;
     }
     return MEXCT_OK;
   }
@@ -171,7 +176,7 @@ mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float
 // padded copy (clamp frame) in chunks of kMaxViews.
 mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, int nP, float sad,
                     const float* angles, int geom, void* d_vol, int vt, const BpShape& shp,
-                    cudaStream_t st) {
+                    cudaStream_t st, const ChunkHook* hook) {
   std::unique_ptr<VoxArgs> a(new VoxArgs);
   fill_vox(*a, W, H, sad);
   if (nP == 0) {
@@ -194,20 +199,45 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
     a->view0 = 0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
     const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
+    // z ranges of the volume in hook->chunks launches (one view chunk, one
+    // view block: the per-voxel operations are those of one launch)
+    const bool zsplit = hook && nP <= kMaxViews && shp.vblocks == 1 && (quad || pair);
+    const int nzb = (H + shp.zc - 1) / shp.zc;
+    const int zstep = zsplit ? (nzb + hook->chunks - 1) / hook->chunks : nzb;
     if (quad) {
       MEXCT_TRY_CUDA(launch_pad_sino_quad(src, stype, W, H, a->nviews, c->spad.p, st), "bp: pad");
-      MEXCT_TRY_CUDA(launch_bp_quad(*a, c->spad.p, stype, d_vol, vt, v0 > 0, shp,
-                                    c->bpart.as<float>(), st),
-                     "bp: launch");
+      for (int zb = 0, ci = 0; zb < nzb; zb += zstep, ++ci) {
+        BpShape sh = shp;
+        sh.zb0 = zb;
+        sh.nzb = zsplit ? zstep : 0;
+        MEXCT_TRY_CUDA(launch_bp_quad(*a, c->spad.p, stype, d_vol, vt, v0 > 0, sh,
+                                      c->bpart.as<float>(), st),
+                       "bp: launch");
+        if (zsplit) {
+          const int z0 = zb * shp.zc;
+          if (mexct_status s2 = hook->fn(ci, z0, std::min(H, z0 + zstep * shp.zc) - z0))
+            return s2;
+        }
+      }
       continue;
     }
     if (pair) {
       MEXCT_TRY_CUDA(launch_pad_sino_pair(static_cast<const float*>(static_cast<const void*>(src)),
                                           W, H, a->nviews, c->spad.as<float2>(), st),
                      "bp: pad");
-      MEXCT_TRY_CUDA(launch_bp_pair(geom, *a, c->spad.as<float2>(), d_vol, vt, v0 > 0, shp,
-                                    c->bpart.as<float>(), st),
-                     "bp: launch");
+      for (int zb = 0, ci = 0; zb < nzb; zb += zstep, ++ci) {
+        BpShape sh = shp;
+        sh.zb0 = zb;
+        sh.nzb = zsplit ? zstep : 0;
+        MEXCT_TRY_CUDA(launch_bp_pair(geom, *a, c->spad.as<float2>(), d_vol, vt, v0 > 0, sh,
+                                      c->bpart.as<float>(), st),
+                       "bp: launch");
+        if (zsplit) {
+          const int z0 = zb * shp.zc;
+          if (mexct_status s2 = hook->fn(ci, z0, std::min(H, z0 + zstep * shp.zc) - z0))
+            return s2;
+        }
+      }
       continue;
     }
     MEXCT_TRY_CUDA(launch_pad_sino(src, stype, W, H, a->nviews, false, c->spad.p, st),
@@ -719,6 +749,85 @@ mexct_status prefilter_tables(mexct_ctx* c, int W, int H, int nP, const float* a
   return MEXCT_OK;
 }
 
+// The context's copy stream (created on first use).
+cudaError_t copy_stream(mexct_ctx* c, cudaStream_t* out) {
+  if (!c->copy_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    for (cudaEvent_t& ev : c->chunk_ev) {
+      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  *out = c->copy_stream;
+  return cudaSuccess;
+}
+
+// Downloads of the chunks recorded by a ChunkHook: chunk i waits for its
+// event and copies `bytes` from d + off to h + off on the copy stream.  All
+// launches are enqueued before the first copy (a pageable destination makes
+// the copy call wait), then both streams are drained.
+struct ChunkCopies {
+  struct Item { size_t off, bytes; };
+  std::vector<Item> items;
+  mexct_status run(mexct_ctx* c, cudaStream_t cs, void* h, const void* d, const char* what) {
+    for (size_t i = 0; i < items.size(); ++i) {
+      MEXCT_TRY_CUDA(cudaStreamWaitEvent(cs, c->chunk_ev[i], 0), what);
+      MEXCT_TRY_CUDA(cudaMemcpyAsync(static_cast<char*>(h) + items[i].off,
+                                     static_cast<const char*>(d) + items[i].off, items[i].bytes,
+                                     cudaMemcpyDeviceToHost, cs),
+                     what);
+    }
+    MEXCT_TRY_CUDA(cudaStreamSynchronize(cs), what);
+    MEXCT_TRY_CUDA(cudaStreamSynchronize(c->stream), what);
+    return MEXCT_OK;
+  }
+};
+
+constexpr int kHostChunks = 8;
+
+mexct_status fp_host_overlapped(mexct_ctx* c, int W, int H, float sad, const float* angles,
+                                int nP, int geom, float* out) {
+  cudaStream_t cs;
+  MEXCT_TRY_CUDA(copy_stream(c, &cs), "fp: copy stream");
+  const size_t P = (size_t)W * H;
+  ChunkCopies cc;
+  ChunkHook hook{kHostChunks, [&](int i, int v0, int n) -> mexct_status {
+                   if (i >= kHostChunks) return set_err(MEXCT_ERR_ARG, "fp: too many chunks");
+                   MEXCT_TRY_CUDA(cudaEventRecord(c->chunk_ev[i], c->stream), "fp: event");
+                   cc.items.push_back({(size_t)v0 * P * 4, (size_t)n * P * 4});
+                   return MEXCT_OK;
+                 }};
+  mexct_status s = fp_run(c, c->in.p, kF32, W, H, sad, angles, nP, geom, c->out.p, kF32,
+                          MEXCT_FP_EXPLICIT, c->stream, &hook);
+  if (s) return s;
+  return cc.run(c, cs, out, c->out.p, "fp: download");
+}
+
+mexct_status bp_host_overlapped(mexct_ctx* c, int W, int H, int nP, float sad,
+                                const float* angles, int geom, const BpShape& shp, float* vol) {
+  cudaStream_t cs;
+  MEXCT_TRY_CUDA(copy_stream(c, &cs), "bp: copy stream");
+  const size_t slice = (size_t)W * W * 4;
+  ChunkCopies cc;
+  ChunkHook hook{kHostChunks, [&](int i, int z0, int nz) -> mexct_status {
+                   if (i >= kHostChunks) return set_err(MEXCT_ERR_ARG, "bp: too many chunks");
+                   MEXCT_TRY_CUDA(cudaEventRecord(c->chunk_ev[i], c->stream), "bp: event");
+                   cc.items.push_back({(size_t)z0 * slice, (size_t)nz * slice});
+                   return MEXCT_OK;
+                 }};
+  mexct_status s = bp_run(c, c->in.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, shp,
+                          c->stream, &hook);
+  if (s) return s;
+  if (cc.items.empty()) {  // the shape ran as one launch: plain download
+    MEXCT_TRY_CUDA(cudaMemcpyAsync(vol, c->out.p, slice * H, cudaMemcpyDeviceToHost, c->stream),
+                   "bp: download");
+    MEXCT_TRY_CUDA(cudaStreamSynchronize(c->stream), "bp: download");
+    return MEXCT_OK;
+  }
+  return cc.run(c, cs, vol, c->out.p, "bp: download");
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -770,6 +879,16 @@ mexct_status mexct_fp(mexct_ctx* ctx, const float* vol, int W, int H,
   mexct_status s = upload(c->in, vol, N * 4, c->stream, "fp: upload");
   if (s) return s;
   MEXCT_TRY_CUDA(c->out.ensure_async(M * 4, c->stream), "fp: workspace");
+  if (nP >= 16 && nP <= kHostChunks * kMaxViews && M * 4 >= ((size_t)64 << 20)) {
+    // the slab FP in view chunks, each chunk's download overlapping the
+    // launches after it (same result as one launch: rays are independent)
+    mexct_shape shp;
+    s = pick_fp_shape(c, c->in.p, kF32, W, H, sad, angles, nP, geom, c->out.p, kF32, c->stream,
+                      &shp);
+    if (s) return s;
+    if (shp.variant == MEXCT_FP_EXPLICIT) return fp_host_overlapped(c, W, H, sad, angles, nP,
+                                                                    geom, out);
+  }
   s = fp_dev_impl(c, c->in.p, kF32, W, H, sad, angles, nP, geom, c->out.p, kF32,
                   MEXCT_FP_AUTO, c->stream);
   if (s) return s;
@@ -832,6 +951,17 @@ mexct_status mexct_bp(mexct_ctx* ctx, const float* sino, int W, int H, int nP,
   mexct_status s = upload(c->in, sino, M * 4, c->stream, "bp: upload");
   if (s) return s;
   MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "bp: workspace");
+  if (nP > 0 && nP <= kMaxViews && N * 4 >= ((size_t)64 << 20)) {
+    // z ranges in turn, each range's download overlapping the launches after
+    // it (same per-voxel operations as one launch), when one view block is used
+    mexct_shape shp{MEXCT_FP_EXPLICIT, 16, 8, 1};
+    s = pick_bp_shape(c, c->in.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, c->stream,
+                      &shp);
+    if (s) return s;
+    if (shp.vblocks == 1)
+      return bp_host_overlapped(c, W, H, nP, sad, angles, geom, BpShape{shp.zc, shp.rows, 1},
+                                vol);
+  }
   s = bp_dev_impl(c, c->in.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, c->stream);
   if (s) return s;
   return finish(c, vol, c->out, N * 4, "bp: download");
