@@ -77,14 +77,16 @@ __device__ __forceinline__ bool finish_partials(double mine, double* partials,
 // (CUDAmex_TVmin_3D.cu:121-152: the second to fourth terms are the first
 // term's components at the +x, +y and +z neighbours), so each voxel's
 // (a, b, c, r) is computed once (one reciprocal square root, one reciprocal)
-// instead of four times.  A CTA of 32 x 8 threads sweeps a column tile along z: thread
-// (tx, ty) computes q at its column in every plane, takes the +x neighbour's
-// value by a shuffle, the +y neighbour's from shared memory (one barrier per
-// plane) and the +z neighbour's from its next plane, and writes the voxel
-// when tx < 31 and ty < 7 (tiles overlap by one column and one row).  The
+// instead of four times.  A CTA of 32 x 16 threads sweeps a column tile along z:
+// thread (tx, ty) computes q at its column in every plane, takes the +x
+// neighbour's value by a shuffle, the +y neighbour's from shared memory (one
+// barrier per plane) and the +z neighbour's from its next plane, and writes the
+// voxel when tx < 31 and ty < 15 (tiles overlap by one column and one row).  The
 // next plane's loads are issued before the current plane is computed.
 // ---------------------------------------------------------------------------
-constexpr int kTvBx = 32, kTvBy = 8, kTvZ = 32;  // threads 32 x 8, 32 planes per CTA
+// 32 x 16 threads (31 x 15 outputs: 91 % of the threads own a voxel, 85 % with
+// 32 x 8; 512^3 step 0.978 -> 0.926 ms), 32 planes per CTA
+constexpr int kTvBx = 32, kTvBy = 16, kTvZ = 32;
 constexpr int kTvOx = kTvBx - 1, kTvOy = kTvBy - 1;  // output voxels per tile row / column
 
 // Sweep of one tile: calls visit(z, x_z, g, out) for every plane z of the
@@ -161,7 +163,7 @@ __device__ __forceinline__ void tv_sweep(const T* __restrict__ v, int Nx, int Ny
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) tv_norm_kernel(
+__global__ void __launch_bounds__(kTvBx * kTvBy) tv_norm_kernel(
     const T* __restrict__ x, int Nx, int Ny, int Nz, float c,
     const double* __restrict__ cmul, double* __restrict__ partials,
     unsigned* __restrict__ counter, float* __restrict__ scale,
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(256) tv_norm_kernel(
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) tv_update_kernel(
+__global__ void __launch_bounds__(kTvBx * kTvBy) tv_update_kernel(
     const T* __restrict__ x, T* __restrict__ y, int Nx, int Ny, int Nz,
     const float* __restrict__ scale) {
   const float a = __ldg(scale);
