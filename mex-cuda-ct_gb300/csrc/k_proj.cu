@@ -203,14 +203,13 @@ cudaError_t launch_fp(int geom, bool border, const RayArgs& a,
                       const void* vx, const void* vy, int vt,
                       const float* pts, void* out, int ot, cudaStream_t st) {
   if (a.nviews <= 0) return cudaSuccess;
-  switch (geom * 2 + (border ? 1 : 0)) {
+  // the ray-per-thread form serves MEXCT_FP_RAY for the standard geometries
+  // (clamp addressing); general3D and the OSC FP use the slab kernel
+  if (border) return cudaErrorInvalidValue;
+  switch (geom) {
     case 0: return fp_types<0, false>(a, vx, vy, vt, pts, out, ot, st);
-    case 1: return fp_types<0, true>(a, vx, vy, vt, pts, out, ot, st);
-    case 2: return fp_types<1, false>(a, vx, vy, vt, pts, out, ot, st);
-    case 3: return fp_types<1, true>(a, vx, vy, vt, pts, out, ot, st);
-    case 4: return fp_types<2, false>(a, vx, vy, vt, pts, out, ot, st);
-    case 5: return fp_types<2, true>(a, vx, vy, vt, pts, out, ot, st);
-    case 7: return fp_types<3, true>(a, vx, vy, vt, pts, out, ot, st);
+    case 1: return fp_types<1, false>(a, vx, vy, vt, pts, out, ot, st);
+    case 2: return fp_types<2, false>(a, vx, vy, vt, pts, out, ot, st);
     default: return cudaErrorInvalidValue;
   }
 }
