@@ -492,8 +492,8 @@ def batched_uneven(count, seed=2026):
     """48 uneven problems (geom 0/1/2, 64^3..256^3, 90..720 views): FP + BP + 5 OSC-TV
     iterations (8 subsets) each.  plain: one problem at a time, one launch per
     operator call, eager OSC-TV.  chosen: all FPs in one persistent launch and all
-    BPs in another, captured in one CUDA graph; OSC-TV solvers replay per-iteration
-    graphs on 8 concurrent streams."""
+    BPs as concurrent per-problem launches on 8 streams, each captured in a CUDA graph;
+    OSC-TV solvers replay per-iteration graphs on 8 concurrent streams."""
     import torch
 
     from mexct import batch, ops, phantoms, solver

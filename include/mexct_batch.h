@@ -30,7 +30,10 @@ mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int 
 /* FP of every problem: one batched padding launch + one persistent launch.
  * Stream-ordered, no host work, capturable in a CUDA graph. */
 mexct_status mexct_batch_fp(mexct_batch* b, void* stream);
-/* BP of every problem (d_sino -> d_rec): one persistent launch. */
+/* BP of every problem (d_sino -> d_rec): per problem a padding launch and its
+ * BP launches (quad / pair view layouts, one view block), fanned out over 8
+ * streams by fork / join events on `stream`, so a capture records them as
+ * concurrent graph branches.  Stream-ordered, no host work. */
 mexct_status mexct_batch_bp(mexct_batch* b, void* stream);
 mexct_status mexct_batch_destroy(mexct_batch* b);
 

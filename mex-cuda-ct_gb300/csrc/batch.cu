@@ -24,15 +24,27 @@ struct mexct_batch {
   int device = 0;
   int n = 0;
   std::vector<Buf> pads;   // 2 per problem: padded volume, both layouts
-  std::vector<Buf> spads;  // 1 per problem: padded sinogram for BP
+  std::vector<Buf> spads;  // 1 per problem: padded sinogram for BP (quad / pair layout)
   std::vector<mexct_problem> probs;
-  Buf fp_desc, bp_desc, trig, counters, err;
-  long long fp_items = 0, bp_items = 0, pad_items = 0;
+  // BP launch arguments per problem and view chunk (at most kMaxViews views)
+  std::vector<std::vector<std::unique_ptr<VoxArgs>>> vox;
+  Buf fp_desc, trig, counters, err;
+  long long fp_items = 0, pad_items = 0;
   int sms = 152;
+  // BP: the problems' launches fan out over kAux streams (fork / join events
+  // on the caller's stream, so a capture records them as graph branches)
+  static constexpr int kAux = 8;
+  cudaStream_t aux[kAux] = {};
+  cudaEvent_t fork = nullptr, join[kAux] = {};
   ~mexct_batch() {
     for (Buf& b : pads) b.release();
     for (Buf& b : spads) b.release();
-    for (Buf* b : {&fp_desc, &bp_desc, &trig, &counters, &err}) b->release();
+    for (Buf* b : {&fp_desc, &trig, &counters, &err}) b->release();
+    for (int k = 0; k < kAux; ++k) {
+      if (aux[k]) cudaStreamDestroy(aux[k]);
+      if (join[k]) cudaEventDestroy(join[k]);
+    }
+    if (fork) cudaEventDestroy(fork);
   }
 };
 
@@ -63,9 +75,17 @@ mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int 
   for (int i = 0; i < n; ++i) ntrig += probs[i].nP;
   std::vector<Trig> trig(ntrig);
   std::vector<BatchFp> fd(n);
-  std::vector<BatchBp> bd(n);
   b->pads.resize(2 * n);
   b->spads.resize(n);
+  b->vox.resize(n);
+  for (int k = 0; k < mexct_batch::kAux; ++k) {
+    MEXCT_TRY_CUDA(cudaStreamCreateWithFlags(&b->aux[k], cudaStreamNonBlocking),
+                   "batch_create: streams");
+    MEXCT_TRY_CUDA(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming),
+                   "batch_create: events");
+  }
+  MEXCT_TRY_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming),
+                 "batch_create: events");
   b->probs.assign(probs, probs + n);
   size_t toff = 0;
   MEXCT_TRY_CUDA(b->trig.ensure(ntrig * sizeof(Trig)), "batch_create: trig");
@@ -107,36 +127,27 @@ mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int 
     f.pad_item0 = b->pad_items;
     const long long nt = (Pf + 31) / 32;
     b->pad_items += nt * nt * (H + 2);
-    BatchBp& g = bd[i];
-    std::memset(&g, 0, sizeof g);
-    g.W = W;
-    g.H = H;
-    g.geom = p.geom;
-    g.nviews = p.nP;
-    g.bx = (W + 31) / 32;
-    g.by = (W + 7) / 8;
-    g.bz = (H + bp_brick_z() - 1) / bp_brick_z();
-    g.v0 = float(H - 1) / 2;   // CUDAmex_BP.cu:249
-    g.sad = p.sad;
-    g.hw = (uint32_t)W / 2u - 1u;  // :73
-    g.item0 = b->bp_items;
-    b->bp_items += (long long)g.bx * g.by * g.bz;
-    MEXCT_TRY_CUDA(b->spads[i].ensure(sino_pad_elems(W, H, p.nP) * sizeof(float)),
+    // BP: views in the quad (cone) or pair (par / fan) layout, one launch per
+    // kMaxViews views (mexct_bp_dev's shapes without view blocks)
+    MEXCT_TRY_CUDA(b->spads[i].ensure(sino_pad_elems(W, H, p.nP) *
+                                      (p.geom == 2 ? sizeof(float4) : sizeof(float2))),
                    "batch_create: padded sinogram");
-    g.sino = b->spads[i].p;
-    g.vol = p.d_rec;
-    g.trig = dtrig + toff;
+    for (int v0 = 0; v0 < p.nP; v0 += kMaxViews) {
+      std::unique_ptr<VoxArgs> va(new VoxArgs);
+      fill_vox(*va, W, H, p.sad);
+      va->nviews = std::min(kMaxViews, p.nP - v0);
+      va->view0 = 0;
+      for (int v = 0; v < va->nviews; ++v) trig_of(p.angles[v0 + v], &va->trig[v]);
+      b->vox[i].push_back(std::move(va));
+    }
     toff += p.nP;
   }
   MEXCT_TRY_CUDA(b->fp_desc.ensure(n * sizeof(BatchFp)), "batch_create: descriptors");
-  MEXCT_TRY_CUDA(b->bp_desc.ensure(n * sizeof(BatchBp)), "batch_create: descriptors");
   MEXCT_TRY_CUDA(b->counters.ensure(64), "batch_create: counters");
   MEXCT_TRY_CUDA(b->err.ensure(64), "batch_create: error word");
   MEXCT_TRY_CUDA(cudaMemcpy(b->trig.p, trig.data(), ntrig * sizeof(Trig), cudaMemcpyHostToDevice),
                  "batch_create: upload");
   MEXCT_TRY_CUDA(cudaMemcpy(b->fp_desc.p, fd.data(), n * sizeof(BatchFp), cudaMemcpyHostToDevice),
-                 "batch_create: upload");
-  MEXCT_TRY_CUDA(cudaMemcpy(b->bp_desc.p, bd.data(), n * sizeof(BatchBp), cudaMemcpyHostToDevice),
                  "batch_create: upload");
   MEXCT_TRY_CUDA(cudaMemset(b->err.p, 0, 64), "batch_create: error word");
   *out = b.release();
@@ -164,15 +175,33 @@ mexct_status mexct_batch_bp(mexct_batch* b, void* stream) {
   DevGuard dg(b->device);
   NvtxRange nvtx("mexct:batch_bp");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MEXCT_TRY_CUDA(cudaEventRecord(b->fork, st), "batch_bp: fork");
+  for (int k = 0; k < mexct_batch::kAux; ++k)
+    MEXCT_TRY_CUDA(cudaStreamWaitEvent(b->aux[k], b->fork, 0), "batch_bp: fork");
   for (int i = 0; i < b->n; ++i) {
     const mexct_problem& p = b->probs[i];
-    MEXCT_TRY_CUDA(launch_pad_sino(p.d_sino, kF32, p.W, p.H, p.nP, false, b->spads[i].p, st),
+    cudaStream_t s = b->aux[i % mexct_batch::kAux];
+    const bool quad = p.geom == 2;
+    MEXCT_TRY_CUDA(quad ? launch_pad_sino_quad(p.d_sino, kF32, p.W, p.H, p.nP, b->spads[i].p, s)
+                        : launch_pad_sino_pair(p.d_sino, p.W, p.H, p.nP,
+                                               b->spads[i].as<float2>(), s),
                    "batch_bp: padding");
+    const size_t vstride = sino_pad_elems(p.W, p.H, 1) * (quad ? sizeof(float4) : sizeof(float2));
+    const BpShape shp{16, 8, 1};
+    int v0 = 0;
+    for (const auto& va : b->vox[i]) {
+      const char* src = static_cast<const char*>(b->spads[i].p) + (size_t)v0 * vstride;
+      MEXCT_TRY_CUDA(quad ? launch_bp_quad(*va, src, kF32, p.d_rec, kF32, v0 > 0, shp, nullptr, s)
+                          : launch_bp_pair(p.geom, *va, reinterpret_cast<const float2*>(src),
+                                           p.d_rec, kF32, v0 > 0, shp, nullptr, s),
+                     "batch_bp: launch");
+      v0 += va->nviews;
+    }
   }
-  unsigned long long* ctr = b->counters.as<unsigned long long>() + 1;
-  MEXCT_TRY_CUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st), "batch_bp: counter");
-  MEXCT_TRY_CUDA(launch_bp_batch(b->bp_desc.as<BatchBp>(), b->n, b->bp_items, ctr, b->sms * 4, st),
-                 "batch_bp: launch");
+  for (int k = 0; k < mexct_batch::kAux; ++k) {
+    MEXCT_TRY_CUDA(cudaEventRecord(b->join[k], b->aux[k]), "batch_bp: join");
+    MEXCT_TRY_CUDA(cudaStreamWaitEvent(st, b->join[k], 0), "batch_bp: join");
+  }
   return MEXCT_OK;
 }
 

@@ -1062,87 +1062,5 @@ cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
 
 namespace mexct {
 
-// ---------------------------------------------------------------------------
-// Batched BP (mexct_batch.h): persistent CTAs over (problem, brick) items.
-// ---------------------------------------------------------------------------
-constexpr int kSmZc = 8;  // z voxels per thread (any ZC gives the same per-voxel arithmetic)
-
-// Geometry of one brick job.
-struct BrickJob {
-  int W, H, nviews, view0;
-  float v0, SR;
-  uint32_t hw;
-  long long P;
-  const Trig* trig;
-  int bx0, by0, z0;
-};
-
-// One 32 x 8 x kSmZc brick through L1 (the body of bp_kernel with the view
-// geometry read from a device table): the batched BP computes exactly what the
-// single-problem BP computes.
-template <int GEOM>
-__device__ __forceinline__ void bp_l1_brick(const BrickJob& A, const float* __restrict__ sino,
-                                            float* __restrict__ vol) {
-  const int ix = A.bx0 + threadIdx.x, iy = A.by0 + threadIdx.y, z0 = A.z0;
-  if (ix >= A.W || iy >= A.W) return;
-  // sino: padded views ([H+4][W+4] each), as for bp_pad_kernel
-  const int Wp = sino_pad_pitch(A.W);
-  const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
-  float acc[kSmZc];
-#pragma unroll
-  for (int j = 0; j < kSmZc; ++j) acc[j] = 0.f;
-  if (in_circle(ix, iy, A.hw)) {
-    const float x = (float)ix - ((float)A.hw + 0.5f);
-    const float y = (float)iy - ((float)A.hw + 0.5f);
-    for (int v = 0; v < A.nviews; ++v) {
-      const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
-      bp_column_pad<GEOM, kSmZc>(sino + (size_t)(A.view0 + v) * vstride, A.W, A.H, Wp, z0, g,
-                                 acc);
-    }
-  }
-  const size_t base = (size_t)iy * A.W + ix;
-  const size_t sz = (size_t)A.W * A.W;
-#pragma unroll
-  for (int j = 0; j < kSmZc; ++j)
-    if (z0 + j < A.H) vol[base + (size_t)(z0 + j) * sz] = acc[j];
-}
-
-// Batched BP: persistent CTAs take (problem, brick) items from a counter.
-__global__ void __launch_bounds__(256) bp_batch_kernel(
-    const BatchBp* __restrict__ probs, int nprob, long long total,
-    unsigned long long* __restrict__ counter) {
-  __shared__ long long s_item;
-  for (;;) {
-    if (threadIdx.x + 32 * threadIdx.y == 0) s_item = (long long)atomicAdd(counter, 1ull);
-    __syncthreads();
-    const long long item = s_item;
-    __syncthreads();
-    if (item >= total) break;
-    int lo = 0, hi = nprob - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (probs[mid].item0 <= item) lo = mid;
-      else hi = mid - 1;
-    }
-    const BatchBp& B = probs[lo];
-    const long long rr = item - B.item0;
-    const int bxi = (int)(rr % B.bx), byi = (int)((rr / B.bx) % B.by), bzi = (int)(rr / ((long long)B.bx * B.by));
-    BrickJob J{B.W, B.H, B.nviews, 0, B.v0, B.sad, B.hw, (long long)B.W * B.H, B.trig,
-               bxi * 32, byi * 8, bzi * kSmZc};
-    if (B.geom == 0) bp_l1_brick<0>(J, (const float*)B.sino, (float*)B.vol);
-    else if (B.geom == 1) bp_l1_brick<1>(J, (const float*)B.sino, (float*)B.vol);
-    else bp_l1_brick<2>(J, (const float*)B.sino, (float*)B.vol);
-    __syncthreads();  // s_item is rewritten by thread 0 at the top of the loop
-  }
-}
-
-int bp_brick_z() { return kSmZc; }
-
-cudaError_t launch_bp_batch(const BatchBp* d_probs, int nprob, long long total,
-                            unsigned long long* counter, int ctas, cudaStream_t st) {
-  if (total <= 0) return cudaSuccess;
-  bp_batch_kernel<<<ctas, dim3(32, 8), 0, st>>>(d_probs, nprob, total, counter);
-  return cudaGetLastError();
-}
 
 }  // namespace mexct

@@ -97,24 +97,13 @@ struct alignas(64) BatchFp {
 };
 
 // One problem of a batched BP launch.
-struct BatchBp {
-  int W, H, geom, nviews, bx, by, bz;  // bx/by/bz: bricks per axis
-  float v0, sad;
-  uint32_t hw;
-  long long item0;            // first work item: bx * by * bz bricks follow
-  const void* sino;
-  void* vol;
-  const Trig* trig;
-};
 
 cudaError_t launch_fp_batch(const BatchFp* d_probs, int nprob, long long total,
                             unsigned long long* counter, unsigned* err, int ctas,
                             cudaStream_t st);
 cudaError_t launch_pad_batch(const BatchFp* d_probs, int nprob, long long total,
                              cudaStream_t st);
-cudaError_t launch_bp_batch(const BatchBp* d_probs, int nprob, long long total,
-                            unsigned long long* counter, int ctas, cudaStream_t st);
-int bp_brick_z();
+
 cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
                               bool border, void* px, void* py, cudaStream_t st);
 // TMA map over a padded volume (Pf x Ps x Pz) with the box shape of the slab

@@ -1,8 +1,8 @@
 """Batched FP/BP over many independent problems (include/mexct_batch.h).
 
-``Batch([...])`` plans one persistent FP launch and one persistent BP launch over
-problems of different sizes, geometries and view counts; ``fp()`` / ``bp()`` are
-stream-ordered and can be captured in a CUDA graph.  Each problem is a dict with
+``Batch([...])`` plans one persistent FP launch and per-problem BP launches (fanned
+out over 8 streams) over problems of different sizes, geometries and view counts;
+``fp()`` / ``bp()`` are stream-ordered and can be captured in a CUDA graph.  Each problem is a dict with
 ``vol`` (H, W, W) float32 CUDA tensor, ``sino`` (nP, H, W), ``rec`` (H, W, W),
 ``angles`` (float32 numpy), ``sad`` and ``geom``.
 """
