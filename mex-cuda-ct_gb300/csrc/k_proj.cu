@@ -549,10 +549,10 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
 // holds the bilinear footprint {P(r,c), P(r,c+1), P(r+1,c), P(r+1,c+1)} of
 // the padded view P, so each voxel's four taps are one 16-byte load.  The
 // arithmetic is bp_column_pad's (GEOM 2), operation for operation.
-template <int ZC, typename S = float>
+template <int ZC, typename S = float, int GEOM = 2>
 __device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __restrict__ p, int W,
-                                               int H, int Wp, int z0, const ColGeom<2>& g,
-                                               float* acc) {
+                                               int H, int Wp, int z0, const ColGeom<GEOM>& g,
+                                               float* acc, int roff = 0) {
   const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
   const float fu = floorf(cu);
   const float au = cu - fu;
@@ -569,8 +569,8 @@ __device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __res
     const float2 cz = __ffma2_rn(zz, dpz2, pz02);
     const float2 fz = make_float2(floorf(cz.x), floorf(cz.y));
     const float2 az = __fadd2_rn(cz, make_float2(-fz.x, -fz.y));
-    const int i0 = min(max(__float2int_rz(fz.x), -kSinoPad), H) + kSinoPad;
-    const int i1 = min(max(__float2int_rz(fz.y), -kSinoPad), H) + kSinoPad;
+    const int i0 = min(max(__float2int_rz(fz.x) - roff, -kSinoPad), H) + kSinoPad;
+    const int i1 = min(max(__float2int_rz(fz.y) - roff, -kSinoPad), H) + kSinoPad;
     const float4 q0 = QuadT<S>::get(col + (size_t)i0 * Wp);
     const float4 q1 = QuadT<S>::get(col + (size_t)i1 * Wp);
     const float2 a = __ffma2_rn(w02, make_float2(q0.x, q1.x), __fmul2_rn(w12, make_float2(q0.y, q1.y)));
@@ -587,7 +587,8 @@ __device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __res
 // texel row) are one 8-byte load.  bp_column_pad's arithmetic (ROWS path).
 template <int GEOM, int ZC>
 __device__ __forceinline__ void bp_column_pair(const float2* __restrict__ p, int W, int H, int Wp,
-                                               int z0, const ColGeom<GEOM>& g, float* acc) {
+                                               int z0, const ColGeom<GEOM>& g, float* acc,
+                                               int roff = 0) {
   const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
   const float fu = floorf(cu);
   const float au = cu - fu;
@@ -598,8 +599,8 @@ __device__ __forceinline__ void bp_column_pair(const float2* __restrict__ p, int
   const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
 #pragma unroll
   for (int j = 0; j < ZC; j += 2) {
-    const float2 q0 = __ldg(col + (size_t)(min(z0 + j, H - 1) + kSinoPad) * Wp);
-    const float2 q1 = __ldg(col + (size_t)(min(z0 + j + 1, H - 1) + kSinoPad) * Wp);
+    const float2 q0 = __ldg(col + (size_t)(min(z0 + j - roff, H - 1) + kSinoPad) * Wp);
+    const float2 q1 = __ldg(col + (size_t)(min(z0 + j + 1 - roff, H - 1) + kSinoPad) * Wp);
     const float2 t = __ffma2_rn(w02, make_float2(q0.x, q1.x),
                                 __ffma2_rn(w12, make_float2(q0.y, q1.y),
                                            make_float2(acc[j], acc[j + 1])));
@@ -631,20 +632,59 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
   if (ix >= A.W || iy >= A.W) return;
   const int vbeg = (int)((long long)A.nviews * vb / vblocks);
   const int vend = (int)((long long)A.nviews * (vb + 1) / vblocks);
+  const int nzo = MODE == 2 ? A.nzs : A.H;  // output slices
+  const bool cont = accumulate && vblocks == 1;
   float acc[ZC];
 #pragma unroll
   for (int j = 0; j < ZC; ++j) acc[j] = 0.f;
   if (in_circle(ix, iy, A.hw)) {
+    // Accumulating launches continue the stored sums view by view, so views
+    // split over several launches give the one-launch result bit for bit.
+    if (cont) {
+      const size_t sz = (size_t)A.W * A.W;
+      const TV* o = vol + (size_t)iy * A.W + ix + (size_t)z0 * sz;
+#pragma unroll
+      for (int j = 0; j < ZC; ++j)
+        if (z0 + j < nzo) acc[j] = ldp(o + (size_t)j * sz);
+    }
     const float x = (float)ix - ((float)A.hw + 0.5f);
     const float y = (float)iy - ((float)A.hw + 0.5f);
     if constexpr (IsQuad<TS>::value) {
-      // cone, quad-layout views (launch_bp_quad)
+      // quad-layout views: cone (launch_bp_quad, launch_bp_sub) or any
+      // geometry on a decoupled detector (launch_bp_det; v interpolated)
       using S = typename IsQuad<TS>::Storage;
       const auto* q = reinterpret_cast<const typename QuadT<S>::T*>(sino);
-      const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
+      if constexpr (MODE == 1) {
+        const size_t vstride = (size_t)Wp * (A.det_h + 2 * kSinoPad);
+        for (int v = vbeg; v < vend; ++v) {
+          const ColGeom<GEOM> g =
+              col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hwd, A.v0d, A.inv_du, A.inv_dv);
+          bp_column_quad<ZC, S, GEOM>(q + (size_t)v * vstride, A.det_w, A.det_h, Wp, z0, g, acc);
+        }
+      } else if constexpr (MODE == 2) {
+        const size_t vstride = (size_t)Wp * (A.nrows + 2 * kSinoPad);
+        for (int v = vbeg; v < vend; ++v) {
+          const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
+                                                 1.f, 1.f);
+          bp_column_quad<ZC, S, GEOM>(q + (size_t)v * vstride, A.W, A.nrows, Wp, A.zoff + z0, g,
+                                      acc, A.row0);
+        }
+      } else {
+        const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
+        for (int v = vbeg; v < vend; ++v) {
+          const ColGeom<2> g = col_geom<2>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f,
+                                           1.f);
+          bp_column_quad<ZC, S>(q + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+        }
+      }
+    } else if constexpr (std::is_same<TS, float2>::value && MODE == 2) {
+      // par / fan z-slab, pair-layout band of rows (launch_bp_sub)
+      const size_t vstride = (size_t)Wp * (A.nrows + 2 * kSinoPad);
       for (int v = vbeg; v < vend; ++v) {
-        const ColGeom<2> g = col_geom<2>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
-        bp_column_quad<ZC, S>(q + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
+                                               1.f, 1.f);
+        bp_column_pair<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.nrows, Wp, A.zoff + z0, g,
+                                 acc, A.row0);
       }
     } else if constexpr (std::is_same<TS, float2>::value) {
       // par / fan, FP32 pair-layout views (launch_bp_pair)
@@ -653,24 +693,6 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
         const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
                                                1.f, 1.f);
         bp_column_pair<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
-      }
-    } else if constexpr (MODE == 1) {
-      // decoupled detector (launch_bp_det): its own size, centre and pitch
-      const size_t vstride = (size_t)Wp * (A.det_h + 2 * kSinoPad);
-      for (int v = vbeg; v < vend; ++v) {
-        const ColGeom<GEOM> g =
-            col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hwd, A.v0d, A.inv_du, A.inv_dv);
-        bp_column_pad<GEOM, ZC, TS, false>(sino + (size_t)v * vstride, A.det_w, A.det_h, Wp, z0,
-                                           g, acc);
-      }
-    } else if constexpr (MODE == 2) {
-      // z-slab: voxel z = zoff + local z, taps in full-detector rows minus row0
-      const size_t vstride = (size_t)Wp * (A.nrows + 2 * kSinoPad);
-      for (int v = vbeg; v < vend; ++v) {
-        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
-                                               1.f, 1.f);
-        bp_column_pad<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.nrows, Wp, A.zoff + z0, g,
-                                acc, A.row0);
       }
     } else {
       const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
@@ -681,9 +703,12 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
       }
     }
   }
+  else if (cont) {
+    return;  // outside the circle: the stored sums stand
+  }
   const size_t base = (size_t)iy * A.W + ix;
   const size_t sz = (size_t)A.W * A.W;
-  const int nzo = MODE == 2 ? A.nzs : A.H;  // output slices
+  TV* const out = vol + base + (size_t)z0 * sz;
   if (vblocks > 1) {
     float* pp = part + (size_t)vb * sz * A.H + base;
 #pragma unroll
@@ -694,8 +719,7 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
 #pragma unroll
   for (int j = 0; j < ZC; ++j) {
     if (z0 + j < nzo) {
-      TV* o = vol + base + (size_t)(z0 + j) * sz;
-      stf(o, accumulate ? ldp(o) + acc[j] : acc[j]);
+      stf(out + (size_t)j * sz, acc[j]);
     }
   }
 }
@@ -821,55 +845,59 @@ cudaError_t launch_bp_pair(int geom, const VoxArgs& a, const float2* sino_pair, 
   return cudaErrorInvalidValue;
 }
 
-// Decoupled-detector BP: FP32 sinogram of det_w x det_h views padded with
-// sino_pad_pitch(det_w), one launch shape (8 z voxels per thread, 32 x 8
-// columns), every geometry interpolating in v.
-cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
+// Decoupled-detector BP: FP32 det_w x det_h views in the quad layout
+// (launch_pad_sino_quad), blocks of 32 x 4 columns, every geometry
+// interpolating in v.
+cudaError_t launch_bp_det(int geom, const VoxArgs& a, const void* sino_quad, float* vol,
                           bool accumulate, cudaStream_t st) {
   if (a.nviews <= 0) return cudaSuccess;
-  constexpr int ZC = 8;
+  // par / fan: a column's z taps are the same in every view and stay in
+  // registers across the view loop; 8 z voxels per thread keep that at ~100
+  // registers without spills
+  constexpr int ZC = 16, ZP = 8;
+  using Q = QuadLayout<float>;
   const int Wp = sino_pad_pitch(a.det_w);
-  const int nz = (a.H + ZC - 1) / ZC;
-  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, nz);
+  const int zc = geom == 2 ? ZC : ZP;
+  const int nz = (a.H + zc - 1) / zc;
+  dim3 blk(32, 4), grd((a.W + 31) / 32, (a.W + 3) / 4, nz);
   const int acc = accumulate ? 1 : 0;
+  const Q* sq = static_cast<const Q*>(sino_quad);
   switch (geom) {
     case 0:
-      bp_pad_kernel<0, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
-                                                                    nz, 1, nullptr, 0);
+      bp_pad_kernel<0, ZP, Q, float, 1><<<grd, blk, 0, st>>>(a, sq, Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     case 1:
-      bp_pad_kernel<1, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
-                                                                    nz, 1, nullptr, 0);
+      bp_pad_kernel<1, ZP, Q, float, 1><<<grd, blk, 0, st>>>(a, sq, Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     case 2:
-      bp_pad_kernel<2, ZC, float, float, 1><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc,
-                                                                    nz, 1, nullptr, 0);
+      bp_pad_kernel<2, ZC, Q, float, 1><<<grd, blk, 0, st>>>(a, sq, Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
+cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const void* sino_lay, float* vol,
                           bool accumulate, cudaStream_t st) {
   if (a.nviews <= 0) return cudaSuccess;
-  constexpr int ZC = 8;
+  constexpr int ZC = 16;
   const int Wp = sino_pad_pitch(a.W);
   const int nz = (a.nzs + ZC - 1) / ZC;
-  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, nz);
+  dim3 blk(32, 4), grd((a.W + 31) / 32, (a.W + 3) / 4, nz);
   const int acc = accumulate ? 1 : 0;
+  using Q = QuadLayout<float>;
   switch (geom) {
     case 0:
-      bp_pad_kernel<0, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
-                                                                 1, nullptr, 0);
+      bp_pad_kernel<0, ZC, float2, float, 2><<<grd, blk, 0, st>>>(
+          a, static_cast<const float2*>(sino_lay), Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     case 1:
-      bp_pad_kernel<1, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
-                                                                 1, nullptr, 0);
+      bp_pad_kernel<1, ZC, float2, float, 2><<<grd, blk, 0, st>>>(
+          a, static_cast<const float2*>(sino_lay), Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     case 2:
-      bp_pad_kernel<2, ZC, float, float, 2><<<grd, blk, 0, st>>>(a, sino_pad, Wp, vol, acc, nz,
-                                                                 1, nullptr, 0);
+      bp_pad_kernel<2, ZC, Q, float, 2><<<grd, blk, 0, st>>>(a, static_cast<const Q*>(sino_lay),
+                                                               Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     default: return cudaErrorInvalidValue;
   }

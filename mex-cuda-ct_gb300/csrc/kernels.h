@@ -188,15 +188,17 @@ cudaError_t launch_bp_pair(int geom, const VoxArgs& a, const float2* sino_pair, 
                            int vtype, bool accumulate, const BpShape& shp, float* part,
                            cudaStream_t st);
 
-// Decoupled-detector BP (FP32 padded sinogram of a.det_w x a.det_h views).
-cudaError_t launch_bp_det(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
+// Decoupled-detector BP from the quad layout (launch_pad_sino_quad, FP32) of
+// a.det_w x a.det_h views.
+cudaError_t launch_bp_det(int geom, const VoxArgs& a, const void* sino_quad, float* vol,
                           bool accumulate, cudaStream_t st);
 
 // Sub-volume BP: slices a.zoff .. a.zoff + a.nzs - 1 (a W x W x a.nzs FP32
-// slab) from a padded FP32 sinogram of detector rows a.row0 .. + a.nrows - 1
-// (which must hold every row the slab's columns reach: mexct_sub_rows).
-// Per voxel the same operations as launch_bp_padded with one view block.
-cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const float* sino_pad, float* vol,
+// slab) from detector rows a.row0 .. + a.nrows - 1 (which must hold every row
+// the slab's columns reach: mexct_sub_rows), laid out as quads (cone,
+// launch_pad_sino_quad) or pairs (par / fan, launch_pad_sino_pair) of the
+// band.  Per voxel the same operations as launch_bp_quad / launch_bp_pair.
+cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const void* sino_lay, float* vol,
                           bool accumulate, cudaStream_t st);
 
 // dst = w * src (first) or dst += w * src over n elements.

@@ -392,16 +392,16 @@ mexct_status bp_det_impl(mexct_ctx* c, const float* d_sino, const mexct_detector
   a->inv_dv = 1.0f / det->dv;
   a->P = (long long)Wd * Hd;
   const int chunk = std::min(nP, kMaxViews);
-  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(Wd, Hd, chunk) * sizeof(float), st),
+  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(Wd, Hd, chunk) * sizeof(float4), st),
                  "bp: workspace");
   for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
     a->nviews = std::min(kMaxViews, nP - v0);
     a->view0 = 0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-    MEXCT_TRY_CUDA(launch_pad_sino(d_sino + (size_t)v0 * a->P, kF32, Wd, Hd, a->nviews, false,
-                                   c->spad.p, st),
+    MEXCT_TRY_CUDA(launch_pad_sino_quad(d_sino + (size_t)v0 * a->P, kF32, Wd, Hd, a->nviews,
+                                        c->spad.p, st),
                    "bp: pad");
-    MEXCT_TRY_CUDA(launch_bp_det(geom, *a, c->spad.as<float>(), d_vol, v0 > 0, st),
+    MEXCT_TRY_CUDA(launch_bp_det(geom, *a, c->spad.p, d_vol, v0 > 0, st),
                    "bp: launch");
   }
   return MEXCT_OK;

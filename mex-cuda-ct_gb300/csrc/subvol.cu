@@ -36,16 +36,22 @@ namespace {
 
 bool bad_wh(int W, int H) { return W <= 0 || H <= 0 || W > 16384 || H > 16384; }
 
+// Bytes per padded texel of the BP layout: quads (cone) or pairs (par / fan).
+size_t lay_bytes(int geom) { return geom == 2 ? sizeof(float4) : sizeof(float2); }
+
 // Detector rows the BP of slab [z0, z0 + nz) reads, with one row of margin
 // each side (cone): pz(z) = (z - v0) U + v0 + 0.5 with U = SR / (SR - s) and
-// |s| <= R, R bounding every voxel column of the W x W slice.
+// |s| <= R.  BP reaches only the columns inside the circle of radius
+// hw = W/2 - 1 about texel (hw, hw) (CUDAmex_BP.cu:73-76), whose centres
+// (ix - hw - 0.5, iy - hw - 0.5) lie within hw + 0.71 of the axis; R = W/2 + 1
+// bounds them with margin.
 void rows_of(int W, int H, float sad, int geom, int z0, int nz, int* row0, int* nrows) {
   if (geom < 2) {
     *row0 = z0;
     *nrows = nz;
     return;
   }
-  const double R = std::sqrt(2.0) * (W / 2.0 + 1.0);
+  const double R = W / 2.0 + 1.0;
   const double SR = sad;
   if (!(SR > R)) {  // the source is inside the volume's cylinder: every row
     *row0 = 0;
@@ -127,10 +133,12 @@ mexct_status fp_sub_impl(mexct_ctx* c, const float* d_slab, int W, int H, int z0
 }
 
 // BP into slab [z0, z0 + nz) from detector rows [row0, row0 + nrows) of every
-// view (device array W x nrows x nP).
+// view (device array W x nrows x nP), laying out and back-projecting at most
+// pad_views views per launch (0: kMaxViews).  Each launch continues the
+// stored sums, so the chunking leaves the result bit for bit unchanged.
 mexct_status bp_sub_impl(mexct_ctx* c, const float* d_rows, int row0, int nrows, int W, int H,
                          int nP, float sad, const float* angles, int geom, int z0, int nz,
-                         float* d_slab, bool accumulate, cudaStream_t st) {
+                         float* d_slab, bool accumulate, cudaStream_t st, int pad_views = 0) {
   if (mexct_status s = check_slab("bp_sub", W, H, z0, nz, nP, geom)) return s;
   if (!d_slab || (nP > 0 && (!d_rows || !angles)))
     return set_err(MEXCT_ERR_ARG, "bp_sub: NULL pointer");
@@ -153,18 +161,20 @@ mexct_status bp_sub_impl(mexct_ctx* c, const float* d_rows, int row0, int nrows,
   a->nzs = nz;
   a->row0 = row0;
   a->nrows = nrows;
-  const int chunk = std::min(nP, kMaxViews);
-  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, nrows, chunk) * sizeof(float), st),
+  const int chunk = std::min(nP, pad_views > 0 ? std::min(pad_views, kMaxViews) : kMaxViews);
+  const bool quad = geom == 2;  // cone: quad layout; par / fan: pair layout
+  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, nrows, chunk) * lay_bytes(geom), st),
                  "bp_sub: workspace");
   const size_t Pr = (size_t)W * nrows;
-  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
-    a->nviews = std::min(kMaxViews, nP - v0);
+  for (int v0 = 0; v0 < nP; v0 += chunk) {
+    a->nviews = std::min(chunk, nP - v0);
     a->view0 = 0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-    MEXCT_TRY_CUDA(launch_pad_sino(d_rows + (size_t)v0 * Pr, kF32, W, nrows, a->nviews, false,
-                                   c->spad.p, st),
+    const float* rows = d_rows + (size_t)v0 * Pr;
+    MEXCT_TRY_CUDA(quad ? launch_pad_sino_quad(rows, kF32, W, nrows, a->nviews, c->spad.p, st)
+                        : launch_pad_sino_pair(rows, W, nrows, a->nviews, c->spad.as<float2>(), st),
                    "bp_sub: pad");
-    MEXCT_TRY_CUDA(launch_bp_sub(geom, *a, c->spad.as<float>(), d_slab, accumulate || v0 > 0, st),
+    MEXCT_TRY_CUDA(launch_bp_sub(geom, *a, c->spad.p, d_slab, accumulate || v0 > 0, st),
                    "bp_sub: launch");
   }
   return MEXCT_OK;
@@ -175,10 +185,15 @@ size_t fp_slab_bytes(int W, int nz) {
   return (size_t)W * W * nz * 4 + 2 * (size_t)slab_pitch(W) * (W + 2) * (nz + 2) * 4;
 }
 
-// Device bytes of a BP step: slab of nz slices, nv views of nr rows and their
-// padded copy.
-size_t bp_step_bytes(int W, int nz, int nr, int nv) {
-  return (size_t)W * W * nz * 4 + (size_t)W * nr * nv * 4 + sino_pad_elems(W, nr, nv) * 4;
+// Views laid out per BP launch of the out-of-core driver: the layout holds a
+// few views while the raw rows hold them all.
+constexpr int kOocPadViews = 32;
+
+// Device bytes of a BP step: slab of nz slices, nv views of nr rows and the
+// layout of up to kOocPadViews of them.
+size_t bp_step_bytes(int W, int nz, int nr, int nv, int geom) {
+  return (size_t)W * W * nz * 4 + (size_t)W * nr * nv * 4 +
+         sino_pad_elems(W, nr, std::min(nv, kOocPadViews)) * lay_bytes(geom);
 }
 
 // Widest row band over the slabs z0 = 0, nz, 2 nz, ... (the bands of the end
@@ -280,16 +295,16 @@ mexct_status mexct_bp_ooc(mexct_ctx* ctx, const float* sino, int W, int H, int n
   int nz = H;
   for (;;) {
     // the thickest slab that fits: bisect (the bytes grow with nz)
-    if (bp_step_bytes(W, nz, bp_rows_max(W, H, sad, geom, nz), nv) > budget_bytes) {
+    if (bp_step_bytes(W, nz, bp_rows_max(W, H, sad, geom, nz), nv, geom) > budget_bytes) {
       int lo = 1, hi = H;  // invariant: hi does not fit
       while (hi - lo > 1) {
         const int mid = lo + (hi - lo) / 2;
-        if (bp_step_bytes(W, mid, bp_rows_max(W, H, sad, geom, mid), nv) <= budget_bytes) lo = mid;
+        if (bp_step_bytes(W, mid, bp_rows_max(W, H, sad, geom, mid), nv, geom) <= budget_bytes) lo = mid;
         else hi = mid;
       }
       nz = lo;
     }
-    if (bp_step_bytes(W, nz, bp_rows_max(W, H, sad, geom, nz), nv) <= budget_bytes) break;
+    if (bp_step_bytes(W, nz, bp_rows_max(W, H, sad, geom, nz), nv, geom) <= budget_bytes) break;
     if (nv == 1)
       return set_err(MEXCT_ERR_BUDGET, "bp_ooc: %zu bytes hold no slab of %d x %d", budget_bytes,
                      W, W);
@@ -317,7 +332,7 @@ mexct_status mexct_bp_ooc(mexct_ctx* ctx, const float* sino, int W, int H, int n
                                        (size_t)W * nr * 4, n, cudaMemcpyHostToDevice, st),
                      "bp_ooc: upload");
       mexct_status s = bp_sub_impl(c, c->in.as<float>(), r0, nr, W, H, n, sad, angles + v0, geom,
-                                   z0, m, c->out.as<float>(), v0 > 0, st);
+                                   z0, m, c->out.as<float>(), v0 > 0, st, kOocPadViews);
       if (s) return s;
     }
     MEXCT_TRY_CUDA(cudaMemcpyAsync(vol + (size_t)z0 * W * W, c->out.p, (size_t)W * W * m * 4,

@@ -5,7 +5,8 @@ the volume's own faces), checked against the oracle on that masked volume; the
 slabs' FPs add up to the whole FP.  BP of a slab from the detector rows
 mexct_sub_rows names is the whole BP's slab bit for bit (fixed launch shape: one
 view block).  The out-of-core drivers with budgets that force several slabs and
-view chunks match the oracle at the 1e-5 bound.  mexct_sub_rows is checked on
+view chunks match the oracle at the 1e-5 bound, and the BP driver, whose view
+chunks continue the stored sums, matches the one-launch BP bit for bit.  mexct_sub_rows is checked on
 the CPU against every voxel column's taps.
 """
 import ctypes
@@ -150,6 +151,17 @@ def test_out_of_core_drivers_match_oracle(cuda, orc, geom, sad):
     assert rel_l2(fp, ref) <= TOL
     bp = ops.bp_ooc(ref.astype(np.float32), sad, ang, geom, 64 * 1024)
     assert rel_l2(bp, orc.bp(ref.astype(np.float32), sad, ang, geom)) <= TOL
+    # view chunks continue the stored sums: bit for bit the one-launch BP
+    import torch
+    from mexct import tune
+    ds = torch.from_numpy(np.ascontiguousarray(ref.astype(np.float32).transpose(2, 1, 0))).cuda()
+    tune.clear()
+    tune.set_mode(tune.FIXED)
+    try:
+        full = ops.bp_dev(ds, sad, ang, geom).cpu().numpy().transpose(2, 1, 0)
+    finally:
+        tune.set_mode(tune.HEURISTIC)
+    assert np.array_equal(bp, full)
     # a budget without room for one slice and one view
     from mexct import _lib
     with pytest.raises(_lib.MexctError) as ei:
