@@ -244,7 +244,9 @@ mexct_status mexct_bp_det_dev(mexct_ctx* ctx, const float* d_sino,
  * nrows - 1 of every view (device array W x nrows x nP; the rows must hold
  * those mexct_sub_rows names); each voxel gets the operations of the
  * whole-volume BP, so the slabs of a volume are its BP (with one view block,
- * MEXCT_TUNE_FIXED, bit for bit). */
+ * MEXCT_TUNE_FIXED, bit for bit).  accumulate != 0 continues the sums stored
+ * in d_slab view by view, so the BPs of consecutive view chunks of a
+ * sinogram accumulate to its one-call BP bit for bit. */
 mexct_status mexct_sub_rows(int W, int H, float sad, int geom, int z0, int nz,
                             int* row0, int* nrows);
 mexct_status mexct_fp_sub_dev(mexct_ctx* ctx, const float* d_slab, int W, int H,
