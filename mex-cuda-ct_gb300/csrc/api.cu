@@ -266,6 +266,8 @@ mexct_status mexct_ctx_destroy(mexct_ctx* c) {
     cudaStreamSynchronize(c->copy_stream);
     for (cudaEvent_t ev : c->chunk_ev)
       if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : c->feed_ev)
+      if (ev) cudaEventDestroy(ev);
     cudaStreamDestroy(c->copy_stream);
   }
   cudaStreamDestroy(c->stream);

@@ -66,6 +66,7 @@ struct mexct_ctx {
   // still running on `stream` (created on first use), and one event per chunk.
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t chunk_ev[8] = {};
+  cudaEvent_t feed_ev[4] = {};  // uploads of the host BP's view parts
   std::recursive_mutex mu;           // serialises calls on this context
   // Host entry points: staged inputs / outputs.
   mexct::Buf in, in2, in3, out;
@@ -162,9 +163,15 @@ struct ChunkHook {
 mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float sad,
                     const float* angles, int nP, int geom, void* d_out, int ot, int variant,
                     cudaStream_t st, const ChunkHook* hook = nullptr);
+// feed (BP, quad / pair layouts, one view chunk and one view block): the views
+// arrive in feed->chunks parts; feed->fn(i, first, count) is called before the
+// work on views first .. first + count - 1 and makes `st` wait for them.  Each
+// part's launch continues the stored sums, so the result is bit-identical to
+// one launch; `hook` then splits the last part's launch by z.
 mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, int nP, float sad,
                     const float* angles, int geom, void* d_vol, int vt, const BpShape& shp,
-                    cudaStream_t st, const ChunkHook* hook = nullptr);
+                    cudaStream_t st, const ChunkHook* hook = nullptr,
+                    const ChunkHook* feed = nullptr);
 // Shape of a call's class from the context's table, its mode's default, or
 // (MEXCT_TUNE_AUTO, outside stream capture) by timing the candidates on the
 // call's own buffers (tune.cu).

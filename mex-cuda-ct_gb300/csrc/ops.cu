@@ -176,7 +176,7 @@ mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float
 // padded copy (clamp frame) in chunks of kMaxViews.
 mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, int nP, float sad,
                     const float* angles, int geom, void* d_vol, int vt, const BpShape& shp,
-                    cudaStream_t st, const ChunkHook* hook) {
+                    cudaStream_t st, const ChunkHook* hook, const ChunkHook* feed) {
   std::unique_ptr<VoxArgs> a(new VoxArgs);
   fill_vox(*a, W, H, sad);
   if (nP == 0) {
@@ -194,57 +194,64 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
   if (shp.vblocks > 1)
     MEXCT_TRY_CUDA(c->bpart.ensure_async(N * shp.vblocks * sizeof(float), st), "bp: workspace");
   const size_t P = (size_t)W * H;
+  const size_t vpad = sino_pad_elems(W, H, 1) * es;  // bytes of one laid-out view
+  // one view chunk and one view block: the z split (hook) and the view parts
+  // (feed) keep each voxel's operations those of one launch
+  const bool single = nP <= kMaxViews && shp.vblocks == 1 && (quad || pair);
+  const bool zsplit = hook && single;
+  const int nparts = feed && single ? std::min(4, std::max(1, feed->chunks)) : 1;
   for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
-    a->nviews = std::min(kMaxViews, nP - v0);
-    a->view0 = 0;
-    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-    const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
-    // z ranges of the volume in hook->chunks launches (one view chunk, one
-    // view block: the per-voxel operations are those of one launch)
-    const bool zsplit = hook && nP <= kMaxViews && shp.vblocks == 1 && (quad || pair);
-    const int nzb = (H + shp.zc - 1) / shp.zc;
-    const int zstep = zsplit ? (nzb + hook->chunks - 1) / hook->chunks : nzb;
-    if (quad) {
-      MEXCT_TRY_CUDA(launch_pad_sino_quad(src, stype, W, H, a->nviews, c->spad.p, st), "bp: pad");
-      for (int zb = 0, ci = 0; zb < nzb; zb += zstep, ++ci) {
-        BpShape sh = shp;
-        sh.zb0 = zb;
-        sh.nzb = zsplit ? zstep : 0;
-        MEXCT_TRY_CUDA(launch_bp_quad(*a, c->spad.p, stype, d_vol, vt, v0 > 0, sh,
+    const int nv = std::min(kMaxViews, nP - v0);
+    if (!quad && !pair) {
+      a->nviews = nv;
+      a->view0 = 0;
+      for (int i = 0; i < nv; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+      const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
+      MEXCT_TRY_CUDA(launch_pad_sino(src, stype, W, H, nv, false, c->spad.p, st), "bp: pad");
+      MEXCT_TRY_CUDA(launch_bp_padded(geom, *a, c->spad.p, stype, d_vol, vt, v0 > 0, shp,
                                       c->bpart.as<float>(), st),
-                       "bp: launch");
-        if (zsplit) {
-          const int z0 = zb * shp.zc;
-          if (mexct_status s2 = hook->fn(ci, z0, std::min(H, z0 + zstep * shp.zc) - z0))
-            return s2;
-        }
-      }
+                     "bp: launch");
       continue;
     }
-    if (pair) {
-      MEXCT_TRY_CUDA(launch_pad_sino_pair(static_cast<const float*>(static_cast<const void*>(src)),
-                                          W, H, a->nviews, c->spad.as<float2>(), st),
+    for (int part = 0; part < nparts; ++part) {
+      // parts of 1/16, 3/16, 1/4 and 1/2 of the views: the first, whose
+      // upload nothing hides, is small
+      static const int kEnd[4] = {1, 4, 8, 16};
+      const int s0 = part == 0 ? 0 : (int)((long long)nv * kEnd[part - 1] / 16);
+      const int s1 = nparts == 1 || part == nparts - 1 ? nv : (int)((long long)nv * kEnd[part] / 16);
+      if (s1 <= s0) continue;
+      if (nparts > 1)
+        if (mexct_status s2 = feed->fn(part, v0 + s0, s1 - s0)) return s2;
+      a->nviews = s1 - s0;
+      a->view0 = 0;
+      for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + s0 + i], &a->trig[i]);
+      const char* src = static_cast<const char*>(d_sino) + (size_t)(v0 + s0) * P * dsize(stype);
+      void* lay = static_cast<char*>(c->spad.p) + (size_t)s0 * vpad;
+      MEXCT_TRY_CUDA(quad ? launch_pad_sino_quad(src, stype, W, H, a->nviews, lay, st)
+                          : launch_pad_sino_pair(reinterpret_cast<const float*>(src), W, H,
+                                                 a->nviews, static_cast<float2*>(lay), st),
                      "bp: pad");
+      // z ranges of the volume in hook->chunks launches for the last part
+      const bool zs = zsplit && part == nparts - 1;
+      const int nzb = (H + shp.zc - 1) / shp.zc;
+      const int zstep = zs ? (nzb + hook->chunks - 1) / hook->chunks : nzb;
+      const bool accum = v0 > 0 || s0 > 0;
       for (int zb = 0, ci = 0; zb < nzb; zb += zstep, ++ci) {
         BpShape sh = shp;
         sh.zb0 = zb;
-        sh.nzb = zsplit ? zstep : 0;
-        MEXCT_TRY_CUDA(launch_bp_pair(geom, *a, c->spad.as<float2>(), d_vol, vt, v0 > 0, sh,
-                                      c->bpart.as<float>(), st),
+        sh.nzb = zs ? zstep : 0;
+        MEXCT_TRY_CUDA(quad ? launch_bp_quad(*a, lay, stype, d_vol, vt, accum, sh,
+                                             c->bpart.as<float>(), st)
+                            : launch_bp_pair(geom, *a, static_cast<const float2*>(lay), d_vol,
+                                             vt, accum, sh, c->bpart.as<float>(), st),
                        "bp: launch");
-        if (zsplit) {
+        if (zs) {
           const int z0 = zb * shp.zc;
           if (mexct_status s2 = hook->fn(ci, z0, std::min(H, z0 + zstep * shp.zc) - z0))
             return s2;
         }
       }
-      continue;
     }
-    MEXCT_TRY_CUDA(launch_pad_sino(src, stype, W, H, a->nviews, false, c->spad.p, st),
-                   "bp: pad");
-    MEXCT_TRY_CUDA(launch_bp_padded(geom, *a, c->spad.p, stype, d_vol, vt, v0 > 0, shp,
-                                    c->bpart.as<float>(), st),
-                   "bp: launch");
   }
   return MEXCT_OK;
 }
@@ -758,6 +765,10 @@ cudaError_t copy_stream(mexct_ctx* c, cudaStream_t* out) {
       e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
       if (e != cudaSuccess) return e;
     }
+    for (cudaEvent_t& ev : c->feed_ev) {
+      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e != cudaSuccess) return e;
+    }
   }
   *out = c->copy_stream;
   return cudaSuccess;
@@ -804,11 +815,31 @@ mexct_status fp_host_overlapped(mexct_ctx* c, int W, int H, float sad, const flo
   return cc.run(c, cs, out, c->out.p, "fp: download");
 }
 
-mexct_status bp_host_overlapped(mexct_ctx* c, int W, int H, int nP, float sad,
+// Host BP with the views uploaded in four parts on the copy stream, each
+// part's BP starting once its views have landed (the later uploads overlap
+// the earlier parts' launches), and the volume's z ranges downloaded as the
+// last part's launches finish.  Bit-identical to one launch.
+mexct_status bp_host_overlapped(mexct_ctx* c, const float* sino, int W, int H, int nP, float sad,
                                 const float* angles, int geom, const BpShape& shp, float* vol) {
   cudaStream_t cs;
   MEXCT_TRY_CUDA(copy_stream(c, &cs), "bp: copy stream");
-  const size_t slice = (size_t)W * W * 4;
+  const size_t slice = (size_t)W * W * 4, P = (size_t)W * H;
+  // the copy stream writes c->in only after the launch stream's earlier work
+  MEXCT_TRY_CUDA(cudaEventRecord(c->feed_ev[0], c->stream), "bp: event");
+  MEXCT_TRY_CUDA(cudaStreamWaitEvent(cs, c->feed_ev[0], 0), "bp: event");
+  int fed = 0;
+  ChunkHook feed{4, [&](int i, int first, int count) -> mexct_status {
+                   if (i >= 4) return set_err(MEXCT_ERR_ARG, "bp: too many view parts");
+                   MEXCT_TRY_CUDA(cudaMemcpyAsync(c->in.as<float>() + (size_t)first * P,
+                                                  sino + (size_t)first * P,
+                                                  (size_t)count * P * 4, cudaMemcpyHostToDevice,
+                                                  cs),
+                                  "bp: upload");
+                   MEXCT_TRY_CUDA(cudaEventRecord(c->feed_ev[i], cs), "bp: event");
+                   MEXCT_TRY_CUDA(cudaStreamWaitEvent(c->stream, c->feed_ev[i], 0), "bp: event");
+                   fed += count;
+                   return MEXCT_OK;
+                 }};
   ChunkCopies cc;
   ChunkHook hook{kHostChunks, [&](int i, int z0, int nz) -> mexct_status {
                    if (i >= kHostChunks) return set_err(MEXCT_ERR_ARG, "bp: too many chunks");
@@ -817,12 +848,14 @@ mexct_status bp_host_overlapped(mexct_ctx* c, int W, int H, int nP, float sad,
                    return MEXCT_OK;
                  }};
   mexct_status s = bp_run(c, c->in.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, shp,
-                          c->stream, &hook);
+                          c->stream, &hook, &feed);
   if (s) return s;
+  if (fed != nP) return set_err(MEXCT_ERR_ARG, "bp: %d of %d views uploaded", fed, nP);
   if (cc.items.empty()) {  // the shape ran as one launch: plain download
     MEXCT_TRY_CUDA(cudaMemcpyAsync(vol, c->out.p, slice * H, cudaMemcpyDeviceToHost, c->stream),
                    "bp: download");
     MEXCT_TRY_CUDA(cudaStreamSynchronize(c->stream), "bp: download");
+    MEXCT_TRY_CUDA(cudaStreamSynchronize(cs), "bp: upload");
     return MEXCT_OK;
   }
   return cc.run(c, cs, vol, c->out.p, "bp: download");
@@ -948,20 +981,24 @@ mexct_status mexct_bp(mexct_ctx* ctx, const float* sino, int W, int H, int nP,
   VALIDATE(bp_dev_impl(nullptr, sino, kF32, W, H, nP, sad, angles, geom, vol, kF32, nullptr));
   CTX_OR_FAIL(c, "bp");
   const size_t N = (size_t)W * W * H, M = (size_t)W * H * nP;
-  mexct_status s = upload(c->in, sino, M * 4, c->stream, "bp: upload");
-  if (s) return s;
+  MEXCT_TRY_CUDA(c->in.ensure_async(M * 4, c->stream), "bp: workspace");
   MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "bp: workspace");
+  mexct_status s = MEXCT_OK;
   if (nP > 0 && nP <= kMaxViews && N * 4 >= ((size_t)64 << 20)) {
-    // z ranges in turn, each range's download overlapping the launches after
-    // it (same per-voxel operations as one launch), when one view block is used
+    // views uploaded in parts under the launches, z ranges downloaded under
+    // the launches after them (same per-voxel operations as one launch), when
+    // one view block is used.  A tuning run (MEXCT_TUNE_AUTO) times its
+    // candidates before the views are uploaded: only its timings are used.
     mexct_shape shp{MEXCT_FP_EXPLICIT, 16, 8, 1};
     s = pick_bp_shape(c, c->in.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, c->stream,
                       &shp);
     if (s) return s;
     if (shp.vblocks == 1)
-      return bp_host_overlapped(c, W, H, nP, sad, angles, geom, BpShape{shp.zc, shp.rows, 1},
-                                vol);
+      return bp_host_overlapped(c, sino, W, H, nP, sad, angles, geom,
+                                BpShape{shp.zc, shp.rows, 1}, vol);
   }
+  s = upload(c->in, sino, M * 4, c->stream, "bp: upload");
+  if (s) return s;
   s = bp_dev_impl(c, c->in.p, kF32, W, H, nP, sad, angles, geom, c->out.p, kF32, c->stream);
   if (s) return s;
   return finish(c, vol, c->out, N * 4, "bp: download");

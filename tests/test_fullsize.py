@@ -77,6 +77,28 @@ def test_headline_scaling_and_additivity(headline):
 
 
 @pytest.mark.parametrize("geom", [0, 2])
+def test_host_entry_points_pipelined_copies(cuda, geom):
+    """256^3 (the size from which the host entry points overlap their copies):
+    FP downloads by view chunks, BP uploads in view parts and downloads by z
+    ranges; both bit-identical to the device entry points."""
+    import torch
+    import mexct
+    from mexct import ops, phantoms
+
+    W, nP = 256, 90
+    vol = phantoms.ellipsoids(W, count=6, seed=9, nz=W)
+    ang = phantoms.angles_full(nP)
+    d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    fp = mexct.CUDAmex_FP(vol, 1000.0, ang, nP, geom)
+    fd = ops.fp_dev(d, 1000.0, ang, geom)
+    assert np.array_equal(fp, fd.cpu().numpy().transpose(2, 1, 0))
+    bp = mexct.CUDAmex_BP(fp, 1000.0, ang, geom)
+    bd = ops.bp_dev(fd, 1000.0, ang, geom)
+    torch.cuda.synchronize()
+    assert np.array_equal(bp, bd.cpu().numpy().transpose(2, 1, 0))
+
+
+@pytest.mark.parametrize("geom", [0, 2])
 def test_more_views_than_one_launch(cuda, orc, geom):
     """2100 views: the entry points split them into launches of at most 2048."""
     import mexct
