@@ -385,11 +385,12 @@ cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews,
 }
 
 // Quad layout of the clamp-padded views (cone BP): padded texel (r, c) of
-// view v -> {P(r,c), P(r,c+1), P(r+1,c), P(r+1,c+1)} with P(r, c) = the view's
-// pixel (clamp(c - kSinoPad), clamp(r - kSinoPad)), as in pad_sino_kernel.
-// FP32 views: a float4 per texel; FP16 / BF16 views: the four 16-bit values
-// in a uint2 (x: P(r,c) | P(r,c+1) << 16, y: the next row), read and
-// converted exactly as the gather form reads them.
+// view v -> {P(r,c), P(r+1,c), P(r,c+1), P(r+1,c+1)} (column c's two rows,
+// then column c+1's) with P(r, c) = the view's pixel (clamp(c - kSinoPad),
+// clamp(r - kSinoPad)), as in pad_sino_kernel.  FP32 views: a float4 per
+// texel; FP16 / BF16 views: the four 16-bit values in a uint2 (x: P(r,c) |
+// P(r+1,c) << 16, y: column c+1), read and converted exactly as the gather
+// form reads them.
 template <typename S> struct QuadT;
 template <> struct QuadT<float> {
   using T = float4;
@@ -443,8 +444,8 @@ __global__ void __launch_bounds__(256) pad_sino_quad_kernel(const S* __restrict_
   const int x0 = min(max(c - kSinoPad, 0), W - 1), x1 = min(max(c + 1 - kSinoPad, 0), W - 1);
   const int y0 = min(max(r - kSinoPad, 0), H - 1), y1 = min(max(r + 1 - kSinoPad, 0), H - 1);
   out[((size_t)v * Hp + r) * Wp + c] =
-      QuadT<S>::make(view[(size_t)y0 * W + x0], view[(size_t)y0 * W + x1],
-                     view[(size_t)y1 * W + x0], view[(size_t)y1 * W + x1]);
+      QuadT<S>::make(view[(size_t)y0 * W + x0], view[(size_t)y1 * W + x0],
+                     view[(size_t)y0 * W + x1], view[(size_t)y1 * W + x1]);
 }
 
 // Pair layout of the clamp-padded views (par / fan BP, FP32): padded texel
@@ -546,8 +547,9 @@ __device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, i
 }
 
 // Cone column over a quad-layout view (launch_pad_sino_quad): texel (r, c)
-// holds the bilinear footprint {P(r,c), P(r,c+1), P(r+1,c), P(r+1,c+1)} of
-// the padded view P, so each voxel's four taps are one 16-byte load.  The
+// holds the bilinear footprint {P(r,c), P(r+1,c), P(r,c+1), P(r+1,c+1)} of
+// the padded view P, so each voxel's four taps are one 16-byte load whose
+// halves (columns c and c+1) feed the packed u lerps of both rows.  The
 // arithmetic is bp_column_pad's (GEOM 2), operation for operation.
 template <int ZC, typename S = float, int GEOM = 2>
 __device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __restrict__ p, int W,
@@ -573,12 +575,13 @@ __device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __res
     const int i1 = min(max(__float2int_rz(fz.y) - roff, -kSinoPad), H) + kSinoPad;
     const float4 q0 = QuadT<S>::get(col + (size_t)i0 * Wp);
     const float4 q1 = QuadT<S>::get(col + (size_t)i1 * Wp);
-    const float2 a = __ffma2_rn(w02, make_float2(q0.x, q1.x), __fmul2_rn(w12, make_float2(q0.y, q1.y)));
-    const float2 b = __ffma2_rn(w02, make_float2(q0.z, q1.z), __fmul2_rn(w12, make_float2(q0.w, q1.w)));
+    // (a, b) of one voxel: the u lerps of rows r and r+1, one packed pair of
+    // operations on the quad's two halves (columns c and c+1)
+    const float2 ab0 = __ffma2_rn(w02, make_float2(q0.x, q0.y), __fmul2_rn(w12, make_float2(q0.z, q0.w)));
+    const float2 ab1 = __ffma2_rn(w02, make_float2(q1.x, q1.y), __fmul2_rn(w12, make_float2(q1.z, q1.w)));
     const float2 omaz = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-az.x, -az.y));
-    const float2 t = __ffma2_rn(omaz, a, __ffma2_rn(az, b, make_float2(acc[j], acc[j + 1])));
-    acc[j] = t.x;
-    acc[j + 1] = t.y;
+    acc[j] = fmaf(omaz.x, ab0.x, fmaf(az.x, ab0.y, acc[j]));
+    acc[j + 1] = fmaf(omaz.y, ab1.x, fmaf(az.y, ab1.y, acc[j + 1]));
   }
 }
 

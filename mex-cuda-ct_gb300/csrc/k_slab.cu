@@ -877,9 +877,9 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       const float r0 = ehat - qv, r1 = ehat * l;
       if (GEOM == 2) {
         // cone: quad layout (the dual BP's one 16-byte load per voxel): the
-        // padded texel P(r, c) is component x of quad (r, c), y of (r, c-1),
-        // z of (r-1, c) and w of (r-1, c-1)
-        const size_t q[4] = {4 * ri, 4 * (ri - 1) + 1, 4 * (ri - Wp) + 2, 4 * (ri - Wp - 1) + 3};
+        // padded texel P(r, c) is component x of quad (r, c), y of (r-1, c),
+        // z of (r, c-1) and w of (r-1, c-1)
+        const size_t q[4] = {4 * ri, 4 * (ri - Wp) + 1, 4 * (ri - 1) + 2, 4 * (ri - Wp - 1) + 3};
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
           E.rpre[q[t]] = r0;
