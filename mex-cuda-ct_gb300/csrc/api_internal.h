@@ -163,7 +163,7 @@ struct ChunkHook {
 mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float sad,
                     const float* angles, int nP, int geom, void* d_out, int ot, int variant,
                     cudaStream_t st, const ChunkHook* hook = nullptr);
-// feed (BP, quad / pair layouts, one view chunk and one view block): the views
+// feed (BP, one view chunk and one view block): the views
 // arrive in feed->chunks parts; feed->fn(i, first, count) is called before the
 // work on views first .. first + count - 1 and makes `st` wait for them.  Each
 // part's launch continues the stored sums, so the result is bit-identical to

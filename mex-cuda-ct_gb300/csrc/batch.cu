@@ -24,7 +24,7 @@ struct mexct_batch {
   int device = 0;
   int n = 0;
   std::vector<Buf> pads;   // 2 per problem: padded volume, both layouts
-  std::vector<Buf> spads;  // 1 per problem: padded sinogram for BP (quad / pair layout)
+  std::vector<Buf> spads;  // 1 per problem: the BP views in the quad layout
   std::vector<mexct_problem> probs;
   // BP launch arguments per problem and view chunk (at most kMaxViews views)
   std::vector<std::vector<std::unique_ptr<VoxArgs>>> vox;
@@ -127,10 +127,9 @@ mexct_status mexct_batch_create(mexct_ctx* ctx, const mexct_problem* probs, int 
     f.pad_item0 = b->pad_items;
     const long long nt = (Pf + 31) / 32;
     b->pad_items += nt * nt * (H + 2);
-    // BP: views in the quad (cone) or pair (par / fan) layout, one launch per
-    // kMaxViews views (mexct_bp_dev's shapes without view blocks)
-    MEXCT_TRY_CUDA(b->spads[i].ensure(sino_pad_elems(W, H, p.nP) *
-                                      (p.geom == 2 ? sizeof(float4) : sizeof(float2))),
+    // BP: views in the quad layout, one launch per kMaxViews views
+    // (mexct_bp_dev's shapes without view blocks)
+    MEXCT_TRY_CUDA(b->spads[i].ensure(sino_pad_elems(W, H, p.nP) * sizeof(float4)),
                    "batch_create: padded sinogram");
     for (int v0 = 0; v0 < p.nP; v0 += kMaxViews) {
       std::unique_ptr<VoxArgs> va(new VoxArgs);
@@ -181,19 +180,15 @@ mexct_status mexct_batch_bp(mexct_batch* b, void* stream) {
   for (int i = 0; i < b->n; ++i) {
     const mexct_problem& p = b->probs[i];
     cudaStream_t s = b->aux[i % mexct_batch::kAux];
-    const bool quad = p.geom == 2;
-    MEXCT_TRY_CUDA(quad ? launch_pad_sino_quad(p.d_sino, kF32, p.W, p.H, p.nP, b->spads[i].p, s)
-                        : launch_pad_sino_pair(p.d_sino, p.W, p.H, p.nP,
-                                               b->spads[i].as<float2>(), s),
+    MEXCT_TRY_CUDA(launch_pad_sino_quad(p.d_sino, kF32, p.W, p.H, p.nP, b->spads[i].p, s),
                    "batch_bp: padding");
-    const size_t vstride = sino_pad_elems(p.W, p.H, 1) * (quad ? sizeof(float4) : sizeof(float2));
+    const size_t vstride = sino_pad_elems(p.W, p.H, 1) * sizeof(float4);
     const BpShape shp{16, 8, 1};
     int v0 = 0;
     for (const auto& va : b->vox[i]) {
       const char* src = static_cast<const char*>(b->spads[i].p) + (size_t)v0 * vstride;
-      MEXCT_TRY_CUDA(quad ? launch_bp_quad(*va, src, kF32, p.d_rec, kF32, v0 > 0, shp, nullptr, s)
-                          : launch_bp_pair(p.geom, *va, reinterpret_cast<const float2*>(src),
-                                           p.d_rec, kF32, v0 > 0, shp, nullptr, s),
+      MEXCT_TRY_CUDA(launch_bp_quad(p.geom, *va, src, kF32, p.d_rec, kF32, v0 > 0, shp, nullptr,
+                                    s),
                      "batch_bp: launch");
       v0 += va->nviews;
     }

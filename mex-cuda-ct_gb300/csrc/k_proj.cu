@@ -335,62 +335,27 @@ __device__ __forceinline__ void bp_column(const TS* __restrict__ p, int W,
   }
 }
 
-// ---------------------------------------------------------------------------
-// Backprojection from a padded sinogram.  Each view is copied once into
-// [H+4][W+4] with two extra rows and columns on every side: the edge value
-// replicated (clamp addressing) or zeros (border addressing).  A tap index
-// then only needs clamping into [-2, n] -- both taps of an index outside the
-// image read pad values, which is what the clamp / border texture fetch
-// returns -- instead of clamping both taps of both axes into the image.
-// ---------------------------------------------------------------------------
-template <typename T, bool BORDER>
-__global__ void __launch_bounds__(256) pad_sino_kernel(const T* __restrict__ in, int W, int H,
-                                                       T* __restrict__ out, int Wp) {
-  const int x = blockIdx.x * 32 + threadIdx.x - kSinoPad;
-  const int y = blockIdx.y * 8 + threadIdx.y - kSinoPad;
-  const int Hp = H + 2 * kSinoPad;
-  if (x >= W + kSinoPad || y >= H + kSinoPad) return;
-  const size_t v = blockIdx.z;
-  T val;
-  if (BORDER && (x < 0 || x >= W || y < 0 || y >= H)) {
-    val = T(0.0f);
-  } else {
-    const int cx = min(max(x, 0), W - 1), cy = min(max(y, 0), H - 1);
-    val = in[(v * H + cy) * W + cx];
-  }
-  out[(v * Hp + (y + kSinoPad)) * Wp + (x + kSinoPad)] = val;
-}
 
+// ---------------------------------------------------------------------------
+// Backprojection from padded views.  Each view is laid out once in [H+4][W+4]
+// texels with two extra rows and columns on every side holding the edge
+// values (clamp addressing; the OSC residual views keep a zero frame, border
+// addressing).  A tap index then only needs clamping into [-2, n] -- both
+// taps of an index outside the image read frame values, which is what the
+// clamp / border texture fetch returns -- instead of clamping both taps of
+// both axes into the image.
+// ---------------------------------------------------------------------------
 size_t sino_pad_elems(int W, int H, int nviews) {
   return (size_t)sino_pad_pitch(W) * (H + 2 * kSinoPad) * nviews;
 }
 
-cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews, bool border,
-                            void* out, cudaStream_t st) {
-  if (nviews <= 0) return cudaSuccess;
-  const int Wp = sino_pad_pitch(W);
-  dim3 blk(32, 8), grd((W + 2 * kSinoPad + 31) / 32, (H + 2 * kSinoPad + 7) / 8, nviews);
-#define PAD_SINO(T)                                                                       \
-  do {                                                                                    \
-    if (border)                                                                           \
-      pad_sino_kernel<T, true><<<grd, blk, 0, st>>>((const T*)in, W, H, (T*)out, Wp);   \
-    else                                                                                  \
-      pad_sino_kernel<T, false><<<grd, blk, 0, st>>>((const T*)in, W, H, (T*)out, Wp);  \
-  } while (0)
-  if (dtype == kF32) PAD_SINO(float);
-  else if (dtype == kF16) PAD_SINO(__half);
-  else PAD_SINO(__nv_bfloat16);
-#undef PAD_SINO
-  return cudaGetLastError();
-}
-
-// Quad layout of the clamp-padded views (cone BP): padded texel (r, c) of
+// Quad layout of the clamp-padded views (every BP): padded texel (r, c) of
 // view v -> {P(r,c), P(r+1,c), P(r,c+1), P(r+1,c+1)} (column c's two rows,
 // then column c+1's) with P(r, c) = the view's pixel (clamp(c - kSinoPad),
-// clamp(r - kSinoPad)), as in pad_sino_kernel.  FP32 views: a float4 per
+// clamp(r - kSinoPad)) (the clamp texture fetch's frame).  FP32 views: a float4 per
 // texel; FP16 / BF16 views: the four 16-bit values in a uint2 (x: P(r,c) |
-// P(r+1,c) << 16, y: column c+1), read and converted exactly as the gather
-// form reads them.
+// P(r+1,c) << 16, y: column c+1), converted to FP32 exactly as a 16-bit
+// load is.
 template <typename S> struct QuadT;
 template <> struct QuadT<float> {
   using T = float4;
@@ -446,30 +411,6 @@ __global__ void __launch_bounds__(256) pad_sino_quad_kernel(const S* __restrict_
   out[((size_t)v * Hp + r) * Wp + c] =
       QuadT<S>::make(view[(size_t)y0 * W + x0], view[(size_t)y1 * W + x0],
                      view[(size_t)y0 * W + x1], view[(size_t)y1 * W + x1]);
-}
-
-// Pair layout of the clamp-padded views (par / fan BP, FP32): padded texel
-// (r, c) -> {P(r,c), P(r,c+1)}.
-__global__ void __launch_bounds__(256) pad_sino_pair_kernel(const float* __restrict__ in, int W,
-                                                            int H, float2* __restrict__ out,
-                                                            int Wp) {
-  const int c = blockIdx.x * 32 + threadIdx.x;
-  const int r = blockIdx.y * 8 + threadIdx.y;
-  const int v = blockIdx.z;
-  const int Hp = H + 2 * kSinoPad;
-  if (c >= Wp || r >= Hp) return;
-  const float* row = in + ((size_t)v * H + min(max(r - kSinoPad, 0), H - 1)) * W;
-  const int x0 = min(max(c - kSinoPad, 0), W - 1), x1 = min(max(c + 1 - kSinoPad, 0), W - 1);
-  out[((size_t)v * Hp + r) * Wp + c] = make_float2(__ldg(row + x0), __ldg(row + x1));
-}
-
-cudaError_t launch_pad_sino_pair(const float* in, int W, int H, int nviews, float2* out,
-                                 cudaStream_t st) {
-  if (nviews <= 0) return cudaSuccess;
-  const int Wp = sino_pad_pitch(W);
-  dim3 blk(32, 8), grd((Wp + 31) / 32, (H + 2 * kSinoPad + 7) / 8, nviews);
-  pad_sino_pair_kernel<<<grd, blk, 0, st>>>(in, W, H, out, Wp);
-  return cudaGetLastError();
 }
 
 cudaError_t launch_pad_sino_quad(const void* in, int stype, int W, int H, int nviews, void* out,
@@ -585,27 +526,29 @@ __device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __res
   }
 }
 
-// Par / fan column over a pair-layout view (launch_pad_sino_pair): texel
-// (r, c) holds {P(r,c), P(r,c+1)}, so each voxel's two taps (its z row is a
-// texel row) are one 8-byte load.  bp_column_pad's arithmetic (ROWS path).
-template <int GEOM, int ZC>
-__device__ __forceinline__ void bp_column_pair(const float2* __restrict__ p, int W, int H, int Wp,
-                                               int z0, const ColGeom<GEOM>& g, float* acc,
-                                               int roff = 0) {
+// Par / fan column over a quad-layout view: the column's z rows are texel
+// rows, so the quad at row r holds column c's rows r and r+1 and column c+1's,
+// i.e. both voxels of a z pair as register pairs: one 16-byte load and two
+// packed operations per pair.  bp_column_pad's arithmetic (ROWS path); row r+1
+// is clamped by the layout exactly as min(z + 1, H - 1) clamps it.
+template <int GEOM, int ZC, typename S = float>
+__device__ __forceinline__ void bp_column_quadrows(const typename QuadT<S>::T* __restrict__ p,
+                                                   int W, int H, int Wp, int z0,
+                                                   const ColGeom<GEOM>& g, float* acc,
+                                                   int roff = 0) {
   const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
   const float fu = floorf(cu);
   const float au = cu - fu;
   const int iu = min(max((int)fu, -kSinoPad), W) + kSinoPad;
   const float w0 = g.w * (1.0f - au), w1 = g.w * au;
-  const float2* col = p + iu;
+  const typename QuadT<S>::T* col = p + iu;
   static_assert(ZC % 2 == 0, "ZC must be even");
   const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
 #pragma unroll
   for (int j = 0; j < ZC; j += 2) {
-    const float2 q0 = __ldg(col + (size_t)(min(z0 + j - roff, H - 1) + kSinoPad) * Wp);
-    const float2 q1 = __ldg(col + (size_t)(min(z0 + j + 1 - roff, H - 1) + kSinoPad) * Wp);
-    const float2 t = __ffma2_rn(w02, make_float2(q0.x, q1.x),
-                                __ffma2_rn(w12, make_float2(q0.y, q1.y),
+    const float4 q = QuadT<S>::get(col + (size_t)(min(z0 + j - roff, H - 1) + kSinoPad) * Wp);
+    const float2 t = __ffma2_rn(w02, make_float2(q.x, q.y),
+                                __ffma2_rn(w12, make_float2(q.z, q.w),
                                            make_float2(acc[j], acc[j + 1])));
     acc[j] = t.x;
     acc[j + 1] = t.y;
@@ -652,57 +595,33 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
     }
     const float x = (float)ix - ((float)A.hw + 0.5f);
     const float y = (float)iy - ((float)A.hw + 0.5f);
-    if constexpr (IsQuad<TS>::value) {
-      // quad-layout views: cone (launch_bp_quad, launch_bp_sub) or any
-      // geometry on a decoupled detector (launch_bp_det; v interpolated)
-      using S = typename IsQuad<TS>::Storage;
-      const auto* q = reinterpret_cast<const typename QuadT<S>::T*>(sino);
-      if constexpr (MODE == 1) {
-        const size_t vstride = (size_t)Wp * (A.det_h + 2 * kSinoPad);
-        for (int v = vbeg; v < vend; ++v) {
-          const ColGeom<GEOM> g =
-              col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hwd, A.v0d, A.inv_du, A.inv_dv);
-          bp_column_quad<ZC, S, GEOM>(q + (size_t)v * vstride, A.det_w, A.det_h, Wp, z0, g, acc);
-        }
-      } else if constexpr (MODE == 2) {
-        const size_t vstride = (size_t)Wp * (A.nrows + 2 * kSinoPad);
-        for (int v = vbeg; v < vend; ++v) {
-          const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
-                                                 1.f, 1.f);
-          bp_column_quad<ZC, S, GEOM>(q + (size_t)v * vstride, A.W, A.nrows, Wp, A.zoff + z0, g,
-                                      acc, A.row0);
-        }
-      } else {
-        const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
-        for (int v = vbeg; v < vend; ++v) {
-          const ColGeom<2> g = col_geom<2>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f,
-                                           1.f);
-          bp_column_quad<ZC, S>(q + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
-        }
-      }
-    } else if constexpr (std::is_same<TS, float2>::value && MODE == 2) {
-      // par / fan z-slab, pair-layout band of rows (launch_bp_sub)
-      const size_t vstride = (size_t)Wp * (A.nrows + 2 * kSinoPad);
+    static_assert(IsQuad<TS>::value, "views in the quad layout");
+    using S = typename IsQuad<TS>::Storage;
+    const auto* q = reinterpret_cast<const typename QuadT<S>::T*>(sino);
+    if constexpr (MODE == 1) {
+      // decoupled detector: every geometry interpolates in v
+      const size_t vstride = (size_t)Wp * (A.det_h + 2 * kSinoPad);
       for (int v = vbeg; v < vend; ++v) {
-        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
-                                               1.f, 1.f);
-        bp_column_pair<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.nrows, Wp, A.zoff + z0, g,
-                                 acc, A.row0);
-      }
-    } else if constexpr (std::is_same<TS, float2>::value) {
-      // par / fan, FP32 pair-layout views (launch_bp_pair)
-      const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
-      for (int v = vbeg; v < vend; ++v) {
-        const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
-                                               1.f, 1.f);
-        bp_column_pair<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+        const ColGeom<GEOM> g =
+            col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hwd, A.v0d, A.inv_du, A.inv_dv);
+        bp_column_quad<ZC, S, GEOM>(q + (size_t)v * vstride, A.det_w, A.det_h, Wp, z0, g, acc);
       }
     } else {
-      const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
+      // MODE 0: the whole detector; MODE 2: a band of rows row0 .. row0 +
+      // nrows - 1 of it for the slab's voxels zoff + z (taps in whole-detector
+      // rows, offset by row0)
+      const int rows = MODE == 2 ? A.nrows : A.H;
+      const int zg = MODE == 2 ? A.zoff + z0 : z0;
+      const int roff = MODE == 2 ? A.row0 : 0;
+      const size_t vstride = (size_t)Wp * (rows + 2 * kSinoPad);
       for (int v = vbeg; v < vend; ++v) {
         const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0,
                                                1.f, 1.f);
-        bp_column_pad<GEOM, ZC>(sino + (size_t)v * vstride, A.W, A.H, Wp, z0, g, acc);
+        if constexpr (GEOM == 2)
+          bp_column_quad<ZC, S>(q + (size_t)v * vstride, A.W, rows, Wp, zg, g, acc, roff);
+        else  // par / fan: the z rows are texel rows
+          bp_column_quadrows<GEOM, ZC, S>(q + (size_t)v * vstride, A.W, rows, Wp, zg, g, acc,
+                                          roff);
       }
     }
   }
@@ -767,85 +686,46 @@ static cudaError_t bp_pad_zc(const VoxArgs& a, const void* sino, int Wp, void* v
   return bp_pad_go<GEOM, 16, TS, TV>(a, sino, Wp, vol, accum, shp, part, st);
 }
 
-template <int GEOM>
-static cudaError_t bp_pad_types(const VoxArgs& a, const void* sino, int stype, int Wp, void* vol,
-                                int vtype, bool accum, const BpShape& shp, float* part,
-                                cudaStream_t st) {
-  if (stype == kF32 && vtype == kF32)
-    return bp_pad_zc<GEOM, float, float>(a, sino, Wp, vol, accum, shp, part, st);
-  if (stype == kF16 && vtype == kF16)
-    return bp_pad_zc<GEOM, __half, __half>(a, sino, Wp, vol, accum, shp, part, st);
-  if (stype == kF16 && vtype == kF32)
-    return bp_pad_zc<GEOM, __half, float>(a, sino, Wp, vol, accum, shp, part, st);
-  if (stype == kBF16 && vtype == kBF16)
-    return bp_pad_zc<GEOM, __nv_bfloat16, __nv_bfloat16>(a, sino, Wp, vol, accum, shp, part, st);
-  if (stype == kBF16 && vtype == kF32)
-    return bp_pad_zc<GEOM, __nv_bfloat16, float>(a, sino, Wp, vol, accum, shp, part, st);
-  return cudaErrorInvalidValue;
-}
-
 bool bp_shape_valid(const BpShape& s) {
   return (s.zc == 8 || s.zc == 16) && (s.rows == 4 || s.rows == 8) && s.vblocks >= 1 &&
          s.vblocks <= 64;
 }
 
-cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, int stype,
-                             void* vol, int vtype, bool accumulate, const BpShape& shp,
-                             float* part, cudaStream_t st) {
-  if (!bp_shape_valid(shp) || (shp.vblocks > 1 && !part)) return cudaErrorInvalidValue;
-  const int Wp = sino_pad_pitch(a.W);
-  switch (geom) {
-    case 0: return bp_pad_types<0>(a, sino_pad, stype, Wp, vol, vtype, accumulate, shp, part, st);
-    case 1: return bp_pad_types<1>(a, sino_pad, stype, Wp, vol, vtype, accumulate, shp, part, st);
-    case 2: return bp_pad_types<2>(a, sino_pad, stype, Wp, vol, vtype, accumulate, shp, part, st);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-cudaError_t launch_bp_quad(const VoxArgs& a, const void* sino_quad, int stype, void* vol,
-                           int vtype, bool accumulate, const BpShape& shp, float* part,
-                           cudaStream_t st) {
-  if (!bp_shape_valid(shp) || (shp.vblocks > 1 && !part)) return cudaErrorInvalidValue;
-  const int Wp = sino_pad_pitch(a.W);
+template <int GEOM>
+static cudaError_t bp_quad_types(const VoxArgs& a, const void* sino_quad, int stype, int Wp,
+                                 void* vol, int vtype, bool accumulate, const BpShape& shp,
+                                 float* part, cudaStream_t st) {
   using QF = QuadLayout<float>;
   using QH = QuadLayout<__half>;
   using QB = QuadLayout<__nv_bfloat16>;
   if (stype == kF32 && vtype == kF32)
-    return bp_pad_zc<2, QF, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+    return bp_pad_zc<GEOM, QF, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   if (stype == kF32 && vtype == kF16)
-    return bp_pad_zc<2, QF, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+    return bp_pad_zc<GEOM, QF, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   if (stype == kF32 && vtype == kBF16)
-    return bp_pad_zc<2, QF, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+    return bp_pad_zc<GEOM, QF, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   if (stype == kF16 && vtype == kF16)
-    return bp_pad_zc<2, QH, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+    return bp_pad_zc<GEOM, QH, __half>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   if (stype == kF16 && vtype == kF32)
-    return bp_pad_zc<2, QH, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+    return bp_pad_zc<GEOM, QH, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   if (stype == kBF16 && vtype == kBF16)
-    return bp_pad_zc<2, QB, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+    return bp_pad_zc<GEOM, QB, __nv_bfloat16>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   if (stype == kBF16 && vtype == kF32)
-    return bp_pad_zc<2, QB, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
+    return bp_pad_zc<GEOM, QB, float>(a, sino_quad, Wp, vol, accumulate, shp, part, st);
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_bp_pair(int geom, const VoxArgs& a, const float2* sino_pair, void* vol,
-                           int vtype, bool accumulate, const BpShape& shp, float* part,
-                           cudaStream_t st) {
+cudaError_t launch_bp_quad(int geom, const VoxArgs& a, const void* sino_quad, int stype,
+                           void* vol, int vtype, bool accumulate, const BpShape& shp,
+                           float* part, cudaStream_t st) {
   if (!bp_shape_valid(shp) || (shp.vblocks > 1 && !part)) return cudaErrorInvalidValue;
   const int Wp = sino_pad_pitch(a.W);
-#define PAIR(G)                                                                              \
-  do {                                                                                       \
-    if (vtype == kF32)                                                                       \
-      return bp_pad_zc<G, float2, float>(a, sino_pair, Wp, vol, accumulate, shp, part, st);  \
-    if (vtype == kF16)                                                                       \
-      return bp_pad_zc<G, float2, __half>(a, sino_pair, Wp, vol, accumulate, shp, part, st); \
-    if (vtype == kBF16)                                                                      \
-      return bp_pad_zc<G, float2, __nv_bfloat16>(a, sino_pair, Wp, vol, accumulate, shp,    \
-                                                 part, st);                                  \
-  } while (0)
-  if (geom == 0) PAIR(0);
-  else if (geom == 1) PAIR(1);
-#undef PAIR
-  return cudaErrorInvalidValue;
+  switch (geom) {
+    case 0: return bp_quad_types<0>(a, sino_quad, stype, Wp, vol, vtype, accumulate, shp, part, st);
+    case 1: return bp_quad_types<1>(a, sino_quad, stype, Wp, vol, vtype, accumulate, shp, part, st);
+    case 2: return bp_quad_types<2>(a, sino_quad, stype, Wp, vol, vtype, accumulate, shp, part, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 // Decoupled-detector BP: FP32 det_w x det_h views in the quad layout
@@ -880,7 +760,7 @@ cudaError_t launch_bp_det(int geom, const VoxArgs& a, const void* sino_quad, flo
   return cudaGetLastError();
 }
 
-cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const void* sino_lay, float* vol,
+cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const void* sino_quad, float* vol,
                           bool accumulate, cudaStream_t st) {
   if (a.nviews <= 0) return cudaSuccess;
   constexpr int ZC = 16;
@@ -889,18 +769,16 @@ cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const void* sino_lay, floa
   dim3 blk(32, 4), grd((a.W + 31) / 32, (a.W + 3) / 4, nz);
   const int acc = accumulate ? 1 : 0;
   using Q = QuadLayout<float>;
+  const Q* sq = static_cast<const Q*>(sino_quad);
   switch (geom) {
     case 0:
-      bp_pad_kernel<0, ZC, float2, float, 2><<<grd, blk, 0, st>>>(
-          a, static_cast<const float2*>(sino_lay), Wp, vol, acc, nz, 1, nullptr, 0);
+      bp_pad_kernel<0, ZC, Q, float, 2><<<grd, blk, 0, st>>>(a, sq, Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     case 1:
-      bp_pad_kernel<1, ZC, float2, float, 2><<<grd, blk, 0, st>>>(
-          a, static_cast<const float2*>(sino_lay), Wp, vol, acc, nz, 1, nullptr, 0);
+      bp_pad_kernel<1, ZC, Q, float, 2><<<grd, blk, 0, st>>>(a, sq, Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     case 2:
-      bp_pad_kernel<2, ZC, Q, float, 2><<<grd, blk, 0, st>>>(a, static_cast<const Q*>(sino_lay),
-                                                               Wp, vol, acc, nz, 1, nullptr, 0);
+      bp_pad_kernel<2, ZC, Q, float, 2><<<grd, blk, 0, st>>>(a, sq, Wp, vol, acc, nz, 1, nullptr, 0);
       break;
     default: return cudaErrorInvalidValue;
   }

@@ -148,16 +148,14 @@ cudaError_t launch_fp_tex(int geom, const RayArgs& a,
                           cudaTextureObject_t tex, float* out,
                           cudaStream_t st);
 
-// Padded sinogram for the voxel-driven BP: [nviews][H+4][W+4], edge values
-// replicated (clamp) or zero (border) in the two-texel frame.
+// Padded views for the voxel-driven BP: [nviews][H+4][W+4] texels, edge
+// values replicated (clamp) in the two-texel frame.
 constexpr int kSinoPad = 2;  // frame width of padded sinogram views
 __host__ __device__ inline int sino_pad_pitch(int W) { return W + 2 * kSinoPad; }
 size_t sino_pad_elems(int W, int H, int nviews);
-cudaError_t launch_pad_sino(const void* in, int dtype, int W, int H, int nviews, bool border,
-                            void* out, cudaStream_t st);
-// Launch shape of the padded-sinogram BP: z voxels per thread (8 or 16),
-// column rows per block (4 or 8), view blocks along grid z (1..64; > 1 needs
-// an FP32 partial-sum workspace of vblocks * W*W*H floats).
+// Launch shape of the BP: z voxels per thread (8 or 16), column rows per
+// block (4 or 8), view blocks along grid z (1..64; > 1 needs an FP32
+// partial-sum workspace of vblocks * W*W*H floats).
 struct BpShape {
   int zc, rows, vblocks;
   // z-blocks (of zc slices) zb0 .. zb0 + nzb - 1 only (nzb = 0: all); with
@@ -166,27 +164,19 @@ struct BpShape {
   int zb0 = 0, nzb = 0;
 };
 bool bp_shape_valid(const BpShape& s);
-// BP of a.nviews views from a padded sinogram (view 0 of the launch first).
-cudaError_t launch_bp_padded(int geom, const VoxArgs& a, const void* sino_pad, int stype,
-                             void* vol, int vtype, bool accumulate, const BpShape& shp,
-                             float* part, cudaStream_t st);
 
-// Cone BP from the quad layout of launch_pad_sino_quad (views of storage
-// type stype: FP32 in 16-byte texels, FP16 / BF16 in 8-byte texels): the same
-// result as launch_bp_padded on the clamp-padded views, bit for bit.
+// Quad layout of the padded views (storage type stype: FP32 in 16-byte
+// texels, FP16 / BF16 in 8-byte texels): texel (r, c) holds {P(r,c),
+// P(r+1,c), P(r,c+1), P(r+1,c+1)} of the clamp-padded view P.
 cudaError_t launch_pad_sino_quad(const void* in, int stype, int W, int H, int nviews, void* out,
                                  cudaStream_t st);
-cudaError_t launch_bp_quad(const VoxArgs& a, const void* sino_quad, int stype, void* vol,
-                           int vtype, bool accumulate, const BpShape& shp, float* part,
-                           cudaStream_t st);
-
-// Par / fan BP (FP32 views) from the pair layout of launch_pad_sino_pair: the
-// same result as launch_bp_padded, bit for bit.
-cudaError_t launch_pad_sino_pair(const float* in, int W, int H, int nviews, float2* out,
-                                 cudaStream_t st);
-cudaError_t launch_bp_pair(int geom, const VoxArgs& a, const float2* sino_pair, void* vol,
-                           int vtype, bool accumulate, const BpShape& shp, float* part,
-                           cudaStream_t st);
+// BP of a.nviews views (view 0 of the launch first) from the quad layout, any
+// geometry: cone reads one quad per voxel and view, par / fan (whose z rows
+// are texel rows) one quad per z pair of voxels.  With accumulate the launch
+// continues the sums stored in vol.
+cudaError_t launch_bp_quad(int geom, const VoxArgs& a, const void* sino_quad, int stype,
+                           void* vol, int vtype, bool accumulate, const BpShape& shp,
+                           float* part, cudaStream_t st);
 
 // Decoupled-detector BP from the quad layout (launch_pad_sino_quad, FP32) of
 // a.det_w x a.det_h views.
@@ -195,10 +185,9 @@ cudaError_t launch_bp_det(int geom, const VoxArgs& a, const void* sino_quad, flo
 
 // Sub-volume BP: slices a.zoff .. a.zoff + a.nzs - 1 (a W x W x a.nzs FP32
 // slab) from detector rows a.row0 .. + a.nrows - 1 (which must hold every row
-// the slab's columns reach: mexct_sub_rows), laid out as quads (cone,
-// launch_pad_sino_quad) or pairs (par / fan, launch_pad_sino_pair) of the
-// band.  Per voxel the same operations as launch_bp_quad / launch_bp_pair.
-cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const void* sino_lay, float* vol,
+// the slab's columns reach: mexct_sub_rows) in the quad layout of the band.
+// Per voxel the same operations as launch_bp_quad.
+cudaError_t launch_bp_sub(int geom, const VoxArgs& a, const void* sino_quad, float* vol,
                           bool accumulate, cudaStream_t st);
 
 // dst = w * src (first) or dst += w * src over n elements.

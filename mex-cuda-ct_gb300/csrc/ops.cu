@@ -185,10 +185,9 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
   }
   if (!bp_shape_valid(shp)) return set_err(MEXCT_ERR_ARG, "bp: invalid launch shape");
   const int chunk = std::min(nP, kMaxViews);
-  // cone: quad layout (one 16-byte load per voxel and view for FP32 views,
-  // 8 bytes for FP16 / BF16); par / fan FP32: pair layout (one 8-byte load)
-  const bool quad = geom == 2, pair = geom < 2 && stype == kF32;
-  const size_t es = quad ? 4 * dsize(stype) : pair ? sizeof(float2) : dsize(stype);
+  // every view in the quad layout: one 16-byte load per voxel and view (cone)
+  // or per z pair of voxels (par / fan) for FP32 views, 8 bytes for FP16 / BF16
+  const size_t es = 4 * dsize(stype);
   MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, H, chunk) * es, st), "bp: workspace");
   const size_t N = (size_t)W * W * H;
   if (shp.vblocks > 1)
@@ -197,22 +196,11 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
   const size_t vpad = sino_pad_elems(W, H, 1) * es;  // bytes of one laid-out view
   // one view chunk and one view block: the z split (hook) and the view parts
   // (feed) keep each voxel's operations those of one launch
-  const bool single = nP <= kMaxViews && shp.vblocks == 1 && (quad || pair);
+  const bool single = nP <= kMaxViews && shp.vblocks == 1;
   const bool zsplit = hook && single;
   const int nparts = feed && single ? std::min(4, std::max(1, feed->chunks)) : 1;
   for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
     const int nv = std::min(kMaxViews, nP - v0);
-    if (!quad && !pair) {
-      a->nviews = nv;
-      a->view0 = 0;
-      for (int i = 0; i < nv; ++i) trig_of(angles[v0 + i], &a->trig[i]);
-      const char* src = static_cast<const char*>(d_sino) + (size_t)v0 * P * dsize(stype);
-      MEXCT_TRY_CUDA(launch_pad_sino(src, stype, W, H, nv, false, c->spad.p, st), "bp: pad");
-      MEXCT_TRY_CUDA(launch_bp_padded(geom, *a, c->spad.p, stype, d_vol, vt, v0 > 0, shp,
-                                      c->bpart.as<float>(), st),
-                     "bp: launch");
-      continue;
-    }
     for (int part = 0; part < nparts; ++part) {
       // parts of 1/16, 3/16, 1/4 and 1/2 of the views: the first, whose
       // upload nothing hides, is small
@@ -227,10 +215,7 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
       for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + s0 + i], &a->trig[i]);
       const char* src = static_cast<const char*>(d_sino) + (size_t)(v0 + s0) * P * dsize(stype);
       void* lay = static_cast<char*>(c->spad.p) + (size_t)s0 * vpad;
-      MEXCT_TRY_CUDA(quad ? launch_pad_sino_quad(src, stype, W, H, a->nviews, lay, st)
-                          : launch_pad_sino_pair(reinterpret_cast<const float*>(src), W, H,
-                                                 a->nviews, static_cast<float2*>(lay), st),
-                     "bp: pad");
+      MEXCT_TRY_CUDA(launch_pad_sino_quad(src, stype, W, H, a->nviews, lay, st), "bp: pad");
       // z ranges of the volume in hook->chunks launches for the last part
       const bool zs = zsplit && part == nparts - 1;
       const int nzb = (H + shp.zc - 1) / shp.zc;
@@ -240,10 +225,8 @@ mexct_status bp_run(mexct_ctx* c, const void* d_sino, int stype, int W, int H, i
         BpShape sh = shp;
         sh.zb0 = zb;
         sh.nzb = zs ? zstep : 0;
-        MEXCT_TRY_CUDA(quad ? launch_bp_quad(*a, lay, stype, d_vol, vt, accum, sh,
-                                             c->bpart.as<float>(), st)
-                            : launch_bp_pair(geom, *a, static_cast<const float2*>(lay), d_vol,
-                                             vt, accum, sh, c->bpart.as<float>(), st),
+        MEXCT_TRY_CUDA(launch_bp_quad(geom, *a, lay, stype, d_vol, vt, accum, sh,
+                                      c->bpart.as<float>(), st),
                        "bp: launch");
         if (zs) {
           const int z0 = zb * shp.zc;

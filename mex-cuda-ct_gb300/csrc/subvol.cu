@@ -36,8 +36,8 @@ namespace {
 
 bool bad_wh(int W, int H) { return W <= 0 || H <= 0 || W > 16384 || H > 16384; }
 
-// Bytes per padded texel of the BP layout: quads (cone) or pairs (par / fan).
-size_t lay_bytes(int geom) { return geom == 2 ? sizeof(float4) : sizeof(float2); }
+// Bytes per padded texel of the BP's quad layout (FP32 views).
+constexpr size_t kLayBytes = sizeof(float4);
 
 // Detector rows the BP of slab [z0, z0 + nz) reads, with one row of margin
 // each side (cone): pz(z) = (z - v0) U + v0 + 0.5 with U = SR / (SR - s) and
@@ -162,8 +162,7 @@ mexct_status bp_sub_impl(mexct_ctx* c, const float* d_rows, int row0, int nrows,
   a->row0 = row0;
   a->nrows = nrows;
   const int chunk = std::min(nP, pad_views > 0 ? std::min(pad_views, kMaxViews) : kMaxViews);
-  const bool quad = geom == 2;  // cone: quad layout; par / fan: pair layout
-  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, nrows, chunk) * lay_bytes(geom), st),
+  MEXCT_TRY_CUDA(c->spad.ensure_async(sino_pad_elems(W, nrows, chunk) * kLayBytes, st),
                  "bp_sub: workspace");
   const size_t Pr = (size_t)W * nrows;
   for (int v0 = 0; v0 < nP; v0 += chunk) {
@@ -171,8 +170,7 @@ mexct_status bp_sub_impl(mexct_ctx* c, const float* d_rows, int row0, int nrows,
     a->view0 = 0;
     for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
     const float* rows = d_rows + (size_t)v0 * Pr;
-    MEXCT_TRY_CUDA(quad ? launch_pad_sino_quad(rows, kF32, W, nrows, a->nviews, c->spad.p, st)
-                        : launch_pad_sino_pair(rows, W, nrows, a->nviews, c->spad.as<float2>(), st),
+    MEXCT_TRY_CUDA(launch_pad_sino_quad(rows, kF32, W, nrows, a->nviews, c->spad.p, st),
                    "bp_sub: pad");
     MEXCT_TRY_CUDA(launch_bp_sub(geom, *a, c->spad.p, d_slab, accumulate || v0 > 0, st),
                    "bp_sub: launch");
@@ -193,7 +191,7 @@ constexpr int kOocPadViews = 32;
 // layout of up to kOocPadViews of them.
 size_t bp_step_bytes(int W, int nz, int nr, int nv, int geom) {
   return (size_t)W * W * nz * 4 + (size_t)W * nr * nv * 4 +
-         sino_pad_elems(W, nr, std::min(nv, kOocPadViews)) * lay_bytes(geom);
+         sino_pad_elems(W, nr, std::min(nv, kOocPadViews)) * kLayBytes;
 }
 
 // Widest row band over the slabs z0 = 0, nz, 2 nz, ... (the bands of the end
