@@ -429,69 +429,21 @@ cudaError_t launch_pad_sino_quad(const void* in, int stype, int W, int H, int nv
   return cudaGetLastError();
 }
 
-// Sample one padded projection along a voxel column: acc[j] += w * B(py, pz).
-// g.py / g.pz0 are texture coordinates (texel centres at i + 0.5).
-// W x H is the detector; ROWS: the column's z rows are texel rows (par / fan
-// with the volume's own detector), otherwise pz is interpolated.  roff: the
-// projection holds detector rows roff .. roff + H - 1 (a band of a taller
-// detector, launch_bp_sub); taps are computed in full-detector coordinates.
-template <int GEOM, int ZC, typename TS, bool ROWS = (GEOM < 2)>
-__device__ __forceinline__ void bp_column_pad(const TS* __restrict__ p, int W, int H, int Wp,
-                                              int z0, const ColGeom<GEOM>& g, float* acc,
-                                              int roff = 0) {
-  // u tap, once per view and column (coordinate bounded so floor fits an int)
-  const float cu = fminf(fmaxf(g.py, -4.0f), (float)W + 4.0f) - 0.5f;
-  const float fu = floorf(cu);
-  const float au = cu - fu;
-  const int iu = min(max((int)fu, -kSinoPad), W) + kSinoPad;
-  const float w0 = g.w * (1.0f - au), w1 = g.w * au;
-  const TS* col = p + iu;
-  // Two z voxels per step with packed FP32x2 arithmetic (x: z, y: z+1); each
-  // lane's operations are those of the one-voxel form, in the same order.
-  static_assert(ZC % 2 == 0, "ZC must be even");
-  const float2 w02 = make_float2(w0, w0), w12 = make_float2(w1, w1);
-  if (ROWS) {
-    // par / fan: the column's z rows are texel rows (pz = iz + 0.5)
-#pragma unroll
-    for (int j = 0; j < ZC; j += 2) {
-      const TS* r0 = col + (size_t)(min(z0 + j - roff, H - 1) + kSinoPad) * Wp;
-      const TS* r1 = col + (size_t)(min(z0 + j + 1 - roff, H - 1) + kSinoPad) * Wp;
-      const float2 v0 = make_float2(ldf(r0), ldf(r1));
-      const float2 v1 = make_float2(ldf(r0 + 1), ldf(r1 + 1));
-      const float2 t = __ffma2_rn(w02, v0, __ffma2_rn(w12, v1, make_float2(acc[j], acc[j + 1])));
-      acc[j] = t.x;
-      acc[j + 1] = t.y;
-    }
-  } else {
-    const float pz0 = g.pz0 - 0.5f;
-    const float2 dpz2 = make_float2(g.dpz, g.dpz), pz02 = make_float2(pz0, pz0);
-#pragma unroll
-    for (int j = 0; j < ZC; j += 2) {
-      const float2 zz = make_float2((float)(z0 + j), (float)(z0 + j + 1));
-      const float2 cz = __ffma2_rn(zz, dpz2, pz02);
-      const float2 fz = make_float2(floorf(cz.x), floorf(cz.y));
-      const float2 az = __fadd2_rn(cz, make_float2(-fz.x, -fz.y));
-      const int i0 = min(max(__float2int_rz(fz.x) - roff, -kSinoPad), H) + kSinoPad;
-      const int i1 = min(max(__float2int_rz(fz.y) - roff, -kSinoPad), H) + kSinoPad;
-      const TS* p0 = col + (size_t)i0 * Wp;
-      const TS* p1 = col + (size_t)i1 * Wp;
-      const float2 a = __ffma2_rn(w02, make_float2(ldf(p0), ldf(p1)),
-                                  __fmul2_rn(w12, make_float2(ldf(p0 + 1), ldf(p1 + 1))));
-      const float2 b = __ffma2_rn(w02, make_float2(ldf(p0 + Wp), ldf(p1 + Wp)),
-                                  __fmul2_rn(w12, make_float2(ldf(p0 + Wp + 1), ldf(p1 + Wp + 1))));
-      const float2 omaz = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-az.x, -az.y));
-      const float2 t = __ffma2_rn(omaz, a, __ffma2_rn(az, b, make_float2(acc[j], acc[j + 1])));
-      acc[j] = t.x;
-      acc[j + 1] = t.y;
-    }
-  }
-}
-
+// A voxel column's samples of one padded view: acc[j] += w * B(py, pz_j) for
+// the column's z voxels z0 + j (CUDAmex_BP.cu:88-190).  g.py / g.pz0 are
+// texture coordinates (texel centres at i + 0.5); B is bilinear in FP32 with
+// the taps of the padded view P: u tap iu = floor(py - 0.5) (coordinate
+// bounded so floor fits an int, index clamped into the frame), w0 = w (1 -
+// au), w1 = w au; per voxel a = fma(w0, P(r, iu), w1 P(r, iu+1)), b the same
+// on row r + 1, acc = fma(1 - az, a, fma(az, b, acc)).  W x H is the detector;
+// roff: the view holds detector rows roff .. roff + H - 1 (a band of a
+// taller detector, launch_bp_sub), taps are computed in whole-detector rows.
+//
 // Cone column over a quad-layout view (launch_pad_sino_quad): texel (r, c)
 // holds the bilinear footprint {P(r,c), P(r+1,c), P(r,c+1), P(r+1,c+1)} of
 // the padded view P, so each voxel's four taps are one 16-byte load whose
-// halves (columns c and c+1) feed the packed u lerps of both rows.  The
-// arithmetic is bp_column_pad's (GEOM 2), operation for operation.
+// halves (columns c and c+1) feed the packed u lerps of both rows.  pz is
+// interpolated: r = floor(pz - 0.5), az its fraction.
 template <int ZC, typename S = float, int GEOM = 2>
 __device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __restrict__ p, int W,
                                                int H, int Wp, int z0, const ColGeom<GEOM>& g,
@@ -529,8 +481,9 @@ __device__ __forceinline__ void bp_column_quad(const typename QuadT<S>::T* __res
 // Par / fan column over a quad-layout view: the column's z rows are texel
 // rows, so the quad at row r holds column c's rows r and r+1 and column c+1's,
 // i.e. both voxels of a z pair as register pairs: one 16-byte load and two
-// packed operations per pair.  bp_column_pad's arithmetic (ROWS path); row r+1
-// is clamped by the layout exactly as min(z + 1, H - 1) clamps it.
+// packed operations per pair.  Row r = min(z, H - 1) with weight 1 (az = 0:
+// acc = fma(w0, P(r, iu), fma(w1, P(r, iu+1), acc))); the layout clamps row
+// r + 1 exactly as min(z + 1, H - 1) does.
 template <int GEOM, int ZC, typename S = float>
 __device__ __forceinline__ void bp_column_quadrows(const typename QuadT<S>::T* __restrict__ p,
                                                    int W, int H, int Wp, int z0,
@@ -657,7 +610,6 @@ __global__ void __launch_bounds__(256) bp_reduce_kernel(const float* __restrict_
   }
 }
 
-constexpr int kBpZc = 16;
 
 template <int GEOM, int ZC, typename TS, typename TV>
 static cudaError_t bp_pad_go(const VoxArgs& a, const void* sino, int Wp, void* vol, bool accum,
@@ -908,16 +860,16 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
   const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
   for (int v = 0; v < A.nviews; ++v) {
     const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
-    // zero frame = border addressing (CUDAmex_oscIter.cu:419-425); cone
-    // residuals in the quad layout written by the FP epilogue
+    // zero frame = border addressing (CUDAmex_oscIter.cu:419-425); residuals
+    // in the quad layout written by the FP epilogue
+    const float4* qpre = reinterpret_cast<const float4*>(rpre) + (size_t)v * vstride;
+    const float4* qpost = reinterpret_cast<const float4*>(rpost) + (size_t)v * vstride;
     if constexpr (GEOM == 2) {
-      bp_column_quad<ZC, float>(reinterpret_cast<const float4*>(rpre) + (size_t)v * vstride, A.W, A.H,
-                         Wp, z0, g, num);
-      bp_column_quad<ZC, float>(reinterpret_cast<const float4*>(rpost) + (size_t)v * vstride, A.W, A.H,
-                         Wp, z0, g, den);
+      bp_column_quad<ZC, float>(qpre, A.W, A.H, Wp, z0, g, num);
+      bp_column_quad<ZC, float>(qpost, A.W, A.H, Wp, z0, g, den);
     } else {
-      bp_column_pad<GEOM, ZC>(rpre + (size_t)v * vstride, A.W, A.H, Wp, z0, g, num);
-      bp_column_pad<GEOM, ZC>(rpost + (size_t)v * vstride, A.W, A.H, Wp, z0, g, den);
+      bp_column_quadrows<GEOM, ZC, float>(qpre, A.W, A.H, Wp, z0, g, num);
+      bp_column_quadrows<GEOM, ZC, float>(qpost, A.W, A.H, Wp, z0, g, den);
     }
   }
   const size_t base = (size_t)iy * A.W + ix;

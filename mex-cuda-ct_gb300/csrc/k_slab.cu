@@ -875,19 +875,14 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       const size_t ri = ((size_t)J.lview * (J.det_h + 2 * kSinoPad) + (iy + kSinoPad)) * Wp +
                         (ix + kSinoPad);
       const float r0 = ehat - qv, r1 = ehat * l;
-      if (GEOM == 2) {
-        // cone: quad layout (the dual BP's one 16-byte load per voxel): the
-        // padded texel P(r, c) is component x of quad (r, c), y of (r-1, c),
-        // z of (r, c-1) and w of (r-1, c-1)
-        const size_t q[4] = {4 * ri, 4 * (ri - Wp) + 1, 4 * (ri - 1) + 2, 4 * (ri - Wp - 1) + 3};
+      // quad layout (the dual BP's one 16-byte load per voxel, cone, or per z
+      // pair, par / fan): the padded texel P(r, c) is component x of quad
+      // (r, c), y of (r-1, c), z of (r, c-1) and w of (r-1, c-1)
+      const size_t q[4] = {4 * ri, 4 * (ri - Wp) + 1, 4 * (ri - 1) + 2, 4 * (ri - Wp - 1) + 3};
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          E.rpre[q[t]] = r0;
-          E.rpost[q[t]] = r1;
-        }
-      } else {
-        E.rpre[ri] = r0;
-        E.rpost[ri] = r1;
+      for (int t = 0; t < 4; ++t) {
+        E.rpre[q[t]] = r0;
+        E.rpost[q[t]] = r1;
       }
     }
   }

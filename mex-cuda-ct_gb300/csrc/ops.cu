@@ -495,10 +495,9 @@ mexct_status osc_dev_impl(mexct_ctx* c, float* d_mu, int mu_type,
   if (!c) return MEXCT_OK;  // validate only
   (void)N;
   (void)P;
-  // Residual views in the padded layout with a zero frame (border addressing).
-  // residual views, padded; cone: quad layout (4 floats per texel)
-  const size_t rbytes =
-      sino_pad_elems(W, H, std::max(maxv, 1)) * sizeof(float) * (geom == 2 ? 4 : 1);
+  // Residual views in the padded quad layout (4 floats per texel) with a zero
+  // frame (border addressing).
+  const size_t rbytes = sino_pad_elems(W, H, std::max(maxv, 1)) * sizeof(float4);
   MEXCT_TRY_CUDA(c->r1.ensure(rbytes), "osc_iter: workspace");
   MEXCT_TRY_CUDA(c->r2.ensure(rbytes), "osc_iter: workspace");
   MEXCT_TRY_CUDA(cudaMemsetAsync(c->r1.p, 0, rbytes, st), "osc_iter: workspace");

@@ -232,7 +232,7 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   MEXCT_TRY_CUDA(s->post.ensure_async(M * 4, a), "osctv_create: post");
   // residual views in the padded layout; their zero frame (border addressing)
   // is written once here and never touched again
-  const size_t rb = sino_pad_elems(W, H, (int)maxv) * 4 * (geom == 2 ? 4 : 1);  // cone: quads
+  const size_t rb = sino_pad_elems(W, H, (int)maxv) * sizeof(float4);  // quad layout
   (void)P;
   MEXCT_TRY_CUDA(s->r1.ensure_async(rb, a), "osctv_create: residual");
   MEXCT_TRY_CUDA(s->r2.ensure_async(rb, a), "osctv_create: residual");
