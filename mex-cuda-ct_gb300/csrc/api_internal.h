@@ -158,6 +158,10 @@ struct ChunkHook {
   std::function<mexct_status(int index, int first, int count)> fn;
 };
 
+// The context's copy stream and its events (created on first use): host <->
+// device copies that overlap the launches on the context's stream.
+cudaError_t copy_stream(mexct_ctx* c, cudaStream_t* out);
+
 // FP with a concrete variant / BP with an explicit launch shape (arguments
 // already checked; ops.cu).
 mexct_status fp_run(mexct_ctx* c, const void* d_vol, int vt, int W, int H, float sad,

@@ -118,6 +118,24 @@ mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
   return prepare_slab_bufs(c->padx, c->pady, c->err, d_vol, vt, W, H, border, geom, mx, my,
                            Pf_out, st);
 }
+
+// The context's copy stream (created on first use).
+cudaError_t copy_stream(mexct_ctx* c, cudaStream_t* out) {
+  if (!c->copy_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    for (cudaEvent_t& ev : c->chunk_ev) {
+      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e != cudaSuccess) return e;
+    }
+    for (cudaEvent_t& ev : c->feed_ev) {
+      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  *out = c->copy_stream;
+  return cudaSuccess;
+}
 }  // namespace mexct
 
 namespace {
@@ -738,23 +756,6 @@ mexct_status prefilter_tables(mexct_ctx* c, int W, int H, int nP, const float* a
   return MEXCT_OK;
 }
 
-// The context's copy stream (created on first use).
-cudaError_t copy_stream(mexct_ctx* c, cudaStream_t* out) {
-  if (!c->copy_stream) {
-    cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return e;
-    for (cudaEvent_t& ev : c->chunk_ev) {
-      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-      if (e != cudaSuccess) return e;
-    }
-    for (cudaEvent_t& ev : c->feed_ev) {
-      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-      if (e != cudaSuccess) return e;
-    }
-  }
-  *out = c->copy_stream;
-  return cudaSuccess;
-}
 
 // Downloads of the chunks recorded by a ChunkHook: chunk i waits for its
 // event and copies `bytes` from d + off to h + off on the copy stream.  All

@@ -251,36 +251,51 @@ mexct_status mexct_fp_ooc(mexct_ctx* ctx, const float* vol, int W, int H, float 
   int nv = (int)std::min<size_t>((size_t)nP, budget_bytes / 2 / view_bytes);
   if (nv < 1) nv = 1;
   const size_t left = budget_bytes > nv * view_bytes ? budget_bytes - nv * view_bytes : 0;
-  // the thickest slab that fits (bytes grow linearly with nz)
+  // the thickest slab that fits with a second slab buffer for the next
+  // upload (bytes grow linearly with nz)
+  auto step_bytes = [&](int z) { return fp_slab_bytes(W, z) + (size_t)W * W * z * 4; };
   int nz = H;
-  if (fp_slab_bytes(W, nz) > left) {
-    const size_t b1 = fp_slab_bytes(W, 1), per = fp_slab_bytes(W, 2) - b1;
+  if (step_bytes(nz) > left) {
+    const size_t b1 = step_bytes(1), per = step_bytes(2) - b1;
     nz = left >= b1 ? (int)std::min<size_t>((size_t)H, 1 + (left - b1) / per) : 1;
   }
-  if (fp_slab_bytes(W, nz) > left)
+  if (step_bytes(nz) > left)
     return set_err(MEXCT_ERR_BUDGET, "fp_ooc: %zu bytes hold no view and slab of %d x %d",
                    budget_bytes, W, W);
   SUB_CTX(c, "fp_ooc");
-  cudaStream_t st = c->stream;
+  cudaStream_t st = c->stream, cs;
+  MEXCT_TRY_CUDA(copy_stream(c, &cs), "fp_ooc: copy stream");
   const size_t slab_bytes = (size_t)W * W * nz * 4;
-  MEXCT_TRY_CUDA(c->in.ensure_async(slab_bytes, st), "fp_ooc: workspace");
+  MEXCT_TRY_CUDA(c->in.ensure_async(2 * slab_bytes, st), "fp_ooc: workspace");
   MEXCT_TRY_CUDA(c->out.ensure_async((size_t)nv * view_bytes, st), "fp_ooc: workspace");
+  // Two slab buffers: slab i uploads on the copy stream into buffer i & 1
+  // once the FP that last read it has run, while the FP of slab i - 1 runs.
+  cudaEvent_t landed[2] = {c->feed_ev[0], c->feed_ev[1]};
+  cudaEvent_t freed[2] = {c->feed_ev[2], c->feed_ev[3]};
+  for (cudaEvent_t e : freed) MEXCT_TRY_CUDA(cudaEventRecord(e, st), "fp_ooc: event");
+  int slab = 0;
   for (int v0 = 0; v0 < nP; v0 += nv) {
     const int n = std::min(nv, nP - v0);
-    for (int z0 = 0; z0 < H; z0 += nz) {
-      const int m = std::min(nz, H - z0);
-      MEXCT_TRY_CUDA(cudaMemcpyAsync(c->in.p, vol + (size_t)z0 * W * W, (size_t)W * W * m * 4,
-                                     cudaMemcpyHostToDevice, st),
+    for (int z0 = 0; z0 < H; z0 += nz, ++slab) {
+      const int m = std::min(nz, H - z0), b = slab & 1;
+      float* buf = c->in.as<float>() + (size_t)b * W * W * nz;
+      MEXCT_TRY_CUDA(cudaStreamWaitEvent(cs, freed[b], 0), "fp_ooc: event");
+      MEXCT_TRY_CUDA(cudaMemcpyAsync(buf, vol + (size_t)z0 * W * W, (size_t)W * W * m * 4,
+                                     cudaMemcpyHostToDevice, cs),
                      "fp_ooc: upload");
-      mexct_status s = fp_sub_impl(c, c->in.as<float>(), W, H, z0, m, sad, angles + v0, n, geom,
+      MEXCT_TRY_CUDA(cudaEventRecord(landed[b], cs), "fp_ooc: event");
+      MEXCT_TRY_CUDA(cudaStreamWaitEvent(st, landed[b], 0), "fp_ooc: event");
+      mexct_status s = fp_sub_impl(c, buf, W, H, z0, m, sad, angles + v0, n, geom,
                                    c->out.as<float>(), z0 > 0, st);
       if (s) return s;
+      MEXCT_TRY_CUDA(cudaEventRecord(freed[b], st), "fp_ooc: event");
     }
     MEXCT_TRY_CUDA(cudaMemcpyAsync(sino + (size_t)v0 * W * H, c->out.p, (size_t)n * view_bytes,
                                    cudaMemcpyDeviceToHost, st),
                    "fp_ooc: download");
   }
   MEXCT_TRY_CUDA(cudaStreamSynchronize(st), "fp_ooc: sync");
+  MEXCT_TRY_CUDA(cudaStreamSynchronize(cs), "fp_ooc: sync");
   return MEXCT_OK;
 }
 
