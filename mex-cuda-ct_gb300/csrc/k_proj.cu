@@ -524,8 +524,13 @@ __global__ void __launch_bounds__(256, GEOM == 2 ? 4 : 1) bp_pad_kernel(const __
                                                      TV* __restrict__ vol, int accumulate,
                                                      int nz, int vblocks,
                                                      float* __restrict__ part, int zb0) {
-  const int ix = blockIdx.x * 32 + threadIdx.x;
-  const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+  // A block covers 32 x blockDim.y columns (blockDim.y = 4 or 8, one warp per
+  // threadIdx.y); each warp takes an 8 x 4 patch of them, whose projections
+  // span fewer detector texels at every view than a 32 x 1 row: fewer L1
+  // wavefronts per quad load.
+  const int w = threadIdx.y, lane = threadIdx.x;
+  const int ix = blockIdx.x * 32 + 8 * (w & 3) + (lane & 7);
+  const int iy = blockIdx.y * blockDim.y + 4 * (w >> 2) + (lane >> 3);
   const int zb = zb0 + blockIdx.z % nz, vb = blockIdx.z / nz;  // nz: z-blocks of the launch
   const int z0 = zb * ZC;
   if (ix >= A.W || iy >= A.W) return;
@@ -846,8 +851,10 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
     const __grid_constant__ VoxArgs A, const float* __restrict__ rpre,
     const float* __restrict__ rpost, TM* __restrict__ mu, TM* __restrict__ padx,
     TM* __restrict__ pady, int Pf) {
-  const int ix = blockIdx.x * 32 + threadIdx.x;
-  const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+  // 8 x 4 column patch per warp, as in bp_pad_kernel (blocks of 32 x 8)
+  const int w = threadIdx.y, lane = threadIdx.x;
+  const int ix = blockIdx.x * 32 + 8 * (w & 3) + (lane & 7);
+  const int iy = blockIdx.y * blockDim.y + 4 * (w >> 2) + (lane >> 3);
   const int z0 = blockIdx.z * ZC;
   if (ix >= A.W || iy >= A.W) return;
   if (!in_circle(ix, iy, A.hw)) return;
