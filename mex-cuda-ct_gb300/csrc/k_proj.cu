@@ -364,16 +364,18 @@ template <> struct QuadT<float> {
   }
   static __device__ __forceinline__ float4 get(const T* p) { return __ldg(p); }
 };
-// 16-bit values as bits and back to float in registers (the conversions
-// ldf applies to a loaded value: exact for both types)
+// 16-bit values as bits (make) and back to float in registers (get; the
+// conversions are exact for both types)
 __device__ __forceinline__ uint32_t bits16(__half h) { return __half_as_ushort(h); }
 __device__ __forceinline__ uint32_t bits16(__nv_bfloat16 h) { return __bfloat16_as_ushort(h); }
-template <typename H16> __device__ __forceinline__ float from_bits16(uint32_t u);
-template <> __device__ __forceinline__ float from_bits16<__half>(uint32_t u) {
-  return __half2float(__ushort_as_half((unsigned short)u));
+// Two packed 16-bit values (low half first) to FP32 in one paired conversion
+// (exact, as the scalar conversions are).
+template <typename H16> __device__ __forceinline__ float2 pair_from_bits16(uint32_t u);
+template <> __device__ __forceinline__ float2 pair_from_bits16<__half>(uint32_t u) {
+  return __half22float2(*reinterpret_cast<const __half2*>(&u));
 }
-template <> __device__ __forceinline__ float from_bits16<__nv_bfloat16>(uint32_t u) {
-  return __bfloat162float(__ushort_as_bfloat16((unsigned short)u));
+template <> __device__ __forceinline__ float2 pair_from_bits16<__nv_bfloat16>(uint32_t u) {
+  return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u));
 }
 template <typename H16> struct QuadT16 {
   using T = uint2;
@@ -382,8 +384,8 @@ template <typename H16> struct QuadT16 {
   }
   static __device__ __forceinline__ float4 get(const T* p) {
     const uint2 q = __ldg(p);
-    return make_float4(from_bits16<H16>(q.x & 0xffffu), from_bits16<H16>(q.x >> 16),
-                       from_bits16<H16>(q.y & 0xffffu), from_bits16<H16>(q.y >> 16));
+    const float2 lo = pair_from_bits16<H16>(q.x), hi = pair_from_bits16<H16>(q.y);
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
   }
 };
 template <> struct QuadT<__half> : QuadT16<__half> {};
