@@ -54,6 +54,32 @@ def test_sub_rows_cover_every_tap(lib, geom, sad):
                 assert r0 <= lo and hi <= r0 + nr - 1, (z0, nz, z, lo, hi, r0, nr)
 
 
+@pytest.mark.parametrize("W,H,sad", [(200, 160, 300.0), (257, 96, 1000.0)])
+def test_sub_rows_cover_every_tap_wide(lib, W, H, sad):
+    """The band bound (the reconstruction circle's radius) at larger, odd and
+    strongly magnified sizes: every in-circle column's taps, at angles that put
+    the circle's edge nearest to and farthest from the source, stay inside."""
+    from mexct import ops
+
+    h = W // 2 - 1
+    ix, iy = np.meshgrid(np.arange(W), np.arange(W), indexing="ij")
+    inside = (ix - h) ** 2 + (iy - h) ** 2 < h * h
+    x = (ix - (h + 0.5))[inside].ravel().astype(np.float64)
+    y = (iy - (h + 0.5))[inside].ravel().astype(np.float64)
+    v0 = (H - 1) / 2.0
+    for z0, nz in [(0, 7), (H // 3, 11), (H - 9, 9), (0, H)]:
+        r0, nr = ops.sub_rows(W, H, sad, 2, z0, nz)
+        assert 0 <= r0 and r0 + nr <= H
+        for beta in np.linspace(0, 2 * np.pi, 16, endpoint=False):
+            s = x * np.cos(beta) + y * np.sin(beta)
+            U = sad / (sad - s)
+            for z in (z0, z0 + nz - 1):  # pz is monotonic in z for each column
+                taps = np.floor((z - v0) * U + v0)
+                lo = int(np.clip(taps.min(), 0, H - 1))
+                hi = int(np.clip(taps.max() + 1, 0, H - 1))
+                assert r0 <= lo and hi <= r0 + nr - 1, (W, z0, nz, z, lo, hi, r0, nr)
+
+
 def test_sub_entry_points_validate(lib):
     from mexct import _lib
 
