@@ -17,10 +17,11 @@
 //
 // Backprojection (CUDAmex_BP.cu:44-221)
 //   One thread per (x, y) voxel column and a chunk of ZC voxels along z held
-//   in registers across all views (or a block of views); per-view geometry
-//   comes from the kernel parameter block (constant bank); the projection taps
-//   come from a padded copy of the sinogram through L1; the volume is written
-//   once.
+//   in registers across all views (or a block of views), each warp on an 8x4
+//   patch of columns; per-view geometry comes from the kernel parameter block
+//   (constant bank); the projection taps come through L1 from the views laid
+//   out once as quads (a texel's 2x2 bilinear footprint in 16 bytes); the
+//   volume is written once.
 #include <algorithm>
 #include <type_traits>
 #include <cstdio>
