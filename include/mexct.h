@@ -48,7 +48,7 @@ typedef int mexct_status;
 
 /* FP implementation variants for the _ex entry points. */
 #define MEXCT_FP_EXPLICIT 0 /* FP32 trilinear, TMA slab-staged (parity path) */
-#define MEXCT_FP_TEXTURE 1  /* hardware 3D texture, 8-bit filter weights */
+#define MEXCT_FP_TEXTURE 1  /* hardware 3D texture: the reference's arithmetic, bit for bit */
 #define MEXCT_FP_RAY 2      /* FP32 trilinear, one ray per thread via L1 */
 #define MEXCT_FP_AUTO 3     /* EXPLICIT or RAY, from the context's shape table */
 

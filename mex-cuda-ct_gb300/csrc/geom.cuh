@@ -1,12 +1,18 @@
 // geom.cuh -- device-side geometry and sampling shared by the mexct kernels.
 //
-// Ray set-up (clip to the volume box, entry point, per-step vector, sample
-// count) is evaluated in binary32 with explicitly rounded operations
-// (__fadd_rn/__fmul_rn/...), so that it never contracts into FMAs and takes
-// exactly the discrete decisions the reference source describes
-// (CUDAmex_FP.cu:82-137 and its copies in the other operators).  Sampling
-// and accumulation are plain FP32 with FMAs: they are continuous in the
-// inputs.
+// Ray set-up (end points, clip to the volume box, entry point, per-step
+// vector, sample count) is evaluated in binary32 with explicitly rounded
+// operations (__fadd_rn/__fmul_rn/__fmaf_rn/...), so that the compiler can
+// neither contract nor reorder it, and takes exactly the discrete decisions
+// the reference takes (CUDAmex_FP.cu:82-137 and its copies in the other
+// operators).  The reference is built with nvcc -O3 and fused multiply-add on
+// (compile.m:25), so its multiply-adds here are fmas; which product of each
+// sum is fused was pinned against outputs of the reference's own kernels run
+// on a GB300: a general3D BP's voxel indices and weights reproduce to 1e-7
+// only with these fmas, and the texture FP variant, which samples as the
+// reference does, reproduces the reference's FP output bit for bit.
+// Sampling and accumulation are plain FP32 with FMAs: they are continuous in
+// the inputs.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -56,6 +62,7 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
 // One axis of the slab clip: alpha of the planes b and -b, or NaN when the
 // ray is parallel to them (|d| < 1e-5 compared in double, as written).
@@ -86,15 +93,14 @@ __device__ __forceinline__ Ray clip_ray(float sx, float sy, float sz, float ex,
   const float amax = fminf(1.f, fminf(xhi, fminf(yhi, zhi)));
   const float ddx = fsub(ex, sx), ddy = fsub(ey, sy), ddz = fsub(ez, sz);
   Ray r;
-  r.cx = fadd(sx, fmul(amin, ddx));
-  r.cy = fadd(sy, fmul(amin, ddy));
-  r.cz = fadd(sz, fmul(amin, ddz));
-  const float px = fadd(sx, fmul(amax, ddx));
-  const float py = fadd(sy, fmul(amax, ddy));
-  const float pz = fadd(sz, fmul(amax, ddz));
+  r.cx = ffma(amin, ddx, sx);
+  r.cy = ffma(amin, ddy, sy);
+  r.cz = ffma(amin, ddz, sz);
+  const float px = ffma(amax, ddx, sx);
+  const float py = ffma(amax, ddy, sy);
+  const float pz = ffma(amax, ddz, sz);
   const float qx = fsub(px, r.cx), qy = fsub(py, r.cy), qz = fsub(pz, r.cz);
-  const float dist =
-      __fsqrt_rn(fadd(fadd(fmul(qx, qx), fmul(qy, qy)), fmul(qz, qz)));
+  const float dist = __fsqrt_rn(ffma(qz, qz, ffma(qx, qx, fmul(qy, qy))));
   r.dx = fmul(fdiv(qx, dist), step);
   r.dy = fmul(fdiv(qy, dist), step);
   r.dz = fmul(fdiv(qz, dist), step);
@@ -137,6 +143,11 @@ __device__ __forceinline__ bool hits_box(const float* s, const float* e, float b
 // counterpart in the reference): pixel pitch du, dv at the isocentre and a
 // sub-pixel offset ou, ov; du = dv = 1, ou = ov = 0 give the reference's
 // binary32 operations exactly (adding 0 and multiplying by 1 are exact).
+// Fused as the reference's build fuses them: in the parallel geometry u*sinB
+// and u*cosB appear in both end points, are rounded once and shared, and the
+// other product of each sum is fused; in fan and cone u appears only in the
+// detector end point, fused as fma(-RD, cosB, -(u*sinB)) and
+// fma(u, cosB, -RD*sinB).
 template <int GEOM>
 __device__ __forceinline__ void std_ray(int ix, int iy, float u0, float v0,
                                         float sb, float cb, float SR, float RD,
@@ -149,9 +160,14 @@ __device__ __forceinline__ void std_ray(int ix, int iy, float u0, float v0,
   if (GEOM == 0) {
     u = du0;
     v = dv0;
-    s[0] = fsub(fmul(SR, cb), fmul(u, sb));
-    s[1] = fadd(fmul(SR, sb), fmul(u, cb));
+    const float usb = fmul(u, sb), ucb = fmul(u, cb);
+    s[0] = ffma(SR, cb, -usb);
+    s[1] = ffma(SR, sb, ucb);
     s[2] = v;
+    e[0] = ffma(-RD, cb, -usb);
+    e[1] = ffma(-RD, sb, ucb);
+    e[2] = v;
+    return;
   } else if (GEOM == 1) {
     u = fdiv(fmul(du0, fadd(SR, RD)), SR);
     v = dv0;
@@ -165,13 +181,15 @@ __device__ __forceinline__ void std_ray(int ix, int iy, float u0, float v0,
     s[1] = fmul(SR, sb);
     s[2] = 0.0f;
   }
-  e[0] = fsub(fmul(-RD, cb), fmul(u, sb));
-  e[1] = fadd(fmul(-RD, sb), fmul(u, cb));
+  e[0] = ffma(-RD, cb, -fmul(u, sb));
+  e[1] = ffma(u, cb, fmul(-RD, sb));
   e[2] = v;
 }
 
 // general3D ray end points rotated by the view angle
-// (CUDAmex_general3D_FP.cu:71-77).
+// (CUDAmex_general3D_FP.cu:71-77, CUDAmex_general3D_BP.cu:73-79), fused as the
+// reference's build fuses them: x' = fma(x, cosB, -(y*sinB)),
+// y' = fma(y, cosB, x*sinB).
 __device__ __forceinline__ void g3d_ray(const float* pts, long long pix,
                                         long long P, float sb, float cb,
                                         float* s, float* e) {
@@ -179,11 +197,11 @@ __device__ __forceinline__ void g3d_ray(const float* pts, long long pix,
               z1 = __ldg(pts + pix + 2 * P);
   const float x2 = __ldg(pts + pix + 3 * P), y2 = __ldg(pts + pix + 4 * P),
               z2 = __ldg(pts + pix + 5 * P);
-  s[0] = fsub(fmul(x1, cb), fmul(y1, sb));
-  s[1] = fadd(fmul(x1, sb), fmul(y1, cb));
+  s[0] = ffma(x1, cb, -fmul(y1, sb));
+  s[1] = ffma(y1, cb, fmul(x1, sb));
   s[2] = z1;
-  e[0] = fsub(fmul(x2, cb), fmul(y2, sb));
-  e[1] = fadd(fmul(x2, sb), fmul(y2, cb));
+  e[0] = ffma(x2, cb, -fmul(y2, sb));
+  e[1] = ffma(y2, cb, fmul(x2, sb));
   e[2] = z2;
 }
 

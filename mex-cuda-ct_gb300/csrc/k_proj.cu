@@ -216,9 +216,14 @@ cudaError_t launch_fp(int geom, bool border, const RayArgs& a,
 }
 
 // ---------------------------------------------------------------------------
-// Hardware-texture FP variant (tex3D with linear filtering): the reference's
-// own sampling path, kept for comparison.  Its 8-bit filter weights put it
-// ~1e-4..1e-3 away from the FP64 oracle.
+// Hardware-texture FP variant: the reference's own sampling path, reproduced
+// operation for operation (CUDAmex_FP.cu:137-148, :235-246, :332-343): one
+// thread per ray, the texture unit's trilinear filter (8-bit weights), the
+// sample point advanced by `currentpoint += stepsize` in binary32, the
+// texture coordinate `currentpoint - b` in binary32, and one FP32 running
+// sum `dval += tex * stepsize`.  With the ray set-up of geom.cuh this gives
+// the reference's output bit for bit; it sits ~1e-4 from the FP64 oracle
+// (8-bit weights, binary32 stepping), where the slab kernel sits at 1e-7.
 // ---------------------------------------------------------------------------
 template <int GEOM>
 __global__ void __launch_bounds__(256) fp_tex_kernel(
@@ -230,23 +235,16 @@ __global__ void __launch_bounds__(256) fp_tex_kernel(
   const int iy = (blockIdx.y / tiles_u) * blockDim.y + threadIdx.y;
   if (ix >= A.det_w || iy >= A.det_h) return;
   const Ray r = make_ray<GEOM>(A, view, ix, iy, nullptr);
-  const float cx = r.cx - A.bx, cy = r.cy - A.by, cz = r.cz - A.bz;
-  float a0 = 0.f, a1 = 0.f;
-  int k = 0;
-  for (; k + 1 < r.n; k += 2) {
-    const float k0 = (float)k, k1 = (float)(k + 1);
-    a0 += tex3D<float>(tex, fmaf(k0, r.dx, cx), fmaf(k0, r.dy, cy),
-                       fmaf(k0, r.dz, cz));
-    a1 += tex3D<float>(tex, fmaf(k1, r.dx, cx), fmaf(k1, r.dy, cy),
-                       fmaf(k1, r.dz, cz));
+  float cx = r.cx, cy = r.cy, cz = r.cz, acc = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < r.n; ++k) {
+    const float t = tex3D<float>(tex, fsub(cx, A.bx), fsub(cy, A.by), fsub(cz, A.bz));
+    acc = ffma(t, A.step, acc);
+    cx = fadd(cx, r.dx);
+    cy = fadd(cy, r.dy);
+    cz = fadd(cz, r.dz);
   }
-  if (k < r.n) {
-    const float k0 = (float)k;
-    a0 += tex3D<float>(tex, fmaf(k0, r.dx, cx), fmaf(k0, r.dy, cy),
-                       fmaf(k0, r.dz, cz));
-  }
-  out[(size_t)(A.view0 + view * A.vstride) * A.P + (size_t)iy * A.det_w + ix] =
-      (a0 + a1) * A.step;
+  out[(size_t)(A.view0 + view * A.vstride) * A.P + (size_t)iy * A.det_w + ix] = acc;
 }
 
 cudaError_t launch_fp_tex(int geom, const RayArgs& a, cudaTextureObject_t tex,

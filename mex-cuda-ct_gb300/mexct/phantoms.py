@@ -114,27 +114,35 @@ def parallel_pts(W: int, H: int, L: float = 1000.0) -> np.ndarray:
 
 
 def helix_pts(W: int, H: int, n_views: int, nz: int, sad: float = 1000.0, turns: float = 2.0,
-              pitch: float = 1.0, seed: int = 0, jitter: float = 0.05):
+              pitch: float = 1.0, seed: int = 0, jitter: float = 0.05, views=None):
     """Cone-beam helix as per-view general3D points [W,H,6,nP] plus the view angles.
 
     The source sits at radius ``sad`` and advances ``pitch*nz`` voxels in z per turn; the
     flat detector sits ``sad`` behind the axis with unit pixels magnified by 2; the points
     are given in the un-rotated frame (the kernels rotate them by each view angle about z).
-    Seeded jitter of the end points avoids perfectly regular rays."""
+    Seeded jitter of the end points avoids perfectly regular rays.  ``views`` (sorted
+    indices) returns only those views of the ``n_views`` helix, with the same values."""
     rng = np.random.default_rng(seed)
     ang = angles_full(n_views, turns)
     zsrc = (np.arange(n_views) / max(n_views - 1, 1) - 0.5) * turns * pitch * nz
     u = (np.arange(W) - (W - 1) / 2.0)[:, None] * 2.0
     v = (np.arange(H) - (H - 1) / 2.0)[None, :] * 2.0
-    pts = np.zeros((W, H, 6, n_views), dtype=np.float32, order="F")
+    keep = list(range(n_views)) if views is None else [int(j) for j in views]
+    slot = {j: i for i, j in enumerate(keep)}
+    pts = np.zeros((W, H, 6, len(keep)), dtype=np.float32, order="F")
     for j in range(n_views):
-        pts[:, :, 0, j] = sad
-        pts[:, :, 1, j] = 0.0
-        pts[:, :, 2, j] = zsrc[j]
-        pts[:, :, 3, j] = -sad
-        pts[:, :, 4, j] = u + rng.uniform(-jitter, jitter, size=(W, H))
-        pts[:, :, 5, j] = zsrc[j] + v + rng.uniform(-jitter, jitter, size=(W, H))
-    return pts, ang
+        ju = rng.uniform(-jitter, jitter, size=(W, H))
+        jv = rng.uniform(-jitter, jitter, size=(W, H))
+        if j not in slot:
+            continue
+        i = slot[j]
+        pts[:, :, 0, i] = sad
+        pts[:, :, 1, i] = 0.0
+        pts[:, :, 2, i] = zsrc[j]
+        pts[:, :, 3, i] = -sad
+        pts[:, :, 4, i] = u + ju
+        pts[:, :, 5, i] = zsrc[j] + v + jv
+    return pts, ang[keep]
 
 
 def poisson_counts(fp: np.ndarray, i0: float = 1e5, seed: int = 0):

@@ -79,11 +79,14 @@ def _load():
             "orc_get_threads": [],
             "orc_set_tex_weights": [i],
             "orc_get_tex_weights": [],
+            "orc_set_ref_steps": [i],
+            "orc_get_ref_steps": [],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)
             fn.argtypes = args
-            fn.restype = None if name in ("orc_set_threads", "orc_set_tex_weights") else ctypes.c_int
+            fn.restype = None if name in ("orc_set_threads", "orc_set_tex_weights",
+                                          "orc_set_ref_steps") else ctypes.c_int
         cb = ctypes.CFUNCTYPE(None, ctypes.c_int, D, ctypes.c_void_p)
         lib.orc_osc_tv.argtypes = [F, F, i, i, i, F, f, i, i, d, i, i, d, I32, D, cb, ctypes.c_void_p]
         lib.orc_osc_tv.restype = ctypes.c_int
@@ -117,12 +120,13 @@ def get_threads() -> int:
     return int(_load().orc_get_threads())
 
 
-TEX_EXACT, TEX8_NEAREST, TEX8_TRUNC = 0, 1, 2
+TEX_EXACT, TEX8_NEAREST, TEX8_TRUNC, TEX_HW = 0, 1, 2, 3
 
 
 def set_tex_weights(mode: int) -> None:
     """Texture-fetch weights of every oracle operator: TEX_EXACT (default),
-    TEX8_NEAREST or TEX8_TRUNC (1/256 fixed point, the texture hardware's)."""
+    TEX8_NEAREST or TEX8_TRUNC (each weight in 1/256 fixed point), or TEX_HW
+    (the GPU texture unit's own weight rule, measured on a GB300)."""
     _load().orc_set_tex_weights(int(mode))
 
 
@@ -143,6 +147,33 @@ class tex_weights:
 
     def __exit__(self, *exc):
         set_tex_weights(self.prev)
+        return False
+
+
+def set_ref_steps(mode: int) -> None:
+    """Sample positions of every FP / BP / OSC operator: 0 = FP64 p0 + k*d
+    (default), 1 = the reference's binary32 incremental stepping
+    (``currentpoint += stepsize``, ``proj_z += U``).  Sums stay FP64."""
+    _load().orc_set_ref_steps(int(mode))
+
+
+def get_ref_steps() -> int:
+    return int(_load().orc_get_ref_steps())
+
+
+class ref_steps:
+    """Context manager: run oracle calls with the given stepping mode."""
+
+    def __init__(self, mode: int = 1):
+        self.mode = mode
+
+    def __enter__(self):
+        self.prev = get_ref_steps()
+        set_ref_steps(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        set_ref_steps(self.prev)
         return False
 
 

@@ -121,6 +121,13 @@ int orc_get_threads(void);
 void orc_set_tex_weights(int mode);
 int orc_get_tex_weights(void);
 
+/* Sample-position arithmetic of every FP / BP / OSC operator: 0 = FP64
+ * positions p0 + k*d (default), 1 = the reference's binary32 incremental
+ * stepping (`currentpoint += stepsize`, `proj_z += U`, binary32 column set-up).
+ * Sums are FP64 in both modes. */
+void orc_set_ref_steps(int mode);
+int orc_get_ref_steps(void);
+
 #ifdef __cplusplus
 }
 #endif

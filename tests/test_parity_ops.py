@@ -79,11 +79,10 @@ def test_config1_cylinder_cone_fp_then_bp(cuda, orc):
 
 @pytest.mark.parametrize("geom", [0, 2])
 def test_fp_texture_variant_difference(cuda, orc, geom):
-    """The hardware-texture FP is measured, not exact: the texture unit keeps its
-    filter weights in 1/256 fixed point.  Its distance to the exact-weight oracle is
-    bounded loosely and reported, and the oracle's 1/256-weight emulation (the
-    filtering the reference's tex3D fetches get) explains it: the texture kernel is
-    closer to the emulation than to exact trilinear."""
+    """The hardware-texture FP follows the reference's arithmetic (the texture
+    unit's 8-bit filter weights, binary32 stepping), so it sits ~1e-4 from the
+    exact-weight oracle and lands on the oracle run with the texture unit's weight
+    rule and the reference's stepping (FP32 summation is the only difference)."""
     import oracle
     import torch
     from mexct import ops, phantoms
@@ -96,13 +95,16 @@ def test_fp_texture_variant_difference(cuda, orc, geom):
     got = out.cpu().numpy().transpose(2, 1, 0)
     errs = {}
     for name, mode in [("exact", oracle.TEX_EXACT), ("tex8_nearest", oracle.TEX8_NEAREST),
-                       ("tex8_trunc", oracle.TEX8_TRUNC)]:
+                       ("hw", oracle.TEX_HW)]:
         with oracle.tex_weights(mode):
             errs[name] = rel_l2(got, orc.fp(vol, 1000.0, ang, nP, geom))
+    with oracle.tex_weights(oracle.TEX_HW), oracle.ref_steps(1):
+        errs["hw_steps"] = rel_l2(got, orc.fp(vol, 1000.0, ang, nP, geom))
     print("texture FP rel-L2 vs oracle (geom %d):" % geom,
           {k: "%.3g" % v for k, v in errs.items()})
-    assert errs["exact"] <= 5e-3
-    assert min(errs["tex8_nearest"], errs["tex8_trunc"]) < errs["exact"]
+    assert errs["exact"] <= 5e-4
+    assert errs["hw_steps"] <= 5e-6
+    assert errs["hw_steps"] < errs["tex8_nearest"] < errs["exact"]
 
 
 def test_general3d_fp_parallel_pts_matches_oracle(cuda, orc):
