@@ -12,12 +12,15 @@ trilinear, the 1e-5 parity path).
   extra   FP/BP GUPS for geomFlag 0 and 1; the chosen forms (hardware-texture FP,
           FP16 storage) with their relative L2 to the plain FP32 result; OSC-TV
           p50/p99 seconds per reconstruction (256^3, 60 views, 20 iterations x 10
-          subsets) plain (FP32, eager launches) vs chosen (CUDA graphs); the FP64
-          C++/OpenMP CPU implementation on a bounded sample (cpu_baseline).
+          subsets) plain (FP32, eager launches) vs chosen (CUDA graphs); the
+          reference's own kernels on the same GPU; the FP64 C++/OpenMP CPU
+          implementation on a bounded sample (cpu_baseline).
 
---impl reference times the CPU implementation alone (the reference has no CPU
-path of its own; its CUDA code uses texture references removed in CUDA 12, so the
-FP64 oracle that restates its algorithms is the CPU reference).
+--impl reference times the reference's own implementation of the step: its CUDA
+kernels, compiled unmodified from its .cu files into oracle/_ref (the reference has
+no CPU path), launched per view by the host steps of its MEX gateways restated in
+oracle/ref_launch.cu, with host arrays in and out as the gateways take them.  Where
+those cubins are absent it falls back to the FP64 CPU restatement (the oracle).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Multi-GPU: one process per GPU (torchrun); every rank runs its own full problem
@@ -44,9 +47,9 @@ for p in (ROOT, PKG):
 
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) per launch of the slab FP kernel, cone 512^3, from the
-# ncu capture summarised in profiles/fp_slab_kernel_cone_512cube_32views.md (32 views),
-# scaled to 720 views (traffic grows with the number of views).
+# DRAM bytes (read + write) per view of the slab FP kernel, cone 512^3: one ncu
+# capture of a 32-view launch (dram__bytes_read.sum + dram__bytes_write.sum), scaled
+# per view (traffic grows with the number of views).
 FP_SLAB_DRAM_BYTES_PER_VIEW = (11.672490e9 + 36.73e6) / 32
 
 
@@ -170,30 +173,91 @@ def metric_name(args):
         args.size, args.views, args.geom)
 
 
-def workload_config(args):
+def workload_config(args, world=1):
     return {"workload": "cone FP+BP %d^3 x %d views, SAD 1000, float32" % (args.size, args.views),
             "l2": "inputs larger than L2 (volume %d MiB, sinogram %d MiB)"
-                  % (4 * args.size ** 3 >> 20, 4 * args.size ** 2 * args.views >> 20)}
+                  % (4 * args.size ** 3 >> 20, 4 * args.size ** 2 * args.views >> 20),
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+def reference_step_times(vol, ang, geom, reps):
+    """Host wall time of the reference's own FP then BP (its kernels from oracle/_ref,
+    per view, with its gateways' copies and synchronisations), per call."""
+    from oracle import reference
+
+    fps, bps = [], []
+    sino = None
+    for _ in range(reps):
+        t = time.perf_counter()
+        sino = reference.fp(vol, 1000.0, ang, len(ang), geom)
+        fps.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        reference.bp(sino, 1000.0, ang, geom)
+        bps.append(time.perf_counter() - t)
+    return fps, bps
 
 
 def run_reference(args, rank):
-    """The reference's computation on the host cores: the FP64 oracle restatement (the
-    reference has no CPU path and its GPU kernels cannot run here).  Rank 0 only;
-    each step is a bounded sample of the workload (FP+BP over a few of its views)."""
+    """The reference's own implementation of the step on the same GPU: rank 0 only
+    (the other ranks exit without work).  Falls back to the FP64 CPU restatement
+    when the reference's cubins are absent."""
     if rank != 0:
         return
+    from mexct import phantoms
+    from oracle import reference
+
+    n, views, geom = args.size, args.views, args.geom
+    if not reference.available():
+        return run_reference_cpu(args)
+    vol = phantoms.ellipsoids(n, count=12, seed=2024, nz=n)
+    ang = phantoms.angles_full(views)
+    reference_step_times(vol, ang, geom, max(args.warmup, 1))
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    t = time.perf_counter()
+    fps, bps = reference_step_times(vol, ang, geom, max(args.steps, 1))
+    el = time.perf_counter() - t
+    clk = clocks.stop()
+    k = max(args.steps, 1)
+    gups = 2.0 * n ** 3 * views * k / el / 1e9
+    N, P = n ** 3, n * n
+    line = {"metric": metric_name(args), "value": round(gups, 3), "unit": "GUPS",
+            "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
+            "ms_per_step": round(el / k * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 12-ellipsoid phantom)", "impl": "reference",
+            "config": workload_config(args),
+            "fp_ms": round(float(np.median(fps)) * 1e3, 1),
+            "bp_ms": round(float(np.median(bps)) * 1e3, 1),
+            "clocks": clk,
+            "cpu_baseline": {"value": round(gups, 3), "unit": "GUPS", "cores": 1, "kind": "reference",
+                             "sample": "the full step (FP then BP of all %d views at %d^3): the "
+                                       "reference's CUDA kernels compiled unmodified for sm_103a, "
+                                       "one launch + synchronisation + host copy per view as its "
+                                       "gateways do, driven by one host thread (the reference "
+                                       "has no CPU path)" % (views, n)},
+            "e2e": {"value": round(gups, 3), "unit": "GUPS",
+                    "h2d_bytes_per_step": 4 * (N + P * views), "d2h_bytes_per_step": 4 * (P * views + N),
+                    "path": "host arrays in and out, as the MEX gateways take them"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_cpu(args):
+    """The FP64 C++/OpenMP restatement on the host cores, each step a bounded sample
+    (FP+BP over a few of the views), when the reference's kernels are not built."""
     cpu_sample(min(args.size, 64), 4, args.geom, seconds_target=0.5)  # warm-up (threads, pages)
     per_step = max(5.0, 60.0 / max(args.steps, 1))
+    t = time.perf_counter()
     samples = [cpu_sample(args.size, args.views, args.geom, seconds_target=per_step)
                for _ in range(max(args.steps, 1))]
+    el = time.perf_counter() - t
     value = float(np.mean([x["value"] for x in samples]))
     s = dict(samples[-1])
     s["value"] = round(value, 4)
-    # time one full step (FP+BP over all views) would take at the sampled rate
-    full_ms = 2.0 * args.size ** 3 * args.views / (value * 1e9) * 1e3
     line = {"metric": metric_name(args), "value": s["value"], "unit": "GUPS",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(full_ms, 1),
+            "ms_per_step": round(el / max(args.steps, 1) * 1e3, 1),
+            "ms_per_step_note": "time of each step's bounded sample, not of a full step",
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded 12-ellipsoid phantom)", "impl": "reference",
             "config": workload_config(args), "cpu_baseline": s,
@@ -349,9 +413,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded 12-ellipsoid phantom)",
-        "config": dict(workload_config(args),
-                       parallelism="replicas" if world > 1 else "single",
-                       fp_slab_ctas_per_sm=ops.fp_slab_occupancy()),
+        "config": workload_config(args, world),
+        "fp_slab_ctas_per_sm": ops.fp_slab_occupancy(),
         "fp_gups": round(N * views / fp_t / 1e9, 3), "bp_gups": round(N * views / bp_t / 1e9, 3),
         "fp_ms": round(fp_t * 1e3, 3), "bp_ms": round(bp_t * 1e3, 3),
         "roofline": {"bound": "hbm", "kernel": dom[0], "achieved": round(achieved, 2),
@@ -413,6 +476,13 @@ def main():
                                  "fp_rel_l2_vs_fp32": rel(s16.float(), ref_sino),
                                  "bp_rel_l2_vs_fp32": rel(r16.float(), rec)}
         del vol16, s16, r16
+        # The reference's own kernels on this GPU at the same workload (host arrays
+        # in and out, as its gateways take them), beside ours.
+        try:
+            extra["reference_kernels"] = reference_section(vol_h, ang, geom, n, views, fp_t, bp_t,
+                                                           ref_sino)
+        except Exception as ex:  # reported, never fatal
+            extra["reference_kernels"] = {"error": "%s: %s" % (type(ex).__name__, ex)}
         # OSC-TV reconstruction latency (config: 256^3, 60 views, 20 it x 10 subsets).
         del ref_sino
         for name, fn in (("autotune", autotune_section),
@@ -437,6 +507,30 @@ def main():
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def reference_section(vol_h, ang, geom, n, views, fp_t, bp_t, our_sino):
+    """Reference FP and BP (its own kernels, per view, host arrays) at the headline
+    workload; its FP against our texture variant (bit for bit) and our exact path."""
+    import torch
+    from mexct import _lib, ops
+    from oracle import reference
+
+    if not reference.available():
+        return {"unavailable": "reference cubins not built or no CUDA device"}
+    fps, bps = reference_step_times(vol_h, ang, geom, 1)
+    rf = reference.fp(vol_h, 1000.0, ang, views, geom)
+    dvol = torch.from_numpy(np.ascontiguousarray(vol_h.transpose(2, 1, 0))).cuda()
+    tex = ops.fp_dev(dvol, 1000.0, ang, geom, variant=_lib.FP_TEXTURE).cpu().numpy().transpose(2, 1, 0)
+    ours = our_sino.cpu().numpy().transpose(2, 1, 0)
+    N = n ** 3
+    return {"fp_ms": round(fps[0] * 1e3, 1), "bp_ms": round(bps[0] * 1e3, 1),
+            "fp_gups": round(N * views / fps[0] / 1e9, 2), "bp_gups": round(N * views / bps[0] / 1e9, 2),
+            "ours_fp_ms": round(fp_t * 1e3, 2), "ours_bp_ms": round(bp_t * 1e3, 2),
+            "texture_variant_equals_reference": bool(np.array_equal(tex, rf)),
+            "rel_l2_exact_path_vs_reference": rel_np(ours, rf),
+            "note": "reference: its CUDA kernels compiled unmodified for sm_103a, one launch, "
+                    "synchronisation and host copy per view, as its gateways run them"}
 
 
 def osc_tv_latency(reps, forms=("plain_fp32", "chosen_graph_fp32", "chosen_graph_bf16")):

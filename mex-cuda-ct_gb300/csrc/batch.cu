@@ -30,7 +30,7 @@ struct mexct_batch {
   std::vector<std::vector<std::unique_ptr<VoxArgs>>> vox;
   Buf fp_desc, trig, counters, err;
   long long fp_items = 0, pad_items = 0;
-  int sms = 152;
+  int sms = 1;  // set from cudaDevAttrMultiProcessorCount at creation
   // BP: the problems' launches fan out over kAux streams (fork / join events
   // on the caller's stream, so a capture records them as graph branches)
   static constexpr int kAux = 8;

@@ -10,6 +10,7 @@
 //   tv_update_kernel gradient recomputed, y = x + scale*g into the other
 //                    buffer of a ping-pong pair.
 // Algorithmic traffic is 12 bytes per voxel per step (read x twice, write y).
+#include <atomic>
 #include <cstdio>
 
 #include "kernels.h"
@@ -274,10 +275,29 @@ __global__ void __launch_bounds__(256) ssd_kernel(
   if (finish_partials(blk, partials, counter, &total)) *out = sqrt(total);
 }
 
+int device_sms() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    dev = 0;
+  }
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    n = 1;
+  }
+  cache[dev].store(n, std::memory_order_relaxed);
+  return n;
+}
+
+size_t ssd_partials_needed() { return (size_t)device_sms() * 4; }
+
 cudaError_t launch_ssd(const void* a, const void* b, int dt, long long n,
                        int zero_first, double* partials, unsigned* counter,
                        double* out, cudaStream_t st) {
-  const int blocks = 152 * 4;
+  const int blocks = (int)ssd_partials_needed();
   if (dt == kF32)
     ssd_kernel<float><<<blocks, 256, 0, st>>>((const float*)a, (const float*)b,
                                               n, zero_first, partials, counter, out);
@@ -303,7 +323,7 @@ __global__ void finite_kernel(T* x, long long n) {
 }
 
 cudaError_t launch_finite(void* x, int dt, long long n, cudaStream_t st) {
-  const int blocks = 152 * 8;
+  const int blocks = device_sms() * 8;
   if (dt == kF32) finite_kernel<float><<<blocks, 256, 0, st>>>((float*)x, n);
   else if (dt == kF16) finite_kernel<__half><<<blocks, 256, 0, st>>>((__half*)x, n);
   else finite_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>((__nv_bfloat16*)x, n);
@@ -320,7 +340,7 @@ __global__ void fill_kernel(T* x, long long n, float v) {
 
 cudaError_t launch_fill(void* x, int dt, long long n, float v,
                         cudaStream_t st) {
-  const int blocks = 152 * 8;
+  const int blocks = device_sms() * 8;
   if (dt == kF32) fill_kernel<float><<<blocks, 256, 0, st>>>((float*)x, n, v);
   else if (dt == kF16) fill_kernel<__half><<<blocks, 256, 0, st>>>((__half*)x, n, v);
   else fill_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>((__nv_bfloat16*)x, n, v);
@@ -339,7 +359,7 @@ __global__ void clamp_copy_kernel(const float* __restrict__ s, float* __restrict
 
 cudaError_t launch_clamp_copy(const float* src, float* dst, long long n, float eps,
                               cudaStream_t st) {
-  clamp_copy_kernel<<<152 * 8, 256, 0, st>>>(src, dst, n, eps);
+  clamp_copy_kernel<<<device_sms() * 8, 256, 0, st>>>(src, dst, n, eps);
   return cudaGetLastError();
 }
 
@@ -354,7 +374,7 @@ __global__ void convert_kernel(const S* __restrict__ s, D* __restrict__ d,
 
 cudaError_t launch_convert(const void* src, int st_, void* dst, int dt,
                            long long n, cudaStream_t st) {
-  const int blocks = 152 * 8;
+  const int blocks = device_sms() * 8;
 #define CV(SA, DA) convert_kernel<SA, DA><<<blocks, 256, 0, st>>>((const SA*)src, (DA*)dst, n)
   if (st_ == kF32 && dt == kF16) CV(float, __half);
   else if (st_ == kF32 && dt == kBF16) CV(float, __nv_bfloat16);

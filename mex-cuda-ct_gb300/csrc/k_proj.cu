@@ -632,7 +632,7 @@ static cudaError_t bp_pad_go(const VoxArgs& a, const void* sino, int Wp, void* v
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || shp.vblocks == 1) return e;
   const long long N = (long long)a.W * a.W * a.H;
-  const int ctas = (int)std::min<long long>((N + 255) / 256, 152ll * 16);
+  const int ctas = (int)std::min<long long>((N + 255) / 256, 16ll * device_sms());
   bp_reduce_kernel<TV><<<ctas, 256, 0, st>>>(part, shp.vblocks, N, (TV*)vol, accum ? 1 : 0);
   return cudaGetLastError();
 }
@@ -757,7 +757,7 @@ __global__ void __launch_bounds__(256) add_scaled_kernel(const float* __restrict
 cudaError_t launch_add_scaled(const float* src, float* dst, long long n, float w, bool first,
                               cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  const int ctas = (int)std::min<long long>((n + 255) / 256, 152ll * 16);
+  const int ctas = (int)std::min<long long>((n + 255) / 256, 16ll * device_sms());
   add_scaled_kernel<<<ctas, 256, 0, st>>>(src, dst, n, w, first ? 1 : 0);
   return cudaGetLastError();
 }

@@ -212,6 +212,11 @@ cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
 // per-thread level) and the
 // step scale -c/||g|| into *scale; tv_update writes y = x + scale*g(x).
 size_t tv_partials_needed(int Nx, int Ny, int Nz);
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
+// cached per device): grid-stride kernels size their grids by it.
+int device_sms();
+// Partial sums launch_ssd writes (one per CTA of its grid on the current device).
+size_t ssd_partials_needed();
 cudaError_t launch_tv_norm(const void* x, int x_type, int Nx, int Ny, int Nz,
                            float c, double* partials, unsigned* counter,
                            float* scale, double* norm, cudaStream_t st);

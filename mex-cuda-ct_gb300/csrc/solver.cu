@@ -222,7 +222,7 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   // running); the caller's stream waits for the allocations.
   cudaStream_t a = s->own;
   const size_t pb = (size_t)slab_pitch(W) * (W + 2) * (H + 2) * dsize(mu_type);
-  const size_t parts = std::max<size_t>(tv_partials_needed(W, W, H), 152 * 4) + 8;
+  const size_t parts = std::max<size_t>(tv_partials_needed(W, W, H), ssd_partials_needed()) + 8;
   MEXCT_TRY_CUDA(s->mu.ensure_async(vb, a), "osctv_create: mu");
   MEXCT_TRY_CUDA(s->mu_old.ensure_async(vb, a), "osctv_create: mu_old");
   MEXCT_TRY_CUDA(s->tvbuf.ensure_async(vb, a), "osctv_create: tv");

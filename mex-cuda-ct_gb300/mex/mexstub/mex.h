@@ -3,7 +3,7 @@
  * use, for building and testing the gateways without MATLAB.
  *
  * With MATLAB present, the gateways compile against MATLAB's own mex.h
- * instead.  In this stub:
+ * instead (mexcuda or mex with MATLAB's include path).  In this stub:
  *   - arrays are column-major buffers with a class id and dimensions;
  *   - mexErrMsgTxt / mexErrMsgIdAndTxt throw mexstub::MexError (MATLAB
  *     longjmps back to the prompt; the stub unwinds back to mxs_call()).

@@ -35,6 +35,18 @@ def cubins_present() -> bool:
     return all(os.path.exists(os.path.join(REF_DIR, c)) for c in CUBINS)
 
 
+def available() -> bool:
+    """Whether the reference's kernels can run here: cubins built, launcher built,
+    a CUDA driver and device present."""
+    if not cubins_present():
+        return False
+    try:
+        _load()
+        return True
+    except (OSError, RuntimeError):
+        return False
+
+
 def build_launcher(force: bool = False) -> str:
     """Compile ref_launch.cu into oracle/_ref/libreflaunch.so (nvcc, this host)."""
     os.makedirs(REF_DIR, exist_ok=True)

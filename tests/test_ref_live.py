@@ -29,6 +29,7 @@ def ref():
 
     if not reference.cubins_present():
         pytest.skip("reference cubins not built (oracle/ref_build.py needs the reference sources)")
+    assert reference.available(), "reference cubins present but their launcher does not load"
     return reference
 
 
