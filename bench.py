@@ -483,6 +483,11 @@ def main():
                                                            ref_sino)
         except Exception as ex:  # reported, never fatal
             extra["reference_kernels"] = {"error": "%s: %s" % (type(ex).__name__, ex)}
+        # The same step from the standalone C++ benchmark (C ABI, cudaMalloc buffers).
+        try:
+            extra["cpp_bench"] = cpp_bench(n, views, geom)
+        except Exception as ex:  # reported, never fatal
+            extra["cpp_bench"] = {"error": "%s: %s" % (type(ex).__name__, ex)}
         # OSC-TV reconstruction latency (config: 256^3, 60 views, 20 it x 10 subsets).
         del ref_sino
         for name, fn in (("autotune", autotune_section),
@@ -507,6 +512,20 @@ def main():
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def cpp_bench(n, views, geom):
+    """The headline step from mex-cuda-ct_gb300/bench/mexct_bench.cpp: the same C ABI
+    driven from C++ with cudaMalloc buffers and CUDA events (no Python in the loop)."""
+    import __graft_entry__ as ge
+
+    exe = ge._builder().build_bench()
+    r = subprocess.run([exe, "--size", str(n), "--views", str(views), "--geom", str(geom),
+                        "--steps", "5", "--warmup", "2"], capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"error": r.stderr.strip()[-600:]}
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    return {k: d[k] for k in ("value", "ms_per_step", "fp_ms", "bp_ms", "e2e", "impl")}
 
 
 def reference_section(vol_h, ang, geom, n, views, fp_t, bp_t, our_sino):

@@ -378,9 +378,10 @@ mexct_status mexct_autotune_bp(mexct_ctx* ctx, const void* d_sino,
  * - It runs on the current device and the given stream.
  * - Volumes above 2^21 voxels (e.g. 128^3) are rejected with
  *   MEXCT_ERR_UNSUPPORTED. So is a shape that needs more than 65536 reduction
- *   partials.
- * - The first call on a device looks up the array's device address, with
- *   that device current. Make that first call before any stream capture.
+ *   partials, or a launch grid beyond 65535 tiles in y or z.
+ * - Every call looks up the array's device address for the current device
+ *   and context. The first call on a device also loads the library's device
+ *   code there: make that first call before any stream capture.
  * - All calls share the array. Calls that overlap on the GPU race. */
 mexct_status mexct_tvmin3d_dev_noalloc(const float* d_vol, int Nx, int Ny,
                                        int Nz, float c, int n_steps,

@@ -101,6 +101,30 @@ def build_mex_stub(force: bool = False) -> str:
     return MEX_LIB
 
 
+BENCH_SRC = os.path.join(HERE, "bench", "mexct_bench.cpp")
+BENCH_BIN = os.path.join(BUILD, "mexct_bench")
+
+
+def build_bench(force: bool = False) -> str:
+    """The standalone C++ benchmark (bench/mexct_bench.cpp) against libmexct:
+    the C ABI and the CUDA runtime only (shared, as libmexct uses it)."""
+    lib = build(force=force)
+    deps = [BENCH_SRC, os.path.join(ROOT, "include", "mexct.h"), lib]
+    if (not force and os.path.exists(BENCH_BIN)
+            and os.path.getmtime(BENCH_BIN) >= max(os.path.getmtime(d) for d in deps)):
+        return BENCH_BIN
+    cmd = [nvcc(), "-O2", "-std=c++17", "-x", "c++", BENCH_SRC, "-o", BENCH_BIN + ".tmp",
+           "-I", os.path.join(ROOT, "include"), "-L", BUILD, "-lmexct", "-cudart", "shared",
+           "-Xlinker", "-rpath,$ORIGIN", "-Xlinker", "-rpath,/usr/local/cuda/lib64",
+           "-Xlinker", "-export-dynamic"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("C++ bench build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(BENCH_BIN + ".tmp", BENCH_BIN)
+    return BENCH_BIN
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
     print(build_mex_stub())
+    print(build_bench())

@@ -210,6 +210,12 @@ size_t tv_partials_needed(int Nx, int Ny, int Nz) {
   return (size_t)g.x * g.y * g.z;
 }
 
+bool tv_shape_launchable(int Nx, int Ny, int Nz) {
+  const long long gx = ((long long)Nx + kTvOx - 1) / kTvOx;
+  const long long gy = ((long long)Ny + kTvOy - 1) / kTvOy, gz = ((long long)Nz + kTvZ - 1) / kTvZ;
+  return gx <= 0x7fffffffLL && gy <= 65535 && gz <= 65535;
+}
+
 static cudaError_t tv_norm_go(const void* x, int xt, int Nx, int Ny, int Nz, float c,
                               const double* cmul, double* partials, unsigned* counter,
                               float* scale, double* norm, cudaStream_t st) {
@@ -273,6 +279,20 @@ __global__ void __launch_bounds__(256) ssd_kernel(
   const double blk = block_sum(ss);
   double total;
   if (finish_partials(blk, partials, counter, &total)) *out = sqrt(total);
+}
+
+__global__ void __launch_bounds__(1024) sum_partials_kernel(const double* __restrict__ p,
+                                                           long long n, double* __restrict__ out) {
+  double acc = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) acc += p[i];
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) *out = acc;
+}
+
+cudaError_t launch_sum_partials(const double* partials, long long n, double* out,
+                                cudaStream_t st) {
+  sum_partials_kernel<<<1, 1024, 0, st>>>(partials, n, out);
+  return cudaGetLastError();
 }
 
 int device_sms() {

@@ -859,7 +859,29 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     // wait for them (bounded) before the buffers are reused or the CTA exits.
     slab_drain(bar, issued, E.err);
   }
-  if (valid) {
+  if (EPI == 2) {
+    // Objective epilogue: sum of pre*e^-l + post*l over the tile in FP64
+    // (fixed order: warp shuffles, then the 8 warps in order).
+    __shared__ double wsum[8];
+    double t = 0.0;
+    if (valid) {
+      const float l = acc * J.step;
+      const size_t gi = (size_t)J.gview * J.P + (size_t)iy * J.det_w + ix;
+      const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
+      t = (double)(pv * expf(-l)) + (double)qv * (double)l;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((tid & 31) == 0) wsum[tid >> 5] = t;
+    __syncthreads();
+    if (tid == 0) {
+      double b = 0.0;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) b += wsum[w];
+      E.obj[(size_t)blockIdx.x * gridDim.y + blockIdx.y] = b;
+    }
+  }
+  if (EPI != 2 && valid) {
     const float l = acc * J.step;
     const size_t pix = (size_t)iy * J.det_w + ix;
     const size_t gi = (size_t)J.gview * J.P + pix;
@@ -1090,6 +1112,27 @@ cudaError_t launch_fp_slab_sub(int geom, const RayArgs& a, const CUtensorMap& mx
   if (geom == 2)
     return slab_go<2, false, 0, float, float, false, true>(a, mx, my, px, py, Pf, out, e, st);
   return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fp_slab_objective(int geom, const RayArgs& a, const CUtensorMap& mx,
+                                     const CUtensorMap& my, const void* px, const void* py,
+                                     int Pf, int vt, const SlabEpi& e, cudaStream_t st) {
+  if (!e.obj || !e.pre || !e.post) return cudaErrorInvalidValue;
+#define GO(G, TV) return slab_go<G, true, 2, TV, float>(a, mx, my, px, py, Pf, nullptr, e, st)
+  if (vt == kF32) {
+    if (geom == 0) GO(0, float);
+    if (geom == 1) GO(1, float);
+    GO(2, float);
+  }
+  if (vt == kF16) {
+    if (geom == 0) GO(0, __half);
+    if (geom == 1) GO(1, __half);
+    GO(2, __half);
+  }
+  if (geom == 0) GO(0, __nv_bfloat16);
+  if (geom == 1) GO(1, __nv_bfloat16);
+  GO(2, __nv_bfloat16);
+#undef GO
 }
 
 cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,

@@ -73,6 +73,7 @@ struct SlabEpi {
   float* rpost;      // [H+4][W+4] with a zero frame (border addressing)
   unsigned* err;     // set to non-zero when a bounded wait gave up
   int wait_us;       // limit of one wait: 0 = default (2 s), < 0 = give up at once
+  double* obj;       // objective epilogue: one FP64 partial sum per CTA
 };
 int slab_pitch(int W);
 // CTAs of the slab FP kernels resident per SM (its launch bounds); persistent
@@ -110,6 +111,17 @@ cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
 // kernel for projection geometry geom.
 cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype,
                            int Pf, int Ps, int Pz, int geom);
+// OSC forward pass (border addressing, step 0.5) of a padded mu whose epilogue
+// adds up the data-fidelity objective pre*e^-l + post*l of every detector
+// pixel of the views in FP64: one partial per CTA into e.obj at index
+// blockIdx.x * gridDim.y + blockIdx.y (views x tiles); nothing else is written.
+cudaError_t launch_fp_slab_objective(int geom, const RayArgs& a, const CUtensorMap& mx,
+                                     const CUtensorMap& my, const void* px, const void* py,
+                                     int Pf, int vt, const SlabEpi& e, cudaStream_t st);
+// Fixed-order FP64 sum of n partials into *out (one CTA; deterministic).
+cudaError_t launch_sum_partials(const double* partials, long long n, double* out,
+                                cudaStream_t st);
+
 cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
                            const CUtensorMap& mx, const CUtensorMap& my,
                            const void* px, const void* py, int Pf, int vt,
@@ -212,6 +224,9 @@ cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
 // per-thread level) and the
 // step scale -c/||g|| into *scale; tv_update writes y = x + scale*g(x).
 size_t tv_partials_needed(int Nx, int Ny, int Nz);
+// Whether the TV kernels' grid for this shape fits the launch limits
+// (gridDim.y and gridDim.z at most 65535).
+bool tv_shape_launchable(int Nx, int Ny, int Nz);
 // Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
 // cached per device): grid-stride kernels size their grids by it.
 int device_sms();

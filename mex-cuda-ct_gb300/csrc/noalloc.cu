@@ -18,11 +18,13 @@
 //     it until the process exits;
 //   - all calls share the array, so calls that overlap on the GPU (different
 //     streams, or different host threads, without ordering) race;
-//   - the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
+//   - every call looks up the array's device address (cudaGetSymbolAddress)
+//     with the caller's device current, so the address always belongs to the
+//     current context (after cudaDeviceReset, or with another context current
+//     on the device, a cached one would not); the first call on a device
+//     also loads the library's device code there, so make that first call
 //     before any stream capture.
 #include <cstdint>
-#include <mutex>
 
 #include "../../include/mexct.h"
 #include "api_internal.h"
@@ -41,9 +43,6 @@ constexpr size_t kScratchBytes = kOffScal + 256;
 // the device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_tv_noalloc_scratch[kScratchBytes];
 
-std::mutex g_addr_mu;
-void* g_addr[64] = {nullptr};  // device address of the scratch, per device
-
 }  // namespace
 
 extern "C" mexct_status mexct_tvmin3d_dev_noalloc(const float* d_vol, int Nx,
@@ -60,26 +59,21 @@ extern "C" mexct_status mexct_tvmin3d_dev_noalloc(const float* d_vol, int Nx,
                    "tvmin3d_noalloc: %d x %d x %d = %zu voxels exceeds the fixed scratch "
                    "limit of %zu voxels; use mexct_tvmin3d_dev",
                    Nx, Ny, Nz, N, kMaxVoxels);
+  if (!tv_shape_launchable(Nx, Ny, Nz))
+    return set_err(MEXCT_ERR_UNSUPPORTED,
+                   "tvmin3d_noalloc: %d x %d x %d exceeds the launch grid limits (at most "
+                   "65535 tiles of %d rows in y and of %d slices in z)",
+                   Nx, Ny, Nz, 15, 32);
   const size_t parts = tv_partials_needed(Nx, Ny, Nz);
   if (parts > kMaxPartials)
     return set_err(MEXCT_ERR_UNSUPPORTED,
                    "tvmin3d_noalloc: shape %d x %d x %d needs %zu reduction partials, "
                    "the fixed scratch holds %zu",
                    Nx, Ny, Nz, parts, kMaxPartials);
-  int dev = -1;
-  MEXCT_TRY_CUDA(cudaGetDevice(&dev), "tvmin3d_noalloc: current device");
-  if (dev < 0 || dev >= 64) return set_err(MEXCT_ERR_UNSUPPORTED, "tvmin3d_noalloc: device %d", dev);
-  unsigned char* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_addr_mu);
-    if (!g_addr[dev]) {
-      void* p = nullptr;
-      MEXCT_TRY_CUDA(cudaGetSymbolAddress(&p, g_tv_noalloc_scratch),
-                     "tvmin3d_noalloc: scratch address");
-      g_addr[dev] = p;
-    }
-    base = static_cast<unsigned char*>(g_addr[dev]);
-  }
+  void* addr = nullptr;
+  MEXCT_TRY_CUDA(cudaGetSymbolAddress(&addr, g_tv_noalloc_scratch),
+                 "tvmin3d_noalloc: scratch address");
+  unsigned char* base = static_cast<unsigned char*>(addr);
   float* pong = reinterpret_cast<float*>(base);
   double* partials = reinterpret_cast<double*>(base + kOffPart);
   unsigned* counter = reinterpret_cast<unsigned*>(base + kOffCnt);

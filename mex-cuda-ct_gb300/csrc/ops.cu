@@ -568,6 +568,9 @@ mexct_status tv_dev_impl(mexct_ctx* c, const void* d_in, int t, int Nx,
   if (Nx <= 0 || Ny <= 0 || Nz <= 0) return set_err(MEXCT_ERR_ARG, "tvmin3d: bad dims");
   if (n_steps < 0) return set_err(MEXCT_ERR_ARG, "tvmin3d: n_steps < 0");
   if (bad_type(t)) return set_err(MEXCT_ERR_ARG, "tvmin3d: bad storage type");
+  if (!tv_shape_launchable(Nx, Ny, Nz))
+    return set_err(MEXCT_ERR_UNSUPPORTED, "tvmin3d: %d x %d x %d exceeds the launch grid limits",
+                   Nx, Ny, Nz);
   if (!c) return MEXCT_OK;  // validate only
   const size_t N = (size_t)Nx * Ny * Nz;
   const size_t bytes = N * dsize(t);

@@ -17,6 +17,7 @@
 // instead of ~70 kernel launches per iteration.
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <vector>
@@ -34,9 +35,10 @@ struct mexct_osctv {
   int W = 0, H = 0, nP = 0, geom = 0, mu_type = kF32;
   float sad = 0.f;
   std::vector<float> angles;
-  Buf mu, mu_old, pre, post, padx, pady, err, r1, r2, tvbuf, red, cnt, scal;
+  Buf mu, mu_old, pre, post, padx, pady, err, r1, r2, tvbuf, red, cnt, scal, objp;
   int k_done = 0;
   bool pre_zeroed = false;
+  bool obj_valid = false;  // the last iteration computed the objective
   struct Key {
     int k_gt1, nsub, use_obj;
     float tvc;
@@ -56,7 +58,8 @@ struct mexct_osctv {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   ~mexct_osctv() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
-    for (Buf* b : {&mu, &mu_old, &pre, &post, &padx, &pady, &err, &r1, &r2, &tvbuf, &red, &cnt, &scal})
+    for (Buf* b : {&mu, &mu_old, &pre, &post, &padx, &pady, &err, &r1, &r2, &tvbuf, &red, &cnt, &scal,
+                   &objp})
       b->release();  // stream-ordered on `own`, after all its work
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
@@ -67,6 +70,9 @@ struct mexct_osctv {
   // Scalars on the device: [0] d_a (double), [1] TV scale (float, as double
   // slot), [2] ||g|| (double), [3] objective (double).
   double* d_a() { return scal.as<double>(); }
+  double* objective() { return scal.as<double>() + 3; }
+  // Detector tiles of one view in the slab FP (32 x 8 pixels each).
+  int tiles() const { return ((W + 31) / 32) * ((H + 7) / 8); }
   float* tv_scale() { return reinterpret_cast<float*>(scal.as<double>() + 1); }
   double* tv_norm() { return scal.as<double>() + 2; }
 };
@@ -106,8 +112,40 @@ bool subset_order(int n, int first, int32_t* picks) {
   return true;
 }
 
+// The FP64 data-fidelity objective sum(pre*e^-l + post*l) over every view
+// and pixel, with l the OSC forward pass (border, step 0.5) of the current mu
+// (the Poisson negative log-likelihood up to a constant; the reference has no
+// counterpart).  One FP of all views, its epilogue reducing per CTA; the
+// partials are summed in a fixed order into the objective scalar.
+mexct_status enqueue_objective(mexct_osctv* s, cudaStream_t st) {
+  CUtensorMap mx, my;
+  int Pf = 0;
+  mexct_status ps = prepare_slab_bufs(s->padx, s->pady, s->err, s->mu.p, s->mu_type, s->W, s->H,
+                                      /*border=*/true, s->geom, &mx, &my, &Pf, st);
+  if (ps) return ps;
+  std::unique_ptr<RayArgs> ra(new RayArgs);
+  fill_std_rays(*ra, s->W, s->H, s->sad, s->geom, /*osc=*/true);
+  const int tiles = s->tiles();
+  for (int v0 = 0; v0 < s->nP; v0 += kMaxViews) {
+    const int nv = std::min(kMaxViews, s->nP - v0);
+    ra->nviews = nv;
+    ra->view0 = v0;
+    ra->vstride = 1;
+    for (int i = 0; i < nv; ++i) trig_of(s->angles[v0 + i], &ra->trig[i]);
+    SlabEpi e{s->pre.as<float>(), s->post.as<float>(), nullptr, nullptr, s->err.as<unsigned>()};
+    e.obj = s->objp.as<double>() + (size_t)v0 * tiles;
+    MEXCT_TRY_CUDA(launch_fp_slab_objective(s->geom, *ra, mx, my, s->padx.p, s->pady.p, Pf,
+                                            s->mu_type, e, st),
+                   "osctv: objective fp");
+  }
+  MEXCT_TRY_CUDA(launch_sum_partials(s->objp.as<double>(), (long long)s->nP * tiles,
+                                     s->objective(), st),
+                 "osctv: objective sum");
+  return MEXCT_OK;
+}
+
 mexct_status enqueue_iteration(mexct_osctv* s, bool k_gt1, int nsub,
-                               const int32_t* picks, float tvc,
+                               const int32_t* picks, float tvc, bool objective,
                                cudaStream_t st) {
   const size_t N = s->N();
   const size_t P = (size_t)s->W * s->H;
@@ -166,6 +204,7 @@ mexct_status enqueue_iteration(mexct_osctv* s, bool k_gt1, int nsub,
     }
     MEXCT_TRY_CUDA(launch_finite(s->mu.p, s->mu_type, (long long)N, st), "osctv: finite");
   }
+  if (objective) return enqueue_objective(s, st);
   return MEXCT_OK;
 }
 
@@ -242,6 +281,8 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   MEXCT_TRY_CUDA(s->err.ensure_async(64, a), "osctv_create: error word");
   MEXCT_TRY_CUDA(s->cnt.ensure_async(64, a), "osctv_create: counter");
   MEXCT_TRY_CUDA(s->scal.ensure_async(64, a), "osctv_create: scalars");
+  MEXCT_TRY_CUDA(s->objp.ensure_async((size_t)nP * s->tiles() * sizeof(double), a),
+                 "osctv_create: objective partials");
   MEXCT_TRY_CUDA(cudaMemsetAsync(s->err.p, 0, 64, a), "osctv_create: error word");
   MEXCT_TRY_CUDA(cudaMemsetAsync(s->cnt.p, 0, 64, a), "osctv_create: counter");
   MEXCT_TRY_CUDA(cudaMemsetAsync(s->scal.p, 0, 64, a), "osctv_create: scalars");
@@ -268,6 +309,10 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
               s->err.as<unsigned>()};
     MEXCT_TRY_CUDA(launch_fp_slab(geom, true, true, *ra, mx, my, s->padx.p, s->pady.p, Pf,
                                   mu_type, nullptr, kF32, e, st),
+                   "osctv_create: kernel setup");
+    e.obj = s->objp.as<double>();
+    MEXCT_TRY_CUDA(launch_fp_slab_objective(geom, *ra, mx, my, s->padx.p, s->pady.p, Pf, mu_type,
+                                            e, st),
                    "osctv_create: kernel setup");
   }
   *out = s.release();
@@ -307,7 +352,8 @@ mexct_status mexct_osctv_run(mexct_osctv* s, const mexct_osctv_params* p,
         cudaGraph_t g = nullptr;
         MEXCT_TRY_CUDA(cudaStreamBeginCapture(s->own, cudaStreamCaptureModeThreadLocal),
                        "osctv_run: begin capture");
-        mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const, s->own);
+        mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const,
+                                           p->objective != 0, s->own);
         cudaError_t ce = cudaStreamEndCapture(s->own, &g);
         if (e != MEXCT_OK) {
           if (g) cudaGraphDestroy(g);
@@ -326,10 +372,12 @@ mexct_status mexct_osctv_run(mexct_osctv* s, const mexct_osctv_params* p,
       MEXCT_TRY_CUDA(cudaEventRecord(s->ev_out, s->own), "osctv_run: join");
       MEXCT_TRY_CUDA(cudaStreamWaitEvent(st, s->ev_out, 0), "osctv_run: join");
     } else {
-      mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const, st);
+      mexct_status e = enqueue_iteration(s, kg1, nsub, picks.data(), p->tv_const,
+                                         p->objective != 0, st);
       if (e != MEXCT_OK) return e;
     }
     s->k_done = k;
+    s->obj_valid = p->objective != 0;
   }
   return MEXCT_OK;
 }
@@ -350,7 +398,7 @@ mexct_status mexct_osctv_stats(mexct_osctv* s, int* iters, double* d_a, double* 
   MEXCT_TRY_CUDA(cudaMemcpy(h, s->scal.p, sizeof h, cudaMemcpyDeviceToHost), "osctv_stats");
   if (iters) *iters = s->k_done;
   if (d_a) *d_a = h[0];
-  if (obj) *obj = std::nan("");
+  if (obj) *obj = s->obj_valid ? h[3] : std::nan("");
   return MEXCT_OK;
 }
 

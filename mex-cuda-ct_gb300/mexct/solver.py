@@ -86,11 +86,14 @@ class OscTvSolver:
         self.h = h
 
     def run(self, first_picks, n_iter, tv_const, n_sub_init, n_sub_final, p_val, use_graph=True,
-            count=None):
+            count=None, objective=False):
+        """Run iterations; first_picks holds one first subset per iteration of this
+        call.  objective: also compute the FP64 data-fidelity objective
+        sum(pre e^-l + post l) of mu after each iteration (see stats())."""
         fp = np.ascontiguousarray(np.asarray(first_picks, dtype=np.int32).ravel())
         count = fp.size if count is None else int(count)
         p = Params(int(n_iter), float(tv_const), int(n_sub_init), int(n_sub_final), float(p_val),
-                   1 if use_graph else 0, 0)
+                   1 if use_graph else 0, 1 if objective else 0)
         _lib.call("mexct_osctv_run", self.h, ctypes.byref(p), _ptr(fp), count,
                   _P(self.stream.cuda_stream))
 
@@ -100,9 +103,11 @@ class OscTvSolver:
         return out
 
     def stats(self):
+        """(iterations run, last d_a, last objective or NaN when the last
+        iteration did not compute it)."""
         it, da, ob = _i(), _d(), _d()
         _lib.call("mexct_osctv_stats", self.h, ctypes.byref(it), ctypes.byref(da), ctypes.byref(ob))
-        return it.value, da.value
+        return it.value, da.value, ob.value
 
     def snapshot(self):
         n = _lib.load().mexct_osctv_state_bytes(self.h)

@@ -70,6 +70,7 @@ def _load():
             "orc_g3d_bp": [F, i, i, i, F, F, i, i, i, D],
             "orc_osc_iter": [D, F, F, i, i, i, i, I32, F, f, i],
             "orc_tvmin3d": [D, i, i, i, d, i],
+            "orc_osc_fp": [D, i, i, f, F, i, i, D],
             "orc_tv_gradient": [D, i, i, i, D],
             "orc_num_subsets": [i, i, d, i, i],
             "orc_subset_order": [i, i, I32],
@@ -335,6 +336,18 @@ def osc_tv(pre, post, angles, sad, geom, n_iter, tv_const, n_sub_init, n_sub_fin
                           float(tv_const), int(n_sub_init), int(n_sub_final), float(p_val),
                           _p(fp_, ctypes.c_int32), _p(mu, ctypes.c_double), cb, None), "osc_tv")
     return mu
+
+
+def osc_fp(mu, sad, angles, geom):
+    """The OSC forward pass (step 0.5, border addressing, CUDAmex_oscIter.cu:
+    140-259) of mu [W,W,H] -> [W,H,nP] (float64)."""
+    mu = np.asfortranarray(np.asarray(mu, dtype=np.float64))
+    W, H = mu.shape[0], mu.shape[2]
+    ang = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).ravel())
+    out = np.zeros((W, H, ang.size), dtype=np.float64, order="F")
+    _check(_load().orc_osc_fp(_p(mu, ctypes.c_double), W, H, float(sad), _p(ang, ctypes.c_float),
+                              ang.size, int(geom), _p(out, ctypes.c_double)), "osc_fp")
+    return out
 
 
 def filter_response(W, filt="ramp", cutoff=1.0):

@@ -796,6 +796,30 @@ int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
   return 0;
 }
 
+// The OSC forward pass alone (CUDAmex_oscIter.cu:140-259): every geometry
+// with step 0.5 and border addressing.  mu [W,W,H] (FP64) -> out [W,H,nP].
+int orc_osc_fp(const double* mu, int W, int H, float sad, const float* angles,
+               int nP, int geom, double* out) {
+  if (!mu || !angles || !out || W <= 0 || H <= 0 || nP < 0) return 1;
+  if (geom < 0 || geom > 2) return 1;
+  const float u0 = float(W - 1) / 2, v0 = float(H - 1) / 2;
+  const float bx = -(float)W / 2.0f, by = bx, bz = -(float)H / 2.0f;
+  const float step = 0.5f;
+  const long long P = (long long)W * H;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
+  for (long long r = 0; r < P * nP; ++r) {
+    const int view = (int)(r / P);
+    const int pix = (int)(r % P);
+    float sb, cb;
+    trig(angles[view], &sb, &cb);
+    float s[3], e[3];
+    std_ray(geom, pix % W, pix / W, u0, v0, sb, cb, sad, sad, s, e);
+    const Ray ray = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], bx, by, bz, step);
+    out[r] = march(ray, step, mu, W, W, H, bx, by, bz, true);
+  }
+  return 0;
+}
+
 int orc_tv_gradient(const double* in, int Nx, int Ny, int Nz, double* out) {
   if (!in || !out || Nx <= 0 || Ny <= 0 || Nz <= 0) return 1;
   const size_t sx = 1, sy = (size_t)Nx, sz = (size_t)Nx * Ny;

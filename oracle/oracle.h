@@ -74,6 +74,11 @@ int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
                  int H, int nP, int nSub, const int32_t* picks,
                  const float* angles, float sad, int geom);
 
+/* The OSC forward pass alone (CUDAmex_oscIter.cu:140-259): step 0.5 for
+ * every geometry, border addressing.  mu [W,W,H] -> out [W,H,nP]. */
+int orc_osc_fp(const double* mu, int W, int H, float sad, const float* angles,
+               int nP, int geom, double* out);
+
 /* TV descent (CUDAmex_TVmin_3D.cu:101-234): n_steps of
  * x <- x - (c/||g||) g with the reference's 13-point TV gradient; border
  * voxels have g = 0.  vol is updated in place. */
