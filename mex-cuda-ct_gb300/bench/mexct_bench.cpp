@@ -211,6 +211,7 @@ int main(int argc, char** argv) {
       "cudaMalloc buffers)\", \"e2e\": {\"value\": %.3f, \"unit\": \"GUPS\", \"h2d_bytes_per_step\": "
       "%zu, \"d2h_bytes_per_step\": %zu, \"path\": \"mexct_fp + mexct_bp, pinned host buffers\"}}\n",
       n, views, geom, gups, steps, warmup, ms / steps, fp_ms, bp_ms, e2e, 4 * (N + S), 4 * (S + N));
+  std::fflush(stdout);
   g_stage = "clean-up";
   cudaFreeHost(h_vol);
   cudaFreeHost(h_sino);

@@ -56,18 +56,45 @@ void Buf::release() {
   is_async = false;
 }
 
+void Buf::release_synced() {
+  if (p && is_async) {
+    cudaDeviceSynchronize();
+    cudaFreeAsync(p, cudaStreamLegacy);
+    cudaStreamSynchronize(cudaStreamLegacy);
+    p = nullptr;
+    n = 0;
+    ast = nullptr;
+    is_async = false;
+    cudaGetLastError();
+    return;
+  }
+  release();
+}
+
 cudaError_t Buf::ensure_async(size_t bytes, cudaStream_t st) {
   if (bytes <= n && p) return cudaSuccess;
   if (p && is_async && ast != st) {
-    // The old block is freed on st once the work queued on its own stream
-    // is done.
-    cudaEvent_t ev = nullptr;
-    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess) {
-      cudaEventRecord(ev, ast);
-      cudaStreamWaitEvent(st, ev, 0);
-      cudaEventDestroy(ev);
+    // The old block was allocated on another stream, which may be a caller's
+    // stream that no longer exists.  Outside a stream capture it is freed
+    // after the device has finished all its work; inside a capture (where the
+    // device cannot be synchronised) the old stream is taken to be alive and
+    // st waits for the work queued on it.
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      cs = cudaStreamCaptureStatusNone;
     }
-    ast = st;
+    if (cs == cudaStreamCaptureStatusNone) {
+      release_synced();
+    } else {
+      cudaEvent_t ev = nullptr;
+      if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess) {
+        cudaEventRecord(ev, ast);
+        cudaStreamWaitEvent(st, ev, 0);
+        cudaEventDestroy(ev);
+      }
+      ast = st;
+    }
   }
   release();
   if (bytes == 0) bytes = 16;
@@ -214,7 +241,8 @@ mexct_status mexct_ctx_trim(mexct_ctx* c) {
   if (!c) return set_err(MEXCT_ERR_ARG, "ctx_trim: NULL context");
   std::lock_guard<std::recursive_mutex> lk(c->mu);
   cudaStreamSynchronize(c->stream);
-  for (Buf* b : c->all_bufs()) b->release();
+  // Workspaces may have been allocated on caller streams that are gone by now.
+  for (Buf* b : c->all_bufs()) b->release_synced();
   if (c->tex) {
     cudaDestroyTextureObject(c->tex);
     c->tex = 0;

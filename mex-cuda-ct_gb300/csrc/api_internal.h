@@ -31,7 +31,13 @@ struct Buf {
   // synchronisation on allocation or release, so work on other streams keeps
   // running.  The buffer is released with cudaFreeAsync on the same stream.
   cudaError_t ensure_async(size_t bytes, cudaStream_t st);
+  // Free in the order of the stream the block was allocated on (that stream
+  // must still exist: the owner's own stream).
   void release();
+  // Free after all work on the device has finished, whatever stream the block
+  // was allocated on: for context workspaces, whose allocation stream may be
+  // a caller's stream that no longer exists.  Synchronises the device.
+  void release_synced();
   template <typename T>
   T* as() const {
     return static_cast<T*>(p);
