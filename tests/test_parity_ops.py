@@ -205,6 +205,26 @@ def test_tvmin3d_matches_oracle(cuda, orc, shape):
     assert rel_l2(got, ref) <= TOL
 
 
+@pytest.mark.parametrize("shape", [(124, 15, 33), (248, 31, 65), (128, 16, 32), (36, 20, 17),
+                                   (123, 15, 33)])
+def test_tv_steps_match_oracle_at_tile_edges(cuda, orc, shape):
+    """One and two TV steps on shapes at the tiles' edges: the four-voxel kernel
+    (x extent a multiple of 4: tiles of 124 x 15 outputs, the last lane and row
+    only supplying neighbour terms) and the scalar one (odd x extent) against the
+    FP64 oracle.  Over 20 steps the descent's normalised step amplifies rounding
+    (2e-6 .. 3e-5 on these thin shapes), so the steps are checked one by one."""
+    import torch
+    from mexct import ops, phantoms
+
+    nx, ny, nz = shape
+    v = phantoms.ellipsoids(max(nx, ny), count=5, seed=3, nz=nz)[:nx, :ny, :]
+    v = np.asfortranarray(v + np.random.default_rng(2).normal(0, 2e-3, v.shape).astype(np.float32))
+    d = torch.from_numpy(np.ascontiguousarray(v.transpose(2, 1, 0))).cuda()
+    for steps in (1, 2):
+        got = ops.tvmin3d_dev(d, 0.03, steps).cpu().numpy().transpose(2, 1, 0)
+        assert rel_l2(got, orc.tvmin3d(v, 0.03, steps)) <= 2e-7, steps
+
+
 @pytest.mark.parametrize("geom", [0, 1, 2])
 @pytest.mark.parametrize("filt", ["ramp", "hamming", "shepp-logan"])
 def test_prefilter_matches_oracle(cuda, orc, geom, filt):
