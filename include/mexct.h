@@ -164,6 +164,22 @@ mexct_status mexct_g3d_bp_dev(mexct_ctx* ctx, const float* d_sino, int W,
                               int H, int nP, const float* angles,
                               const float* d_pts, int pts_per_view, int S,
                               int Z, float* d_vol, void* stream);
+
+/* Matched-adjoint general3D BP (no counterpart in the reference: its BP,
+ * CUDAmex_general3D_BP.cu:61-188, deposits into two corners with shifted
+ * weights and is not the transpose of its FP; its eight-corner form is left
+ * commented out at :172-179).  The exact transpose of mexct_g3d_fp of this
+ * library: the same rays and FP32 sample positions, the eight trilinear taps
+ * of each sample, p*0.5*w into each tap inside the volume, so that
+ * <g3d_fp(x), y> = <x, g3d_bp_matched(y)> up to FP32 rounding (what iterative
+ * solvers with a gradient need).  Arguments as mexct_g3d_bp / _dev. */
+mexct_status mexct_g3d_bp_matched(mexct_ctx* ctx, const float* sino, int W, int H,
+                                  int nP, const float* angles, const float* pts,
+                                  int pts_per_view, int S, int Z, float* vol);
+mexct_status mexct_g3d_bp_matched_dev(mexct_ctx* ctx, const float* d_sino, int W,
+                                      int H, int nP, const float* angles,
+                                      const float* d_pts, int pts_per_view, int S,
+                                      int Z, float* d_vol, void* stream);
 mexct_status mexct_osc_iter_dev(mexct_ctx* ctx, float* d_mu,
                                 const float* d_pre, const float* d_post,
                                 int W, int H, int nP, int nSub,

@@ -830,6 +830,100 @@ __global__ void __launch_bounds__(256) g3d_bp_kernel(
   }
 }
 
+// ---------------------------------------------------------------------------
+// Matched-adjoint general3D BP (no counterpart in the reference, whose BP is a
+// two-corner scatter that is not the transpose of its FP; the eight-corner form
+// left commented out at CUDAmex_general3D_BP.cu:172-179 points this way).  The
+// exact transpose of the general3D FP of this library (the slab kernel, border
+// addressing, step 0.5): the same rays and the same FP32 sample positions
+// fma(k, d, t0) in tap space, the eight trilinear taps of each sample, and
+// p * step * w added to each tap voxel inside the volume (frame taps, which
+// the FP reads as zeros, are dropped).  A run of samples in the same cell is
+// summed in registers and lands in one atomic per corner.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void adj_flush(float* __restrict__ vol, int S, int Z, int ci, int cj,
+                                          int ck, const float (&w)[8]) {
+  // ci, cj, ck: lower tap in padded (voxel + 1) coordinates
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const int i = ci + (t & 1) - 1, j = cj + ((t >> 1) & 1) - 1, k = ck + (t >> 2) - 1;
+    if (w[t] != 0.f && i >= 0 && i < S && j >= 0 && j < S && k >= 0 && k < Z)
+      atomicAdd(vol + (size_t)i + (size_t)S * ((size_t)j + (size_t)S * k), w[t]);
+  }
+}
+
+__global__ void __launch_bounds__(256) g3d_bp_adjoint_kernel(
+    const __grid_constant__ RayArgs A, const float* __restrict__ sino,
+    const float* __restrict__ pts, float* __restrict__ vol) {
+  const int view = blockIdx.x;
+  const int tiles_u = (A.det_w + 31) >> 5;
+  const int ix = (blockIdx.y % tiles_u) * 32 + threadIdx.x;
+  const int iy = (blockIdx.y / tiles_u) * blockDim.y + threadIdx.y;
+  if (ix >= A.det_w || iy >= A.det_h) return;
+  const float p = __ldg(sino + (size_t)(A.view0 + view * A.vstride) * A.P +
+                        (size_t)iy * A.det_w + ix);
+  if (p == 0.f) return;
+  const Ray r = make_ray<3>(A, view, ix, iy, pts);
+  const int S = A.S, Z = A.Z;
+  // tap space: padded coordinate minus 0.5 = world - b + 0.5 (as the slab FP)
+  const float tx0 = (r.cx - A.bx) + 0.5f, ty0 = (r.cy - A.by) + 0.5f, tz0 = (r.cz - A.bz) + 0.5f;
+  // samples whose taps can touch the padded volume: t in [0, P - 1) per axis
+  float klo = 0.f, khi = (float)r.n;
+  auto clampk = [&](float t0, float d, float hi) {
+    if (d == 0.f) {
+      if (!(t0 >= 0.f && t0 < hi)) khi = -1.f;
+    } else {
+      const float k1 = (0.f - t0) / d, k2 = (hi - t0) / d;
+      klo = fmaxf(klo, fminf(k1, k2));
+      khi = fminf(khi, fmaxf(k1, k2));
+    }
+  };
+  clampk(tx0, r.dx, (float)(S + 1));
+  clampk(ty0, r.dy, (float)(S + 1));
+  clampk(tz0, r.dz, (float)(Z + 1));
+  if (!(khi >= klo)) return;
+  const int k0 = max((int)floorf(klo) - 1, 0), k1 = min((int)ceilf(khi) + 1, r.n);
+  const float ps = p * A.step;
+  float w[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  int ci = -1000000, cj = 0, ck = 0;
+  for (int k = k0; k < k1; ++k) {
+    const float kf = (float)k;
+    const float tx = fmaf(kf, r.dx, tx0), ty = fmaf(kf, r.dy, ty0), tz = fmaf(kf, r.dz, tz0);
+    const float fx = floorf(tx), fy = floorf(ty), fz = floorf(tz);
+    const int i = (int)fx, j = (int)fy, l = (int)fz;
+    if (i < -1 || i > S || j < -1 || j > S || l < -1 || l > Z) continue;  // all taps outside
+    if (i != ci || j != cj || l != ck) {
+      if (ci != -1000000) adj_flush(vol, S, Z, ci, cj, ck, w);
+#pragma unroll
+      for (int t = 0; t < 8; ++t) w[t] = 0.f;
+      ci = i;
+      cj = j;
+      ck = l;
+    }
+    const float ax = tx - fx, ay = ty - fy, az = tz - fz;
+    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
+    const float p00 = ps * by * bz, p10 = ps * ay * bz, p01 = ps * by * az, p11 = ps * ay * az;
+    w[0] = fmaf(bx, p00, w[0]);
+    w[1] = fmaf(ax, p00, w[1]);
+    w[2] = fmaf(bx, p10, w[2]);
+    w[3] = fmaf(ax, p10, w[3]);
+    w[4] = fmaf(bx, p01, w[4]);
+    w[5] = fmaf(ax, p01, w[5]);
+    w[6] = fmaf(bx, p11, w[6]);
+    w[7] = fmaf(ax, p11, w[7]);
+  }
+  if (ci != -1000000) adj_flush(vol, S, Z, ci, cj, ck, w);
+}
+
+cudaError_t launch_g3d_bp_adjoint(const RayArgs& a, const float* sino, const float* pts,
+                                  float* vol, cudaStream_t st) {
+  if (a.nviews <= 0) return cudaSuccess;
+  const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
+  dim3 blk(32, 8), grd(a.nviews, tiles);
+  g3d_bp_adjoint_kernel<<<grd, blk, 0, st>>>(a, sino, pts, vol);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
                           const float* pts, float* vol, cudaStream_t st) {
   if (a.nviews <= 0) return cudaSuccess;

@@ -207,6 +207,10 @@ cudaError_t launch_add_scaled(const float* src, float* dst, long long n, float w
                               cudaStream_t st);
 
 // general3D ray-driven two-corner scatter BP (CUDAmex_general3D_BP.cu:61-188).
+// Matched-adjoint general3D BP: the transpose of the general3D slab FP
+// (accumulates into vol; no counterpart in the reference).
+cudaError_t launch_g3d_bp_adjoint(const RayArgs& a, const float* sino, const float* pts,
+                                  float* vol, cudaStream_t st);
 cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
                           const float* pts, float* vol, cudaStream_t st);
 

@@ -485,6 +485,28 @@ mexct_status g3d_bp_dev_impl(mexct_ctx* c, const float* d_sino, int W, int H,
   return MEXCT_OK;
 }
 
+// Matched-adjoint general3D BP: the transpose of g3d_fp_dev_impl.
+mexct_status g3d_bp_matched_impl(mexct_ctx* c, const float* d_sino, int W, int H, int nP,
+                                 const float* angles, const float* d_pts, int per_view, int S,
+                                 int Z, float* d_vol, cudaStream_t st) {
+  if (!d_sino || !d_pts || !d_vol || (!angles && nP > 0))
+    return set_err(MEXCT_ERR_ARG, "g3d_bp_matched: NULL pointer");
+  if (bad_dims(S, Z) || bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "g3d_bp_matched: bad dims");
+  if (nP < 0) return set_err(MEXCT_ERR_ARG, "g3d_bp_matched: bad view count %d", nP);
+  if (!c) return MEXCT_OK;  // validate only
+  MEXCT_TRY_CUDA(cudaMemsetAsync(d_vol, 0, (size_t)S * S * Z * sizeof(float), st),
+                 "g3d_bp_matched: zero");
+  std::unique_ptr<RayArgs> a(new RayArgs);
+  fill_g3d(*a, S, Z, W, H, per_view ? 1 : 0);
+  for (int v0 = 0; v0 < nP; v0 += kMaxViews) {
+    a->nviews = std::min(kMaxViews, nP - v0);
+    a->view0 = v0;
+    for (int i = 0; i < a->nviews; ++i) trig_of(angles[v0 + i], &a->trig[i]);
+    MEXCT_TRY_CUDA(launch_g3d_bp_adjoint(*a, d_sino, d_pts, d_vol, st), "g3d_bp_matched: launch");
+  }
+  return MEXCT_OK;
+}
+
 // ---------------------------------------------------------------------------
 // OSC iteration (CUDAmex_oscIter.cu:504-557): per subset, the fused FP +
 // residual over the subset's views, then the fused dual BP + update.
@@ -1028,6 +1050,35 @@ mexct_status mexct_g3d_bp_dev(mexct_ctx* ctx, const float* d_sino, int W,
   CTX_OR_FAIL(c, "g3d_bp");
   return g3d_bp_dev_impl(c, d_sino, W, H, nP, angles, d_pts, per_view, S, Z, d_vol,
                          as_stream(stream));
+}
+
+mexct_status mexct_g3d_bp_matched_dev(mexct_ctx* ctx, const float* d_sino, int W, int H,
+                                      int nP, const float* angles, const float* d_pts,
+                                      int per_view, int S, int Z, float* d_vol, void* stream) {
+  VALIDATE(g3d_bp_matched_impl(nullptr, d_sino, W, H, nP, angles, d_pts, per_view, S, Z, d_vol,
+                               nullptr));
+  CTX_OR_FAIL(c, "g3d_bp_matched");
+  return g3d_bp_matched_impl(c, d_sino, W, H, nP, angles, d_pts, per_view, S, Z, d_vol,
+                             as_stream(stream));
+}
+
+mexct_status mexct_g3d_bp_matched(mexct_ctx* ctx, const float* sino, int W, int H, int nP,
+                                  const float* angles, const float* pts, int per_view, int S,
+                                  int Z, float* vol) {
+  VALIDATE(g3d_bp_matched_impl(nullptr, sino, W, H, nP, angles, pts, per_view, S, Z, vol,
+                               nullptr));
+  CTX_OR_FAIL(c, "g3d_bp_matched");
+  const size_t N = (size_t)S * S * Z, M = (size_t)W * H * nP;
+  const size_t npts = (size_t)W * H * 6 * (per_view ? nP : 1);
+  mexct_status s = upload(c->in, sino, M * 4, c->stream, "g3d_bp_matched: upload");
+  if (s) return s;
+  s = upload(c->in2, pts, npts * 4, c->stream, "g3d_bp_matched: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "g3d_bp_matched: workspace");
+  s = g3d_bp_matched_impl(c, c->in.as<float>(), W, H, nP, angles, c->in2.as<float>(), per_view,
+                          S, Z, c->out.as<float>(), c->stream);
+  if (s) return s;
+  return finish(c, vol, c->out, N * 4, "g3d_bp_matched: download");
 }
 
 mexct_status mexct_g3d_bp(mexct_ctx* ctx, const float* sino, int W, int H,

@@ -13,5 +13,6 @@ from .ops import (  # noqa: F401
     CUDAmex_oscIter,
     CUDAmex_TVmin_3D,
     FBP_recon,
+    general3D_BP_matched,
     preFilterSinogram,
 )

@@ -149,6 +149,26 @@ def CUDAmex_general3D_BP(sino, angles, pts, M, N):
     return out
 
 
+def general3D_BP_matched(sino, angles, pts, M, N):
+    """The transpose of CUDAmex_general3D_FP (no counterpart in the reference):
+    eight-corner trilinear scatter at the FP's own sample positions, so that
+    <FP(x), y> = <x, BP(y)> up to FP32 rounding.  Same arguments as
+    CUDAmex_general3D_BP -> float32 [M, M, N]."""
+    sino = _f32F(sino, "projections")
+    if sino.ndim == 2:
+        sino = sino[:, :, None]
+    W, H, nP = sino.shape
+    pts, per_view = _pts(pts)
+    if pts.shape[:2] != (W, H):
+        raise ValueError("pts is %s, projections are %s" % (pts.shape[:2], (W, H)))
+    ang = _angles(angles, nP)
+    S, Z = int(_scalar(M, "M")), int(_scalar(N, "N"))
+    out = np.empty((S, S, Z), dtype=np.float32, order="F")
+    _lib.call("mexct_g3d_bp_matched", None, _ptr(sino), W, H, nP, _ptr(ang), _ptr(pts), per_view,
+              S, Z, _ptr(out))
+    return out
+
+
 def CUDAmex_oscIter(mu, pre, post, numSubsets, subsetPicks, angles, SAD, geomFlag):
     """CUDAmex_oscIter(mu, pre, post, nSub, subsetPicks, angles, SAD, geomFlag).
 
@@ -391,6 +411,19 @@ def g3d_bp_dev(sino, angles, pts, S, Z, out=None, stream=None):
         out = torch.empty((Z, S, S), dtype=torch.float32, device=sino.device)
     _lib.call("mexct_g3d_bp_dev", None, _dptr(sino), W, H, nP, _ptr(ang), _dptr(pts), per_view,
               int(S), int(Z), _dptr(out), _stream(stream))
+    return out
+
+
+def g3d_bp_matched_dev(sino, angles, pts, S, Z, out=None, stream=None):
+    """Device form of general3D_BP_matched: sino (nP, H, W) -> (Z, S, S)."""
+    import torch
+    nP, H, W = sino.shape
+    ang = _angles(angles, nP)
+    per_view = 1 if pts.dim() == 4 else 0
+    if out is None:
+        out = torch.empty((Z, S, S), dtype=torch.float32, device=sino.device)
+    _lib.call("mexct_g3d_bp_matched_dev", None, _dptr(sino), W, H, nP, _ptr(ang), _dptr(pts),
+              per_view, int(S), int(Z), _dptr(out), _stream(stream))
     return out
 
 

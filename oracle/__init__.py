@@ -68,6 +68,7 @@ def _load():
             "orc_bp_det": [F, i, i, i, f, F, i, i, i, f, f, D],
             "orc_g3d_fp": [F, i, i, F, F, i, i, i, i, D],
             "orc_g3d_bp": [F, i, i, i, F, F, i, i, i, D],
+            "orc_g3d_bp_matched": [F, i, i, i, F, F, i, i, i, D],
             "orc_osc_iter": [D, F, F, i, i, i, i, I32, F, f, i],
             "orc_tvmin3d": [D, i, i, i, d, i],
             "orc_osc_fp": [D, i, i, f, F, i, i, D],
@@ -261,6 +262,24 @@ def g3d_bp(sino, angles, pts, S, Z):
     _check(lib.orc_g3d_bp(_p(sino, ctypes.c_float), W, H, nP, _p(ang, ctypes.c_float),
                           _p(pts, ctypes.c_float), per_view, int(S), int(Z),
                           _p(out, ctypes.c_double)), "g3d_bp")
+    return out
+
+
+def g3d_bp_matched(sino, angles, pts, S, Z):
+    """The exact transpose of g3d_fp (eight-corner trilinear scatter at the FP's
+    sample positions): sino [W,H,nP] -> vol [S,S,Z] (float64)."""
+    lib = _load()
+    sino = _f32(sino)
+    if sino.ndim == 2:
+        sino = sino[:, :, None]
+    W, H, nP = sino.shape
+    pts = _f32(pts)
+    per_view = 1 if pts.ndim == 4 else 0
+    ang = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).ravel())
+    out = np.zeros((int(S), int(S), int(Z)), dtype=np.float64, order="F")
+    _check(lib.orc_g3d_bp_matched(_p(sino, ctypes.c_float), W, H, nP, _p(ang, ctypes.c_float),
+                                  _p(pts, ctypes.c_float), per_view, int(S), int(Z),
+                                  _p(out, ctypes.c_double)), "g3d_bp_matched")
     return out
 
 

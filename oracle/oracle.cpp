@@ -632,6 +632,68 @@ int orc_g3d_fp(const float* vol, int S, int Z, const float* angles,
   return 0;
 }
 
+// The exact transpose of orc_g3d_fp (no counterpart in the reference): the
+// same rays and FP64 sample positions, each sample's eight trilinear weights
+// (border addressing: taps outside the volume dropped) times p * step added
+// to the tap voxels.  Per-thread FP64 volumes, reduced in thread order.
+int orc_g3d_bp_matched(const float* sino, int W, int H, int nP, const float* angles,
+                       const float* pts, int pts_per_view, int S, int Z, double* vol) {
+  if (!sino || !angles || !pts || !vol || S <= 0 || Z <= 0 || W <= 0 || H <= 0 || nP < 0)
+    return 1;
+  const float bx = -(float)S / 2.0f, by = bx, bz = -(float)Z / 2.0f;
+  const float step = 0.5f;
+  const size_t N = (size_t)S * S * Z;
+  const long long P = (long long)W * H;
+  const int nt = nthreads();
+  std::vector<std::vector<double>> part(nt);
+#pragma omp parallel num_threads(nt)
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    std::vector<double>& acc = part[tid];
+    acc.assign(N, 0.0);
+#pragma omp for schedule(dynamic, 16)
+    for (long long r = 0; r < P * nP; ++r) {
+      const int view = (int)(r / P);
+      const long long pix = r % P;
+      const double p = sino[(size_t)P * view + pix];
+      if (p == 0.0) continue;
+      const float* pt = pts + (pts_per_view ? (size_t)6 * P * view : 0);
+      float sb, cb;
+      trig(angles[view], &sb, &cb);
+      float sx, sy, ex, ey;
+      g3d_rotate(pt[pix], pt[pix + P], sb, cb, &sx, &sy);
+      g3d_rotate(pt[pix + 3 * P], pt[pix + 4 * P], sb, cb, &ex, &ey);
+      const Ray ray = clip_ray(sx, sy, pt[pix + 2 * P], ex, ey, pt[pix + 5 * P], bx, by, bz, step);
+      for (int k = 0; k < ray.n; ++k) {
+        const double c0 = (double)ray.cx + (double)k * (double)ray.dx - (double)bx - 0.5;
+        const double c1 = (double)ray.cy + (double)k * (double)ray.dy - (double)by - 0.5;
+        const double c2 = (double)ray.cz + (double)k * (double)ray.dz - (double)bz - 0.5;
+        const double f0 = std::floor(c0), f1 = std::floor(c1), f2 = std::floor(c2);
+        if (f0 < -2 || f0 > S || f1 < -2 || f1 > S || f2 < -2 || f2 > Z) continue;
+        const double a = c0 - f0, b = c1 - f1, g = c2 - f2;
+        const int i0 = (int)f0, j0 = (int)f1, k0 = (int)f2;
+        for (int t = 0; t < 8; ++t) {
+          const int i = i0 + (t & 1), j = j0 + ((t >> 1) & 1), kk = k0 + (t >> 2);
+          if (i < 0 || i >= S || j < 0 || j >= S || kk < 0 || kk >= Z) continue;
+          const double w = ((t & 1) ? a : 1.0 - a) * (((t >> 1) & 1) ? b : 1.0 - b) *
+                           ((t >> 2) ? g : 1.0 - g);
+          acc[(size_t)i + (size_t)S * ((size_t)j + (size_t)S * kk)] += p * (double)step * w;
+        }
+      }
+    }
+  }
+  std::memset(vol, 0, N * sizeof(double));
+  for (int t = 0; t < nt; ++t) {
+    if (part[t].empty()) continue;
+#pragma omp parallel for num_threads(nt)
+    for (long long i = 0; i < (long long)N; ++i) vol[i] += part[t][i];
+  }
+  return 0;
+}
+
 // CUDAmex_general3D_BP.cu:194-282 (gateway) and :61-188 (kernel).  The
 // positions advance incrementally in binary32 and the voxel indices and
 // weights are binary32, exactly as in the reference (they are discontinuous

@@ -67,6 +67,10 @@ int orc_g3d_fp(const float* vol, int S, int Z, const float* angles,
 int orc_g3d_bp(const float* sino, int W, int H, int nP, const float* angles,
                const float* pts, int pts_per_view, int S, int Z, double* vol);
 
+/* The exact transpose of orc_g3d_fp (no counterpart in the reference). */
+int orc_g3d_bp_matched(const float* sino, int W, int H, int nP, const float* angles,
+                       const float* pts, int pts_per_view, int S, int Z, double* vol);
+
 /* One OSC iteration over all subsets (CUDAmex_oscIter.cu:94-358,504-557):
  * mu [W,W,H] is updated in place (FP64 state); pre/post [W,H,nP] are NOT
  * modified.  picks: nSub int32 subset indices (0-based). */

@@ -393,3 +393,21 @@ def test_taller_detector_rows_outside_the_volume_are_zero(orc, geom):
     tall = orc.fp_det(vol, 1000.0, ang, geom, W, H + 4)
     assert np.array_equal(tall[:, 2:H + 2], orc.fp(vol, 1000.0, ang, 2, geom))
     assert np.count_nonzero(tall[:, :2]) == 0 and np.count_nonzero(tall[:, H + 2:]) == 0
+
+
+def test_matched_general3d_bp_is_the_transpose_of_the_fp(orc):
+    """The oracle's matched-adjoint general3D BP is the exact transpose of its
+    general3D FP: <FP x, y> = <x, BP y> to FP64 rounding, for helix rays that
+    cross, graze and miss the volume."""
+    from mexct import phantoms
+
+    S, Z = 24, 18
+    pts, ang = phantoms.helix_pts(20, 14, 5, Z, sad=60.0, seed=4)
+    rng = np.random.default_rng(3)
+    x = np.asfortranarray(rng.uniform(0, 1, (S, S, Z)).astype(np.float32))
+    y = np.asfortranarray(rng.uniform(-1, 1, (20, 14, 5)).astype(np.float32))
+    fx = orc.g3d_fp(x, ang, pts, 5)
+    bty = orc.g3d_bp_matched(y, ang, pts, S, Z)
+    lhs = float(np.sum(fx * y.astype(np.float64)))
+    rhs = float(np.sum(x.astype(np.float64) * bty))
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0)
