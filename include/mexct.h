@@ -242,6 +242,20 @@ mexct_status mexct_bp_det_dev(mexct_ctx* ctx, const float* d_sino,
                               const float* angles, int geom, int W, int H,
                               float* d_vol, void* stream);
 
+/* One OSC iteration (as mexct_osc_iter_dev) with the scanner's detector
+ * decoupled from the volume (no counterpart in the reference, whose oscIter
+ * ties the detector to the volume's face): pre/post are FP32 counts on a
+ * det_w x det_h x nP detector of pitch du x dv; the forward pass casts one ray
+ * per pixel centre (det->ss must be 1) with the residual epilogue, and the
+ * dual BP interpolates the residuals in u and v for every geometry.  FP32 mu
+ * [W,W,H] is updated in place.  det_w = W, det_h = H, du = dv = 1 is the
+ * reference's detector. */
+mexct_status mexct_osc_iter_det_dev(mexct_ctx* ctx, float* d_mu, const float* d_pre,
+                                    const float* d_post, const mexct_detector* det,
+                                    int W, int H, int nP, int nSub,
+                                    const int32_t* picks, const float* angles,
+                                    float sad, int geom, void* stream);
+
 /* ---- sub-volumes and out-of-core FP / BP --------------------------------- */
 
 /* No counterpart in the reference (its oscIter keeps whole volumes on the

@@ -941,7 +941,10 @@ cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
 // Dual BP of the residuals with border addressing (CUDAmex_oscIter.cu:305-356)
 // into register accumulators, then mu <- max(mu + mu*num/den, 0) inside the
 // circle (:119-134).  num/den never touch memory.
-template <int GEOM, int ZC, typename TM>
+// DET: a decoupled detector (A.det_w x A.det_h pixels of reciprocal pitch
+// A.inv_du, A.inv_dv; no counterpart in the reference): every geometry
+// interpolates its residuals in v, as the detector BP does.
+template <int GEOM, int ZC, typename TM, bool DET = false>
 __global__ void __launch_bounds__(256) osc_bp_update_kernel(
     const __grid_constant__ VoxArgs A, const float* __restrict__ rpre,
     const float* __restrict__ rpost, TM* __restrict__ mu, TM* __restrict__ padx,
@@ -958,15 +961,20 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
   for (int j = 0; j < ZC; ++j) num[j] = den[j] = 0.f;
   const float x = (float)ix - ((float)A.hw + 0.5f);
   const float y = (float)iy - ((float)A.hw + 0.5f);
-  const int Wp = sino_pad_pitch(A.W);
-  const size_t vstride = (size_t)Wp * (A.H + 2 * kSinoPad);
+  const int Wp = sino_pad_pitch(DET ? A.det_w : A.W);
+  const size_t vstride = (size_t)Wp * ((DET ? A.det_h : A.H) + 2 * kSinoPad);
   for (int v = 0; v < A.nviews; ++v) {
-    const ColGeom<GEOM> g = col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
+    const ColGeom<GEOM> g =
+        DET ? col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, A.hwd, A.v0d, A.inv_du, A.inv_dv)
+            : col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
     // zero frame = border addressing (CUDAmex_oscIter.cu:419-425); residuals
     // in the quad layout written by the FP epilogue
     const float4* qpre = reinterpret_cast<const float4*>(rpre) + (size_t)v * vstride;
     const float4* qpost = reinterpret_cast<const float4*>(rpost) + (size_t)v * vstride;
-    if constexpr (GEOM == 2) {
+    if constexpr (DET) {
+      bp_column_quad<ZC, float, GEOM>(qpre, A.det_w, A.det_h, Wp, z0, g, num);
+      bp_column_quad<ZC, float, GEOM>(qpost, A.det_w, A.det_h, Wp, z0, g, den);
+    } else if constexpr (GEOM == 2) {
       bp_column_quad<ZC, float>(qpre, A.W, A.H, Wp, z0, g, num);
       bp_column_quad<ZC, float>(qpost, A.W, A.H, Wp, z0, g, den);
     } else {
@@ -993,6 +1001,22 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
       }
     }
   }
+}
+
+cudaError_t launch_osc_bp_update_det(int geom, const VoxArgs& a, const float* rpre,
+                                     const float* rpost, void* mu, int mt, void* padx,
+                                     void* pady, int Pf, cudaStream_t st) {
+  constexpr int ZC = 4;
+  if (mt != kF32) return cudaErrorInvalidValue;
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + ZC - 1) / ZC);
+#define OSC_BP(G)                                                                      \
+  osc_bp_update_kernel<G, ZC, float, true><<<grd, blk, 0, st>>>(a, rpre, rpost, (float*)mu, \
+                                                                (float*)padx, (float*)pady, Pf)
+  if (geom == 0) OSC_BP(0);
+  else if (geom == 1) OSC_BP(1);
+  else OSC_BP(2);
+#undef OSC_BP
+  return cudaGetLastError();
 }
 
 cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,

@@ -1096,6 +1096,15 @@ cudaError_t launch_fp_slab_det(int geom, const RayArgs& a, const CUtensorMap& mx
   return cudaErrorInvalidValue;
 }
 
+cudaError_t launch_fp_slab_osc_det(int geom, const RayArgs& a, const CUtensorMap& mx,
+                                   const CUtensorMap& my, const void* px, const void* py, int Pf,
+                                   const SlabEpi& e, cudaStream_t st) {
+  if (geom == 0) return slab_go<0, true, 1, float, float, true>(a, mx, my, px, py, Pf, nullptr, e, st);
+  if (geom == 1) return slab_go<1, true, 1, float, float, true>(a, mx, my, px, py, Pf, nullptr, e, st);
+  if (geom == 2) return slab_go<2, true, 1, float, float, true>(a, mx, my, px, py, Pf, nullptr, e, st);
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_fp_slab_g3d(const RayArgs& a, const CUtensorMap& mx, const CUtensorMap& my,
                                const void* px, const void* py, int Pf, float* out,
                                const SlabEpi& e, cudaStream_t st) {

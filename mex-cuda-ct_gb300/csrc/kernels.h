@@ -219,6 +219,15 @@ cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
 // rpre/rpost: padded residual views (sino_pad_pitch layout, zero frame).
 // With padx/pady non-null the updated mu is also written into the padded
 // volumes of the slab FP (pitch Pf), so the next subset needs no padding pass.
+// The OSC forward pass with the residual epilogue onto a decoupled detector
+// (a.det_w, a.det_h, a.du, a.dv; one ray per pixel; FP32 mu) and the dual BP
+// + update reading those residuals (no counterpart in the reference).
+cudaError_t launch_fp_slab_osc_det(int geom, const RayArgs& a, const CUtensorMap& mx,
+                                   const CUtensorMap& my, const void* px, const void* py, int Pf,
+                                   const SlabEpi& e, cudaStream_t st);
+cudaError_t launch_osc_bp_update_det(int geom, const VoxArgs& a, const float* rpre,
+                                     const float* rpost, void* mu, int mt, void* padx,
+                                     void* pady, int Pf, cudaStream_t st);
 cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
                                  const float* rpre, const float* rpost,
                                  void* mu, int mu_type, void* padx, void* pady, int Pf,

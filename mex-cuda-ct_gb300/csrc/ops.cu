@@ -485,6 +485,85 @@ mexct_status g3d_bp_dev_impl(mexct_ctx* c, const float* d_sino, int W, int H,
   return MEXCT_OK;
 }
 
+// OSC iteration onto a decoupled detector (no counterpart in the reference,
+// whose detector is the volume's face): pre/post are det_w x det_h x nP; the
+// forward pass casts one ray per pixel centre (ss must be 1) and the dual BP
+// interpolates the residuals bilinearly in u and v.  FP32 mu.
+mexct_status osc_det_impl(mexct_ctx* c, float* d_mu, const float* d_pre, const float* d_post,
+                          const mexct_detector* det, int W, int H, int nP, int nSub,
+                          const int32_t* picks, const float* angles, float sad, int geom,
+                          cudaStream_t st) {
+  if (!d_mu || !d_pre || !d_post || !picks || (!angles && nP > 0))
+    return set_err(MEXCT_ERR_ARG, "osc_iter_det: NULL pointer");
+  if (bad_dims(W, H)) return set_err(MEXCT_ERR_ARG, "osc_iter_det: bad dims");
+  if (nP < 0 || nSub <= 0)
+    return set_err(MEXCT_ERR_ARG, "osc_iter_det: bad nProj %d / nSub %d", nP, nSub);
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "osc_iter_det: invalid geometry %d", geom);
+  if (mexct_status s = bad_detector(det, "osc_iter_det")) return s;
+  if (det->ss != 1)
+    return set_err(MEXCT_ERR_UNSUPPORTED, "osc_iter_det: ss = %d (one ray per pixel only)", det->ss);
+  int maxv = 0;
+  for (int si = 0; si < nSub; ++si) {
+    const int sel = picks[si];
+    const int nv = (sel < 0 || sel >= nP) ? 0 : (nP - 1 - sel) / nSub + 1;
+    maxv = std::max(maxv, nv);
+  }
+  if (maxv > kMaxViews)
+    return set_err(MEXCT_ERR_UNSUPPORTED, "osc_iter_det: %d views in one subset (max %d)", maxv,
+                   kMaxViews);
+  if (!c) return MEXCT_OK;
+  const int Wd = det->det_w, Hd = det->det_h;
+  const size_t rbytes = sino_pad_elems(Wd, Hd, std::max(maxv, 1)) * sizeof(float4);
+  MEXCT_TRY_CUDA(c->r1.ensure(rbytes), "osc_iter_det: workspace");
+  MEXCT_TRY_CUDA(c->r2.ensure(rbytes), "osc_iter_det: workspace");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(c->r1.p, 0, rbytes, st), "osc_iter_det: workspace");
+  MEXCT_TRY_CUDA(cudaMemsetAsync(c->r2.p, 0, rbytes, st), "osc_iter_det: workspace");
+  CUtensorMap mx, my;
+  int Pf = 0;
+  mexct_status ps = prepare_slab(c, d_mu, kF32, W, H, /*border=*/true, geom, &mx, &my, &Pf, st);
+  if (ps) return ps;
+  std::unique_ptr<RayArgs> ra(new RayArgs);
+  std::unique_ptr<VoxArgs> va(new VoxArgs);
+  fill_std_rays(*ra, W, H, sad, geom, /*osc=*/true);
+  ra->det_w = Wd;
+  ra->det_h = Hd;
+  ra->u0 = float(Wd - 1) / 2;
+  ra->v0 = float(Hd - 1) / 2;
+  ra->P = (long long)Wd * Hd;
+  ra->du = det->du;
+  ra->dv = det->dv;
+  fill_vox(*va, W, H, sad);
+  va->det_w = Wd;
+  va->det_h = Hd;
+  va->hwd = (float)(Wd / 2) - 1.0f;
+  va->v0d = float(Hd - 1) / 2;
+  va->inv_du = 1.0f / det->du;
+  va->inv_dv = 1.0f / det->dv;
+  va->P = (long long)Wd * Hd;
+  for (int si = 0; si < nSub; ++si) {
+    const int sel = picks[si];
+    const int nv = (sel < 0 || sel >= nP) ? 0 : (nP - 1 - sel) / nSub + 1;
+    ra->nviews = nv;
+    ra->view0 = sel;
+    ra->vstride = nSub;
+    va->nviews = nv;
+    for (int i = 0; i < nv; ++i) {
+      trig_of(angles[sel + i * nSub], &ra->trig[i]);
+      va->trig[i] = ra->trig[i];
+    }
+    if (nv > 0) {
+      SlabEpi e{d_pre, d_post, c->r1.as<float>(), c->r2.as<float>(), c->err.as<unsigned>(),
+                c->wait_us};
+      MEXCT_TRY_CUDA(launch_fp_slab_osc_det(geom, *ra, mx, my, c->padx.p, c->pady.p, Pf, e, st),
+                     "osc_iter_det: fp");
+    }
+    MEXCT_TRY_CUDA(launch_osc_bp_update_det(geom, *va, c->r1.as<float>(), c->r2.as<float>(), d_mu,
+                                            kF32, c->padx.p, c->pady.p, Pf, st),
+                   "osc_iter_det: bp/update");
+  }
+  return MEXCT_OK;
+}
+
 // Matched-adjoint general3D BP: the transpose of g3d_fp_dev_impl.
 mexct_status g3d_bp_matched_impl(mexct_ctx* c, const float* d_sino, int W, int H, int nP,
                                  const float* angles, const float* d_pts, int per_view, int S,
@@ -1050,6 +1129,17 @@ mexct_status mexct_g3d_bp_dev(mexct_ctx* ctx, const float* d_sino, int W,
   CTX_OR_FAIL(c, "g3d_bp");
   return g3d_bp_dev_impl(c, d_sino, W, H, nP, angles, d_pts, per_view, S, Z, d_vol,
                          as_stream(stream));
+}
+
+mexct_status mexct_osc_iter_det_dev(mexct_ctx* ctx, float* d_mu, const float* d_pre,
+                                    const float* d_post, const mexct_detector* det, int W, int H,
+                                    int nP, int nSub, const int32_t* picks, const float* angles,
+                                    float sad, int geom, void* stream) {
+  VALIDATE(osc_det_impl(nullptr, d_mu, d_pre, d_post, det, W, H, nP, nSub, picks, angles, sad,
+                        geom, nullptr));
+  CTX_OR_FAIL(c, "osc_iter_det");
+  return osc_det_impl(c, d_mu, d_pre, d_post, det, W, H, nP, nSub, picks, angles, sad, geom,
+                      as_stream(stream));
 }
 
 mexct_status mexct_g3d_bp_matched_dev(mexct_ctx* ctx, const float* d_sino, int W, int H,

@@ -65,6 +65,7 @@ SIGNATURES = {
     "mexct_g3d_fp_dev": [_P, _P, _i, _i, _P, _P, _i, _i, _i, _i, _P, _P],
     "mexct_g3d_bp_dev": [_P, _P, _i, _i, _i, _P, _P, _i, _i, _i, _P, _P],
     "mexct_g3d_bp_matched": [_P, _P, _i, _i, _i, _P, _P, _i, _i, _i, _P],
+    "mexct_osc_iter_det_dev": [_P, _P, _P, _P, _P, _i, _i, _i, _i, _P, _P, _f, _i, _P],
     "mexct_g3d_bp_matched_dev": [_P, _P, _i, _i, _i, _P, _P, _i, _i, _i, _P, _P],
     "mexct_osc_iter_dev": [_P, _P, _P, _P, _i, _i, _i, _i, _P, _P, _f, _i, _P],
     "mexct_tvmin3d_dev": [_P, _P, _i, _i, _i, _f, _i, _P, _P],

@@ -438,6 +438,20 @@ def osc_iter_dev(mu, pre, post, n_sub, picks, angles, sad, geom, stream=None):
     return mu
 
 
+def osc_iter_det_dev(mu, pre, post, n_sub, picks, angles, sad, geom, du=1.0, dv=1.0, stream=None):
+    """One OSC iteration onto a decoupled detector: mu (H, W, W) float32 updated in
+    place; pre/post (nP, det_h, det_w) float32 counts of pitch du x dv."""
+    H, W, _ = mu.shape
+    nP, det_h, det_w = pre.shape
+    picks = np.ascontiguousarray(np.asarray(picks, dtype=np.int32).ravel())
+    ang = _angles(angles, nP)
+    det = _lib.Detector(int(det_w), int(det_h), float(du), float(dv), 1)
+    _lib.call("mexct_osc_iter_det_dev", None, _dptr(mu), _dptr(pre), _dptr(post),
+              ctypes.addressof(det), W, H, nP, int(n_sub), _ptr(picks), _ptr(ang), float(sad),
+              _geom_flag(geom), _stream(stream))
+    return mu
+
+
 def tvmin3d_dev(vol, c, n_steps=20, out=None, stream=None):
     import torch
     Nz, Ny, Nx = vol.shape

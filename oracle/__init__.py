@@ -70,6 +70,7 @@ def _load():
             "orc_g3d_bp": [F, i, i, i, F, F, i, i, i, D],
             "orc_g3d_bp_matched": [F, i, i, i, F, F, i, i, i, D],
             "orc_osc_iter": [D, F, F, i, i, i, i, I32, F, f, i],
+            "orc_osc_iter_det": [D, F, F, i, i, i, i, I32, F, f, i, i, i, f, f],
             "orc_tvmin3d": [D, i, i, i, d, i],
             "orc_osc_fp": [D, i, i, f, F, i, i, D],
             "orc_tv_gradient": [D, i, i, i, D],
@@ -297,6 +298,24 @@ def osc_iter(mu, pre, post, n_sub, picks, angles, sad, geom):
                             _p(post, ctypes.c_float), W, H, nP, int(n_sub),
                             _p(picks, ctypes.c_int32), _p(ang, ctypes.c_float), float(sad),
                             int(geom)), "osc_iter")
+    return mu
+
+
+def osc_iter_det(mu, pre, post, n_sub, picks, angles, sad, geom, du, dv):
+    """One OSC iteration onto a decoupled detector: pre/post [Wd,Hd,nP] counts of
+    pitch du x dv; returns the updated mu [W,W,H] (float64)."""
+    lib = _load()
+    mu = np.array(mu, dtype=np.float64, order="F", copy=True)
+    pre = _f32(pre)
+    post = _f32(post)
+    W, _, H = mu.shape
+    Wd, Hd, nP = pre.shape
+    picks = np.ascontiguousarray(np.asarray(picks, dtype=np.int32).ravel())
+    ang = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).ravel())
+    _check(lib.orc_osc_iter_det(_p(mu, ctypes.c_double), _p(pre, ctypes.c_float),
+                                _p(post, ctypes.c_float), W, H, nP, int(n_sub),
+                                _p(picks, ctypes.c_int32), _p(ang, ctypes.c_float), float(sad),
+                                int(geom), Wd, Hd, float(du), float(dv)), "osc_iter_det")
     return mu
 
 

@@ -775,18 +775,28 @@ int orc_g3d_bp(const float* sino, int W, int H, int nP, const float* angles,
 
 // CUDAmex_oscIter.cu:362-584 (gateway), :94-136 (zero / update),
 // :140-271 (FP + residual), :272-358 (dual BP).  FP64 state.
-int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
-                 int H, int nP, int nSub, const int32_t* picks,
-                 const float* angles, float sad, int geom) {
+// With a decoupled detector (Wd >= 1; no counterpart in the reference):
+// pre/post are Wd x Hd x nP counts of pitch du x dv, one ray per pixel centre
+// (a ray that misses the volume gives l = 0), and the dual BP samples the
+// residual views of the detector (border addressing).  Wd < 0: the volume's
+// own detector, the reference's operations.
+int osc_iter_impl(double* mu, const float* pre, const float* post, int W,
+                  int H, int nP, int nSub, const int32_t* picks,
+                  const float* angles, float sad, int geom, int Wd, int Hd,
+                  float du, float dv) {
   if (!mu || !pre || !post || !angles || W <= 0 || H <= 0 || nP < 0 ||
       nSub <= 0 || !picks)
     return 1;
   if (geom < 0 || geom > 2) return 1;
-  const float u0 = float(W - 1) / 2, v0 = float(H - 1) / 2;
+  const bool det = Wd > 0;
+  if (det && (Hd <= 0 || !(du > 0.f) || !(dv > 0.f))) return 1;
+  const int DW = det ? Wd : W, DH = det ? Hd : H;
+  const float u0 = float(DW - 1) / 2, v0r = float(DH - 1) / 2;
+  const float v0 = float(H - 1) / 2;
   const float bx = -(float)W / 2.0f, by = bx, bz = -(float)H / 2.0f;
   const float step = 0.5f;  // :244, every geometry
   const uint32_t hw = (uint32_t)W / 2u - 1u;
-  const size_t P = (size_t)W * H;
+  const size_t P = (size_t)DW * DH;
   const size_t N = (size_t)W * W * H;
   std::vector<double> num(N), den(N);
   for (int si = 0; si < nSub; ++si) {
@@ -802,14 +812,20 @@ int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
       const int vi = (int)(r / P);
       const int pix = (int)(r % P);
       const int view = views[vi];
-      const int ix = pix % W, iy = pix / W;
+      const int ix = pix % DW, iy = pix / DW;
       float sb, cb;
       trig(angles[view], &sb, &cb);
       float s[3], e[3];
-      std_ray(geom, ix, iy, u0, v0, sb, cb, sad, sad, s, e);
-      const Ray ray =
-          clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], bx, by, bz, step);
-      const double l = march(ray, step, mu, W, W, H, bx, by, bz, true);
+      if (det)
+        std_ray(geom, ix, iy, u0, v0r, sb, cb, sad, sad, s, e, du, dv);
+      else
+        std_ray(geom, ix, iy, u0, v0r, sb, cb, sad, sad, s, e);
+      double l = 0.0;
+      if (!det || hits_box(s, e, bx, by, bz)) {
+        const Ray ray =
+            clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], bx, by, bz, step);
+        l = march(ray, step, mu, W, W, H, bx, by, bz, true);
+      }
       const double pv = pre[P * view + pix], qv = post[P * view + pix];
       const double ehat = pv * std::exp(-l);
       rpre[r] = ehat - qv;
@@ -829,7 +845,7 @@ int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
         trig(angles[views[vi]], &sb, &cb);
         const double* a = rpre.data() + P * vi;
         const double* b = rpost.data() + P * vi;
-        if (g_ref_steps) {
+        if (g_ref_steps && !det) {
           const BpColF c = bp_column_ref(geom, ix, iy, hw, v0, sb, cb, sad);
           float pz = c.pz0;
           for (int iz = 0; iz < H; ++iz) {
@@ -840,12 +856,13 @@ int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
           }
           continue;
         }
-        const BpCol c = bp_column(geom, ix, iy, hw, v0, sb, cb, sad);
+        const BpCol c = det ? bp_column(geom, ix, iy, hw, v0, sb, cb, sad, DW, DH, du, dv)
+                            : bp_column(geom, ix, iy, hw, v0, sb, cb, sad);
         for (int iz = 0; iz < H; ++iz) {
           const double pz = c.pz0 + c.dpz * iz;
           const size_t idx = (size_t)col + (size_t)W * W * iz;
-          num[idx] += c.wgt * tex2(a, W, H, c.py, pz, true);
-          den[idx] += c.wgt * tex2(b, W, H, c.py, pz, true);
+          num[idx] += c.wgt * tex2(a, DW, DH, c.py, pz, true);
+          den[idx] += c.wgt * tex2(b, DW, DH, c.py, pz, true);
         }
       }
       for (int iz = 0; iz < H; ++iz) {
@@ -856,6 +873,21 @@ int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
     }
   }
   return 0;
+}
+
+int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
+                 int H, int nP, int nSub, const int32_t* picks,
+                 const float* angles, float sad, int geom) {
+  return osc_iter_impl(mu, pre, post, W, H, nP, nSub, picks, angles, sad, geom, -1, -1, 1.0f,
+                       1.0f);
+}
+
+int orc_osc_iter_det(double* mu, const float* pre, const float* post, int W,
+                     int H, int nP, int nSub, const int32_t* picks,
+                     const float* angles, float sad, int geom, int Wd, int Hd,
+                     float du, float dv) {
+  if (Wd <= 0) return 1;
+  return osc_iter_impl(mu, pre, post, W, H, nP, nSub, picks, angles, sad, geom, Wd, Hd, du, dv);
 }
 
 // The OSC forward pass alone (CUDAmex_oscIter.cu:140-259): every geometry

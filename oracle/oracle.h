@@ -78,6 +78,13 @@ int orc_osc_iter(double* mu, const float* pre, const float* post, int W,
                  int H, int nP, int nSub, const int32_t* picks,
                  const float* angles, float sad, int geom);
 
+/* orc_osc_iter onto a decoupled detector (no counterpart in the reference):
+ * pre/post [Wd,Hd,nP] of pitch du x dv, one ray per pixel centre. */
+int orc_osc_iter_det(double* mu, const float* pre, const float* post, int W,
+                     int H, int nP, int nSub, const int32_t* picks,
+                     const float* angles, float sad, int geom, int Wd, int Hd,
+                     float du, float dv);
+
 /* The OSC forward pass alone (CUDAmex_oscIter.cu:140-259): step 0.5 for
  * every geometry, border addressing.  mu [W,W,H] -> out [W,H,nP]. */
 int orc_osc_fp(const double* mu, int W, int H, float sad, const float* angles,
