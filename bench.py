@@ -850,7 +850,46 @@ def out_of_core(n=768, views=360, geom=2, budget=1 << 30):
     out["bp_in_core"] = {"s": round(t3 - t2, 3), "gups": round(N * views / (t3 - t2) / 1e9, 3)}
     out["bp_out_of_core"] = {"s": round(t4 - t3, 3), "gups": round(N * views / (t4 - t3) / 1e9, 3),
                              "rel_l2_vs_in_core": rel_np(bp_oc, bp_in)}
+    del vol, fp_in, fp_oc, bp_in, bp_oc
+    out["osc_tv"] = osc_tv_out_of_core()
     return out
+
+
+def osc_tv_out_of_core(n=256, views=60, n_iter=20, nsub=10, slabs=4):
+    """OSC-TV at the few-view workload (256^3 ellipsoids, 60 cone views, 20
+    iterations x 10 subsets, TV 0.2), host arrays in and out: the in-core one-shot
+    entry point against the out-of-core solver (mu in host memory, z-slabs) held to
+    the budget of `slabs` slabs."""
+    from mexct import phantoms, solver
+
+    vol = phantoms.ellipsoids(n, count=10, seed=3, nz=n)
+    ang = phantoms.angles_full(views)
+    fp = line_integrals(vol, ang)
+    pre, post = phantoms.poisson_counts(fp, 1e5, seed=4)
+    picks = [int(v) for v in np.random.default_rng(5).integers(0, nsub, n_iter)]
+    g = {"type": "cone3d", "SAD": 1000.0}
+    _, full = solver.ooc_plan(n, n, views, 2, n_iter, nsub, nsub, 1.0, 1 << 40)
+    budget = full // slabs * 2  # two slab buffer sets of ~1/slabs of the volume each
+    nz, nbytes = solver.ooc_plan(n, n, views, 2, n_iter, nsub, nsub, 1.0, budget)
+    solver.OSC_TV_recon(pre, post, ang, g, 1, 0.2, nsub, nsub, 1.0, picks[:1])  # warm-up
+    t0 = time.perf_counter()
+    ref = solver.OSC_TV_recon(pre, post, ang, g, n_iter, 0.2, nsub, nsub, 1.0, picks)
+    t1 = time.perf_counter()
+    got, _ = solver.OSC_TV_recon_ooc(pre, post, ang, g, n_iter, 0.2, nsub, nsub, 1.0, picks, budget)
+    t2 = time.perf_counter()
+    return {"workload": "cone %d^3 x %d views, %d iterations x %d subsets, TV 0.2, host arrays"
+                        % (n, views, n_iter, nsub),
+            "in_core_s": round(t1 - t0, 3), "out_of_core_s": round(t2 - t1, 3),
+            "slab_slices": nz, "device_bytes": int(nbytes),
+            "one_slab_device_bytes": int(full),
+            "rel_l2_vs_in_core": rel_np(got, ref)}
+
+
+def line_integrals(vol, ang):
+    """Noise-free line integrals for the count model (the library's own FP)."""
+    import mexct
+
+    return mexct.CUDAmex_FP(vol, 1000.0, ang, len(ang), 2)
 
 
 def rel_np(a, b):

@@ -67,6 +67,33 @@ mexct_status mexct_osc_tv_recon(mexct_ctx* ctx, const float* pre,
                                 int n_sub_final, float p_val,
                                 const int32_t* first_picks, float* recon);
 
+/* OSC_TV_recon out of core: as mexct_osc_tv_recon, with mu in host memory
+ * streaming through the device in z-slabs, using at most budget_bytes of
+ * device memory (no counterpart in the reference, which lists sub-volume
+ * reconstruction of larger images as a TODO: CUDAmex_oscIter.cu:28-29).
+ * The slab is the whole volume when it fits, else the thickest multiple of 4
+ * slices that does (*slab_planes, if non-NULL); the views of the largest
+ * subset and the slab buffers must fit (MEXCT_ERR_BUDGET otherwise).  Per
+ * voxel the operations are the in-core solver's; a subset's line integrals
+ * are FP32 sums of the slabs' parts and the FP64 norms are combined slab by
+ * slab.  Host memory: 2 volumes and the clamped counts, pinned. */
+mexct_status mexct_osc_tv_recon_ooc(mexct_ctx* ctx, const float* pre,
+                                    const float* post, int W, int H, int nP,
+                                    const float* angles, float sad, int geom,
+                                    int n_iter, float tv_const,
+                                    int n_sub_init, int n_sub_final,
+                                    float p_val, const int32_t* first_picks,
+                                    size_t budget_bytes, float* recon,
+                                    int* slab_planes);
+
+/* The slab thickness (slices) and device bytes mexct_osc_tv_recon_ooc uses
+ * for a problem within budget_bytes (host-side; MEXCT_ERR_BUDGET if no slab
+ * fits). */
+mexct_status mexct_osc_tv_ooc_plan(int W, int H, int nP, int geom, int n_iter,
+                                   int n_sub_init, int n_sub_final,
+                                   float p_val, size_t budget_bytes,
+                                   int* slab_planes, size_t* device_bytes);
+
 /* Subset schedule helpers (OSC_TV_recon.m:76-102). */
 int mexct_num_subsets(int s_init, int s_final, float p_val, int max_iters,
                       int k);

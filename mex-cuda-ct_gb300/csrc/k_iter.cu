@@ -463,6 +463,28 @@ cudaError_t launch_sum_partials(const double* partials, long long n, double* out
   return cudaGetLastError();
 }
 
+// Norms of the parts of a volume (z-slabs) combined in index order:
+// out = sqrt(sum parts[i]^2); with scale non-null also the TV step scale
+// -c * (*cmul) / out, as the last CTA of the norm kernel writes it.
+__global__ void combine_norms_kernel(const double* __restrict__ parts, int n,
+                                     double* __restrict__ out, float c,
+                                     const double* __restrict__ cmul, float* __restrict__ scale) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += parts[i] * parts[i];
+  const double m = sqrt(s);
+  *out = m;
+  if (scale) {
+    const double ce = cmul ? (double)c * *cmul : (double)c;
+    *scale = (float)(-ce / m);
+  }
+}
+
+cudaError_t launch_combine_norms(const double* parts, int n, double* out, float c,
+                                 const double* cmul, float* scale, cudaStream_t st) {
+  combine_norms_kernel<<<1, 1, 0, st>>>(parts, n, out, c, cmul, scale);
+  return cudaGetLastError();
+}
+
 int device_sms() {
   static std::atomic<int> cache[64];
   int dev = 0;

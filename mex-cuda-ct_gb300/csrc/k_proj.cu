@@ -953,7 +953,10 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
   const int w = threadIdx.y, lane = threadIdx.x;
   const int ix = blockIdx.x * 32 + 8 * (w & 3) + (lane & 7);
   const int iy = blockIdx.y * blockDim.y + 4 * (w >> 2) + (lane >> 3);
-  const int z0 = blockIdx.z * ZC;
+  // slices zl .. zl + ZC - 1 of the output (slices zoff .. zoff + nzs - 1 of
+  // the volume: the whole volume, or a z-slab of it)
+  const int zl = blockIdx.z * ZC;
+  const int z0 = A.zoff + zl;
   if (ix >= A.W || iy >= A.W) return;
   if (!in_circle(ix, iy, A.hw)) return;
   float num[ZC], den[ZC];
@@ -987,8 +990,8 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
   const size_t Ps = (size_t)A.W + 2;
 #pragma unroll
   for (int j = 0; j < ZC; ++j) {
-    const int z = z0 + j;
-    if (z < A.H) {
+    const int z = zl + j;
+    if (z < A.nzs) {
       TM* o = mu + base + (size_t)z * sz;
       const float f = ldp(o);
       const float m = fmaxf(f + (f * num[j] / den[j]), 0.f);
@@ -1008,7 +1011,7 @@ cudaError_t launch_osc_bp_update_det(int geom, const VoxArgs& a, const float* rp
                                      void* pady, int Pf, cudaStream_t st) {
   constexpr int ZC = 4;
   if (mt != kF32) return cudaErrorInvalidValue;
-  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + ZC - 1) / ZC);
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.nzs + ZC - 1) / ZC);
 #define OSC_BP(G)                                                                      \
   osc_bp_update_kernel<G, ZC, float, true><<<grd, blk, 0, st>>>(a, rpre, rpost, (float*)mu, \
                                                                 (float*)padx, (float*)pady, Pf)
@@ -1024,7 +1027,9 @@ cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
                                  void* mu, int mt, void* padx, void* pady, int Pf,
                                  cudaStream_t st) {
   constexpr int ZC = 4;
-  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.H + ZC - 1) / ZC);
+  if (a.zoff % ZC != 0 || a.zoff < 0 || a.nzs < 1 || a.zoff + a.nzs > a.H)
+    return cudaErrorInvalidValue;
+  dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.nzs + ZC - 1) / ZC);
 #define OSC_BP(G, T)                                                                 \
   osc_bp_update_kernel<G, ZC, T><<<grd, blk, 0, st>>>(a, rpre, rpost, (T*)mu, (T*)padx, \
                                                       (T*)pady, Pf)
@@ -1045,9 +1050,43 @@ cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
   return cudaGetLastError();
 }
 
-}  // namespace mexct
+// Residual views of one OSC subset from its line integrals l (W x H x n
+// views, e.g. the sum of the z-slabs' forward passes): pre e^-l - post and
+// pre e^-l l (CUDAmex_oscIter.cu:262-268), the values the slab FP's residual
+// epilogue writes, into the same padded quad layout.
+__global__ void __launch_bounds__(256) osc_residual_kernel(const float* __restrict__ l,
+                                                           const float* __restrict__ pre,
+                                                           const float* __restrict__ post, int W,
+                                                           int H, long long n,
+                                                           float* __restrict__ rpre,
+                                                           float* __restrict__ rpost) {
+  const long long P = (long long)W * H;
+  const int Wp = sino_pad_pitch(W);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const long long v = i / P;
+    const int pix = (int)(i - v * P);
+    const int iy = pix / W, ix = pix - iy * W;
+    const float lv = __ldg(l + i), pv = __ldg(pre + i), qv = __ldg(post + i);
+    const float ehat = pv * expf(-lv);
+    const float r0 = ehat - qv, r1 = ehat * lv;
+    const size_t ri = ((size_t)v * (H + 2 * kSinoPad) + (iy + kSinoPad)) * Wp + (ix + kSinoPad);
+    const size_t q[4] = {4 * ri, 4 * (ri - Wp) + 1, 4 * (ri - 1) + 2, 4 * (ri - Wp - 1) + 3};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      rpre[q[t]] = r0;
+      rpost[q[t]] = r1;
+    }
+  }
+}
 
-namespace mexct {
-
+cudaError_t launch_osc_residual(const float* l, const float* pre, const float* post, int W, int H,
+                                int nviews, float* rpre, float* rpost, cudaStream_t st) {
+  const long long n = (long long)W * H * nviews;
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = std::min<long long>((n + 255) / 256, 16ll * device_sms());
+  osc_residual_kernel<<<(unsigned)blocks, 256, 0, st>>>(l, pre, post, W, H, n, rpre, rpost);
+  return cudaGetLastError();
+}
 
 }  // namespace mexct

@@ -159,11 +159,12 @@ cudaError_t launch_pad_volume(const void* src, int dtype, int W, int H, int Pf,
 }
 
 cudaError_t launch_pad_volume_sub(const float* src, int W, int nz, int Pf, bool zero_lo,
-                                  bool zero_hi, float* px, float* py, cudaStream_t st) {
+                                  bool zero_hi, float* px, float* py, cudaStream_t st,
+                                  bool border) {
   const int Ps = W + 2, Pz = nz + 2;
   dim3 blk(32, 8), g1((Pf + 31) / 32, (Ps + 7) / 8, Pz);
   dim3 g2((Pf + 31) / 32, (Pf + 31) / 32, Pz);
-  const int mode = (zero_lo ? 2 : 0) | (zero_hi ? 4 : 0);
+  const int mode = border ? 1 : ((zero_lo ? 2 : 0) | (zero_hi ? 4 : 0));
   pad_x_kernel<float><<<g1, blk, 0, st>>>(src, px, W, nz, Pf, mode);
   pad_transpose_kernel<float><<<g2, blk, 0, st>>>(px, py, Ps, Pf);
   return cudaGetLastError();

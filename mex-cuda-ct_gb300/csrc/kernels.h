@@ -121,6 +121,11 @@ cudaError_t launch_fp_slab_objective(int geom, const RayArgs& a, const CUtensorM
 // Fixed-order FP64 sum of n partials into *out (one CTA; deterministic).
 cudaError_t launch_sum_partials(const double* partials, long long n, double* out,
                                 cudaStream_t st);
+// out = sqrt(sum of parts[i]^2) over n norms of the parts of a volume, in
+// index order; with scale non-null also scale = -c * (*cmul) / out (cmul
+// may be null: factor 1).
+cudaError_t launch_combine_norms(const double* parts, int n, double* out, float c,
+                                 const double* cmul, float* scale, cudaStream_t st);
 
 cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
                            const CUtensorMap& mx, const CUtensorMap& my,
@@ -144,17 +149,20 @@ cudaError_t launch_fp_slab_det(int geom, const RayArgs& a, const CUtensorMap& mx
 
 // Slab FP (FP32) of a z-slab of the volume (a.zoff, a.zrows, a.zlo, a.zhi,
 // a.accum): the slab's padded tensors hold its slices with a clamp frame at
-// the volume's own faces and zeros elsewhere, so the FPs of the slabs add up
-// to the FP of the whole volume.
+// the volume's own faces and zeros elsewhere (or a zero frame everywhere:
+// border addressing), so the FPs of the slabs add up to the FP of the whole
+// volume.
 cudaError_t launch_fp_slab_sub(int geom, const RayArgs& a, const CUtensorMap& mx,
                                const CUtensorMap& my, const void* px, const void* py, int Pf,
                                float* out, const SlabEpi& e, cudaStream_t st);
 
 // Padded layouts of a z-slab of nz slices (FP32): frame rows below / above
 // the slab are zero where zero_lo / zero_hi (an inner slab face), else edge
-// copies (the volume's own face, clamp addressing).
+// copies (the volume's own face, clamp addressing); with border the whole
+// frame is zero (border addressing).
 cudaError_t launch_pad_volume_sub(const float* src, int W, int nz, int Pf, bool zero_lo,
-                                  bool zero_hi, float* px, float* py, cudaStream_t st);
+                                  bool zero_hi, float* px, float* py, cudaStream_t st,
+                                  bool border = false);
 
 cudaError_t launch_fp_tex(int geom, const RayArgs& a,
                           cudaTextureObject_t tex, float* out,
@@ -228,10 +236,16 @@ cudaError_t launch_fp_slab_osc_det(int geom, const RayArgs& a, const CUtensorMap
 cudaError_t launch_osc_bp_update_det(int geom, const VoxArgs& a, const float* rpre,
                                      const float* rpost, void* mu, int mt, void* padx,
                                      void* pady, int Pf, cudaStream_t st);
+// Updates slices a.zoff .. a.zoff + a.nzs - 1 (a.zoff a multiple of 4) held
+// at mu (and at slab-local rows of padx / pady).
 cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
                                  const float* rpre, const float* rpost,
                                  void* mu, int mu_type, void* padx, void* pady, int Pf,
                                  cudaStream_t st);
+// Residual views (padded quad layout) of nviews views from their line
+// integrals l and counts pre / post, all W x H x nviews FP32.
+cudaError_t launch_osc_residual(const float* l, const float* pre, const float* post, int W, int H,
+                                int nviews, float* rpre, float* rpost, cudaStream_t st);
 
 // TV (CUDAmex_TVmin_3D.cu:101-234).  tv_norm computes ||g||^2 (FP64 above the
 // per-thread level) and the

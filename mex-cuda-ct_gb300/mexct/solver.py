@@ -33,6 +33,10 @@ _lib.register("mexct_osctv_snapshot", [_P, _P, _P])
 _lib.register("mexct_osctv_restore", [_P, _P, _P])
 _lib.register("mexct_osctv_destroy", [_P])
 _lib.register("mexct_osc_tv_recon", [_P, _P, _P, _i, _i, _i, _P, _f, _i, _i, _f, _i, _i, _f, _P, _P])
+_lib.register("mexct_osc_tv_recon_ooc", [_P, _P, _P, _i, _i, _i, _P, _f, _i, _i, _f, _i, _i, _f, _P,
+                                         ctypes.c_size_t, _P, ctypes.POINTER(_i)])
+_lib.register("mexct_osc_tv_ooc_plan", [_i, _i, _i, _i, _i, _i, _i, _f, ctypes.c_size_t,
+                                        ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_size_t)])
 _lib.register("mexct_num_subsets", [_i, _i, _f, _i, _i])
 _lib.register("mexct_subset_order", [_i, _i, _P])
 
@@ -64,6 +68,38 @@ def OSC_TV_recon(pre, post, scanAngles, geom, numIter, TV_constant, numSubsInit,
               g, int(numIter), float(TV_constant), int(numSubsInit), int(numSubsFinal),
               float(pVal), _ptr(fp), _ptr(out))
     return out
+
+
+def ooc_plan(W, H, nP, geom, numIter, numSubsInit, numSubsFinal, pVal, budget_bytes):
+    """(slab thickness in slices, device bytes) of OSC_TV_recon_ooc within budget_bytes."""
+    g = int(geom) if isinstance(geom, (int, np.integer)) else _geom_struct(geom)[0]
+    planes, nbytes = _i(0), ctypes.c_size_t(0)
+    _lib.call("mexct_osc_tv_ooc_plan", int(W), int(H), int(nP), g, int(numIter), int(numSubsInit),
+              int(numSubsFinal), float(pVal), int(budget_bytes), ctypes.byref(planes),
+              ctypes.byref(nbytes))
+    return planes.value, nbytes.value
+
+
+def OSC_TV_recon_ooc(pre, post, scanAngles, geom, numIter, TV_constant, numSubsInit,
+                     numSubsFinal, pVal, first_picks, budget_bytes):
+    """OSC_TV_recon with mu in host memory, streamed through the device in
+    z-slabs within budget_bytes of device memory.  Returns (recon, slab
+    thickness in slices)."""
+    pre = _f32F(pre, "pre")
+    post = _f32F(post, "post")
+    W, H, nP = post.shape
+    g, sad = _geom_struct(geom)
+    ang = _angles(scanAngles, nP)
+    fp = np.ascontiguousarray(np.asarray(first_picks, dtype=np.int32).ravel())
+    if fp.size < int(numIter):
+        raise ValueError("first_picks needs one entry per iteration")
+    out = np.empty((W, W, H), dtype=np.float32, order="F")
+    planes = _i(0)
+    _lib.call("mexct_osc_tv_recon_ooc", None, _ptr(pre), _ptr(post), W, H, nP, _ptr(ang),
+              float(sad), g, int(numIter), float(TV_constant), int(numSubsInit),
+              int(numSubsFinal), float(pVal), _ptr(fp), int(budget_bytes), _ptr(out),
+              ctypes.byref(planes))
+    return out, planes.value
 
 
 class OscTvSolver:
