@@ -18,9 +18,12 @@ extern "C" {
  * iteration, and from k = 2 the FP64 step norm d_a, 20 TV steps with
  * c = TV_constant*d_a and NaN/Inf -> 0.  Storage of mu may be MEXCT_F32
  * or MEXCT_BF16 (pre/post stay FP32: counts exceed FP16 range; every sum
- * accumulates in FP32, every norm in FP64).  MEXCT_F16 is accepted but
+ * accumulates in FP32, every norm in FP64).  MEXCT_F16 mu is accepted but
  * underflows the initial mu = 1e-10 (below FP16's smallest subnormal), so the
- * multiplicative update stays at 0: use BF16 for a low-precision OSC-TV. */
+ * multiplicative update stays at 0.  BF16 mu (8-bit mantissa) lands ~1e-1 from
+ * the FP32 iterates after 20 iterations: outside a 1e-3 accuracy bound.  The
+ * low-precision form near it keeps mu and the counts in FP32 and stores the
+ * residual views in FP16 (mexct_osctv_create_ex). */
 typedef struct mexct_osctv mexct_osctv;
 
 typedef struct mexct_osctv_params {
@@ -40,6 +43,18 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre,
                                 const float* angles, float sad, int geom,
                                 int mu_type, void* stream,
                                 mexct_osctv** out);
+/* As mexct_osctv_create, with the storage of the residual views (the OSC
+ * forward pass's pre e^-l - post and pre e^-l l, read by the dual BP) chosen:
+ * MEXCT_F32, or MEXCT_F16 (FP32 mu only) holding the residuals times one power
+ * of two that brings the largest count to <= 2^15 (FP16 cannot hold counts
+ * above 65504; the update num/den does not depend on a common scale of the
+ * two residuals).  The counts stay FP32: rounding them to FP16 moves the
+ * reconstruction itself.  Every sum accumulates in FP32, every norm in FP64. */
+mexct_status mexct_osctv_create_ex(mexct_ctx* ctx, const float* d_pre,
+                                   const float* d_post, int W, int H, int nP,
+                                   const float* angles, float sad, int geom,
+                                   int mu_type, int data_type, void* stream,
+                                   mexct_osctv** out);
 /* Run iterations k0+1 .. k0+n (k0 = iterations already run); first_picks
  * holds one 0-based first subset per iteration of this call. */
 mexct_status mexct_osctv_run(mexct_osctv* s, const mexct_osctv_params* p,

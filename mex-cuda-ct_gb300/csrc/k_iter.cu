@@ -573,6 +573,27 @@ cudaError_t launch_clamp_copy(const float* src, float* dst, long long n, float e
   return cudaGetLastError();
 }
 
+// Largest finite value of n FP32 values as an order-preserving integer key
+// (atomicMax on the bits of a non-negative float orders like the float; a
+// negative or NaN value counts as 0).  *out must start at 0.
+__global__ void max_nonneg_kernel(const float* __restrict__ x, long long n,
+                                  unsigned* __restrict__ out) {
+  unsigned m = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float v = x[i];
+    if (v > 0.f && v <= 3.4028235e38f) m = max(m, __float_as_uint(v));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+cudaError_t launch_max_nonneg(const float* x, long long n, unsigned* out, cudaStream_t st) {
+  max_nonneg_kernel<<<device_sms() * 8, 256, 0, st>>>(x, n, out);
+  return cudaGetLastError();
+}
+
 template <typename S, typename D>
 __global__ void convert_kernel(const S* __restrict__ s, D* __restrict__ d,
                                long long n) {

@@ -944,11 +944,12 @@ cudaError_t launch_g3d_bp(const RayArgs& a, const float* sino,
 // DET: a decoupled detector (A.det_w x A.det_h pixels of reciprocal pitch
 // A.inv_du, A.inv_dv; no counterpart in the reference): every geometry
 // interpolates its residuals in v, as the detector BP does.
-template <int GEOM, int ZC, typename TM, bool DET = false>
+template <int GEOM, int ZC, typename TM, bool DET = false, typename SD = float>
 __global__ void __launch_bounds__(256) osc_bp_update_kernel(
-    const __grid_constant__ VoxArgs A, const float* __restrict__ rpre,
-    const float* __restrict__ rpost, TM* __restrict__ mu, TM* __restrict__ padx,
+    const __grid_constant__ VoxArgs A, const void* __restrict__ rpre,
+    const void* __restrict__ rpost, TM* __restrict__ mu, TM* __restrict__ padx,
     TM* __restrict__ pady, int Pf) {
+  using Q = typename QuadT<SD>::T;  // residual quads: float4, or four FP16 in a uint2
   // 8 x 4 column patch per warp, as in bp_pad_kernel (blocks of 32 x 8)
   const int w = threadIdx.y, lane = threadIdx.x;
   const int ix = blockIdx.x * 32 + 8 * (w & 3) + (lane & 7);
@@ -972,17 +973,17 @@ __global__ void __launch_bounds__(256) osc_bp_update_kernel(
             : col_geom<GEOM>(x, y, A.trig[v], A.SR, A.v0, (float)A.hw, A.v0, 1.f, 1.f);
     // zero frame = border addressing (CUDAmex_oscIter.cu:419-425); residuals
     // in the quad layout written by the FP epilogue
-    const float4* qpre = reinterpret_cast<const float4*>(rpre) + (size_t)v * vstride;
-    const float4* qpost = reinterpret_cast<const float4*>(rpost) + (size_t)v * vstride;
+    const Q* qpre = static_cast<const Q*>(rpre) + (size_t)v * vstride;
+    const Q* qpost = static_cast<const Q*>(rpost) + (size_t)v * vstride;
     if constexpr (DET) {
-      bp_column_quad<ZC, float, GEOM>(qpre, A.det_w, A.det_h, Wp, z0, g, num);
-      bp_column_quad<ZC, float, GEOM>(qpost, A.det_w, A.det_h, Wp, z0, g, den);
+      bp_column_quad<ZC, SD, GEOM>(qpre, A.det_w, A.det_h, Wp, z0, g, num);
+      bp_column_quad<ZC, SD, GEOM>(qpost, A.det_w, A.det_h, Wp, z0, g, den);
     } else if constexpr (GEOM == 2) {
-      bp_column_quad<ZC, float>(qpre, A.W, A.H, Wp, z0, g, num);
-      bp_column_quad<ZC, float>(qpost, A.W, A.H, Wp, z0, g, den);
+      bp_column_quad<ZC, SD>(qpre, A.W, A.H, Wp, z0, g, num);
+      bp_column_quad<ZC, SD>(qpost, A.W, A.H, Wp, z0, g, den);
     } else {
-      bp_column_quadrows<GEOM, ZC, float>(qpre, A.W, A.H, Wp, z0, g, num);
-      bp_column_quadrows<GEOM, ZC, float>(qpost, A.W, A.H, Wp, z0, g, den);
+      bp_column_quadrows<GEOM, ZC, SD>(qpre, A.W, A.H, Wp, z0, g, num);
+      bp_column_quadrows<GEOM, ZC, SD>(qpost, A.W, A.H, Wp, z0, g, den);
     }
   }
   const size_t base = (size_t)iy * A.W + ix;
@@ -1023,13 +1024,24 @@ cudaError_t launch_osc_bp_update_det(int geom, const VoxArgs& a, const float* rp
 }
 
 cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
-                                 const float* rpre, const float* rpost,
+                                 const void* rpre, const void* rpost,
                                  void* mu, int mt, void* padx, void* pady, int Pf,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, int dt) {
   constexpr int ZC = 4;
   if (a.zoff % ZC != 0 || a.zoff < 0 || a.nzs < 1 || a.zoff + a.nzs > a.H)
     return cudaErrorInvalidValue;
   dim3 blk(32, 8), grd((a.W + 31) / 32, (a.W + 7) / 8, (a.nzs + ZC - 1) / ZC);
+  if (dt == kF16) {  // FP16 residual views (FP32 mu)
+    if (mt != kF32) return cudaErrorInvalidValue;
+#define OSC_BP16(G)                                                                      \
+  osc_bp_update_kernel<G, ZC, float, false, __half><<<grd, blk, 0, st>>>(                \
+      a, rpre, rpost, (float*)mu, (float*)padx, (float*)pady, Pf)
+    if (geom == 0) OSC_BP16(0);
+    else if (geom == 1) OSC_BP16(1);
+    else OSC_BP16(2);
+#undef OSC_BP16
+    return cudaGetLastError();
+  }
 #define OSC_BP(G, T)                                                                 \
   osc_bp_update_kernel<G, ZC, T><<<grd, blk, 0, st>>>(a, rpre, rpost, (T*)mu, (T*)padx, \
                                                       (T*)pady, Pf)

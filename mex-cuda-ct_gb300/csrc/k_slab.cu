@@ -868,7 +868,8 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     if (valid) {
       const float l = acc * J.step;
       const size_t gi = (size_t)J.gview * J.P + (size_t)iy * J.det_w + ix;
-      const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
+      const float pv = __ldg(static_cast<const float*>(E.pre) + gi);
+      const float qv = __ldg(static_cast<const float*>(E.post) + gi);
       t = (double)(pv * expf(-l)) + (double)qv * (double)l;
     }
 #pragma unroll
@@ -891,7 +892,8 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       stf(o, (SUB && J.accum) ? ldp(o) + l : l);
     } else {
       // CUDAmex_oscIter.cu:262-268: pre' = pre e^-l - post, post' = pre e^-l l.
-      const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
+      const float pv = __ldg(static_cast<const float*>(E.pre) + gi);
+      const float qv = __ldg(static_cast<const float*>(E.post) + gi);
       const float ehat = pv * expf(-l);
       // padded residual view [H+4][W+4] (zero frame kept by the caller)
       const int Wp = sino_pad_pitch(J.det_w);
@@ -904,8 +906,14 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       const size_t q[4] = {4 * ri, 4 * (ri - Wp) + 1, 4 * (ri - 1) + 2, 4 * (ri - Wp - 1) + 3};
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        E.rpre[q[t]] = r0;
-        E.rpost[q[t]] = r1;
+        if constexpr (std::is_same<TO, float>::value) {
+          static_cast<float*>(E.rpre)[q[t]] = r0;
+          static_cast<float*>(E.rpost)[q[t]] = r1;
+        } else {
+          // 16-bit residual views hold the residuals times a power of two
+          stf(static_cast<TO*>(E.rpre) + q[t], r0 * E.rscale);
+          stf(static_cast<TO*>(E.rpost) + q[t], r1 * E.rscale);
+        }
       }
     }
   }
@@ -1151,6 +1159,13 @@ cudaError_t launch_fp_slab(int geom, bool border, bool osc, const RayArgs& a,
                            const SlabEpi& e, cudaStream_t st) {
 #define GO(G, B, EP, TV, TO) return slab_go<G, B, EP, TV, TO>(a, mx, my, px, py, Pf, out, e, st)
   if (osc) {
+    // ot: storage of the residual views (FP16 with FP32 mu only)
+    if (ot == kF16) {
+      if (vt != kF32) return cudaErrorInvalidValue;
+      if (geom == 0) GO(0, true, 1, float, __half);
+      if (geom == 1) GO(1, true, 1, float, __half);
+      GO(2, true, 1, float, __half);
+    }
     if (vt == kF32) {
       if (geom == 0) GO(0, true, 1, float, float);
       if (geom == 1) GO(1, true, 1, float, float);

@@ -65,15 +65,18 @@ cudaError_t launch_fp(int geom, bool border, const RayArgs& a,
 
 // Slab-staged FP (k_slab.cu): padded volumes in both layouts, TMA tensor maps
 // over them, and the kernel.  With osc = true the kernel samples the
-// zero-padded mu with step 0.5 and writes the OSC residuals instead.
+// zero-padded mu with step 0.5 and writes the OSC residuals instead; ot is
+// then the storage of the residual views (kF32, or kF16 with FP32 mu, holding
+// the residuals times e.rscale).
 struct SlabEpi {
-  const float* pre;  // OSC: pre/post counts and residual outputs
-  const float* post;
-  float* rpre;       // residuals in the padded-sinogram layout of each view:
-  float* rpost;      // [H+4][W+4] with a zero frame (border addressing)
+  const float* pre;  // OSC: pre/post counts and residual outputs (FP32, or FP16
+  const float* post; // times rscale: the launch's residual type)
+  void* rpre;        // residuals in the padded-sinogram layout of each view:
+  void* rpost;       // [H+4][W+4] with a zero frame (border addressing)
   unsigned* err;     // set to non-zero when a bounded wait gave up
   int wait_us;       // limit of one wait: 0 = default (2 s), < 0 = give up at once
   double* obj;       // objective epilogue: one FP64 partial sum per CTA
+  float rscale = 1.f;  // 16-bit residual views: residuals times this power of two
 };
 int slab_pitch(int W);
 // CTAs of the slab FP kernels resident per SM (its launch bounds); persistent
@@ -237,11 +240,12 @@ cudaError_t launch_osc_bp_update_det(int geom, const VoxArgs& a, const float* rp
                                      const float* rpost, void* mu, int mt, void* padx,
                                      void* pady, int Pf, cudaStream_t st);
 // Updates slices a.zoff .. a.zoff + a.nzs - 1 (a.zoff a multiple of 4) held
-// at mu (and at slab-local rows of padx / pady).
+// at mu (and at slab-local rows of padx / pady).  dt: storage of the residual
+// views (kF32, or kF16 with FP32 mu).
 cudaError_t launch_osc_bp_update(int geom, const VoxArgs& a,
-                                 const float* rpre, const float* rpost,
+                                 const void* rpre, const void* rpost,
                                  void* mu, int mu_type, void* padx, void* pady, int Pf,
-                                 cudaStream_t st);
+                                 cudaStream_t st, int dt = kF32);
 // Residual views (padded quad layout) of nviews views from their line
 // integrals l and counts pre / post, all W x H x nviews FP32.
 cudaError_t launch_osc_residual(const float* l, const float* pre, const float* post, int W, int H,
@@ -281,6 +285,9 @@ cudaError_t launch_fill(void* x, int dtype, long long n, float v,
                         cudaStream_t st);
 cudaError_t launch_clamp_copy(const float* src, float* dst, long long n,
                               float eps, cudaStream_t st);
+// *out = bits of the largest positive finite value of x (0 if none); *out must
+// start at 0.
+cudaError_t launch_max_nonneg(const float* x, long long n, unsigned* out, cudaStream_t st);
 cudaError_t launch_convert(const void* src, int src_type, void* dst,
                            int dst_type, long long n, cudaStream_t st);
 

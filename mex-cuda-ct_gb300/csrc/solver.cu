@@ -33,6 +33,10 @@ struct mexct_osctv {
   mexct_ctx* ctx = nullptr;
   int device = 0;
   int W = 0, H = 0, nP = 0, geom = 0, mu_type = kF32;
+  // Storage of the residual views: kF32, or kF16 holding the residuals times
+  // 2^-data_exp (the OSC update num/den does not depend on a common scale of
+  // the two residuals).
+  int data_type = kF32, data_exp = 0;
   float sad = 0.f;
   std::vector<float> angles;
   Buf mu, mu_old, pre, post, padx, pady, err, r1, r2, tvbuf, red, cnt, scal, objp;
@@ -175,14 +179,15 @@ mexct_status enqueue_iteration(mexct_osctv* s, bool k_gt1, int nsub,
       va->trig[i] = ra->trig[i];
     }
     if (nv > 0) {
-      SlabEpi e{s->pre.as<float>(), s->post.as<float>(), s->r1.as<float>(), s->r2.as<float>(),
+      SlabEpi e{s->pre.as<float>(), s->post.as<float>(), s->r1.p, s->r2.p,
                 s->err.as<unsigned>()};
+      e.rscale = std::ldexp(1.0f, -s->data_exp);
       MEXCT_TRY_CUDA(launch_fp_slab(s->geom, true, true, *ra, mx, my, s->padx.p, s->pady.p, Pf,
-                                    s->mu_type, nullptr, kF32, e, st),
+                                    s->mu_type, nullptr, s->data_type, e, st),
                      "osctv: fp");
     }
-    MEXCT_TRY_CUDA(launch_osc_bp_update(s->geom, *va, s->r1.as<float>(), s->r2.as<float>(),
-                                        s->mu.p, s->mu_type, s->padx.p, s->pady.p, Pf, st),
+    MEXCT_TRY_CUDA(launch_osc_bp_update(s->geom, *va, s->r1.p, s->r2.p, s->mu.p, s->mu_type,
+                                        s->padx.p, s->pady.p, Pf, st, s->data_type),
                    "osctv: bp/update");
   }
   (void)P;
@@ -226,6 +231,14 @@ mexct_status mexct_subset_order(int n_sub, int first_pick, int32_t* picks) {
 mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float* d_post,
                                 int W, int H, int nP, const float* angles, float sad, int geom,
                                 int mu_type, void* stream, mexct_osctv** out) {
+  return mexct_osctv_create_ex(ctx, d_pre, d_post, W, H, nP, angles, sad, geom, mu_type,
+                               MEXCT_F32, stream, out);
+}
+
+mexct_status mexct_osctv_create_ex(mexct_ctx* ctx, const float* d_pre, const float* d_post,
+                                   int W, int H, int nP, const float* angles, float sad,
+                                   int geom, int mu_type, int data_type, void* stream,
+                                   mexct_osctv** out) {
   if (!out) return set_err(MEXCT_ERR_ARG, "osctv_create: out is NULL");
   *out = nullptr;
   if (!d_pre || !d_post || !angles) return set_err(MEXCT_ERR_ARG, "osctv_create: NULL pointer");
@@ -234,6 +247,10 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   if (geom < 0 || geom > 2) return set_err(MEXCT_ERR_ARG, "osctv_create: invalid geometry %d", geom);
   if (mu_type != kF32 && mu_type != kF16 && mu_type != kBF16)
     return set_err(MEXCT_ERR_ARG, "osctv_create: bad storage type %d", mu_type);
+  if (data_type != kF32 && data_type != kF16)
+    return set_err(MEXCT_ERR_ARG, "osctv_create: bad data storage type %d", data_type);
+  if (data_type == kF16 && mu_type != kF32)
+    return set_err(MEXCT_ERR_UNSUPPORTED, "osctv_create: FP16 residual views need FP32 mu");
   mexct_ctx* c = resolve(ctx);
   if (!c) return set_err(MEXCT_ERR_CUDA, "osctv_create: no CUDA device / context");
   DevGuard dg(c->device);
@@ -247,6 +264,7 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   s->geom = geom;
   s->sad = sad;
   s->mu_type = mu_type;
+  s->data_type = data_type;
   s->angles.assign(angles, angles + nP);
   MEXCT_TRY_CUDA(cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking), "osctv_create: stream");
   MEXCT_TRY_CUDA(cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming), "osctv_create: event");
@@ -267,11 +285,12 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   MEXCT_TRY_CUDA(s->tvbuf.ensure_async(vb, a), "osctv_create: tv");
   MEXCT_TRY_CUDA(s->padx.ensure_async(pb, a), "osctv_create: padded mu");
   MEXCT_TRY_CUDA(s->pady.ensure_async(pb, a), "osctv_create: padded mu");
+  const size_t db = dsize(data_type);
   MEXCT_TRY_CUDA(s->pre.ensure_async(M * 4, a), "osctv_create: pre");
   MEXCT_TRY_CUDA(s->post.ensure_async(M * 4, a), "osctv_create: post");
   // residual views in the padded layout; their zero frame (border addressing)
   // is written once here and never touched again
-  const size_t rb = sino_pad_elems(W, H, (int)maxv) * sizeof(float4);  // quad layout
+  const size_t rb = sino_pad_elems(W, H, (int)maxv) * 4 * db;  // quad layout
   (void)P;
   MEXCT_TRY_CUDA(s->r1.ensure_async(rb, a), "osctv_create: residual");
   MEXCT_TRY_CUDA(s->r2.ensure_async(rb, a), "osctv_create: residual");
@@ -290,6 +309,23 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
   MEXCT_TRY_CUDA(cudaStreamWaitEvent(st, s->ev_in, 0), "osctv_create: join");
   // OSC_TV_recon.m:33 mu = 1e-10; :35-37 pre/post clamped to >= 1e-6.
   MEXCT_TRY_CUDA(launch_fill(s->mu.p, mu_type, (long long)N, 1e-10f, st), "osctv_create: mu");
+  if (data_type == kF16) {
+    // one power-of-two scale for both residuals (|pre e^-l - post| and
+    // pre e^-l l are below max(pre, post)): the largest count to <= 2^15
+    unsigned* d_max = reinterpret_cast<unsigned*>(s->scal.as<double>() + 4);
+    MEXCT_TRY_CUDA(cudaMemsetAsync(d_max, 0, sizeof(unsigned), st), "osctv_create: scale");
+    MEXCT_TRY_CUDA(launch_max_nonneg(d_pre, (long long)M, d_max, st), "osctv_create: scale");
+    MEXCT_TRY_CUDA(launch_max_nonneg(d_post, (long long)M, d_max, st), "osctv_create: scale");
+    unsigned bits = 0;
+    MEXCT_TRY_CUDA(cudaMemcpyAsync(&bits, d_max, sizeof bits, cudaMemcpyDeviceToHost, st),
+                   "osctv_create: scale");
+    MEXCT_TRY_CUDA(cudaStreamSynchronize(st), "osctv_create: scale");
+    float mx;
+    std::memcpy(&mx, &bits, sizeof mx);
+    int e = 0;
+    while (e < 100 && std::ldexp((double)mx, -e) > 32768.0) ++e;
+    s->data_exp = e;
+  }
   MEXCT_TRY_CUDA(launch_clamp_copy(d_pre, s->pre.as<float>(), (long long)M, 1e-6f, st),
                  "osctv_create: pre");
   MEXCT_TRY_CUDA(launch_clamp_copy(d_post, s->post.as<float>(), (long long)M, 1e-6f, st),
@@ -305,10 +341,9 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre, const float*
     std::unique_ptr<RayArgs> ra(new RayArgs);
     fill_std_rays(*ra, W, H, sad, geom, true);
     ra->nviews = 0;  // no work: sets attributes only
-    SlabEpi e{s->pre.as<float>(), s->post.as<float>(), s->r1.as<float>(), s->r2.as<float>(),
-              s->err.as<unsigned>()};
+    SlabEpi e{s->pre.as<float>(), s->post.as<float>(), s->r1.p, s->r2.p, s->err.as<unsigned>()};
     MEXCT_TRY_CUDA(launch_fp_slab(geom, true, true, *ra, mx, my, s->padx.p, s->pady.p, Pf,
-                                  mu_type, nullptr, kF32, e, st),
+                                  mu_type, nullptr, data_type, e, st),
                    "osctv_create: kernel setup");
     e.obj = s->objp.as<double>();
     MEXCT_TRY_CUDA(launch_fp_slab_objective(geom, *ra, mx, my, s->padx.p, s->pady.p, Pf, mu_type,

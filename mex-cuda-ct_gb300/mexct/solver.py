@@ -25,6 +25,8 @@ class Params(ctypes.Structure):
 
 
 _lib.register("mexct_osctv_create", [_P, _P, _P, _i, _i, _i, _P, _f, _i, _i, _P, ctypes.POINTER(_P)])
+_lib.register("mexct_osctv_create_ex", [_P, _P, _P, _i, _i, _i, _P, _f, _i, _i, _i, _P,
+                                        ctypes.POINTER(_P)])
 _lib.register("mexct_osctv_run", [_P, ctypes.POINTER(Params), _P, _i, _P])
 _lib.register("mexct_osctv_mu", [_P, _P, _P])
 _lib.register("mexct_osctv_stats", [_P, ctypes.POINTER(_i), ctypes.POINTER(_d), ctypes.POINTER(_d)])
@@ -103,22 +105,28 @@ def OSC_TV_recon_ooc(pre, post, scanAngles, geom, numIter, TV_constant, numSubsI
 
 
 class OscTvSolver:
-    """Resident OSC-TV state for device tensors pre/post (nP, H, W) float32."""
+    """Resident OSC-TV state for device tensors pre/post (nP, H, W) float32.
 
-    def __init__(self, pre, post, angles, sad, geom, mu_dtype=None, stream=None):
+    mu_dtype: storage of mu (float32, bfloat16; float16 underflows the initial
+    mu).  data_dtype: storage of the residual views between the forward pass and
+    the dual BP (float32, or float16 with one power-of-two scale; FP32 mu only)."""
+
+    def __init__(self, pre, post, angles, sad, geom, mu_dtype=None, stream=None,
+                 data_dtype=None):
         import torch
 
         self._torch = torch
         nP, H, W = pre.shape
         self.W, self.H, self.nP = W, H, nP
         self.angles = _angles(angles, nP)
-        code = {None: _lib.F32, torch.float32: _lib.F32, torch.float16: _lib.F16,
-                torch.bfloat16: _lib.BF16}[mu_dtype]
+        codes = {None: _lib.F32, torch.float32: _lib.F32, torch.float16: _lib.F16,
+                 torch.bfloat16: _lib.BF16}
+        code, dcode = codes[mu_dtype], codes[data_dtype]
         self.stream = stream if stream is not None else torch.cuda.current_stream()
         h = _P()
-        _lib.call("mexct_osctv_create", None, _P(pre.data_ptr()), _P(post.data_ptr()), W, H, nP,
-                  _ptr(self.angles), float(sad), int(geom), code, _P(self.stream.cuda_stream),
-                  ctypes.byref(h))
+        _lib.call("mexct_osctv_create_ex", None, _P(pre.data_ptr()), _P(post.data_ptr()), W, H,
+                  nP, _ptr(self.angles), float(sad), int(geom), code, dcode,
+                  _P(self.stream.cuda_stream), ctypes.byref(h))
         self.h = h
 
     def run(self, first_picks, n_iter, tv_const, n_sub_init, n_sub_final, p_val, use_graph=True,
