@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--osc-reps", type=int, default=5)
     ap.add_argument("--batch-problems", type=int, default=48)
     ap.add_argument("--serve-requests", type=int, default=60)
+    ap.add_argument("--config5", action="store_true",
+                    help="run only the serving workload at its stated mix (minutes of GPU time)")
     ap.add_argument("--ops-once", action="store_true",
                     help="run one call of each secondary operator on 256^3 and exit "
                          "(the workload of the secondary-kernel profiles)")
@@ -312,6 +314,10 @@ def main():
     V = ctypes.c_void_p
     if args.ops_once:
         ops_once()
+        return
+    if args.config5:
+        if rank == 0:
+            config5(args)
         return
 
     n, views, geom = args.size, args.views, args.geom
@@ -1007,40 +1013,46 @@ def autotune_section(classes=((64, 90, 2), (96, 180, 0), (128, 360, 2), (256, 72
     return out
 
 
-def serving(count, seed=7):
+def serving(count, seed=7, sizes=(128, 256), size_p=(0.7, 0.3), views=(60, 180, 360),
+            serial_sample=None, saturated=True, budget_gb=48):
     """Open-loop Poisson arrivals of FDK / OSC-TV (10 iterations x 10 subsets)
-    requests on 128^3 / 256^3 volumes with 60..360 views, random geometry, FP32 or
-    BF16 mu; lambda set for ~80% of the one-at-a-time service rate.  The same
-    request stream runs through a one-slot server (plain: FIFO, one request on the
-    device at a time) and a four-slot server (chosen: admission by HBM footprint,
-    requests overlap on their own streams).  Reports p50/p99 latency (submission to
-    completion) and volumes/s, and checks every result against the one-request
-    entry points."""
+    requests on seeded ellipsoid volumes of the given sizes and view counts, random
+    geometry, FP32 or FP16 storage (OSC-TV: FP16 residual views with FP32 mu);
+    lambda set for ~80% of the one-at-a-time service rate.  The same request stream
+    runs through a one-slot server (plain: FIFO, one request on the device at a time)
+    and a four-slot server (chosen: admission by HBM footprint, requests overlap on
+    their own streams).  Reports p50/p99 latency (submission to completion) and
+    volumes/s, and checks results against the one-request entry points: every
+    request (serial_sample None), or a seeded sample of serial_sample requests, whose
+    mean service time then sets lambda."""
     import torch
 
     import mexct
-    from mexct import ops, phantoms, serve, solver
+    from mexct import _lib, ops, phantoms, serve, solver
 
     rng = np.random.default_rng(seed)
     datasets = {}
-    for n in (128, 256):
-        for nv in (60, 180, 360):
-            vol = phantoms.ellipsoids(n, count=8, seed=n + nv, nz=n)
+    for n in sizes:
+        vol = phantoms.ellipsoids(n, count=8, seed=n, nz=n)
+        d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+        for nv in views:
             ang = phantoms.angles_full(nv)
-            d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
             fpd = ops.fp_dev(d, 1000.0, ang, 2)
             torch.cuda.synchronize()
             fp = fpd.cpu().numpy().transpose(2, 1, 0)
+            del fpd
             pre = np.full(fp.shape, 1e5, dtype=np.float32, order="F")
             post = np.asfortranarray(rng.poisson(1e5 * np.exp(-fp.astype(np.float64)))
                                      .astype(np.float32))
             datasets[(n, nv)] = (pre, post, ang)
+        del d
+        torch.cuda.empty_cache()
     reqs = []
     for i in range(count):
-        n = int(rng.choice([128, 256], p=[0.7, 0.3]))
-        nv = int(rng.choice([60, 180, 360]))
+        n = int(rng.choice(list(sizes), p=list(size_p)))
+        nv = int(rng.choice(list(views)))
         reqs.append({"kind": int(rng.integers(0, 2)), "key": (n, nv), "geom": int(rng.integers(0, 3)),
-                     "mu": int(rng.choice([0, 2])), "picks": rng.integers(0, 10, 10)})
+                     "f16": bool(rng.integers(0, 2)), "picks": rng.integers(0, 10, 10)})
     gs = {0: "par3d", 1: "fan3d", 2: "cone3d"}
 
     def alone(r):
@@ -1048,21 +1060,24 @@ def serving(count, seed=7):
         if r["kind"] == 0:
             return mexct.FBP_recon(pre, post, ang, {"type": gs[r["geom"]], "SAD": 1000.0},
                                    "hamming", 1.0, 1.0)
-        if r["mu"] == 0:
+        if not r["f16"]:
             return solver.OSC_TV_recon(pre, post, ang, {"type": gs[r["geom"]], "SAD": 1000.0}, 10,
                                        0.2, 10, 10, 1.0, r["picks"])
         srv = serve.Server(slots=1, budget_bytes=64 << 30)
-        t = srv.submit_osctv(pre, post, ang, r["geom"], r["picks"], n_iter=10, n_sub=10, mu_type=2)
+        t = srv.submit_osctv(pre, post, ang, r["geom"], r["picks"], n_iter=10, n_sub=10,
+                             data_type=_lib.F16)
         out = srv.wait(t)[0]
         srv.close()
         return out
 
     alone(reqs[0])  # warm-up
-    serial = []
+    check = list(range(count)) if serial_sample is None else sorted(
+        rng.choice(count, min(serial_sample, count), replace=False).tolist())
+    serial = {}
     t0 = time.perf_counter()
-    for r in reqs:
-        serial.append(alone(r))
-    mean_s = (time.perf_counter() - t0) / count
+    for i in check:
+        serial[i] = alone(reqs[i])
+    mean_s = (time.perf_counter() - t0) / len(check)
     lam = 0.8 / mean_s
     gaps = rng.exponential(1.0 / lam, count)
 
@@ -1071,13 +1086,13 @@ def serving(count, seed=7):
         if r["kind"] == 0:
             return srv.submit_fdk(pre, post, ang, r["geom"])
         return srv.submit_osctv(pre, post, ang, r["geom"], r["picks"], n_iter=10, n_sub=10,
-                                mu_type=r["mu"])
+                                data_type=_lib.F16 if r["f16"] else _lib.F32)
 
     def run(slots, open_loop):
         """The request stream through a server with `slots` slots: open loop (the
         Poisson arrival times) or closed (everything queued at once, for peak
         volumes/s).  Latency = completion - submission."""
-        srv = serve.Server(slots=slots, budget_bytes=48 << 30)
+        srv = serve.Server(slots=slots, budget_bytes=int(budget_gb) << 30)
         tickets = []
         t0 = time.perf_counter()
         due = t0
@@ -1089,28 +1104,48 @@ def serving(count, seed=7):
                     time.sleep(due - now)
             tickets.append(submit(srv, r))
         lat, same = [], 0
-        for a, t in zip(serial, tickets):
+        for i, t in enumerate(tickets):
             rec, tm = srv.wait(t)
             lat.append(tm["total_s"])
-            same += int(np.array_equal(rec, a))
+            if i in serial:
+                same += int(np.array_equal(rec, serial[i]))
         makespan = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
         return {"p50_s": round(float(np.percentile(lat, 50)), 4),
                 "p99_s": round(float(np.percentile(lat, 99)), 4),
                 "volumes_per_s": round(count / makespan, 3),
-                "identical_to_alone": "%d/%d" % (same, count),
+                "identical_to_alone": "%d/%d" % (same, len(serial)),
                 "max_concurrent": st["max_concurrent"],
                 "peak_hbm_gb": round(st["peak_bytes"] / 2**30, 2)}
 
     out = {"requests": count, "lambda_per_s": round(lam, 3),
-           "mean_service_s": round(mean_s, 4)}
-    out["plain"] = {"slots": 1, "poisson": run(1, True), "saturated": run(1, False)}
-    out["chosen"] = {"slots": 4, "poisson": run(4, True), "saturated": run(4, False)}
-    out["workload"] = ("FDK or OSC-TV (10 it x 10 subsets) on 128^3/256^3, 60/180/360 views, "
-                       "geom 0/1/2, FP32/BF16 mu; Poisson arrivals at 80%% of the one-at-a-time "
-                       "service rate (%.3f /s), and all requests queued at once (saturated)" % lam)
+           "mean_service_s": round(mean_s, 4), "serial_checked": len(check)}
+    out["plain"] = {"slots": 1, "poisson": run(1, True)}
+    out["chosen"] = {"slots": 4, "poisson": run(4, True)}
+    if saturated:
+        out["plain"]["saturated"] = run(1, False)
+        out["chosen"]["saturated"] = run(4, False)
+    out["workload"] = ("FDK or OSC-TV (10 it x 10 subsets) on %s^3 volumes, %s views, geom 0/1/2, "
+                       "FP32 or FP16 storage (OSC-TV FP16 residual views); Poisson arrivals at 80%% "
+                       "of the one-at-a-time service rate (%.3f /s)%s"
+                       % ("/".join(map(str, sizes)), "/".join(map(str, views)), lam,
+                          ", and all requests queued at once (saturated)" if saturated else ""))
     return out
+
+
+def config5(args):
+    """The serving workload at its stated mix: Poisson arrivals at ~80% load of FDK or
+    OSC-TV (10 x 10) requests on 128^3..512^3 volumes with 60..720 views, random
+    geometry, FP32 or FP16 storage; p50/p99 and volumes/s of a one-slot and a four-slot
+    server, results checked against one-request calls on a seeded sample.  Opt-in
+    (bench.py --config5 [--serve-requests N]): at ~0.5 s of GPU work per request it
+    runs for minutes per 100 requests."""
+    line = {"config5": serving(args.serve_requests, seed=11, sizes=(128, 256, 384, 512),
+                               size_p=(0.25, 0.25, 0.25, 0.25), views=(60, 240, 480, 720),
+                               serial_sample=min(40, args.serve_requests), saturated=False,
+                               budget_gb=96)}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

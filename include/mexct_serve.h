@@ -39,6 +39,8 @@ typedef struct mexct_request {
   float p_val;
   const int32_t* first_picks; /* OSC-TV: n_iter 0-based first subsets */
   double simulate_s;     /* > 0: no GPU work, the slot is held this long */
+  int data_type;         /* OSC-TV: storage of the residual views, MEXCT_F32
+                            (0 counts as F32) or MEXCT_F16 (FP32 mu only) */
 } mexct_request;
 
 typedef struct mexct_server mexct_server;

@@ -151,7 +151,8 @@ mexct_status prepare_slab_bufs(Buf& px, Buf& py, Buf& err, const void* d_vol, in
 mexct_status osc_tv_recon_typed(mexct_ctx* ctx, const float* pre, const float* post, int W, int H,
                                 int nP, const float* angles, float sad, int geom, int n_iter,
                                 float tv_const, int n_sub_init, int n_sub_final, float p_val,
-                                const int32_t* first_picks, int mu_type, float* recon);
+                                const int32_t* first_picks, int mu_type, float* recon,
+                                int data_type = 0);
 mexct_status prepare_slab(mexct_ctx* c, const void* d_vol, int vt, int W, int H,
                           bool border, int geom, CUtensorMap* mx, CUtensorMap* my, int* Pf_out,
                           cudaStream_t st);

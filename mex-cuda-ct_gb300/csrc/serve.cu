@@ -52,7 +52,7 @@ mexct_status run_job(Job& j, mexct_ctx* c) {
                      r.cutoff, r.q, r.recon);
   return osc_tv_recon_typed(c, r.pre, r.post, r.W, r.H, r.nP, r.angles, r.sad, r.geom,
                             r.n_iter, r.tv_const, r.n_sub_init, r.n_sub_final, r.p_val,
-                            j.picks.data(), r.mu_type, r.recon);
+                            j.picks.data(), r.mu_type, r.recon, r.data_type);
 }
 
 }  // namespace
@@ -120,9 +120,15 @@ size_t mexct_request_bytes(const mexct_request* r) {
   const size_t pad = (size_t)slab_pitch(r->W) * (r->W + 2) * (r->H + 2);
   if (r->kind == MEXCT_REQ_FDK) return 4 * (3 * M + N) + 4 * (size_t)r->nP * r->W + (1 << 20);
   const size_t ds = r->mu_type == MEXCT_F32 ? 4 : 2;
-  // staging (pre, post, recon) + solver (pre, post, residuals sized for one
-  // subset of up to nP views, mu, mu_old, TV buffer, two padded copies).
-  return 4 * (2 * M + N) + 4 * (2 * M) + 4 * (2 * M) + ds * (3 * N + 2 * pad) + (1 << 20);
+  // the largest subset's residual views: two views in the padded quad layout
+  // (four values per texel) per view
+  const int smin = std::max(1, std::min(r->n_sub_init, r->n_sub_final));
+  const int nv = (r->nP + smin - 1) / smin;
+  const size_t rs = r->data_type == MEXCT_F16 ? 2 : 4;
+  const size_t quads = 2 * sino_pad_elems(r->W, r->H, nv) * 4 * rs;
+  // staging (pre, post, recon) + solver (pre, post, residual views, mu,
+  // mu_old, TV buffer, two padded copies).
+  return 4 * (2 * M + N) + 4 * (2 * M) + quads + ds * (3 * N + 2 * pad) + (1 << 20);
 }
 
 mexct_status mexct_server_create(int device, int slots, size_t budget, mexct_server** out) {

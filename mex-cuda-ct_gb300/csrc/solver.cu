@@ -271,9 +271,7 @@ mexct_status mexct_osctv_create_ex(mexct_ctx* ctx, const float* d_pre, const flo
   MEXCT_TRY_CUDA(cudaEventCreateWithFlags(&s->ev_out, cudaEventDisableTiming), "osctv_create: event");
   const size_t N = s->N(), M = s->M(), vb = N * dsize(mu_type);
   const size_t P = (size_t)W * H;
-  const size_t maxv = (size_t)nP;  // a subset holds at most nP views
-  if (maxv > (size_t)kMaxViews)
-    return set_err(MEXCT_ERR_UNSUPPORTED, "osctv_create: %d views (max %d)", nP, kMaxViews);
+
   // Buffers are allocated stream-ordered on the solver's stream, so creating
   // and destroying solvers never synchronises the device (other streams keep
   // running); the caller's stream waits for the allocations.
@@ -285,17 +283,10 @@ mexct_status mexct_osctv_create_ex(mexct_ctx* ctx, const float* d_pre, const flo
   MEXCT_TRY_CUDA(s->tvbuf.ensure_async(vb, a), "osctv_create: tv");
   MEXCT_TRY_CUDA(s->padx.ensure_async(pb, a), "osctv_create: padded mu");
   MEXCT_TRY_CUDA(s->pady.ensure_async(pb, a), "osctv_create: padded mu");
-  const size_t db = dsize(data_type);
   MEXCT_TRY_CUDA(s->pre.ensure_async(M * 4, a), "osctv_create: pre");
   MEXCT_TRY_CUDA(s->post.ensure_async(M * 4, a), "osctv_create: post");
-  // residual views in the padded layout; their zero frame (border addressing)
-  // is written once here and never touched again
-  const size_t rb = sino_pad_elems(W, H, (int)maxv) * 4 * db;  // quad layout
+  // the residual views are sized by mexct_osctv_run for its largest subset
   (void)P;
-  MEXCT_TRY_CUDA(s->r1.ensure_async(rb, a), "osctv_create: residual");
-  MEXCT_TRY_CUDA(s->r2.ensure_async(rb, a), "osctv_create: residual");
-  MEXCT_TRY_CUDA(cudaMemsetAsync(s->r1.p, 0, rb, a), "osctv_create: residual");
-  MEXCT_TRY_CUDA(cudaMemsetAsync(s->r2.p, 0, rb, a), "osctv_create: residual");
   MEXCT_TRY_CUDA(s->red.ensure_async(parts * sizeof(double), a), "osctv_create: reduction");
   MEXCT_TRY_CUDA(s->err.ensure_async(64, a), "osctv_create: error word");
   MEXCT_TRY_CUDA(s->cnt.ensure_async(64, a), "osctv_create: counter");
@@ -361,6 +352,36 @@ mexct_status mexct_osctv_run(mexct_osctv* s, const mexct_osctv_params* p,
   DevGuard dg(s->device);
   NvtxRange nvtx("mexct:osctv_run");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  {
+    // Residual views for the largest subset of this call's iterations, in the
+    // padded quad layout; their zero frame (border addressing) is written when
+    // they are allocated and never touched again.
+    int nvmax = 1;
+    for (int i = 0; i < n; ++i) {
+      const int ns = num_subsets(p->n_sub_init, p->n_sub_final, p->p_val, p->n_iter,
+                                 s->k_done + 1 + i);
+      if (ns > 0) nvmax = std::max(nvmax, (s->nP + ns - 1) / ns);
+    }
+    if (nvmax > kMaxViews)
+      return set_err(MEXCT_ERR_UNSUPPORTED, "osctv_run: subset of %d views (max %d)", nvmax,
+                     kMaxViews);
+    const size_t rb = sino_pad_elems(s->W, s->H, nvmax) * 4 * dsize(s->data_type);
+    if (!s->r1.p || rb > s->r1.n) {
+      // work queued on the caller's stream may still read the old views
+      MEXCT_TRY_CUDA(cudaEventRecord(s->ev_in, st), "osctv_run: join");
+      MEXCT_TRY_CUDA(cudaStreamWaitEvent(s->own, s->ev_in, 0), "osctv_run: join");
+      MEXCT_TRY_CUDA(s->r1.ensure_async(rb, s->own), "osctv_run: residual");
+      MEXCT_TRY_CUDA(s->r2.ensure_async(rb, s->own), "osctv_run: residual");
+      MEXCT_TRY_CUDA(cudaMemsetAsync(s->r1.p, 0, s->r1.n, s->own), "osctv_run: residual");
+      MEXCT_TRY_CUDA(cudaMemsetAsync(s->r2.p, 0, s->r2.n, s->own), "osctv_run: residual");
+      MEXCT_TRY_CUDA(cudaEventRecord(s->ev_out, s->own), "osctv_run: join");
+      MEXCT_TRY_CUDA(cudaStreamWaitEvent(st, s->ev_out, 0), "osctv_run: join");
+      // captured iterations hold the old buffers (an executing graph is freed
+      // when it completes)
+      for (auto& g : s->graphs) cudaGraphExecDestroy(g.second);
+      s->graphs.clear();
+    }
+  }
   for (int i = 0; i < n; ++i) {
     const int k = s->k_done + 1;  // 1-based iteration number
     const int nsub = num_subsets(p->n_sub_init, p->n_sub_final, p->p_val, p->n_iter, k);
@@ -504,7 +525,8 @@ namespace mexct {
 mexct_status osc_tv_recon_typed(mexct_ctx* ctx, const float* pre, const float* post, int W, int H,
                                 int nP, const float* angles, float sad, int geom, int n_iter,
                                 float tv_const, int n_sub_init, int n_sub_final, float p_val,
-                                const int32_t* first_picks, int mu_type, float* recon) {
+                                const int32_t* first_picks, int mu_type, float* recon,
+                                int data_type) {
   if (!pre || !post || !angles || !recon || !first_picks)
     return set_err(MEXCT_ERR_ARG, "osc_tv_recon: NULL pointer");
   if (W <= 0 || H <= 0 || nP <= 0 || n_iter < 1)
@@ -522,8 +544,9 @@ mexct_status osc_tv_recon_typed(mexct_ctx* ctx, const float* pre, const float* p
   MEXCT_TRY_CUDA(cudaMemcpyAsync(c->in2.p, post, M * 4, cudaMemcpyHostToDevice, c->stream),
                  "osc_tv_recon: upload");
   mexct_osctv* s = nullptr;
-  mexct_status r = mexct_osctv_create(c, c->in.as<float>(), c->in2.as<float>(), W, H, nP, angles,
-                                      sad, geom, mu_type, c->stream, &s);
+  mexct_status r = mexct_osctv_create_ex(c, c->in.as<float>(), c->in2.as<float>(), W, H, nP,
+                                         angles, sad, geom, mu_type,
+                                         data_type == 0 ? (int)kF32 : data_type, c->stream, &s);
   if (r) return r;
   mexct_osctv_params p{n_iter, tv_const, n_sub_init, n_sub_final, p_val, 1, 0};
   r = mexct_osctv_run(s, &p, first_picks, n_iter, c->stream);

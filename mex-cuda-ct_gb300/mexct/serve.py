@@ -24,7 +24,7 @@ class Request(ctypes.Structure):
                 ("mu_type", _i), ("angles", _P), ("pre", _P), ("post", _P), ("recon", _P),
                 ("filter", _i), ("cutoff", _f), ("q", _f), ("n_iter", _i), ("tv_const", _f),
                 ("n_sub_init", _i), ("n_sub_final", _i), ("p_val", _f), ("first_picks", _P),
-                ("simulate_s", _d)]
+                ("simulate_s", _d), ("data_type", _i)]
 
 
 class Stats(ctypes.Structure):
@@ -73,13 +73,15 @@ class Server:
         return self._submit(r, (pre, post, ang, rec))
 
     def submit_osctv(self, pre, post, angles, geom, first_picks, n_iter=10, tv_const=0.2,
-                     n_sub=10, sad=1000.0, mu_type=_lib.F32, n_sub_final=None, p_val=1.0):
+                     n_sub=10, sad=1000.0, mu_type=_lib.F32, n_sub_final=None, p_val=1.0,
+                     data_type=_lib.F32):
+        """data_type: storage of the residual views (F32, or F16 with FP32 mu)."""
         pre, post, ang, rec, W, H, nP = self._arrays(pre, post, angles)
         fp = np.ascontiguousarray(np.asarray(first_picks, dtype=np.int32).ravel())
         r = Request(OSCTV, W, H, nP, int(geom), float(sad), int(mu_type), ang.ctypes.data,
                     pre.ctypes.data, post.ctypes.data, rec.ctypes.data, 0, 0.0, 0.0, int(n_iter),
                     float(tv_const), int(n_sub), int(n_sub if n_sub_final is None else n_sub_final),
-                    float(p_val), fp.ctypes.data, 0.0)
+                    float(p_val), fp.ctypes.data, 0.0, int(data_type))
         return self._submit(r, (pre, post, ang, rec, fp))
 
     def submit_simulated(self, seconds, W=64, H=64, nP=60, kind=FDK):
@@ -88,9 +90,9 @@ class Server:
         return self._submit(r, None)
 
     @staticmethod
-    def request_bytes(kind, W, H, nP, mu_type=_lib.F32):
+    def request_bytes(kind, W, H, nP, mu_type=_lib.F32, n_sub=1, data_type=_lib.F32):
         r = Request(kind, W, H, nP, 0, 1000.0, int(mu_type), None, None, None, None, 0, 0.0, 0.0,
-                    1, 0.0, 1, 1, 1.0, None, 0.0)
+                    1, 0.0, int(n_sub), int(n_sub), 1.0, None, 0.0, int(data_type))
         return int(_lib.load().mexct_request_bytes(ctypes.byref(r)))
 
     def wait(self, ticket, timeout=-1.0):
