@@ -409,10 +409,11 @@ struct SlabJob {
   int zoff, zrows, accum;  // sub-volume slab (RayArgs)
   float zlo, zhi;
   const float* pts;        // general3D: ray end points of this view (6 planes of P)
-  Trig tr;
-  long long P;      // detector pixels per view
-  long long gview;  // sinogram / pre / post slot of the view
-  long long lview;  // residual slot (OSC epilogue)
+  Trig tr[2];       // the job's views (nv of them; general3D: one)
+  int nv;
+  long long P;         // detector pixels per view
+  long long gview[2];  // sinogram / pre / post slot of each view
+  long long lview[2];  // residual slot of each view (OSC epilogue)
   int tu0, tv0;     // tile origin on the detector
   const CUtensorMap* tmx;
   const CUtensorMap* tmy;
@@ -438,7 +439,7 @@ __device__ __forceinline__ int plan_nzr(uint32_t p) { return (int)(p >> 27); }
 struct SlabShared {
   uint64_t bar[2];
   uint32_t plans[kMaxPlans];
-  float corner[4][6];
+  float corner[8][6];  // corner rays of a tile: four per view
   int gbi[8];         // general3D: ray bounds over the tile, order-preserving int keys
   int amin, amax, pos, neg;
   int abort;          // set by a timed-out wait
@@ -455,30 +456,26 @@ __device__ __forceinline__ void slab_init_barriers(SlabShared& S) {
   __syncthreads();
 }
 
-// One tile: sweep the volume along the view's dominant axis slab by slab.
-// Ends with a CTA barrier, so the shared state can be reused by the next job.
-// ZL (decoupled detector): par / fan rays whose constant z falls between
-// texel rows interpolate in z as well, and rays that miss the volume sample
-// nothing.
-// SUB: a z-slab of the volume (launch_fp_slab_sub); each ray samples only
-// the k whose z taps can reach the slab's rows.
-template <int GEOM, int EPI, typename TV, typename TO, bool ZL = false, bool SUB = false>
-__device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, SlabShared& S,
-                                          uint32_t& phase, uint32_t& issued,
-                                          const SlabEpi& E) {
-  using C = SlabCfg<GEOM>;
-  constexpr bool Z2 = (GEOM >= 2);  // z changes along the ray
-  // trilinear samples; otherwise par/fan rays sample exact z texel rows
-  constexpr bool ZW = Z2 || ZL;
-  const int tid = threadIdx.x + 32 * threadIdx.y;
-  const int u0 = J.tu0, v0 = J.tv0;
-  const int ix = u0 + threadIdx.x, iy = v0 + threadIdx.y;
-  const bool valid = ix < J.det_w && iy < J.det_h;
-  const Trig tr = J.tr;
-  const bool xdom = fabsf(tr.c) >= fabsf(tr.s);  // rays run mostly along x
-  const int Ps = J.S + 2, Pz = J.Z + 2, Pf = J.Pf;
+// Per-ray state of a tile's sweep: tap-space entry point and step, par / fan
+// z row and weight, next sample, end, accumulator.
+struct RayLane {
+  float ta0, tf0, tz0, da, df, dz;
+  float fzc, wzc;  // par / fan: the ray's z tap row and its weight
+  int k, n;
+  float acc;
+  bool valid;
+};
 
-  float s[3], e[3];
+// Ray of detector pixel (ix, iy) in tap space (padded texture coordinate
+// minus 0.5, i.e. world - b + 0.5) with its first sample and sample count.
+// ZL (decoupled detector): a ray that misses the volume samples nothing.
+// SUB: only the k whose z taps can reach the slab's rows.  GEOM 3: the k whose
+// taps can touch the padded volume.
+template <int GEOM, bool ZL, bool SUB>
+__device__ __forceinline__ void ray_setup(const SlabJob& J, const Trig tr, bool view_ok, int ix,
+                                          int iy, bool xdom, int Ps, int Pz, RayLane& L,
+                                          float s[3], float e[3]) {
+  L.valid = view_ok && ix < J.det_w && iy < J.det_h;
   if constexpr (GEOM == 3) {
     const long long pix = (long long)min(iy, J.det_h - 1) * J.det_w + min(ix, J.det_w - 1);
     g3d_ray(J.pts, pix, J.P, tr.s, tr.c, s, e);
@@ -487,14 +484,12 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
                   J.RD, s, e, J.du, J.dv, J.ou, J.ov);
   }
   const Ray r = clip_ray(s[0], s[1], s[2], e[0], e[1], e[2], J.bx, J.by, J.bz, J.step);
-  // Tap space: padded texture coordinate minus 0.5, i.e. world - b + 0.5.
   const float ca = xdom ? r.cx - J.bx : r.cy - J.by;
   const float cf = xdom ? r.cy - J.by : r.cx - J.bx;
   const float ta0 = ca + 0.5f, tf0 = cf + 0.5f, tz0 = (r.cz - J.bz) + 0.5f;
   const float da = xdom ? r.dx : r.dy, df = xdom ? r.dy : r.dx, dz = r.dz;
-  // On a decoupled detector (ZL) a ray that misses the volume samples nothing.
   const bool miss = ZL && !hits_box(s, e, J.bx, J.by, J.bz);
-  int n = (valid && !miss) ? r.n : 0;
+  int n = (L.valid && !miss) ? r.n : 0;
   int k0 = 0;  // first sample
   if (SUB && n > 0) {
     // Samples with tz in [zlo, zhi) can touch the slab's rows; the others
@@ -515,7 +510,6 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       }
     }
   }
-
   if (GEOM == 3 && n > 0) {
     // general3D rays are not clipped when they miss the volume (the
     // reference marches them between two points outside it): keep the
@@ -558,6 +552,193 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
       n = 0;
     }
   }
+  L.ta0 = ta0; L.tf0 = tf0; L.tz0 = tz0;
+  L.da = da; L.df = df; L.dz = dz;
+  // par / fan rays keep one z tap row for the whole ray
+  L.fzc = floorf(tz0);
+  L.wzc = tz0 - L.fzc;
+  L.k = k0;
+  L.n = n;
+  L.acc = 0.f;
+}
+
+// Samples of one ray whose a-tap lies in the slab [alo, ahi] (sweep direction
+// D), from the slab's buffer b, two per iteration where possible: positions
+// fma(k, d, t0) on both lanes of a pair.  Tap indices are kept as floats
+// (exact below 2^24) so a sample costs one float->int conversion for its
+// shared-memory index.
+template <int GEOM, bool ZW, int D, typename TV>
+__device__ __forceinline__ void smem_ray(RayLane& L, const TV* b, float2 off2, float alo_f,
+                                         float ahi_f) {
+  using C = SlabCfg<GEOM>;
+  constexpr bool Z2 = (GEOM >= 2);
+  const float2 da2 = make_float2(L.da, L.da), df2 = make_float2(L.df, L.df);
+  const float2 dz2 = make_float2(L.dz, L.dz);
+  const float2 ta02 = make_float2(L.ta0, L.ta0), tf02 = make_float2(L.tf0, L.tf0);
+  const float2 tz02 = make_float2(L.tz0, L.tz0);
+  const float2 fz02 = make_float2(L.fzc, L.fzc), wz02 = make_float2(L.wzc, L.wzc);
+  int k = L.k;
+  const int n = L.n;
+  float acc = L.acc;
+  while (k < n) {
+    const float k0 = (float)k;
+    const float2 kk = make_float2(k0, k0 + 1.0f);
+    const float2 ta2 = __ffma2_rn(kk, da2, ta02);
+    const float fa0 = floorf(ta2.x);
+    if (D > 0 ? fa0 > ahi_f : fa0 < alo_f) break;
+    const float fa1 = floorf(ta2.y);
+    const bool two = (k + 1 < n) && (D > 0 ? fa1 <= ahi_f : fa1 >= alo_f);
+    const float2 tf2 = __ffma2_rn(kk, df2, tf02);
+    const float2 fa2 = make_float2(fa0, fa1);
+    const float2 ff2 = make_float2(floorf(tf2.x), floorf(tf2.y));
+    float2 fz2 = fz02, wz2 = wz02;
+    if (Z2) {
+      const float2 tz2 = __ffma2_rn(kk, dz2, tz02);
+      fz2 = make_float2(floorf(tz2.x), floorf(tz2.y));
+      wz2 = sub2(tz2, fz2);
+    }
+    const float2 wa2 = sub2(ta2, fa2), wf2 = sub2(tf2, ff2);
+    const float2 x2 = __ffma2_rn(fz2, make_float2((float)C::Plane, (float)C::Plane),
+                                 __ffma2_rn(fa2, make_float2((float)C::F, (float)C::F),
+                                            __fadd2_rn(ff2, off2)));
+    // Tap indices are exact in FP32 (< 2^24); a negative one wraps to a
+    // large unsigned value and is clamped like one past the end.
+    const unsigned i0 = min((unsigned)__float2int_rn(x2.x), (unsigned)C::MaxIdx);
+    if (two) {
+      const unsigned i1 = min((unsigned)__float2int_rn(x2.y), (unsigned)C::MaxIdx);
+      const float2 v = sample_pair<ZW>(b + i0, b + i1, C::F, C::Plane, wa2, wf2, wz2);
+      acc += v.x;
+      acc += v.y;
+      k += 2;
+    } else {
+      acc += sample_at<ZW>(b + i0, C::F, C::Plane, wa2.x, wf2.x, wz2.x);
+      k += 1;
+      break;
+    }
+  }
+  L.k = k;
+  L.acc = acc;
+}
+
+// The rays of one thread in two views through the slab in step: sample k_A of
+// ray A and k_B of ray B on the two lanes of each FP32x2 operation (per ray the
+// same operations as smem_ray), while both have a sample in the slab; the ray
+// left over finishes with smem_ray.
+template <int GEOM, bool ZW, int D, typename TV>
+__device__ __forceinline__ void smem_ray_pair(RayLane& A, RayLane& B, const TV* b, float2 off2,
+                                              float alo_f, float ahi_f) {
+  using C = SlabCfg<GEOM>;
+  constexpr bool Z2 = (GEOM >= 2);
+  const float2 da2 = make_float2(A.da, B.da), df2 = make_float2(A.df, B.df);
+  const float2 dz2 = make_float2(A.dz, B.dz);
+  const float2 ta02 = make_float2(A.ta0, B.ta0), tf02 = make_float2(A.tf0, B.tf0);
+  const float2 tz02 = make_float2(A.tz0, B.tz0);
+  const float2 fz02 = make_float2(A.fzc, B.fzc), wz02 = make_float2(A.wzc, B.wzc);
+  int ka = A.k, kb = B.k;
+  float acca = A.acc, accb = B.acc;
+  while (ka < A.n && kb < B.n) {
+    const float2 kk = make_float2((float)ka, (float)kb);
+    const float2 ta2 = __ffma2_rn(kk, da2, ta02);
+    const float2 fa2 = make_float2(floorf(ta2.x), floorf(ta2.y));
+    if (D > 0 ? fmaxf(fa2.x, fa2.y) > ahi_f : fminf(fa2.x, fa2.y) < alo_f) break;
+    const float2 tf2 = __ffma2_rn(kk, df2, tf02);
+    const float2 ff2 = make_float2(floorf(tf2.x), floorf(tf2.y));
+    float2 fz2 = fz02, wz2 = wz02;
+    if (Z2) {
+      const float2 tz2 = __ffma2_rn(kk, dz2, tz02);
+      fz2 = make_float2(floorf(tz2.x), floorf(tz2.y));
+      wz2 = sub2(tz2, fz2);
+    }
+    const float2 wa2 = sub2(ta2, fa2), wf2 = sub2(tf2, ff2);
+    const float2 x2 = __ffma2_rn(fz2, make_float2((float)C::Plane, (float)C::Plane),
+                                 __ffma2_rn(fa2, make_float2((float)C::F, (float)C::F),
+                                            __fadd2_rn(ff2, off2)));
+    const unsigned i0 = min((unsigned)__float2int_rn(x2.x), (unsigned)C::MaxIdx);
+    const unsigned i1 = min((unsigned)__float2int_rn(x2.y), (unsigned)C::MaxIdx);
+    const float2 v = sample_pair<ZW>(b + i0, b + i1, C::F, C::Plane, wa2, wf2, wz2);
+    acca += v.x;
+    accb += v.y;
+    ++ka;
+    ++kb;
+  }
+  A.k = ka;
+  A.acc = acca;
+  B.k = kb;
+  B.acc = accb;
+  smem_ray<GEOM, ZW, D>(A, b, off2, alo_f, ahi_f);
+  smem_ray<GEOM, ZW, D>(B, b, off2, alo_f, ahi_f);
+}
+
+// The same samples of one ray from the padded volume in global memory (a
+// slab whose bundle did not fit the box, or after a wait gave up).
+template <int GEOM, bool ZW, bool SUB, typename TV>
+__device__ __forceinline__ void global_ray(RayLane& L, const TV* gv, const SlabJob& J, int dir,
+                                           float alo_f, float ahi_f, int Ps, int Pz, int Pf) {
+  constexpr bool Z2 = (GEOM >= 2);
+  int k = L.k;
+  float acc = L.acc;
+  while (k < L.n) {
+    const float kq = (float)k;
+    const float tq = fmaf(kq, L.da, L.ta0);
+    const float fq = floorf(tq);
+    if (dir > 0 ? fq > ahi_f : fq < alo_f) break;
+    const float tfq = fmaf(kq, L.df, L.tf0);
+    const float tzq = Z2 ? fmaf(kq, L.dz, L.tz0) : L.tz0;
+    const float ffq = floorf(tfq), fzq = floorf(tzq);
+    const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
+    const int gz = min(max((int)fzq, 0), Pz - 2);
+    if (SUB)
+      acc += sample_rows<ZW>(gv + (size_t)gf + (size_t)Pf * (size_t)ga, gz - J.zoff, J.zrows, Pf,
+                             Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
+    else
+      acc += sample_at<ZW>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz), Pf,
+                           Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
+    ++k;
+  }
+  L.k = k;
+  L.acc = acc;
+}
+
+// One tile: sweep the volume along the views' dominant axis slab by slab.
+// Ends with a CTA barrier, so the shared state can be reused by the next job.
+// V views per CTA (the tile's pixels in J.nv <= V consecutive views with the
+// same dominant axis): every slab's box covers the bundles of all of them, and
+// each thread samples its pixel's ray in every view.
+// ZL (decoupled detector): par / fan rays whose constant z falls between
+// texel rows interpolate in z as well, and rays that miss the volume sample
+// nothing.
+// SUB: a z-slab of the volume (launch_fp_slab_sub); each ray samples only
+// the k whose z taps can reach the slab's rows.
+template <int GEOM, int EPI, typename TV, typename TO, bool ZL = false, bool SUB = false,
+          int V = 1>
+__device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, SlabShared& S,
+                                          uint32_t& phase, uint32_t& issued,
+                                          const SlabEpi& E, int vb = 0, int nvj = -1) {
+  static_assert(V == 1 || V == 2, "one or two views per CTA");
+  // this call's views: J's views vb .. vb + nvj - 1 (nvj < 0: all of J's)
+  if (nvj < 0) nvj = J.nv;
+  const Trig trv[2] = {vb ? J.tr[1] : J.tr[0], J.tr[1]};
+  const long long gvv[2] = {vb ? J.gview[1] : J.gview[0], J.gview[1]};
+  const long long lvv[2] = {vb ? J.lview[1] : J.lview[0], J.lview[1]};
+  using C = SlabCfg<GEOM>;
+  constexpr bool Z2 = (GEOM >= 2);  // z changes along the ray
+  // trilinear samples; otherwise par/fan rays sample exact z texel rows
+  constexpr bool ZW = Z2 || ZL;
+  constexpr int NC = 4 * V;  // corner rays: four per view
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  const int u0 = J.tu0, v0 = J.tv0;
+  const int ix = u0 + threadIdx.x, iy = v0 + threadIdx.y;
+  const bool xdom = fabsf(trv[0].c) >= fabsf(trv[0].s);  // rays run mostly along x
+  const int Ps = J.S + 2, Pz = J.Z + 2, Pf = J.Pf;
+
+  // An absent second view (J.nv = 1) repeats the first one's geometry with no
+  // samples, so its corner rays change no box.
+  RayLane L[V];
+  float se[V][6];
+#pragma unroll
+  for (int r = 0; r < V; ++r)
+    ray_setup<GEOM, ZL, SUB>(J, r < nvj ? trv[r] : trv[0], r < nvj, ix, iy, xdom, Ps, Pz, L[r],
+                             &se[r][0], &se[r][3]);
 
   if (tid == 0) {
     S.amin = 0x7fffffff;
@@ -568,25 +749,41 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
 #pragma unroll
       for (int i = 0; i < 8; ++i) S.gbi[i] = (i & 1) ? (int)0x80000000 : 0x7fffffff;
   }
-  // Corner rays of the valid part of the tile bound the bundle.
+  // Corner rays of the valid part of the tile bound the bundle (slot 4r + c:
+  // c bit 0 right column, bit 1 bottom row).
   const int lx = min(31, J.det_w - 1 - u0), ly = min(7, J.det_h - 1 - v0);
-  const int cid = (threadIdx.x == 0 && threadIdx.y == 0)     ? 0
-                  : (threadIdx.x == lx && threadIdx.y == 0)  ? 1
-                  : (threadIdx.x == 0 && threadIdx.y == ly)  ? 2
-                  : (threadIdx.x == lx && threadIdx.y == ly) ? 3
-                                                             : -1;
   __syncthreads();
-  if (cid >= 0) {
-    S.corner[cid][0] = s[0]; S.corner[cid][1] = s[1]; S.corner[cid][2] = s[2];
-    S.corner[cid][3] = e[0]; S.corner[cid][4] = e[1]; S.corner[cid][5] = e[2];
+  {
+    const bool top = threadIdx.y == 0, bot = (int)threadIdx.y == ly;
+    const bool lft = threadIdx.x == 0, rgt = (int)threadIdx.x == lx;
+#pragma unroll
+    for (int r = 0; r < V; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (((c & 2) ? bot : top) && ((c & 1) ? rgt : lft))
+#pragma unroll
+          for (int i = 0; i < 6; ++i) S.corner[4 * r + c][i] = se[r][i];
   }
-  if (n > 0) {
-    const int t_first = __float2int_rd((SUB || GEOM == 3) ? fmaf((float)k0, da, ta0) : ta0);
-    const int t_last = __float2int_rd(fmaf((float)(n - 1), da, ta0));
-    atomicMin(&S.amin, min(t_first, t_last));
-    atomicMax(&S.amax, max(t_first, t_last));
-    if (da > 0.f) atomicAdd(&S.pos, 1);
-    else atomicAdd(&S.neg, 1);
+  {
+    int lo = 0x7fffffff, hi = -0x7fffffff, np = 0, nn = 0;
+#pragma unroll
+    for (int r = 0; r < V; ++r) {
+      if (L[r].n > 0) {
+        const int t_first =
+            __float2int_rd((SUB || GEOM == 3) ? fmaf((float)L[r].k, L[r].da, L[r].ta0) : L[r].ta0);
+        const int t_last = __float2int_rd(fmaf((float)(L[r].n - 1), L[r].da, L[r].ta0));
+        lo = min(lo, min(t_first, t_last));
+        hi = max(hi, max(t_first, t_last));
+        if (L[r].da > 0.f) ++np;
+        else ++nn;
+      }
+    }
+    if (np + nn > 0) {
+      atomicMin(&S.amin, lo);
+      atomicMax(&S.amax, hi);
+      if (np) atomicAdd(&S.pos, np);
+      if (nn) atomicAdd(&S.neg, nn);
+    }
   }
   __syncthreads();
   const int s_amin = S.amin, s_amax = S.amax;
@@ -607,16 +804,20 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     bool bad = false;
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = (i & 1) ? -3.0e38f : 3.0e38f;
-    if (n > 0) {
-      if (!(fabsf(da) >= 1e-3f)) {
-        bad = true;
-      } else {
-        const float mf = df / da, mz = dz / da;
-        const float Fr = fmaf(aref - ta0, mf, tf0), Zr = fmaf(aref - ta0, mz, tz0);
-        v[0] = v[1] = Fr;
-        v[2] = v[3] = mf;
-        v[4] = v[5] = Zr;
-        v[6] = v[7] = mz;
+#pragma unroll
+    for (int r = 0; r < V; ++r) {
+      if (L[r].n > 0) {
+        if (!(fabsf(L[r].da) >= 1e-3f)) {
+          bad = true;
+        } else {
+          const float mf = L[r].df / L[r].da, mz = L[r].dz / L[r].da;
+          const float Fr = fmaf(aref - L[r].ta0, mf, L[r].tf0);
+          const float Zr = fmaf(aref - L[r].ta0, mz, L[r].tz0);
+          v[0] = fminf(v[0], Fr); v[1] = fmaxf(v[1], Fr);
+          v[2] = fminf(v[2], mf); v[3] = fmaxf(v[3], mf);
+          v[4] = fminf(v[4], Zr); v[5] = fmaxf(v[5], Zr);
+          v[6] = fminf(v[6], mz); v[7] = fmaxf(v[7], mz);
+        }
       }
     }
 #pragma unroll
@@ -658,23 +859,24 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
     }
   };
 
-  // Plan every slab of the tile up front, 32 slabs per pass of the CTA: the 8
-  // lanes of a group evaluate the 4 corner rays at the 2 a-ends of their slab
-  // in FP32 (error ~1e-4 voxel, covered by the 1-voxel margin), reduce the
-  // f/z extent by shuffles, and the group's first lane stores the box.
+  // Plan every slab of the tile up front, 256 / (2 NC) slabs per pass of the
+  // CTA: the 2 NC lanes of a group evaluate the NC corner rays at the 2
+  // a-ends of their slab in FP32 (error ~1e-4 voxel, covered by the 1-voxel
+  // margin), reduce the f/z extent by shuffles, and the group's first lane
+  // stores the box.
   {
     const float bfw = xdom ? J.by : J.bx;  // world offset of the f axis
     const float baw = xdom ? J.bx : J.by;  // world offset of the a axis
     const int np = min(nslab, C::MaxPlans);
-    const int c = tid & 3, w = (tid >> 2) & 1;
+    const int c = tid % NC, w = (tid / NC) & 1;
     const float sa = xdom ? S.corner[c][0] : S.corner[c][1];
     const float sf = xdom ? S.corner[c][1] : S.corner[c][0];
     const float ea = xdom ? S.corner[c][3] : S.corner[c][4];
     const float ef = xdom ? S.corner[c][4] : S.corner[c][3];
     const float sz = S.corner[c][2], ez = S.corner[c][5];
     const float den = ea - sa;
-    for (int base = 0; base < np; base += 32) {
-      const int j = base + (tid >> 3);
+    for (int base = 0; base < np; base += 256 / (2 * NC)) {
+      const int j = base + tid / (2 * NC);
       const bool act = j < np;
       int alo, ahi;
       slab_range(j, alo, ahi);
@@ -701,13 +903,13 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
         zmx = act ? zv : -3.0e38f;
       }
 #pragma unroll
-      for (int o = 4; o > 0; o >>= 1) {
+      for (int o = NC; o > 0; o >>= 1) {
         fmn = fminf(fmn, __shfl_xor_sync(0xffffffffu, fmn, o));
         fmx = fmaxf(fmx, __shfl_xor_sync(0xffffffffu, fmx, o));
         zmn = fminf(zmn, __shfl_xor_sync(0xffffffffu, zmn, o));
         zmx = fmaxf(zmx, __shfl_xor_sync(0xffffffffu, zmx, o));
       }
-      if (act && (tid & 7) == 0) {
+      if (act && (tid % (2 * NC)) == 0) {
         const int align = sizeof(TV) == 4 ? 4 : 8;
         const float flo = floorf(fmn - bfw + 0.5f) - 1.0f;
         const float fhi = floorf(fmx - bfw + 0.5f) + 2.0f;
@@ -754,16 +956,9 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   };
   if (tid == 0 && nslab > 0) issue(0);
 
-  // One accumulator, samples added in ray order: the sum does not depend on
-  // how the samples fall into slabs or on which path (shared / global) took them.
-  float acc = 0.f;
-  const float2 da2 = make_float2(da, da), df2 = make_float2(df, df), dz2 = make_float2(dz, dz);
-  const float2 ta02 = make_float2(ta0, ta0), tf02 = make_float2(tf0, tf0);
-  const float2 tz02 = make_float2(tz0, tz0);
-  // par / fan rays keep one z tap row for the whole ray
-  const float fzc = floorf(tz0);
-  const float2 fz02 = make_float2(fzc, fzc), wz02 = make_float2(tz0 - fzc, tz0 - fzc);
-  int k = k0;
+  // One accumulator per ray, samples added in ray order: the sum does not
+  // depend on how the samples fall into slabs or on which path (shared /
+  // global) took them.
   for (int j = 0; j < nslab; ++j) {
     // Buffer (j+1)&1 was released by the barrier that ended slab j-1.
     if (tid == 0 && j + 1 < nslab) issue(j + 1);
@@ -780,78 +975,24 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
                                     E.wait_us);
       phase ^= 1u << (j & 1);
     }
-    // Samples of this lane whose a-tap lies in [alo, ahi], two per iteration
-    // where possible.  Tap indices are kept as floats (exact below 2^24) so a
-    // sample costs one float->int conversion for its shared-memory index.
     const float alo_f = (float)alo, ahi_f = (float)ahi;
-    const float off = -(float)(plan_z0(pk) * C::Plane + alo * C::F + plan_f0(pk));
-    const float2 off2 = make_float2(off, off);
     // The sweep direction and the sample source are uniform over a slab, so
     // each gets its own loop: the shared-memory loops compare against one
     // bound with no per-sample selects or source branch.
-    auto smem_loop = [&](auto dirc) {
-      constexpr int D = decltype(dirc)::value;
-      while (k < n) {
-        // Samples k and k+1: positions fma(k, d, t0) on both lanes of a pair.
-        const float k0 = (float)k;
-        const float2 kk = make_float2(k0, k0 + 1.0f);
-        const float2 ta2 = __ffma2_rn(kk, da2, ta02);
-        const float fa0 = floorf(ta2.x);
-        if (D > 0 ? fa0 > ahi_f : fa0 < alo_f) break;
-        const float fa1 = floorf(ta2.y);
-        const bool two = (k + 1 < n) && (D > 0 ? fa1 <= ahi_f : fa1 >= alo_f);
-        const float2 tf2 = __ffma2_rn(kk, df2, tf02);
-        const float2 fa2 = make_float2(fa0, fa1);
-        const float2 ff2 = make_float2(floorf(tf2.x), floorf(tf2.y));
-        float2 fz2 = fz02, wz2 = wz02;
-        if (Z2) {
-          const float2 tz2 = __ffma2_rn(kk, dz2, tz02);
-          fz2 = make_float2(floorf(tz2.x), floorf(tz2.y));
-          wz2 = sub2(tz2, fz2);
-        }
-        const float2 wa2 = sub2(ta2, fa2), wf2 = sub2(tf2, ff2);
-        const float2 x2 = __ffma2_rn(fz2, make_float2((float)C::Plane, (float)C::Plane),
-                                     __ffma2_rn(fa2, make_float2((float)C::F, (float)C::F),
-                                                __fadd2_rn(ff2, off2)));
-        // Tap indices are exact in FP32 (< 2^24); a negative one wraps to a
-        // large unsigned value and is clamped like one past the end.
-        const unsigned i0 = min((unsigned)__float2int_rn(x2.x), (unsigned)C::MaxIdx);
-        if (two) {
-          const unsigned i1 = min((unsigned)__float2int_rn(x2.y), (unsigned)C::MaxIdx);
-          const float2 v = sample_pair<ZW>(b + i0, b + i1, C::F, C::Plane, wa2, wf2, wz2);
-          acc += v.x;
-          acc += v.y;
-          k += 2;
-        } else {
-          acc += sample_at<ZW>(b + i0, C::F, C::Plane, wa2.x, wf2.x, wz2.x);
-          k += 1;
-          break;
-        }
-      }
-    };
     if (from_smem) {
-      if (dir > 0) smem_loop(std::integral_constant<int, 1>{});
-      else smem_loop(std::integral_constant<int, -1>{});
-    } else {
-      // Fallback: the same samples, taps from the padded volume in global memory.
-      while (k < n) {
-        const float kq = (float)k;
-        const float tq = fmaf(kq, da, ta0);
-        const float fq = floorf(tq);
-        if (dir > 0 ? fq > ahi_f : fq < alo_f) break;
-        const float tfq = fmaf(kq, df, tf0);
-        const float tzq = Z2 ? fmaf(kq, dz, tz0) : tz0;
-        const float ffq = floorf(tfq), fzq = floorf(tzq);
-        const int ga = min(max((int)fq, 0), Ps - 2), gf = min(max((int)ffq, 0), Pf - 2);
-        const int gz = min(max((int)fzq, 0), Pz - 2);
-        if (SUB)
-          acc += sample_rows<ZW>(gv + (size_t)gf + (size_t)Pf * (size_t)ga, gz - J.zoff,
-                                 J.zrows, Pf, Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
-        else
-          acc += sample_at<ZW>(gv + (size_t)gf + (size_t)Pf * ((size_t)ga + (size_t)Ps * gz),
-                               Pf, Pf * Ps, tq - fq, tfq - ffq, tzq - fzq);
-        ++k;
+      const float off = -(float)(plan_z0(pk) * C::Plane + alo * C::F + plan_f0(pk));
+      const float2 off2 = make_float2(off, off);
+      if constexpr (V == 2) {
+        if (dir > 0) smem_ray_pair<GEOM, ZW, 1>(L[0], L[1], b, off2, alo_f, ahi_f);
+        else smem_ray_pair<GEOM, ZW, -1>(L[0], L[1], b, off2, alo_f, ahi_f);
+      } else {
+        if (dir > 0) smem_ray<GEOM, ZW, 1>(L[0], b, off2, alo_f, ahi_f);
+        else smem_ray<GEOM, ZW, -1>(L[0], b, off2, alo_f, ahi_f);
       }
+    } else {
+#pragma unroll
+      for (int r = 0; r < V; ++r)
+        global_ray<GEOM, ZW, SUB>(L[r], gv, J, dir, alo_f, ahi_f, Ps, Pz, Pf);
     }
     __syncthreads();
   }
@@ -862,57 +1003,62 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   }
   if (EPI == 2) {
     // Objective epilogue: sum of pre*e^-l + post*l over the tile in FP64
-    // (fixed order: warp shuffles, then the 8 warps in order).
+    // (fixed order: the thread's views, warp shuffles, then the 8 warps in
+    // order), added to the CTA's partial (zeroed by the caller).
     __shared__ double wsum[8];
     double t = 0.0;
-    if (valid) {
-      const float l = acc * J.step;
-      const size_t gi = (size_t)J.gview * J.P + (size_t)iy * J.det_w + ix;
-      const float pv = __ldg(static_cast<const float*>(E.pre) + gi);
-      const float qv = __ldg(static_cast<const float*>(E.post) + gi);
-      t = (double)(pv * expf(-l)) + (double)qv * (double)l;
+#pragma unroll
+    for (int r = 0; r < V; ++r) {
+      if (L[r].valid) {
+        const float l = L[r].acc * J.step;
+        const size_t gi = (size_t)gvv[r] * J.P + (size_t)iy * J.det_w + ix;
+        const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
+        t += (double)(pv * expf(-l)) + (double)qv * (double)l;
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     if ((tid & 31) == 0) wsum[tid >> 5] = t;
     __syncthreads();
     if (tid == 0) {
-      double b = 0.0;
+      double bs = 0.0;
 #pragma unroll
-      for (int w = 0; w < 8; ++w) b += wsum[w];
-      E.obj[(size_t)blockIdx.x * gridDim.y + blockIdx.y] = b;
+      for (int w = 0; w < 8; ++w) bs += wsum[w];
+      E.obj[(size_t)blockIdx.x * gridDim.y + blockIdx.y] += bs;
     }
   }
-  if (EPI != 2 && valid) {
-    const float l = acc * J.step;
-    const size_t pix = (size_t)iy * J.det_w + ix;
-    const size_t gi = (size_t)J.gview * J.P + pix;
-    if (EPI == 0) {
-      TO* o = static_cast<TO*>(J.out) + gi;
-      stf(o, (SUB && J.accum) ? ldp(o) + l : l);
-    } else {
-      // CUDAmex_oscIter.cu:262-268: pre' = pre e^-l - post, post' = pre e^-l l.
-      const float pv = __ldg(static_cast<const float*>(E.pre) + gi);
-      const float qv = __ldg(static_cast<const float*>(E.post) + gi);
-      const float ehat = pv * expf(-l);
-      // padded residual view [H+4][W+4] (zero frame kept by the caller)
-      const int Wp = sino_pad_pitch(J.det_w);
-      const size_t ri = ((size_t)J.lview * (J.det_h + 2 * kSinoPad) + (iy + kSinoPad)) * Wp +
-                        (ix + kSinoPad);
-      const float r0 = ehat - qv, r1 = ehat * l;
-      // quad layout (the dual BP's one 16-byte load per voxel, cone, or per z
-      // pair, par / fan): the padded texel P(r, c) is component x of quad
-      // (r, c), y of (r-1, c), z of (r, c-1) and w of (r-1, c-1)
-      const size_t q[4] = {4 * ri, 4 * (ri - Wp) + 1, 4 * (ri - 1) + 2, 4 * (ri - Wp - 1) + 3};
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        if constexpr (std::is_same<TO, float>::value) {
-          static_cast<float*>(E.rpre)[q[t]] = r0;
-          static_cast<float*>(E.rpost)[q[t]] = r1;
-        } else {
-          // 16-bit residual views hold the residuals times a power of two
-          stf(static_cast<TO*>(E.rpre) + q[t], r0 * E.rscale);
-          stf(static_cast<TO*>(E.rpost) + q[t], r1 * E.rscale);
+  for (int r = 0; r < V; ++r) {
+    if (EPI != 2 && L[r].valid) {
+      const float l = L[r].acc * J.step;
+      const size_t pix = (size_t)iy * J.det_w + ix;
+      const size_t gi = (size_t)gvv[r] * J.P + pix;
+      if (EPI == 0) {
+        TO* o = static_cast<TO*>(J.out) + gi;
+        stf(o, (SUB && J.accum) ? ldp(o) + l : l);
+      } else {
+        // CUDAmex_oscIter.cu:262-268: pre' = pre e^-l - post, post' = pre e^-l l.
+        const float pv = __ldg(E.pre + gi), qv = __ldg(E.post + gi);
+        const float ehat = pv * expf(-l);
+        // padded residual view [H+4][W+4] (zero frame kept by the caller)
+        const int Wp = sino_pad_pitch(J.det_w);
+        const size_t ri = ((size_t)lvv[r] * (J.det_h + 2 * kSinoPad) + (iy + kSinoPad)) * Wp +
+                          (ix + kSinoPad);
+        const float r0 = ehat - qv, r1 = ehat * l;
+        // quad layout (the dual BP's one 16-byte load per voxel, cone, or per z
+        // pair, par / fan): the padded texel P(r, c) is component x of quad
+        // (r, c), y of (r-1, c), z of (r, c-1) and w of (r-1, c-1)
+        const size_t q[4] = {4 * ri, 4 * (ri - Wp) + 1, 4 * (ri - 1) + 2, 4 * (ri - Wp - 1) + 3};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if constexpr (std::is_same<TO, float>::value) {
+            static_cast<float*>(E.rpre)[q[t]] = r0;
+            static_cast<float*>(E.rpost)[q[t]] = r1;
+          } else {
+            // 16-bit residual views hold the residuals times a power of two
+            stf(static_cast<TO*>(E.rpre) + q[t], r0 * E.rscale);
+            stf(static_cast<TO*>(E.rpost) + q[t], r1 * E.rscale);
+          }
         }
       }
     }
@@ -932,7 +1078,9 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   TV* buf1 = buf0 + kBufElems;
   slab_init_barriers(S);
   uint32_t phase = 0u, issued = 0u;  // issued: copies per buffer (thread 0)
-  const int view = blockIdx.x;
+  // two consecutive views per CTA (general3D: one)
+  constexpr int V = GEOM == 3 ? 1 : 2;
+  const int view0 = blockIdx.x * V;
   const int tiles_u = (A.det_w + 31) >> 5;
   SlabJob J;
   J.det_w = A.det_w; J.det_h = A.det_h; J.S = A.S; J.Z = A.Z; J.Pf = Pf;
@@ -940,15 +1088,28 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   J.SR = A.SR; J.RD = A.RD; J.step = A.step;
   J.du = A.du; J.dv = A.dv; J.ou = A.ou; J.ov = A.ov;
   J.zoff = A.zoff; J.zrows = A.zrows; J.accum = A.accum; J.zlo = A.zlo; J.zhi = A.zhi;
-  J.tr = A.trig[view];
+  J.nv = min(V, A.nviews - view0);
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int vr = view0 + min(r, J.nv - 1);
+    J.tr[r] = A.trig[vr];
+    J.gview[r] = A.view0 + (long long)vr * A.vstride;
+    J.lview[r] = vr;
+  }
   J.P = A.P;
-  J.gview = A.view0 + (long long)view * A.vstride;
-  J.pts = GEOM == 3 ? A.pts + (A.pts_per_view ? (size_t)6 * A.P * J.gview : 0) : nullptr;
-  J.lview = view;
+  J.pts = GEOM == 3 ? A.pts + (A.pts_per_view ? (size_t)6 * A.P * J.gview[0] : 0) : nullptr;
   J.tu0 = (blockIdx.y % tiles_u) * 32;
   J.tv0 = (blockIdx.y / tiles_u) * 8;
   J.tmx = &tmx; J.tmy = &tmy; J.px = px; J.py = py; J.out = out;
-  slab_tile<GEOM, EPI, TV, TO, ZL, SUB>(J, buf0, buf1, S, phase, issued, E);
+  const bool split = V == 2 && J.nv == 2 &&
+                     (fabsf(J.tr[0].c) >= fabsf(J.tr[0].s)) != (fabsf(J.tr[1].c) >= fabsf(J.tr[1].s));
+  if (!split) {
+    slab_tile<GEOM, EPI, TV, TO, ZL, SUB, V>(J, buf0, buf1, S, phase, issued, E);
+  } else {
+    // the two views sweep different axes: one view at a time
+    slab_tile<GEOM, EPI, TV, TO, ZL, SUB, V>(J, buf0, buf1, S, phase, issued, E, 0, 1);
+    slab_tile<GEOM, EPI, TV, TO, ZL, SUB, V>(J, buf0, buf1, S, phase, issued, E, 1, 1);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -988,10 +1149,11 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_batch_kernel(
     J.SR = B.sad; J.RD = B.sad; J.step = B.step;
     J.du = 1.0f; J.dv = 1.0f; J.ou = 0.0f; J.ov = 0.0f;
     J.zoff = 0; J.zrows = B.H + 2; J.accum = 0; J.zlo = 0.f; J.zhi = 0.f; J.pts = nullptr;
-    J.tr = B.trig[view];
+    J.tr[0] = J.tr[1] = B.trig[view];
+    J.nv = 1;
     J.P = (long long)B.W * B.H;
-    J.gview = view;
-    J.lview = view;
+    J.gview[0] = J.gview[1] = view;
+    J.lview[0] = J.lview[1] = view;
     J.tu0 = (tile % B.tiles_u) * 32;
     J.tv0 = (tile / B.tiles_u) * 8;
     J.tmx = &B.tmx; J.tmy = &B.tmy; J.px = B.px; J.py = B.py; J.out = B.out;
@@ -1091,7 +1253,8 @@ static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtens
   }
   if (a.nviews <= 0) return cudaSuccess;
   const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
-  dim3 blk(32, 8), grd(a.nviews, tiles);
+  const int per_cta = GEOM == 3 ? 1 : 2;  // views per CTA (fp_slab_kernel)
+  dim3 blk(32, 8), grd((a.nviews + per_cta - 1) / per_cta, tiles);
   k<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e);
   return cudaGetLastError();
 }

@@ -130,6 +130,9 @@ mexct_status enqueue_objective(mexct_osctv* s, cudaStream_t st) {
   std::unique_ptr<RayArgs> ra(new RayArgs);
   fill_std_rays(*ra, s->W, s->H, s->sad, s->geom, /*osc=*/true);
   const int tiles = s->tiles();
+  // CTAs add their sums to their partial (a CTA covers up to two views)
+  MEXCT_TRY_CUDA(cudaMemsetAsync(s->objp.p, 0, (size_t)s->nP * tiles * sizeof(double), st),
+                 "osctv: objective partials");
   for (int v0 = 0; v0 < s->nP; v0 += kMaxViews) {
     const int nv = std::min(kMaxViews, s->nP - v0);
     ra->nviews = nv;
