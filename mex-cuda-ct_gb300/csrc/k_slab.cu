@@ -35,6 +35,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
@@ -1071,16 +1072,18 @@ template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = fa
 __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
     const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
     const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
-    const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E) {
+    const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E, int pair) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ SlabShared S;
   TV* buf0 = reinterpret_cast<TV*>(smem_raw);
   TV* buf1 = buf0 + kBufElems;
   slab_init_barriers(S);
   uint32_t phase = 0u, issued = 0u;  // issued: copies per buffer (thread 0)
-  // two consecutive views per CTA (general3D: one)
+  // two consecutive views per CTA where the launch pairs them (pair != 0:
+  // their bundles overlap), else one; general3D one
   constexpr int V = GEOM == 3 ? 1 : 2;
-  const int view0 = blockIdx.x * V;
+  const int per = (V == 2 && pair) ? 2 : 1;
+  const int view0 = blockIdx.x * per;
   const int tiles_u = (A.det_w + 31) >> 5;
   SlabJob J;
   J.det_w = A.det_w; J.det_h = A.det_h; J.S = A.S; J.Z = A.Z; J.Pf = Pf;
@@ -1088,7 +1091,7 @@ __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
   J.SR = A.SR; J.RD = A.RD; J.step = A.step;
   J.du = A.du; J.dv = A.dv; J.ou = A.ou; J.ov = A.ov;
   J.zoff = A.zoff; J.zrows = A.zrows; J.accum = A.accum; J.zlo = A.zlo; J.zhi = A.zhi;
-  J.nv = min(V, A.nviews - view0);
+  J.nv = min(per, A.nviews - view0);
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
     const int vr = view0 + min(r, J.nv - 1);
@@ -1202,6 +1205,22 @@ cudaError_t make_slab_tmap(CUtensorMap* map, const void* base, int dtype, int Pf
 
 int slab_pitch(int W) { return ((W + 2 + 7) / 8) * 8; }
 
+// Whether views 2i and 2i+1 of a launch share their slab boxes: the box
+// covers a tile's bundle with ~18 voxels to spare along f, and two views
+// delta apart shift the bundle by up to delta times the volume's half
+// diagonal W/sqrt(2), so pairs are taken while that shift stays within
+// ~6 voxels (0.95 degrees at W = 512: 720 views over 2 pi pair, 360 do not).
+bool slab_pair_views(const RayArgs& a) {
+  if (a.nviews < 2) return false;
+  const double lim = 8.5 / (double)std::max(a.S, 1);
+  const double cmin = std::cos(lim);
+  for (int i = 0; i + 1 < a.nviews; i += 2) {
+    const Trig p = a.trig[i], q = a.trig[i + 1];
+    if ((double)p.c * q.c + (double)p.s * q.s < cmin) return false;
+  }
+  return true;
+}
+
 // Dynamic shared memory of the slab kernels and the largest shared-memory
 // carveout: kSlabCtas CTAs of 57 KB each need nearly all of an SM's 228 KB.
 template <typename K>
@@ -1253,9 +1272,9 @@ static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtens
   }
   if (a.nviews <= 0) return cudaSuccess;
   const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
-  const int per_cta = GEOM == 3 ? 1 : 2;  // views per CTA (fp_slab_kernel)
-  dim3 blk(32, 8), grd((a.nviews + per_cta - 1) / per_cta, tiles);
-  k<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e);
+  const int pair = GEOM != 3 && slab_pair_views(a) ? 1 : 0;
+  dim3 blk(32, 8), grd(pair ? (a.nviews + 1) / 2 : a.nviews, tiles);
+  k<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e, pair);
   return cudaGetLastError();
 }
 

@@ -79,6 +79,9 @@ struct SlabEpi {
   float rscale = 1.f;  // 16-bit residual views: residuals times this power of two
 };
 int slab_pitch(int W);
+// Whether the slab FP kernels take views 2i and 2i+1 of a launch in one CTA
+// (adjacent angles close enough that one slab box serves both bundles).
+bool slab_pair_views(const RayArgs& a);
 // CTAs of the slab FP kernels resident per SM (its launch bounds); persistent
 // launches size their grids by it.
 int slab_ctas_per_sm();
