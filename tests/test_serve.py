@@ -40,6 +40,23 @@ def test_budget_caps_concurrency_and_small_requests_backfill(lib):
     s.close()
 
 
+def test_osctv_footprint_counts_the_largest_subset(lib):
+    """An OSC-TV request is charged its residual views for the largest subset
+    only (two padded quad-layout views per subset view), in FP32 or FP16, next to
+    its volumes and counts."""
+    from mexct import _lib, serve
+
+    W, H, nP = 512, 512, 720
+    b1 = serve.Server.request_bytes(1, W, H, nP, n_sub=1)
+    b10 = serve.Server.request_bytes(1, W, H, nP, n_sub=10)
+    b10h = serve.Server.request_bytes(1, W, H, nP, n_sub=10, data_type=_lib.F16)
+    quad = 4 * (W + 4) * (H + 4)  # values per padded view
+    assert b1 - b10 == 2 * quad * 4 * (720 - 72)
+    assert b10 - b10h == 2 * quad * 2 * 72
+    vol, counts = 4 * W * W * H, 4 * W * H * nP
+    assert b10h > 4 * counts + vol  # staging and solver copies of pre / post, and mu
+
+
 def test_slots_overlap_independent_requests(lib):
     from mexct import serve
 
