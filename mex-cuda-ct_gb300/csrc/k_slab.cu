@@ -1067,22 +1067,21 @@ __device__ __forceinline__ void slab_tile(const SlabJob& J, TV* buf0, TV* buf1, 
   __syncthreads();
 }
 
+// V views per CTA: 2 where the launch pairs adjacent views (their bundles
+// overlap: slab_pair_views), else 1.
 template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = false,
-          bool SUB = false>
+          bool SUB = false, int V = 1>
 __global__ void __launch_bounds__(256, kSlabCtas) fp_slab_kernel(
     const __grid_constant__ RayArgs A, const __grid_constant__ CUtensorMap tmx,
     const __grid_constant__ CUtensorMap tmy, const TV* __restrict__ px,
-    const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E, int pair) {
+    const TV* __restrict__ py, int Pf, TO* __restrict__ out, const SlabEpi E) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ SlabShared S;
   TV* buf0 = reinterpret_cast<TV*>(smem_raw);
   TV* buf1 = buf0 + kBufElems;
   slab_init_barriers(S);
   uint32_t phase = 0u, issued = 0u;  // issued: copies per buffer (thread 0)
-  // two consecutive views per CTA where the launch pairs them (pair != 0:
-  // their bundles overlap), else one; general3D one
-  constexpr int V = GEOM == 3 ? 1 : 2;
-  const int per = (V == 2 && pair) ? 2 : 1;
+  const int per = V;
   const int view0 = blockIdx.x * per;
   const int tiles_u = (A.det_w + 31) >> 5;
   SlabJob J;
@@ -1262,19 +1261,24 @@ template <int GEOM, bool BORDER, int EPI, typename TV, typename TO, bool ZL = fa
 static cudaError_t slab_go(const RayArgs& a, const CUtensorMap& mx, const CUtensorMap& my,
                            const void* px, const void* py, int Pf, void* out,
                            const SlabEpi& e, cudaStream_t st) {
-  auto k = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO, ZL, SUB>;
+  auto k1 = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO, ZL, SUB, 1>;
+  auto k2 = fp_slab_kernel<GEOM, BORDER, EPI, TV, TO, ZL, SUB, GEOM == 3 ? 1 : 2>;
   const size_t smem = 2 * (size_t)kBufElems * sizeof(TV) + 128;
   static bool attr_set = false;  // once per instantiation (before any capture)
   if (!attr_set) {
-    cudaError_t err = set_slab_attrs(k, smem);
+    cudaError_t err = set_slab_attrs(k1, smem);
+    if (err == cudaSuccess) err = set_slab_attrs(k2, smem);
     if (err != cudaSuccess) return err;
     attr_set = true;
   }
   if (a.nviews <= 0) return cudaSuccess;
   const int tiles = ((a.det_w + 31) / 32) * ((a.det_h + 7) / 8);
-  const int pair = GEOM != 3 && slab_pair_views(a) ? 1 : 0;
+  const bool pair = GEOM != 3 && slab_pair_views(a);
   dim3 blk(32, 8), grd(pair ? (a.nviews + 1) / 2 : a.nviews, tiles);
-  k<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e, pair);
+  if (pair)
+    k2<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e);
+  else
+    k1<<<grd, blk, smem, st>>>(a, mx, my, (const TV*)px, (const TV*)py, Pf, (TO*)out, e);
   return cudaGetLastError();
 }
 

@@ -76,3 +76,35 @@ def test_batch_graph_replay(cuda):
     for p, (s, r) in zip(probs, ref):
         assert torch.equal(p["sino"], s) and torch.equal(p["rec"], r)
     b.close()
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+def test_paired_views_equal_single_view_tiles(cuda, geom):
+    """Views 1 degree apart at W = 64 are close enough for the slab FP to take two
+    per CTA (one box serves both bundles); per ray the arithmetic is that of one
+    view, so the result equals the batched kernel's (one view per CTA) bit for
+    bit -- with an odd view count (the last CTA has one view) and pairs on both
+    sides of 45 and 135 degrees (views that sweep different axes run one at a
+    time in their CTA)."""
+    import torch
+    from mexct import batch, ops, phantoms, tune
+
+    W, H = 64, 40
+    ang = np.deg2rad(40.0 + np.arange(101, dtype=np.float64)).astype(np.float32)
+    vol = phantoms.ellipsoids(W, count=4, seed=31 + geom, nz=H)
+    d = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    p = {"vol": d, "sino": torch.zeros((len(ang), H, W), device="cuda"),
+         "rec": torch.zeros((H, W, W), device="cuda"), "angles": ang, "sad": 1000.0,
+         "geom": geom}
+    b = batch.Batch([p])
+    b.fp()
+    torch.cuda.synchronize()
+    tune.clear()
+    tune.set_mode(tune.FIXED)
+    try:
+        s = ops.fp_dev(d, 1000.0, ang, geom)
+        torch.cuda.synchronize()
+        assert torch.equal(s, p["sino"])
+    finally:
+        tune.set_mode(tune.HEURISTIC)
+    b.close()
