@@ -47,10 +47,11 @@ for p in (ROOT, PKG):
 
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) per view of the slab FP kernel, cone 512^3: one ncu
-# capture of a 32-view launch (dram__bytes_read.sum + dram__bytes_write.sum), scaled
-# per view (traffic grows with the number of views).
-FP_SLAB_DRAM_BYTES_PER_VIEW = (11.672490e9 + 36.73e6) / 32
+# DRAM bytes (read + write) per view of the slab FP kernel, cone 512^3 x 720 views:
+# one single-pass ncu capture of the whole 720-view launch (dram__bytes_read.sum +
+# dram__bytes_write.sum = 14.92 GB + 0.761 GB), per view.  Fewer views per launch
+# reuse less of each tile's bundle from L2 (64 views: 185 MB per view).
+FP_SLAB_DRAM_BYTES_PER_VIEW = (14.92e9 + 0.76112e9) / 720
 
 
 def parse():
