@@ -134,3 +134,19 @@ def test_ooc_empty_subsets_match_in_core(cuda):
     assert np.isfinite(got).all() and np.isfinite(incore).all()
     assert np.array_equal(got == 0, incore == 0)
     assert np.allclose(got, incore, rtol=2e-3, atol=1e-12)
+
+
+def test_ooc_argument_errors(lib):
+    """Arguments are checked before any device work (no GPU needed)."""
+    from mexct import _lib, solver
+
+    pre = np.ones((16, 8, 6), dtype=np.float32, order="F")
+    ang = np.linspace(0, np.pi, 6).astype(np.float32)
+    g = {"type": "cone3d", "SAD": SAD}
+    with pytest.raises(_lib.MexctError, match="status 1"):
+        solver.OSC_TV_recon_ooc(pre, pre, ang, g, 0, 0.2, 3, 3, 1.0, [0], 1 << 30)
+    with pytest.raises(ValueError):
+        solver.OSC_TV_recon_ooc(pre, pre, ang, g, 2, 0.2, 3, 3, 1.0, [0], 1 << 30)
+    with pytest.raises(_lib.MexctError, match="status 1"):
+        _lib.call("mexct_osc_tv_recon_ooc", None, None, None, 16, 8, 6, None, 1000.0, 2, 1, 0.2,
+                  3, 3, 1.0, None, 1 << 30, None, None)
