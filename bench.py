@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--osc-reps", type=int, default=5)
     ap.add_argument("--batch-problems", type=int, default=48)
     ap.add_argument("--serve-requests", type=int, default=60)
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="time the FP64 oracle at the cylinder / ellipsoid / OSC-TV workloads "
+                         "(minutes of host time) beside the library's host entry points")
     ap.add_argument("--config5", action="store_true",
                     help="run only the serving workload at its stated mix (minutes of GPU time)")
     ap.add_argument("--ops-once", action="store_true",
@@ -169,6 +172,65 @@ def cpu_sample(size, views, geom, seconds_target=15.0):
     return {"value": round(gups, 4), "unit": "GUPS", "cores": threads, "kind": "port",
             "sample": "%d^3 volume, FP+BP over %d of %d views, geomFlag %d (FP64 C++/OpenMP "
                       "restatement of the reference, %d threads)" % (n, k, views, geom, threads)}
+
+
+def cpu_configs():
+    """The FP64 oracle (the CPU baseline) at the cylinder, ellipsoid and few-view
+    OSC-TV workloads at full size on all host cores, beside the library's host entry
+    points on the same inputs (host arrays in and out).  Opt-in: bench.py
+    --cpu-configs (minutes of host time)."""
+    import mexct
+    import oracle
+    from mexct import phantoms, solver
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    out = {"cores": threads}
+
+    def timed(fn):
+        t = time.perf_counter()
+        r = fn()
+        return r, time.perf_counter() - t
+
+    # cylinder 128^3, 256 cone views: FP, then BP of that FP
+    vol = phantoms.cylinder(128)
+    ang = np.linspace(0, 2 * np.pi, 256).astype(np.float32)
+    sino, t_cf = timed(lambda: oracle.fp(vol, 1000.0, ang, 256, 2).astype(np.float32))
+    _, t_cb = timed(lambda: oracle.bp(sino, 1000.0, ang, 2))
+    mexct.CUDAmex_FP(vol, 1000.0, ang, 256, 2)  # warm-up
+    gs, t_gf = timed(lambda: mexct.CUDAmex_FP(vol, 1000.0, ang, 256, 2))
+    _, t_gb = timed(lambda: mexct.CUDAmex_BP(gs, 1000.0, ang, 2))
+    out["cylinder_128_cone_256views"] = {"cpu_s": round(t_cf + t_cb, 3),
+                                         "gpu_host_calls_s": round(t_gf + t_gb, 4)}
+    # ellipsoids 384^3, 512 views: FP, Hamming FDK (pre-filter + BP) per geometry
+    vol = phantoms.ellipsoids(384, count=12, seed=2)
+    ang = phantoms.angles_full(512)
+    for geom in (0, 1, 2):
+        g = {"type": ["par3d", "fan3d", "cone3d"][geom], "SAD": 1000.0}
+        sino, t_cf = timed(lambda: oracle.fp(vol, 1000.0, ang, 512, geom).astype(np.float32))
+        filt, t_cp = timed(lambda: oracle.prefilter(sino, geom, ang, "hamming", 1.0, 1.0).astype(np.float32))
+        _, t_cb = timed(lambda: oracle.bp(filt, 1000.0, ang, geom))
+        gs, t_gf = timed(lambda: mexct.CUDAmex_FP(vol, 1000.0, ang, 512, geom))
+        gfl, t_gp = timed(lambda: mexct.preFilterSinogram(gs, g, ang, "hamming", 1.0, 1.0))
+        _, t_gb = timed(lambda: mexct.CUDAmex_BP(gfl, 1000.0, ang, geom))
+        out["ellipsoid_384_512views_geom%d" % geom] = {
+            "cpu_fp_s": round(t_cf, 2), "cpu_fdk_s": round(t_cp + t_cb, 2),
+            "gpu_host_calls_fp_s": round(t_gf, 4), "gpu_host_calls_fdk_s": round(t_gp + t_gb, 4)}
+    # few-view OSC-TV: 256^3, 60 cone views, 20 iterations x 10 subsets
+    vol = phantoms.ellipsoids(256, count=10, seed=7)
+    ang = phantoms.angles_full(60)
+    fp = mexct.CUDAmex_FP(vol, 1000.0, ang, 60, 2).astype(np.float64)
+    rng = np.random.default_rng(11)
+    post = np.asfortranarray(rng.poisson(1e5 * np.exp(-fp)).astype(np.float32))
+    pre = np.full(post.shape, 1e5, dtype=np.float32, order="F")
+    picks = rng.integers(0, 10, 20).astype(np.int32)
+    _, t_c = timed(lambda: oracle.osc_tv(pre, post, ang, 1000.0, 2, 20, 0.2, 10, 10, 1.0, picks))
+    g = {"type": "cone3d", "SAD": 1000.0}
+    solver.OSC_TV_recon(pre, post, ang, g, 1, 0.2, 10, 10, 1.0, picks[:1])  # warm-up
+    _, t_g = timed(lambda: solver.OSC_TV_recon(pre, post, ang, g, 20, 0.2, 10, 10, 1.0, picks))
+    out["osc_tv_256_60views_20x10"] = {"cpu_s": round(t_c, 2), "gpu_host_call_s": round(t_g, 4)}
+    return out
 
 
 def metric_name(args):
@@ -319,6 +381,10 @@ def main():
     if args.config5:
         if rank == 0:
             config5(args)
+        return
+    if args.cpu_configs:
+        if rank == 0:
+            print(json.dumps({"cpu_configs": cpu_configs()}), flush=True)
         return
 
     n, views, geom = args.size, args.views, args.geom
