@@ -882,7 +882,12 @@ struct ChunkCopies {
   }
 };
 
+// z ranges of the host BP's downloads
 constexpr int kHostChunks = 8;
+// view chunks of the host FP: each launch boundary costs part of a wave (one
+// 512^3 x 720-view cone FP on a GB300: 178.5 ms in one launch, 181.3 in 4,
+// 185.1 in 8), the last chunk's download is exposed; 4 balances the two
+constexpr int kFpHostChunks = 4;
 
 mexct_status fp_host_overlapped(mexct_ctx* c, int W, int H, float sad, const float* angles,
                                 int nP, int geom, float* out) {
@@ -890,8 +895,8 @@ mexct_status fp_host_overlapped(mexct_ctx* c, int W, int H, float sad, const flo
   MEXCT_TRY_CUDA(copy_stream(c, &cs), "fp: copy stream");
   const size_t P = (size_t)W * H;
   ChunkCopies cc;
-  ChunkHook hook{kHostChunks, [&](int i, int v0, int n) -> mexct_status {
-                   if (i >= kHostChunks) return set_err(MEXCT_ERR_ARG, "fp: too many chunks");
+  ChunkHook hook{kFpHostChunks, [&](int i, int v0, int n) -> mexct_status {
+                   if (i >= kFpHostChunks) return set_err(MEXCT_ERR_ARG, "fp: too many chunks");
                    MEXCT_TRY_CUDA(cudaEventRecord(c->chunk_ev[i], c->stream), "fp: event");
                    cc.items.push_back({(size_t)v0 * P * 4, (size_t)n * P * 4});
                    return MEXCT_OK;
@@ -999,7 +1004,7 @@ mexct_status mexct_fp(mexct_ctx* ctx, const float* vol, int W, int H,
   mexct_status s = upload(c->in, vol, N * 4, c->stream, "fp: upload");
   if (s) return s;
   MEXCT_TRY_CUDA(c->out.ensure_async(M * 4, c->stream), "fp: workspace");
-  if (nP >= 16 && nP <= kHostChunks * kMaxViews && M * 4 >= ((size_t)64 << 20)) {
+  if (nP >= 16 && nP <= kFpHostChunks * kMaxViews && M * 4 >= ((size_t)64 << 20)) {
     // the slab FP in view chunks, each chunk's download overlapping the
     // launches after it (same result as one launch: rays are independent)
     mexct_shape shp;
