@@ -305,7 +305,9 @@ mexct_status mexct_osctv_create_ex(mexct_ctx* ctx, const float* d_pre, const flo
   MEXCT_TRY_CUDA(launch_fill(s->mu.p, mu_type, (long long)N, 1e-10f, st), "osctv_create: mu");
   if (data_type == kF16) {
     // one power-of-two scale for both residuals (|pre e^-l - post| and
-    // pre e^-l l are below max(pre, post)): the largest count to <= 2^15
+    // pre e^-l l are below max(pre, post)): the largest count to (2^14, 2^15],
+    // so counts of any magnitude (photon counts or intensities below 1) keep
+    // FP16's 11-bit precision away from its subnormal range
     unsigned* d_max = reinterpret_cast<unsigned*>(s->scal.as<double>() + 4);
     MEXCT_TRY_CUDA(cudaMemsetAsync(d_max, 0, sizeof(unsigned), st), "osctv_create: scale");
     MEXCT_TRY_CUDA(launch_max_nonneg(d_pre, (long long)M, d_max, st), "osctv_create: scale");
@@ -316,8 +318,10 @@ mexct_status mexct_osctv_create_ex(mexct_ctx* ctx, const float* d_pre, const flo
     MEXCT_TRY_CUDA(cudaStreamSynchronize(st), "osctv_create: scale");
     float mx;
     std::memcpy(&mx, &bits, sizeof mx);
+    const double top = std::max((double)mx, 1e-6);  // the clamped counts' largest
     int e = 0;
-    while (e < 100 && std::ldexp((double)mx, -e) > 32768.0) ++e;
+    while (e < 100 && std::ldexp(top, -e) > 32768.0) ++e;
+    while (e > -100 && std::ldexp(top, -(e - 1)) <= 32768.0) --e;
     s->data_exp = e;
   }
   MEXCT_TRY_CUDA(launch_clamp_copy(d_pre, s->pre.as<float>(), (long long)M, 1e-6f, st),

@@ -149,6 +149,36 @@ def test_fp16_residual_views_track_fp64_oracle(cuda, orc, geom):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("form", ["fp32", "fp16 residual views"])
+def test_counts_times_power_of_two_give_the_same_mu(cuda, form):
+    """The OSC update is mu + mu num/den with num and den backprojections of
+    residuals linear in the counts (OSC_TV_recon.m:51-60), and the TV step depends
+    on mu only, so counts times 2^-20 (intensities below 1) give the same mu bit for
+    bit.  With FP16 residual views this holds because the stored scale follows the
+    counts both ways (largest count to (2^14, 2^15]); a scale that only shrank
+    would leave such residuals in FP16's subnormal range."""
+    import torch
+    from mexct import solver
+
+    W, H, nP = 32, 24, 24
+    _, ang, pre, post = _problem(W, H, nP, 2, seed=3)
+    pre, post = np.maximum(pre, 2.0), np.maximum(post, 2.0)  # above the 1e-6 clamp
+    ddt = torch.float16 if form != "fp32" else None
+    kw = dict(n_iter=3, tv_const=0.2, n_sub_init=6, n_sub_final=3, p_val=1.0)
+    mus = []
+    for scale in (1.0, 2.0 ** -20):
+        dpre = torch.from_numpy(np.ascontiguousarray((pre * scale).transpose(2, 1, 0))).cuda()
+        dpost = torch.from_numpy(np.ascontiguousarray((post * scale).transpose(2, 1, 0))).cuda()
+        s = solver.OscTvSolver(dpre, dpost, ang, 1000.0, 2, data_dtype=ddt)
+        s.run([1, 4, 0], **kw)
+        mus.append(s.mu().clone())
+        s.close()
+    torch.cuda.synchronize()
+    assert torch.isfinite(mus[0]).all() and mus[0].abs().max() > 0
+    assert torch.equal(mus[0], mus[1])
+
+
+@pytest.mark.gpu
 def test_bf16_storage_one_iteration(cuda):
     """BF16 storage of mu (FP32 accumulation, FP64 norms): one OSC iteration stays
     within 1e-2 relative L2 of the FP32 form (BF16 keeps an 8-bit mantissa).  FP16

@@ -98,8 +98,11 @@ def test_ooc_slabs_vs_in_core_and_fp64_oracle(cuda, orc, geom, H):
           "oracle %.3g (in-core vs oracle %.3g)" % (e1, n_iter, e_in, e_orc,
                                                      rel_l2(incore, ref[n_iter])))
     assert np.isfinite(got).all()
-    assert e1 <= 2e-6
-    assert e_in <= 1e-3
+    # parallel rays keep their z, so each ray's samples lie in one slab: the
+    # slab parts are the in-core sums (measured: equal after iteration 1, 5e-7
+    # after 3); cone rays cross slabs (FP32 sums of parts: 6.5e-8, then 8e-5)
+    assert e1 <= (1e-7 if geom == 0 else 2e-6)
+    assert e_in <= (2e-5 if geom == 0 else 1e-3)
     assert e_orc <= 5e-3
 
 
