@@ -46,9 +46,10 @@ mexct_status mexct_osctv_create(mexct_ctx* ctx, const float* d_pre,
 /* As mexct_osctv_create, with the storage of the residual views (the OSC
  * forward pass's pre e^-l - post and pre e^-l l, read by the dual BP) chosen:
  * MEXCT_F32, or MEXCT_F16 (FP32 mu only) holding the residuals times one power
- * of two that brings the largest count to <= 2^15 (FP16 cannot hold counts
- * above 65504; the update num/den does not depend on a common scale of the
- * two residuals).  The counts stay FP32: rounding them to FP16 moves the
+ * of two that brings the largest count into (2^14, 2^15] (FP16 cannot hold
+ * counts above 65504, and small intensities would fall into its subnormal
+ * range; the update num/den does not depend on a common scale of the two
+ * residuals).  The counts stay FP32: rounding them to FP16 moves the
  * reconstruction itself.  Every sum accumulates in FP32, every norm in FP64. */
 mexct_status mexct_osctv_create_ex(mexct_ctx* ctx, const float* d_pre,
                                    const float* d_post, int W, int H, int nP,
