@@ -1,6 +1,6 @@
 """GPU parity of every operator against the FP64 oracle, through the C ABI.
 
-FP32 results must be within 1e-5 relative L2 of the oracle (spec tolerance);
+FP32 results must be within 1e-5 relative L2 of the oracle (the required tolerance);
 the per-operator tolerance is written next to each assertion.
 """
 import numpy as np
@@ -271,6 +271,36 @@ def test_fp_slab_large_detector_multiple_tiles(cuda, orc, geom):
     got = mexct.CUDAmex_FP(vol, 1000.0, ang, nP, geom)
     ref = orc.fp(vol, 1000.0, ang, nP, geom)
     assert rel_l2(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+def test_tall_volume_every_detector_row(cuda, orc, geom):
+    """H = 40 > 32 ceil(W / 32) = 32: the reference's FP grid is sized by W
+    (CUDAmex_FP.cu:432-440), so its rows 32..39 are never written and stay 0.
+    Every row is computed here (a stated deviation), FP and its texture variant
+    alike, within the FP32 bar of the oracle; BP covers every slice."""
+    import oracle
+    import torch
+    import mexct
+    from mexct import _lib, ops
+
+    W, H, nP = 24, 40, 6
+    rng = np.random.default_rng(40 + geom)
+    vol = np.asfortranarray(rng.uniform(0.5, 1.5, (W, W, H)).astype(np.float32))
+    ang = np.linspace(0.1, 2 * np.pi, nP, endpoint=False).astype(np.float32)
+    got = mexct.CUDAmex_FP(vol, 1000.0, ang, nP, geom)
+    ref = orc.fp(vol, 1000.0, ang, nP, geom)
+    assert np.count_nonzero(got[:, 32:, :]) > 0.9 * got[:, 32:, :].size
+    assert rel_l2(got, ref) <= TOL
+    dvol = torch.from_numpy(np.ascontiguousarray(vol.transpose(2, 1, 0))).cuda()
+    tex = ops.fp_dev(dvol, 1000.0, ang, geom, variant=_lib.FP_TEXTURE)
+    tex = tex.cpu().numpy().transpose(2, 1, 0)
+    assert np.count_nonzero(tex[:, 32:, :]) > 0.9 * tex[:, 32:, :].size
+    with oracle.tex_weights(oracle.TEX_HW), oracle.ref_steps(1):
+        ref_hw = orc.fp(vol, 1000.0, ang, nP, geom)  # 8-bit weights, binary32 steps
+    assert rel_l2(tex, ref_hw) <= 5e-6
+    bp = mexct.CUDAmex_BP(got, 1000.0, ang, geom)
+    assert rel_l2(bp, orc.bp(got, 1000.0, ang, geom)) <= TOL
 
 
 @pytest.mark.parametrize("variant", [0, 2])

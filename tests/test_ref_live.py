@@ -99,3 +99,25 @@ def test_ellipsoid_384_general3d_helix_vs_reference(cuda, ref, ell384):
         rb += ref.g3d_bp(lf[..., j:j + 1], av[j:j + 1], pv[..., j], 384, 384)
     lb = mexct.CUDAmex_general3D_BP(lf, av, pv, 384, 384)
     assert rel_l2(lb, rb) <= 5e-6  # same binary32 indices and weights; float atomics order only
+
+
+@pytest.mark.parametrize("geom", [0, 1, 2])
+def test_tall_volume_rows_beyond_the_reference_grid(cuda, ref, geom):
+    """The reference's FP grid is sized by W (CUDAmex_FP.cu:432-440): with W = 24
+    and H = 40 its detector rows 32..39 are never written and stay 0.  The texture
+    variant equals the reference bit for bit on rows 0..31 and, like the exact path,
+    computes rows 32..39 as well (a stated deviation)."""
+    import mexct
+
+    W, H, nP = 24, 40, 6
+    rng = np.random.default_rng(40 + geom)
+    vol = np.asfortranarray(rng.uniform(0.5, 1.5, (W, W, H)).astype(np.float32))
+    ang = np.linspace(0.1, 2 * np.pi, nP, endpoint=False).astype(np.float32)
+    rf = ref.fp(vol, SAD, ang, nP, geom)
+    assert np.count_nonzero(rf[:, 32:, :]) == 0
+    tex = _tex_fp(vol, ang, geom)
+    assert np.array_equal(tex[:, :32, :], rf[:, :32, :])
+    assert np.count_nonzero(tex[:, 32:, :]) > 0.9 * tex[:, 32:, :].size
+    lf = mexct.CUDAmex_FP(vol, SAD, ang, nP, geom)
+    # random voxels: the 8-bit weights move each lerp by up to |dv| / 512
+    assert rel_l2(lf[:, :32, :], rf[:, :32, :]) <= 1e-3
