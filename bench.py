@@ -496,7 +496,9 @@ def main():
                      "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
                      if peak_kind == "measured" else "fallback 6.8 TB/s",
                      "traffic": dom[3],
-                     "note": "gather-bound projector: compulsory bytes 4(N+P*nP) over the launch"},
+                     "note": "gather-bound projector: compulsory bytes 4(N+P*nP) over the "
+                             "launch; its bound is on chip (ncu: the L1/shared-memory data "
+                             "pipe at ~80 % of its wavefront peak, 67-71 % of issue slots)"},
         "clocks": clk,
         # per step: pad_x, pad_transpose, fp_slab, pad_sino_quad, bp_pad
         "gpu_launches": 5 * args.steps,
