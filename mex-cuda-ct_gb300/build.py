@@ -81,13 +81,14 @@ MEX_LIB = os.path.join(BUILD, "libmexct_mex.so")
 
 
 def build_mex_stub(force: bool = False) -> str:
-    """The six MEX gateways against the stub mex.h, linked into one shared
+    """The MEX gateways against the stub mex.h, linked into one shared
     library with a by-name call interface (mxs_call), for testing without MATLAB."""
     lib = build(force=force)
     srcs = sorted(os.path.join(MEX_DIR, f) for f in os.listdir(MEX_DIR) if f.endswith(".cpp"))
     srcs.append(os.path.join(MEX_DIR, "mexstub", "mexstub.cpp"))
     deps = srcs + [os.path.join(MEX_DIR, "gateway.h"), os.path.join(MEX_DIR, "mexstub", "mex.h"),
-                   os.path.join(ROOT, "include", "mexct.h"), lib]
+                   os.path.join(ROOT, "include", "mexct.h"),
+                   os.path.join(ROOT, "include", "mexct_solver.h"), lib]
     if (not force and os.path.exists(MEX_LIB)
             and os.path.getmtime(MEX_LIB) >= max(os.path.getmtime(d) for d in deps)):
         return MEX_LIB

@@ -538,6 +538,7 @@ mexct_status osc_tv_recon_typed(mexct_ctx* ctx, const float* pre, const float* p
     return set_err(MEXCT_ERR_ARG, "osc_tv_recon: NULL pointer");
   if (W <= 0 || H <= 0 || nP <= 0 || n_iter < 1)
     return set_err(MEXCT_ERR_ARG, "osc_tv_recon: bad dims / iterations");
+  if (geom < 0 || geom > 2) return set_err(MEXCT_ERR_ARG, "osc_tv_recon: invalid geometry %d", geom);
   mexct_ctx* c = resolve(ctx);
   if (!c) return set_err(MEXCT_ERR_CUDA, "osc_tv_recon: no CUDA device / context");
   std::lock_guard<std::recursive_mutex> lk(c->mu);

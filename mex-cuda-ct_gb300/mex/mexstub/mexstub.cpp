@@ -99,6 +99,7 @@ void mexFunction_CUDAmex_general3D_FP(int, mxArray**, int, const mxArray**);
 void mexFunction_CUDAmex_general3D_BP(int, mxArray**, int, const mxArray**);
 void mexFunction_CUDAmex_oscIter(int, mxArray**, int, const mxArray**);
 void mexFunction_CUDAmex_TVmin_3D(int, mxArray**, int, const mxArray**);
+void mexFunction_CUDAmex_OSC_TV_recon(int, mxArray**, int, const mxArray**);
 
 mxArray* mxs_create(int cls, int ndim, const size_t* dims, const void* data) {
   mxArray* a = mxCreateNumericArray((mwSize)ndim, (const mwSize*)dims, (mxClassID)cls, mxREAL);
@@ -123,6 +124,7 @@ int mxs_call(const char* name, int nlhs, mxArray** plhs, int nrhs, const mxArray
       {"CUDAmex_general3D_BP", mexFunction_CUDAmex_general3D_BP},
       {"CUDAmex_oscIter", mexFunction_CUDAmex_oscIter},
       {"CUDAmex_TVmin_3D", mexFunction_CUDAmex_TVmin_3D},
+      {"CUDAmex_OSC_TV_recon", mexFunction_CUDAmex_OSC_TV_recon},
   };
   auto it = table.find(name ? name : "");
   if (it == table.end()) return 2;
