@@ -242,6 +242,16 @@ mexct_status mexct_bp_det_dev(mexct_ctx* ctx, const float* d_sino,
                               const float* angles, int geom, int W, int H,
                               float* d_vol, void* stream);
 
+/* Host-array forms of the two above (MATLAB layouts, as mexct_fp / mexct_bp:
+ * vol [W, W, H], sinogram [det_w, det_h, nP], both x / u fastest): one
+ * upload, the device operator, one download, synchronous. */
+mexct_status mexct_fp_det(mexct_ctx* ctx, const float* vol, int W, int H, float sad,
+                          const float* angles, int nP, int geom,
+                          const mexct_detector* det, float* out);
+mexct_status mexct_bp_det(mexct_ctx* ctx, const float* sino,
+                          const mexct_detector* det, int nP, float sad,
+                          const float* angles, int geom, int W, int H, float* vol);
+
 /* One OSC iteration (as mexct_osc_iter_dev) with the scanner's detector
  * decoupled from the volume (no counterpart in the reference, whose oscIter
  * ties the detector to the volume's face): pre/post are FP32 counts on a

@@ -1068,6 +1068,37 @@ mexct_status mexct_bp_det_dev(mexct_ctx* ctx, const float* d_sino, const mexct_d
   return bp_det_impl(c, d_sino, det, nP, sad, angles, geom, W, H, d_vol, as_stream(stream));
 }
 
+mexct_status mexct_fp_det(mexct_ctx* ctx, const float* vol, int W, int H, float sad,
+                          const float* angles, int nP, int geom, const mexct_detector* det,
+                          float* out) {
+  VALIDATE(fp_det_impl(nullptr, vol, W, H, sad, angles, nP, geom, det, out, nullptr));
+  CTX_OR_FAIL(c, "fp_det");
+  const size_t N = (size_t)W * W * H;
+  const size_t M = (size_t)det->det_w * (size_t)det->det_h * (size_t)nP;
+  mexct_status s = upload(c->in, vol, N * 4, c->stream, "fp_det: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->out.ensure_async(M * 4, c->stream), "fp_det: workspace");
+  s = fp_det_impl(c, c->in.as<float>(), W, H, sad, angles, nP, geom, det, c->out.as<float>(),
+                  c->stream);
+  if (s) return s;
+  return finish(c, out, c->out, M * 4, "fp_det: download");
+}
+
+mexct_status mexct_bp_det(mexct_ctx* ctx, const float* sino, const mexct_detector* det, int nP,
+                          float sad, const float* angles, int geom, int W, int H, float* vol) {
+  VALIDATE(bp_det_impl(nullptr, sino, det, nP, sad, angles, geom, W, H, vol, nullptr));
+  CTX_OR_FAIL(c, "bp_det");
+  const size_t N = (size_t)W * W * H;
+  const size_t M = (size_t)det->det_w * (size_t)det->det_h * (size_t)nP;
+  mexct_status s = upload(c->in, sino, M * 4, c->stream, "bp_det: upload");
+  if (s) return s;
+  MEXCT_TRY_CUDA(c->out.ensure_async(N * 4, c->stream), "bp_det: workspace");
+  s = bp_det_impl(c, c->in.as<float>(), det, nP, sad, angles, geom, W, H, c->out.as<float>(),
+                  c->stream);
+  if (s) return s;
+  return finish(c, vol, c->out, N * 4, "bp_det: download");
+}
+
 mexct_status mexct_bp(mexct_ctx* ctx, const float* sino, int W, int H, int nP,
                       float sad, const float* angles, int geom, float* vol) {
   VALIDATE(bp_dev_impl(nullptr, sino, kF32, W, H, nP, sad, angles, geom, vol, kF32, nullptr));

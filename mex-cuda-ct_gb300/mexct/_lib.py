@@ -74,6 +74,8 @@ SIGNATURES = {
     "mexct_bp_dev_ex": [_P, _P, _i, _i, _i, _i, _f, _P, _i, _P, _i, _P],
     "mexct_fp_det_dev": [_P, _P, _i, _i, _f, _P, _i, _i, _P, _P, _P],
     "mexct_bp_det_dev": [_P, _P, _P, _i, _f, _P, _i, _i, _i, _P, _P],
+    "mexct_fp_det": [_P, _P, _i, _i, _f, _P, _i, _i, _P, _P],
+    "mexct_bp_det": [_P, _P, _P, _i, _f, _P, _i, _i, _i, _P],
     "mexct_sub_rows": [_i, _i, _f, _i, _i, _i, _c.POINTER(_i), _c.POINTER(_i)],
     "mexct_fp_sub_dev": [_P, _P, _i, _i, _i, _i, _f, _P, _i, _i, _P, _i, _P],
     "mexct_bp_sub_dev": [_P, _P, _i, _i, _i, _i, _i, _f, _P, _i, _i, _i, _P, _i, _P],

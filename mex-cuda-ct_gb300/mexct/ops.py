@@ -327,6 +327,41 @@ def bp_det_dev(sino, sad, angles, geom, W, H, du=1.0, dv=1.0, out=None, stream=N
     return out
 
 
+def fp_det(vol, sad, angles, geom, det_w, det_h, du=1.0, dv=1.0, ss=1):
+    """FP of a host volume [W, W, H] onto a det_w x det_h detector of pitch du x dv
+    with ss x ss rays per pixel -> float32 sinogram [det_w, det_h, nP] (MATLAB layout)."""
+    vol = _f32F(vol, "vol")
+    if vol.ndim == 2:
+        vol = vol[:, :, None]
+    if vol.ndim != 3 or vol.shape[0] != vol.shape[1]:
+        raise ValueError("vol must be [W, W, H], got %s" % (vol.shape,))
+    W, _, H = vol.shape
+    ang = _angles(angles, 0)
+    nP = ang.size
+    det = _lib.Detector(int(det_w), int(det_h), float(du), float(dv), int(ss))
+    out = np.empty((int(det_w), int(det_h), nP), dtype=np.float32, order="F")
+    _lib.call("mexct_fp_det", None, _ptr(vol), W, H, float(sad), _ptr(ang), nP, _geom_flag(geom),
+              ctypes.addressof(det), _ptr(out))
+    return out
+
+
+def bp_det(sino, sad, angles, geom, W, H, du=1.0, dv=1.0):
+    """BP of a host sinogram [det_w, det_h, nP] of pitch du x dv -> float32 volume
+    [W, W, H] (MATLAB layout)."""
+    sino = _f32F(sino, "projections")
+    if sino.ndim == 2:
+        sino = sino[:, :, None]
+    if sino.ndim != 3:
+        raise ValueError("projections must be [det_w, det_h, nP], got %s" % (sino.shape,))
+    det_w, det_h, nP = sino.shape
+    ang = _angles(angles, nP)
+    det = _lib.Detector(int(det_w), int(det_h), float(du), float(dv), 1)
+    out = np.empty((int(W), int(W), int(H)), dtype=np.float32, order="F")
+    _lib.call("mexct_bp_det", None, _ptr(sino), ctypes.addressof(det), nP, float(sad), _ptr(ang),
+              _geom_flag(geom), int(W), int(H), _ptr(out))
+    return out
+
+
 def sub_rows(W, H, sad, geom, z0, nz):
     """Detector rows (row0, nrows) that the BP of slab z0 .. z0 + nz - 1 reads."""
     r0, nr = ctypes.c_int(), ctypes.c_int()

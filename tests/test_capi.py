@@ -151,3 +151,33 @@ def test_detector_entry_points_validate_the_detector(lib):
     assert lib.mexct_bp_det_dev(None, _p(buf), ctypes.addressof(d), 2, 1000.0, _p(ang), 5, 8, 4,
                                 _p(buf), None) == _lib.ERR_ARG
     assert "invalid geometry 5" in _lib.last_error()
+
+
+def test_host_detector_entry_points_validate_before_device_work(lib):
+    """The host-array forms mexct_fp_det / mexct_bp_det check the detector, the
+    geometry and their pointers before any upload; with valid arguments and no
+    GPU they stop at the missing device."""
+    import torch
+    from mexct import _lib
+
+    buf = np.zeros(64, F)
+    ang = np.zeros(2, F)
+    for det in [(0, 4, 1.0, 1.0, 1), (8, 4, -1.0, 1.0, 1), (8, 4, 1.0, 1.0, 9)]:
+        d = _lib.Detector(*det)
+        assert lib.mexct_fp_det(None, _p(buf), 8, 4, 1000.0, _p(ang), 2, 0, ctypes.addressof(d),
+                                _p(buf)) == _lib.ERR_ARG, det
+    assert lib.mexct_fp_det(None, _p(buf), 8, 4, 1000.0, _p(ang), 2, 0, None,
+                            _p(buf)) == _lib.ERR_ARG
+    d = _lib.Detector(8, 4, 1.0, 1.0, 1)
+    assert lib.mexct_fp_det(None, None, 8, 4, 1000.0, _p(ang), 2, 0, ctypes.addressof(d),
+                            _p(buf)) == _lib.ERR_ARG
+    assert lib.mexct_bp_det(None, _p(buf), ctypes.addressof(d), 2, 1000.0, _p(ang), 5, 8, 4,
+                            _p(buf)) == _lib.ERR_ARG
+    assert "invalid geometry 5" in _lib.last_error()
+    assert lib.mexct_bp_det(None, _p(buf), ctypes.addressof(d), 2, 1000.0, _p(ang), 0, 8, 4,
+                            None) == _lib.ERR_ARG
+    if not torch.cuda.is_available():
+        assert lib.mexct_fp_det(None, _p(buf), 8, 4, 1000.0, _p(ang), 2, 0, ctypes.addressof(d),
+                                _p(buf)) == _lib.ERR_CUDA
+        assert lib.mexct_bp_det(None, _p(buf), ctypes.addressof(d), 2, 1000.0, _p(ang), 0, 8, 4,
+                                _p(buf)) == _lib.ERR_CUDA

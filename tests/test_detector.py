@@ -1,4 +1,5 @@
-"""Decoupled detector (mexct_fp_det_dev / mexct_bp_det_dev) against the oracle.
+"""Decoupled detector (mexct_fp_det_dev / mexct_bp_det_dev and their host-array
+forms mexct_fp_det / mexct_bp_det) against the oracle.
 
 The reference's detector is the volume's face: W x H pixels of unit pitch and
 one ray per pixel centre.  These entry points take any det_w x det_h detector
@@ -103,6 +104,23 @@ def test_default_detector_is_the_standard_operator(case, geom):
     e = (torch.linalg.vector_norm((bp - bp_std).double()) /
          torch.linalg.vector_norm(bp_std.double())).item()
     assert e <= 1e-6
+
+
+@pytest.mark.parametrize("geom", [0, 2])
+def test_host_array_forms_equal_the_device_forms(case, geom):
+    """mexct_fp_det / mexct_bp_det take host arrays in the MATLAB layouts and
+    return what the device entry points return, bit for bit (super-sampled FP
+    onto a 31 x 21 detector of pitch 1.1 x 0.9, then its BP)."""
+    from mexct import ops
+
+    vol, ang, d = case
+    Wd, Hd, du, dv, ss = DETECTORS[3]
+    fh = ops.fp_det(vol, 1000.0, ang, geom, Wd, Hd, du, dv, ss)
+    fd = _host(ops.fp_det_dev(d, 1000.0, ang, geom, Wd, Hd, du, dv, ss))
+    assert fh.shape == (Wd, Hd, NP) and np.array_equal(fh, fd)
+    bh = ops.bp_det(fh, 1000.0, ang, geom, W, H, du, dv)
+    bd = _host(ops.bp_det_dev(_dev(fh), 1000.0, ang, geom, W, H, du, dv))
+    assert bh.shape == (W, W, H) and np.array_equal(bh, bd)
 
 
 def test_supersampled_fp_is_the_mean_of_shifted_detectors(case):
