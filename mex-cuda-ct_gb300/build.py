@@ -20,7 +20,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmexct.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["k_proj.cu", "k_slab.cu", "k_iter.cu", "batch.cu", "api.cu", "ops.cu", "solver.cu",
-           "serve.cu", "noalloc.cu", "tune.cu", "subvol.cu", "solver_ooc.cu", "fileio.cpp"]
+           "serve.cu", "noalloc.cu", "tune.cu", "subvol.cu", "solver_ooc.cu", "fileio.cpp",
+           "mat73.cpp"]
 
 
 def nvcc() -> str:

@@ -9,10 +9,12 @@
 //  - MAT (Level 5, the format of MATLAB's save up to -v7): a 128-byte header,
 //    then one data element per variable, either a miMATRIX or a miCOMPRESSED
 //    element (zlib stream) holding one.  Numeric classes of any storage type
-//    are converted to float32 (real part); -v7.3 files are HDF5 and are not
-//    read.  Compressed elements are inflated by the DEFLATE decoder below,
-//    written from RFC 1951 (block formats, canonical Huffman codes, length /
-//    distance tables) and RFC 1950 (zlib header, Adler-32 check).
+//    are converted to float32 (real part).  -v7.3 files are HDF5 and are
+//    read by mat73.cpp.  Compressed elements (and HDF5's deflated chunks) are
+//    inflated by the DEFLATE decoder below, written from RFC 1951 (block
+//    formats, canonical Huffman codes, length / distance tables) and RFC 1950
+//    (zlib header, Adler-32 check).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
@@ -23,6 +25,7 @@
 #include <vector>
 
 #include "../../include/mexct.h"
+#include "fileio_internal.h"
 
 namespace mexct {
 mexct_status set_err(mexct_status code, const char* fmt, ...);
@@ -35,6 +38,17 @@ bool read_file(const char* path, std::vector<uint8_t>& buf) {
   FILE* f = std::fopen(path, "rb");
   if (!f) return false;
   buf.clear();
+  // one read of the whole file where its size is known (a scan is GBs), then
+  // whatever follows (a file that grew, or one that cannot seek) in pieces
+  if (std::fseek(f, 0, SEEK_END) == 0) {
+    const long size = std::ftell(f);
+    if (size > 0 && std::fseek(f, 0, SEEK_SET) == 0) {
+      buf.resize((size_t)size);
+      buf.resize(std::fread(buf.data(), 1, buf.size(), f));
+    } else {
+      std::rewind(f);
+    }
+  }
   uint8_t chunk[1 << 16];
   size_t n;
   while ((n = std::fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + n);
@@ -46,9 +60,15 @@ bool read_file(const char* path, std::vector<uint8_t>& buf) {
 // ---------------------------------------------------------------------------
 // DEFLATE (RFC 1951) and the zlib wrapper (RFC 1950)
 // ---------------------------------------------------------------------------
+constexpr int kFastBits = 9;  // codes up to this length decode with one table lookup
+
 struct Huffman {
   int count[16];  // codes of each length
   int symbol[320];  // symbols in canonical code order
+  // the next kFastBits input bits -> symbol and code length (0: a longer
+  // code, decoded bit by bit)
+  int16_t fast_sym[1 << kFastBits];
+  uint8_t fast_len[1 << kFastBits];
 };
 
 class Inflater {
@@ -57,25 +77,35 @@ class Inflater {
 
   // Decodes blocks until the final one; false on malformed or truncated input.
   bool run(std::vector<uint8_t>& out) {
+    // out is grown ahead of the writes (bytes [0, used_) are the output) and
+    // trimmed once at the end
+    used_ = out.size();
     int last;
+    bool ok = true;
     do {
       last = (int)bits(1);
       const int type = (int)bits(2);
-      if (bad_) return false;
-      bool ok;
+      if (bad_) {
+        ok = false;
+        break;
+      }
       if (type == 0) ok = stored(out);
       else if (type == 1) ok = fixed(out);
       else if (type == 2) ok = dynamic(out);
       else ok = false;
-      if (!ok || bad_) return false;
+      if (!ok || bad_) {
+        ok = false;
+        break;
+      }
     } while (!last);
-    return true;
+    out.resize(used_);
+    return ok;
   }
   size_t consumed() const { return pos_ - (size_t)(cnt_ / 8); }
 
  private:
   const uint8_t* p_;
-  size_t n_, pos_ = 0;
+  size_t n_, pos_ = 0, used_ = 0;
   uint64_t buf_ = 0;
   int cnt_ = 0;
   bool bad_ = false;
@@ -100,6 +130,7 @@ class Inflater {
   // of unused codes (0: complete).
   static int build(Huffman& h, const uint8_t* len, int n) {
     for (int l = 0; l < 16; ++l) h.count[l] = 0;
+    std::memset(h.fast_len, 0, sizeof h.fast_len);
     for (int s = 0; s < n; ++s) h.count[len[s]]++;
     if (h.count[0] == n) return 0;
     int left = 1;
@@ -113,12 +144,50 @@ class Inflater {
     for (int l = 1; l < 15; ++l) offs[l + 1] = offs[l] + h.count[l];
     for (int s = 0; s < n; ++s)
       if (len[s]) h.symbol[offs[len[s]]++] = s;
+    // Lookup table: symbol s of length l <= kFastBits has the canonical code
+    // next[l]++ (most significant bit first); the stream holds it reversed,
+    // so every table index whose low l bits are the reversed code maps to s.
+    if (left == 0) {
+      int next[16];
+      int code = 0;
+      next[0] = 0;
+      for (int l = 1; l < 16; ++l) {
+        code = (code + h.count[l - 1] * (l > 1)) << 1;
+        next[l] = code;
+      }
+      for (int s = 0; s < n; ++s) {
+        const int l = len[s];
+        if (l == 0) continue;
+        const int c = next[l]++;
+        if (l > kFastBits) continue;
+        int r = 0;
+        for (int b = 0; b < l; ++b) r |= ((c >> b) & 1) << (l - 1 - b);
+        for (int fill = 0; fill < (1 << (kFastBits - l)); ++fill) {
+          h.fast_sym[r | (fill << l)] = (int16_t)s;
+          h.fast_len[r | (fill << l)] = (uint8_t)l;
+        }
+      }
+    }
     return left;
   }
 
   // One symbol: the code's bits arrive most significant first; codes of
   // each length are consecutive integers starting at `first`.
   int decode(const Huffman& h) {
+    while (cnt_ < kFastBits && pos_ < n_) {
+      buf_ |= (uint64_t)p_[pos_++] << cnt_;
+      cnt_ += 8;
+    }
+    const int i = (int)(buf_ & ((1u << kFastBits) - 1));
+    const int fl = h.fast_len[i];
+    if (fl != 0 && fl <= cnt_) {  // only bits that arrived (missing ones read as 0)
+      buf_ >>= fl;
+      cnt_ -= fl;
+      return h.fast_sym[i];
+    }
+    return decode_slow(h);
+  }
+  int decode_slow(const Huffman& h) {
     int code = 0, first = 0, index = 0;
     for (int l = 1; l < 16; ++l) {
       code |= (int)bits(1);
@@ -137,39 +206,116 @@ class Inflater {
     cnt_ -= cnt_ & 7;
     const uint32_t len = bits(16), nlen = bits(16);
     if (bad_ || len != (~nlen & 0xffffu)) return false;
-    for (uint32_t i = 0; i < len; ++i) out.push_back((uint8_t)bits(8));
-    return !bad_;
+    if (out.size() - used_ < len) out.resize(std::max<size_t>(2 * out.size(), used_ + len));
+    uint32_t left = len;
+    for (; left > 0 && cnt_ >= 8; --left) {  // bytes already in the bit buffer
+      out[used_++] = (uint8_t)buf_;
+      buf_ >>= 8;
+      cnt_ -= 8;
+    }
+    if (left > n_ - pos_) return false;
+    std::memcpy(out.data() + used_, p_ + pos_, left);
+    used_ += left;
+    pos_ += left;
+    return true;
   }
 
+  // Literal / length / distance symbols of one block until its end code.
+  // The bit buffer lives in locals here: the output bytes are stored through
+  // a uint8_t pointer, which may alias any member, so members would be
+  // reloaded after every byte.  The slow (long-code) path and the extra-bit
+  // reads at the end of the input go through the members.
   bool codes(std::vector<uint8_t>& out, const Huffman& lit, const Huffman& dist) {
-    static const int lbase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
-                                  31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
-    static const int lext[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
-                                 2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
-    static const int dbase[30] = {1,    2,    3,    4,    5,    7,     9,     13,    17,  25,
-                                  33,   49,   65,   97,   129,  193,   257,   385,   513, 769,
-                                  1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
-    static const int dext[30] = {0, 0, 0, 0, 1, 1, 2, 2,  3,  3,  4,  4,  5,  5,  6,
-                                 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
-    for (;;) {
-      int sym = decode(lit);
-      if (sym < 0) return false;
-      if (sym < 256) {
-        out.push_back((uint8_t)sym);
-      } else if (sym == 256) {
-        return true;
-      } else {
-        sym -= 257;
-        if (sym >= 29) return false;
-        const size_t len = (size_t)lbase[sym] + bits(lext[sym]);
-        const int ds = decode(dist);
-        if (ds < 0 || ds >= 30) return false;
-        const size_t d = (size_t)dbase[ds] + bits(dext[ds]);
-        if (bad_ || d > out.size()) return false;
-        const size_t from = out.size() - d;
-        for (size_t i = 0; i < len; ++i) out.push_back(out[from + i]);  // may overlap
+    static const uint16_t lbase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                                       31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+    static const uint8_t lext[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                                     2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+    static const uint16_t dbase[30] = {1,    2,    3,    4,    5,    7,     9,     13,    17,  25,
+                                       33,   49,   65,   97,   129,  193,   257,   385,   513, 769,
+                                       1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+    static const uint8_t dext[30] = {0, 0, 0, 0, 1, 1, 2, 2,  3,  3,  4,  4,  5,  5,  6,
+                                     6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+    const uint8_t* const in = p_;
+    const size_t n = n_;
+    uint64_t buf = buf_;
+    int cnt = cnt_;
+    size_t pos = pos_;
+    size_t size = used_;
+    uint8_t* w = out.data();
+    size_t cap = out.size();
+    auto refill = [&] {
+      while (cnt <= 56 && pos < n) {
+        buf |= (uint64_t)in[pos++] << cnt;
+        cnt += 8;
       }
+    };
+    auto save = [&] {
+      buf_ = buf;
+      cnt_ = cnt;
+      pos_ = pos;
+    };
+    auto load = [&] {
+      buf = buf_;
+      cnt = cnt_;
+      pos = pos_;
+    };
+    auto sym_of = [&](const Huffman& h) -> int {
+      refill();
+      const int i = (int)(buf & ((1u << kFastBits) - 1));
+      const int fl = h.fast_len[i];
+      if (fl != 0 && fl <= cnt) {  // only bits that arrived (missing ones read as 0)
+        buf >>= fl;
+        cnt -= fl;
+        return h.fast_sym[i];
+      }
+      save();
+      const int v = decode_slow(h);
+      load();
+      return v;
+    };
+    auto extra = [&](int k) -> uint32_t {  // k <= 13 bits
+      refill();
+      if (cnt < k) {
+        bad_ = true;
+        return 0;
+      }
+      const uint32_t v = (uint32_t)(buf & ((1u << k) - 1));
+      buf >>= k;
+      cnt -= k;
+      return v;
+    };
+    bool ok = false;
+    for (;;) {
+      if (cap - size < 258) {  // room for the longest match
+        out.resize(std::max<size_t>(2 * cap, size + (1u << 16)));
+        w = out.data();
+        cap = out.size();
+      }
+      int sym = sym_of(lit);
+      if (sym < 0) break;
+      if (sym < 256) {
+        w[size++] = (uint8_t)sym;
+        continue;
+      }
+      if (sym == 256) {
+        ok = true;
+        break;
+      }
+      sym -= 257;
+      if (sym >= 29) break;
+      const size_t len = (size_t)lbase[sym] + extra(lext[sym]);
+      const int ds = sym_of(dist);
+      if (ds < 0 || ds >= 30) break;
+      const size_t d = (size_t)dbase[ds] + extra(dext[ds]);
+      if (bad_ || d > size) break;
+      uint8_t* to = w + size;
+      const uint8_t* from = to - d;
+      for (size_t i = 0; i < len; ++i) to[i] = from[i];  // may overlap: byte by byte
+      size += len;
     }
+    save();
+    used_ = size;
+    return ok && !bad_;
   }
 
   struct FixedCodes {
@@ -231,11 +377,21 @@ class Inflater {
   }
 };
 
+// Adler-32 (RFC 1950 section 8.2) with the modulo taken once per block: with
+// a, b < 65521 at a block's start, after k bytes b <= 65520 (k + 1) + 255 k (k + 1) / 2,
+// which stays below 2^32 for k <= 5552.
 uint32_t adler32(const uint8_t* p, size_t n) {
   uint32_t a = 1, b = 0;
-  for (size_t i = 0; i < n; ++i) {
-    a = (a + p[i]) % 65521u;
-    b = (b + a) % 65521u;
+  while (n > 0) {
+    const size_t k = n < 5552 ? n : 5552;
+    for (size_t i = 0; i < k; ++i) {
+      a += p[i];
+      b += a;
+    }
+    a %= 65521u;
+    b %= 65521u;
+    p += k;
+    n -= k;
   }
   return (b << 16) | a;
 }
@@ -371,14 +527,18 @@ struct MatFile {
   std::vector<uint8_t> raw;
   std::vector<std::vector<uint8_t>> inflated;  // storage of decompressed variables
   std::vector<MatVar> vars;
+  bool h5 = false;  // a -v7.3 (HDF5) file: its variables are in h5vars
+  std::vector<mexct::Mat73Var> h5vars;
 };
 
 mexct_status load_mat(const char* path, MatFile& mf) {
   if (!path) return set_err(MEXCT_ERR_ARG, "mat: NULL path");
   if (!read_file(path, mf.raw)) return set_err(MEXCT_ERR_IO, "mat: cannot read %s", path);
   if (mf.raw.size() < 128) return set_err(MEXCT_ERR_IO, "mat: %s is not a MAT-file", path);
-  if (std::memcmp(mf.raw.data(), "MATLAB 7.3", 10) == 0)
-    return set_err(MEXCT_ERR_UNSUPPORTED, "mat: %s is a -v7.3 (HDF5) MAT-file", path);
+  if (std::memcmp(mf.raw.data(), "MATLAB 7.3", 10) == 0 || mexct::mat73_is_hdf5(mf.raw)) {
+    mf.h5 = true;
+    return mexct::mat73_list(mf.raw, path, mf.h5vars);
+  }
   const char e0 = (char)mf.raw[126], e1 = (char)mf.raw[127];
   bool swap;
   if (e0 == 'I' && e1 == 'M') swap = false;       // written little-endian
@@ -420,6 +580,26 @@ mexct_status find_var(const MatFile& mf, const char* path, const char* name, con
       if (v.name == name) {
         if (!v.numeric)
           return set_err(MEXCT_ERR_UNSUPPORTED, "mat: %s in %s is not a numeric array", name, path);
+        *out = &v;
+        return MEXCT_OK;
+      }
+    } else if (v.numeric) {
+      *out = &v;
+      return MEXCT_OK;
+    }
+  }
+  if (name && *name) return set_err(MEXCT_ERR_ARG, "mat: no variable %s in %s", name, path);
+  return set_err(MEXCT_ERR_ARG, "mat: no numeric variable in %s", path);
+}
+
+mexct_status find_var73(const MatFile& mf, const char* path, const char* name,
+                        const mexct::Mat73Var** out) {
+  for (const mexct::Mat73Var& v : mf.h5vars) {
+    if (name && *name) {
+      if (v.name == name) {
+        if (!v.numeric)
+          return set_err(MEXCT_ERR_UNSUPPORTED, "mat: %s in %s is not a numeric array (%s)", name,
+                         path, v.mclass.empty() ? "group" : v.mclass.c_str());
         *out = &v;
         return MEXCT_OK;
       }
@@ -494,6 +674,12 @@ mexct_status parse_vff(const std::vector<uint8_t>& f, const char* path, VffInfo&
 
 }  // namespace
 
+namespace mexct {
+bool zlib_inflate_bytes(const uint8_t* p, size_t n, std::vector<uint8_t>& out) {
+  return zlib_inflate(p, n, out);
+}
+}  // namespace mexct
+
 extern "C" {
 
 mexct_status mexct_mat_list(const char* path, char* names, size_t capacity) {
@@ -501,6 +687,10 @@ mexct_status mexct_mat_list(const char* path, char* names, size_t capacity) {
   if (mexct_status s = load_mat(path, mf)) return s;
   std::string all;
   for (const MatVar& v : mf.vars) {
+    if (!all.empty()) all += '\n';
+    all += v.name;
+  }
+  for (const mexct::Mat73Var& v : mf.h5vars) {
     if (!all.empty()) all += '\n';
     all += v.name;
   }
@@ -514,6 +704,14 @@ mexct_status mexct_mat_info(const char* path, const char* name, int* ndims, long
   if (!ndims || !dims) return set_err(MEXCT_ERR_ARG, "mat: NULL output");
   MatFile mf;
   if (mexct_status s = load_mat(path, mf)) return s;
+  if (mf.h5) {
+    const mexct::Mat73Var* v = nullptr;
+    if (mexct_status s = find_var73(mf, path, name, &v)) return s;
+    if (v->dims.size() > 8) return set_err(MEXCT_ERR_UNSUPPORTED, "mat: more than 8 dimensions");
+    *ndims = (int)v->dims.size();
+    for (size_t i = 0; i < v->dims.size(); ++i) dims[i] = v->dims[i];
+    return MEXCT_OK;
+  }
   const MatVar* v = nullptr;
   if (mexct_status s = find_var(mf, path, name, &v)) return s;
   if (v->dims.size() > 8) return set_err(MEXCT_ERR_UNSUPPORTED, "mat: more than 8 dimensions");
@@ -525,6 +723,11 @@ mexct_status mexct_mat_info(const char* path, const char* name, int* ndims, long
 mexct_status mexct_mat_read(const char* path, const char* name, float* out, long long count) {
   MatFile mf;
   if (mexct_status s = load_mat(path, mf)) return s;
+  if (mf.h5) {
+    const mexct::Mat73Var* v = nullptr;
+    if (mexct_status s = find_var73(mf, path, name, &v)) return s;
+    return mexct::mat73_read(mf.raw, path, *v, out, count);
+  }
   const MatVar* v = nullptr;
   if (mexct_status s = find_var(mf, path, name, &v)) return s;
   long long n = 1;

@@ -119,11 +119,11 @@ def test_writer_is_read_by_scipy(lib, tmp_path):
 def test_unsupported_and_missing(lib, tmp_path):
     from mexct import _lib, fileio
 
-    p = tmp_path / "h5.mat"
+    p = tmp_path / "h5.mat"  # a -v7.3 header with no HDF5 data behind it
     p.write_bytes(b"MATLAB 7.3 MAT-file, Platform: GLNXA64".ljust(512, b" "))
     with pytest.raises(_lib.MexctError) as ei:
         fileio.read_mat(p)
-    assert ei.value.status == _lib.ERR_UNSUPPORTED
+    assert ei.value.status == _lib.ERR_IO
     with pytest.raises(_lib.MexctError) as ei:
         fileio.read_mat(tmp_path / "absent.mat")
     assert ei.value.status == _lib.ERR_IO
