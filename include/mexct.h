@@ -320,9 +320,13 @@ mexct_status mexct_bp_ooc(mexct_ctx* ctx, const float* sino, int W, int H,
  * order): mexct_mat_list writes the variable names, '\n'-separated;
  * mexct_mat_info gives a variable's dimensions (name NULL or "": the first
  * numeric one); mexct_mat_read converts its real part (any numeric class) to
- * float32, count = the product of the dimensions.  -v7.3 (HDF5) files:
- * MEXCT_ERR_UNSUPPORTED.  mexct_mat_write writes one single-precision
- * variable, creating the file or (append != 0) adding to it.
+ * float32, count = the product of the dimensions.  -v7.3 files (HDF5, which
+ * MATLAB needs for arrays above 2 GB) are read by the same three calls: the
+ * root group's numeric and logical datasets (complex: the real part),
+ * contiguous, compact or chunked with deflate / shuffle / Fletcher-32; other
+ * HDF5 features give MEXCT_ERR_UNSUPPORTED.  mexct_mat_write writes one
+ * single-precision variable (Level 5), creating the file or (append != 0)
+ * adding to it.
  *
  * VFF ("ncaa" header, single-band raster slices, big-endian data; bits 8
  * unsigned, 16 signed, 32 float): mexct_vff_info gives the size X, Y, Z (Z = 1

@@ -1,4 +1,5 @@
-"""Scanner data files: MATLAB Level 5 MAT-files and VFF volumes (include/mexct.h,
+"""Scanner data files: MATLAB MAT-files (Level 5 read and written, -v7.3 / HDF5 read)
+and VFF volumes (include/mexct.h,
 "scanner data files").  Arrays come back as float32, column-major (Fortran order),
 the layout the MEX-style entry points take."""
 from __future__ import annotations
@@ -15,7 +16,8 @@ def _b(s):
 
 
 def mat_list(path) -> list[str]:
-    """Names of the variables in a MAT-file, in file order."""
+    """Names of the variables in a MAT-file: in file order (Level 5), in name order
+    (-v7.3)."""
     buf = ctypes.create_string_buffer(1 << 16)
     _lib.call("mexct_mat_list", _b(path), buf, len(buf))
     txt = buf.value.decode()
