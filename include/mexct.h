@@ -325,8 +325,8 @@ mexct_status mexct_bp_ooc(mexct_ctx* ctx, const float* sino, int W, int H,
  * root group's numeric and logical datasets (complex: the real part),
  * contiguous, compact or chunked with deflate / shuffle / Fletcher-32; other
  * HDF5 features give MEXCT_ERR_UNSUPPORTED.  mexct_mat_write writes one
- * single-precision variable (Level 5), creating the file or (append != 0)
- * adding to it.
+ * single-precision variable, creating the file or (append != 0) adding to it
+ * (see mexct_mat_write_ex for the format).
  *
  * VFF ("ncaa" header, single-band raster slices, big-endian data; bits 8
  * unsigned, 16 signed, 32 float): mexct_vff_info gives the size X, Y, Z (Z = 1
@@ -340,6 +340,18 @@ mexct_status mexct_mat_read(const char* path, const char* name, float* out,
 mexct_status mexct_mat_write(const char* path, const char* name,
                              const float* data, int ndims,
                              const long long* dims, int append);
+/* mexct_mat_write with the file format chosen: MEXCT_MAT_V5 (Level 5, at most
+ * 4 GiB per variable), MEXCT_MAT_V73 (-v7.3 / HDF5: a contiguous single
+ * dataset with MATLAB_class "single", as MATLAB writes it; appending relinks
+ * the root group at the end of the file) or MEXCT_MAT_AUTO (what
+ * mexct_mat_write does: the format of the file appended to, else -v7.3 for a
+ * variable of 2 GB or more, which MATLAB reads only from -v7.3). */
+#define MEXCT_MAT_AUTO 0
+#define MEXCT_MAT_V5 5
+#define MEXCT_MAT_V73 73
+mexct_status mexct_mat_write_ex(const char* path, const char* name,
+                                const float* data, int ndims,
+                                const long long* dims, int append, int format);
 mexct_status mexct_vff_info(const char* path, int* dims, float* spacing,
                             int* bits);
 mexct_status mexct_vff_read(const char* path, float* out, long long count);

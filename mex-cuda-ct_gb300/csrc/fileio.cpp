@@ -744,11 +744,47 @@ mexct_status mexct_mat_read(const char* path, const char* name, float* out, long
 
 mexct_status mexct_mat_write(const char* path, const char* name, const float* data, int ndims,
                              const long long* dims, int append) {
+  return mexct_mat_write_ex(path, name, data, ndims, dims, append, MEXCT_MAT_AUTO);
+}
+
+mexct_status mexct_mat_write_ex(const char* path, const char* name, const float* data, int ndims,
+                                const long long* dims, int append, int format) {
   if (!path || !name || !*name || !dims || ndims < 2 || ndims > 8)
     return set_err(MEXCT_ERR_ARG, "mat: bad arguments (name, 2..8 dims)");
+  if (format != MEXCT_MAT_AUTO && format != MEXCT_MAT_V5 && format != MEXCT_MAT_V73)
+    return set_err(MEXCT_ERR_ARG, "mat: unknown format %d", format);
+  unsigned long long total = 1;
+  for (int i = 0; i < ndims; ++i) {
+    if (dims[i] < 0) return set_err(MEXCT_ERR_ARG, "mat: bad dimension");
+    if (dims[i] != 0 && total > (1ull << 40) / (unsigned long long)dims[i])
+      return set_err(MEXCT_ERR_ARG, "mat: more than 2^40 elements");
+    total *= (unsigned long long)dims[i];
+  }
+  // the file being appended to decides; else -v7.3 where MATLAB needs it (a
+  // variable of 2 GB or more)
+  bool existing_h5 = false, existing = false;
+  if (append) {
+    FILE* g = std::fopen(path, "rb");
+    if (g) {
+      std::vector<uint8_t> head(1032);
+      head.resize(std::fread(head.data(), 1, head.size(), g));
+      std::fclose(g);
+      existing = head.size() >= 128;
+      existing_h5 = existing && (mexct::mat73_is_hdf5(head) ||
+                                 std::memcmp(head.data(), "MATLAB 7.3", 10) == 0);
+    }
+  }
+  int fmt = format;
+  if (fmt == MEXCT_MAT_AUTO)
+    fmt = existing ? (existing_h5 ? MEXCT_MAT_V73 : MEXCT_MAT_V5)
+                   : (4 * total >= (1ull << 31) ? MEXCT_MAT_V73 : MEXCT_MAT_V5);
+  if (existing && (fmt == MEXCT_MAT_V73) != existing_h5)
+    return set_err(MEXCT_ERR_ARG, "mat: %s is a %s file; cannot append a %s variable", path,
+                   existing_h5 ? "-v7.3" : "Level 5", fmt == MEXCT_MAT_V73 ? "-v7.3" : "Level 5");
+  if (fmt == MEXCT_MAT_V73) return mexct::mat73_write(path, name, data, ndims, dims, existing);
   long long n = 1;
   for (int i = 0; i < ndims; ++i) {
-    if (dims[i] < 0 || dims[i] > 0x7fffffffLL) return set_err(MEXCT_ERR_ARG, "mat: bad dimension");
+    if (dims[i] > 0x7fffffffLL) return set_err(MEXCT_ERR_ARG, "mat: bad dimension");
     n *= dims[i];
   }
   const size_t nl = std::strlen(name);

@@ -37,4 +37,10 @@ mexct_status mat73_list(const std::vector<uint8_t>& f, const char* path,
 mexct_status mat73_read(const std::vector<uint8_t>& f, const char* path, const Mat73Var& v,
                         float* out, long long count);
 
+// Writes one single-precision variable (dims in MATLAB order) as a -v7.3
+// MAT-file: a new file, or (append) one more variable of an existing one with
+// a version 0/1 superblock, its root group relinked at the end of the file.
+mexct_status mat73_write(const char* path, const char* name, const float* data, int ndims,
+                         const long long* dims, bool append);
+
 }  // namespace mexct

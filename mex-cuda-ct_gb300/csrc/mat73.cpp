@@ -23,10 +23,20 @@
 //    not verified);
 //  - attributes v1-v3, for MATLAB_class and MATLAB_empty.
 // A chunked dataset's chunks are decoded on several host threads.
+// Written (mat73_write): single-precision variables as MATLAB lays them out
+// (version 0 superblock, version 1 object headers, a symbol-table root group,
+// contiguous data with MATLAB_class "single"); appending relinks the root
+// group at the end of the file.
 // Every offset is checked against the file size, every walk is bounded: a
 // damaged file gives an error, not a crash.
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <atomic>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -63,6 +73,7 @@ const uint8_t kSignature[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
 class File {
  public:
   explicit File(const std::vector<uint8_t>& f) : p_(f.data()), n_(f.size()) {}
+  File(const uint8_t* p, uint64_t n) : p_(p), n_(n) {}
   uint64_t size() const { return n_; }
   const uint8_t* at(uint64_t off, uint64_t len) const {
     if (off > n_ || len > n_ - off) bad("a structure runs past the end of the file");
@@ -771,6 +782,242 @@ void read_all(File& h, const Dataset& D, float* out, uint64_t n) {
   if (failed) throw first;
 }
 
+// ---- writing -------------------------------------------------------------------
+
+// Bytes of the metadata written after a variable's data, with the absolute
+// file offset of its first byte (addresses are written relative to `base`).
+struct Blob {
+  std::vector<uint8_t> b;
+  uint64_t origin = 0, base = 0;
+  uint64_t here() const { return origin + b.size(); }
+  uint64_t rel() const { return here() - base; }
+  void align8() {
+    while (here() % 8) b.push_back(0);
+  }
+  void u(uint64_t v, int n) {
+    for (int i = 0; i < n; ++i) b.push_back((uint8_t)(v >> (8 * i)));
+  }
+  void raw(const void* p, size_t n) {
+    const uint8_t* q = static_cast<const uint8_t*>(p);
+    b.insert(b.end(), q, q + n);
+  }
+  void zeros(size_t n) { b.insert(b.end(), n, 0); }
+};
+
+constexpr uint64_t kUndef = ~0ull;
+
+// One object header message (version 1 header): type, size, flags, reserved,
+// data padded to 8 bytes.
+void message(std::vector<uint8_t>& out, uint32_t type, const std::vector<uint8_t>& data) {
+  const size_t n = (data.size() + 7) / 8 * 8;
+  Blob m;
+  m.u(type, 2);
+  m.u(n, 2);
+  m.u(0, 4);
+  m.raw(data.data(), data.size());
+  m.zeros(n - data.size());
+  out.insert(out.end(), m.b.begin(), m.b.end());
+}
+
+void object_header(Blob& out, const std::vector<std::pair<uint32_t, std::vector<uint8_t>>>& msgs) {
+  std::vector<uint8_t> body;
+  for (const auto& m : msgs) message(body, m.first, m.second);
+  out.u(1, 1);  // version
+  out.u(0, 1);
+  out.u(msgs.size(), 2);
+  out.u(1, 4);  // reference count
+  out.u(body.size(), 4);
+  out.u(0, 4);  // padding to 8 bytes
+  out.raw(body.data(), body.size());
+}
+
+// MATLAB_class (or another attribute) with a string or a scalar uint8 value.
+std::vector<uint8_t> attr_msg(const char* name, const std::string* str, int u8value) {
+  Blob a, dt, ds;
+  if (str) {
+    dt.u(0x13, 1);  // string, version 1; null-terminated ASCII
+    dt.u(0, 3);
+    dt.u(str->size(), 4);
+  } else {
+    dt.u(0x10, 1);  // fixed-point, version 1, little-endian unsigned
+    dt.u(0, 3);
+    dt.u(1, 4);
+    dt.u(0, 2);
+    dt.u(8, 2);
+  }
+  ds.u(1, 1);  // scalar dataspace, version 1
+  ds.zeros(7);
+  const size_t nl = std::strlen(name) + 1;
+  a.u(1, 1);
+  a.u(0, 1);
+  a.u(nl, 2);
+  a.u(dt.b.size(), 2);
+  a.u(ds.b.size(), 2);
+  a.raw(name, nl);
+  a.zeros((8 - nl % 8) % 8);
+  a.raw(dt.b.data(), dt.b.size());
+  a.zeros((8 - dt.b.size() % 8) % 8);
+  a.raw(ds.b.data(), ds.b.size());
+  if (str) a.raw(str->data(), str->size());
+  else a.u((uint64_t)u8value, 1);
+  return a.b;
+}
+
+// The object header of a single-precision variable whose data sit at `data`
+// (relative address), dims in the file's order (MATLAB's reversed).  An empty
+// array stores its MATLAB dimensions as uint64 data with MATLAB_empty.
+void dataset_header(Blob& out, const std::vector<uint64_t>& fdims, uint64_t data, uint64_t bytes,
+                    bool empty) {
+  Blob sp, ty, fill, lay;
+  sp.u(1, 1);
+  sp.u(fdims.size(), 1);
+  sp.u(1, 1);  // maximum dimensions present
+  sp.zeros(5);
+  for (uint64_t d : fdims) sp.u(d, 8);
+  for (uint64_t d : fdims) sp.u(d, 8);
+  if (empty) {
+    ty.u(0x10, 1);  // uint64, little-endian
+    ty.u(0, 3);
+    ty.u(8, 4);
+    ty.u(0, 2);
+    ty.u(64, 2);
+  } else {
+    ty.u(0x11, 1);  // IEEE float32, little-endian
+    ty.u(0x20, 1);
+    ty.u(31, 1);
+    ty.u(0, 1);
+    ty.u(4, 4);
+    ty.u(0, 2);    // bit offset
+    ty.u(32, 2);   // precision
+    ty.u(23, 1);   // exponent location
+    ty.u(8, 1);    // exponent size
+    ty.u(0, 1);    // mantissa location
+    ty.u(23, 1);   // mantissa size
+    ty.u(127, 4);  // exponent bias
+  }
+  fill.u(2, 1);  // fill value message v2: allocated early, never written, undefined
+  fill.u(1, 1);
+  fill.u(2, 1);
+  fill.u(0, 1);
+  lay.u(3, 1);  // layout v3, contiguous
+  lay.u(1, 1);
+  lay.u(data, 8);
+  lay.u(bytes, 8);
+  const std::string single = "single";
+  std::vector<std::pair<uint32_t, std::vector<uint8_t>>> msgs = {
+      {0x01, sp.b}, {0x03, ty.b}, {0x05, fill.b}, {0x08, lay.b},
+      {0x0C, attr_msg("MATLAB_class", &single, 0)}};
+  if (empty) msgs.push_back({0x0C, attr_msg("MATLAB_empty", nullptr, 1)});
+  object_header(out, msgs);
+}
+
+// A root group holding `links` (sorted by name): local heap, symbol table
+// nodes of up to 2 leafK entries, one B-tree node of up to 2 intK children,
+// and the group's object header.  Returns the relative addresses of the
+// header, the B-tree and the heap.
+struct RootAddrs {
+  uint64_t header, btree, heap;
+};
+
+RootAddrs write_root(Blob& out, const std::vector<Link>& links, uint32_t leafK, uint32_t intK) {
+  // heap data: "" at 0, then the names, each null-terminated to 8 bytes
+  std::vector<uint64_t> name_off;
+  Blob heapdata;
+  heapdata.zeros(8);
+  for (const Link& l : links) {
+    name_off.push_back(heapdata.b.size());
+    heapdata.raw(l.name.data(), l.name.size());
+    heapdata.zeros(8 - l.name.size() % 8);
+  }
+  out.align8();
+  const uint64_t hdata = out.rel();
+  out.raw(heapdata.b.data(), heapdata.b.size());
+  out.align8();
+  const uint64_t heap = out.rel();
+  out.raw("HEAP", 4);
+  out.u(0, 4);  // version 0, reserved
+  out.u(heapdata.b.size(), 8);
+  out.u(1, 8);  // no free block: the value the HDF5 library writes and accepts for it
+  out.u(hdata, 8);
+  // symbol table nodes
+  const size_t per = 2 * (size_t)leafK;
+  std::vector<uint64_t> snods, last;
+  for (size_t i = 0; i < links.size(); i += per) {  // links: at least the new variable
+    const size_t n = std::min(per, links.size() - i);
+    out.align8();
+    snods.push_back(out.rel());
+    out.raw("SNOD", 4);
+    out.u(1, 1);
+    out.u(0, 1);
+    out.u(n, 2);
+    for (size_t k = 0; k < per; ++k) {
+      if (k < n) {
+        out.u(name_off[i + k], 8);
+        out.u(links[i + k].header, 8);
+      } else {
+        out.zeros(16);
+      }
+      out.zeros(24);  // cache type 0, reserved, scratch pad
+    }
+    last.push_back(name_off[i + n - 1]);
+  }
+  // one B-tree node (group nodes, level 0), allocated at full size
+  out.align8();
+  const uint64_t tree = out.rel();
+  out.raw("TREE", 4);
+  out.u(0, 1);
+  out.u(0, 1);
+  out.u(snods.size(), 2);
+  out.u(kUndef, 8);
+  out.u(kUndef, 8);
+  out.u(0, 8);  // key 0: the empty name
+  for (size_t i = 0; i < 2 * (size_t)intK; ++i) {
+    if (i < snods.size()) {
+      out.u(snods[i], 8);
+      out.u(last[i], 8);
+    } else {
+      out.zeros(16);
+    }
+  }
+  // the root group's object header: its symbol table
+  out.align8();
+  const uint64_t header = out.rel();
+  Blob st;
+  st.u(tree, 8);
+  st.u(heap, 8);
+  object_header(out, {{0x11, st.b}});
+  return {header, tree, heap};
+}
+
+bool write_all(FILE* f, const void* p, size_t n) {
+  return n == 0 || std::fwrite(p, 1, n, f) == n;
+}
+
+// Read-only mapping of a whole file.
+struct Mapped {
+  const uint8_t* p = nullptr;
+  size_t n = 0;
+  ~Mapped() {
+    if (p) munmap(const_cast<uint8_t*>(p), n);
+  }
+  bool open(const char* path) {
+    const int fd = ::open(path, O_RDONLY);
+    if (fd < 0) return false;
+    struct stat st;
+    bool ok = fstat(fd, &st) == 0 && st.st_size > 0;
+    if (ok) {
+      void* m = mmap(nullptr, (size_t)st.st_size, PROT_READ, MAP_PRIVATE, fd, 0);
+      ok = m != MAP_FAILED;
+      if (ok) {
+        p = static_cast<const uint8_t*>(m);
+        n = (size_t)st.st_size;
+      }
+    }
+    ::close(fd);
+    return ok;
+  }
+};
+
 Mat73Var describe(File& h, const Link& l) {
   Mat73Var v;
   v.name = l.name;
@@ -844,6 +1091,147 @@ mexct_status mat73_read(const std::vector<uint8_t>& f, const char* path, const M
     if (!out) return set_err(MEXCT_ERR_ARG, "mat: NULL output");
     read_all(h, D, out, n);
     return MEXCT_OK;
+  } catch (const Bad& b) {
+    return fail(path, b);
+  } catch (const std::bad_alloc&) {
+    return set_err(MEXCT_ERR_OOM, "mat: %s: out of host memory", path);
+  }
+}
+
+mexct_status mat73_write(const char* path, const char* name, const float* data, int ndims,
+                         const long long* dims, bool append) {
+  const size_t nl = std::strlen(name);
+  if (nl == 0 || nl > 63) return set_err(MEXCT_ERR_ARG, "mat: a name of 1 to 63 characters");
+  uint64_t n = 1;
+  std::vector<uint64_t> fdims;  // the file's order: MATLAB's reversed
+  for (int i = ndims - 1; i >= 0; --i) {
+    if (dims[i] < 0) return set_err(MEXCT_ERR_ARG, "mat: a negative dimension");
+    fdims.push_back((uint64_t)dims[i]);
+    if (dims[i] != 0 && n > (1ull << 40) / (uint64_t)dims[i])
+      return set_err(MEXCT_ERR_ARG, "mat: more than 2^40 elements");
+    n *= (uint64_t)dims[i];
+  }
+  if (n > 0 && !data) return set_err(MEXCT_ERR_ARG, "mat: NULL data");
+  const bool empty = n == 0;
+  try {
+    std::vector<Link> links;
+    uint64_t sb = 512, end = 0;
+    int sbver = 0;
+    uint32_t leafK = 4, intK = 16;
+    if (append) {
+      Mapped m;
+      if (!m.open(path)) return set_err(MEXCT_ERR_IO, "mat: cannot read %s", path);
+      File h(m.p, m.n);
+      uint64_t s = 0;
+      if (!find_superblock(h, &s)) bad("no HDF5 superblock");
+      sbver = (int)h.u8(s + 8);
+      if (sbver > 1) unsupported("appending to a file with a version 2 or 3 superblock");
+      if (h.u8(s + 13) != 8 || h.u8(s + 14) != 8)
+        unsupported("appending to a file whose offsets or lengths are not 8 bytes");
+      leafK = h.u16(s + 16);
+      intK = h.u16(s + 18);
+      if (leafK < 1 || intK < 1) bad("a zero B-tree K in the superblock");
+      const Root r = superblock(h);
+      links = root_links(h, r);
+      for (Link& l : links) {
+        if (l.name == name)
+          return set_err(MEXCT_ERR_ARG, "mat: %s already holds a variable %s", path, name);
+        l.header -= s;  // back to a relative address
+      }
+      sb = s;
+      end = m.n;
+    }
+    const size_t cap = 2 * (size_t)leafK * 2 * (size_t)intK;
+    if (links.size() + 1 > cap)
+      unsupported("a root group of more variables than one B-tree node holds");
+    FILE* f = std::fopen(path, append ? "r+b" : "wb");
+    if (!f) return set_err(MEXCT_ERR_IO, "mat: cannot write %s", path);
+    bool ok = true;
+    if (!append) {  // MATLAB's user block, then room for the superblock
+      char ub[512];
+      std::memset(ub, 0, sizeof ub);
+      std::memset(ub, ' ', 116);
+      const char* txt = "MATLAB 7.3 MAT-file, written by mexct-gb300, HDF5 schema 1.00 .";
+      std::memcpy(ub, txt, std::strlen(txt));
+      ub[124] = 0x00;  // version 0x0200, little-endian
+      ub[125] = 0x02;
+      ub[126] = 'I';
+      ub[127] = 'M';
+      const uint8_t zero[96] = {};
+      ok = write_all(f, ub, sizeof ub) && write_all(f, zero, sizeof zero);
+      end = 512 + 96;
+    } else {
+      ok = std::fseek(f, 0, SEEK_END) == 0;
+    }
+    // the variable's data (8-byte aligned), then its header and the new root
+    const uint64_t pad = (8 - end % 8) % 8;
+    const uint8_t zeros[8] = {};
+    ok = ok && write_all(f, zeros, pad);
+    const uint64_t data_at = end + pad;
+    uint64_t bytes;
+    if (empty) {
+      std::vector<uint64_t> md;
+      for (int i = 0; i < ndims; ++i) md.push_back((uint64_t)dims[i]);
+      bytes = 8 * md.size();
+      ok = ok && write_all(f, md.data(), bytes);  // little-endian host
+    } else {
+      bytes = 4 * n;
+      ok = ok && write_all(f, data, bytes);
+    }
+    Blob meta;
+    meta.origin = data_at + bytes;
+    meta.base = sb;
+    meta.align8();
+    const uint64_t vh = meta.rel();
+    dataset_header(meta, empty ? std::vector<uint64_t>{(uint64_t)ndims} : fdims, data_at - sb,
+                   bytes, empty);
+    links.push_back({name, vh});
+    std::sort(links.begin(), links.end(),
+              [](const Link& a, const Link& b) { return a.name < b.name; });
+    const RootAddrs ra = write_root(meta, links, leafK, intK);
+    ok = ok && write_all(f, meta.b.data(), meta.b.size());
+    const uint64_t eof = meta.here() - sb;
+    // superblock: new file, or the changed fields of the old one
+    Blob sup;
+    if (!append) {
+      sup.raw(kSignature, 8);
+      sup.u(0, 1);  // superblock, free-space, root entry, reserved, shared header versions
+      sup.u(0, 1);
+      sup.u(0, 1);
+      sup.u(0, 1);
+      sup.u(0, 1);
+      sup.u(8, 1);  // sizes of offsets and lengths
+      sup.u(8, 1);
+      sup.u(0, 1);
+      sup.u(leafK, 2);
+      sup.u(intK, 2);
+      sup.u(0, 4);  // consistency flags
+      sup.u(0, 8);  // base address
+      sup.u(kUndef, 8);
+      sup.u(eof, 8);
+      sup.u(kUndef, 8);
+      sup.u(0, 8);  // root entry: name offset, header, cache type 1, reserved, scratch
+      sup.u(ra.header, 8);
+      sup.u(1, 4);
+      sup.u(0, 4);
+      sup.u(ra.btree, 8);
+      sup.u(ra.heap, 8);
+      ok = ok && std::fseek(f, (long)sb, SEEK_SET) == 0 && write_all(f, sup.b.data(), sup.b.size());
+    } else {
+      const uint64_t e0 = sb + (sbver == 1 ? 28 : 24);  // base address field
+      Blob eofb, root;
+      eofb.u(eof, 8);
+      root.u(ra.header, 8);
+      root.u(1, 4);
+      root.u(0, 4);
+      root.u(ra.btree, 8);
+      root.u(ra.heap, 8);
+      ok = ok && std::fseek(f, (long)(e0 + 16), SEEK_SET) == 0 && write_all(f, eofb.b.data(), 8);
+      ok = ok && std::fseek(f, (long)(e0 + 32 + 8), SEEK_SET) == 0 &&
+           write_all(f, root.b.data(), root.b.size());
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? MEXCT_OK : set_err(MEXCT_ERR_IO, "mat: writing %s failed", path);
   } catch (const Bad& b) {
     return fail(path, b);
   } catch (const std::bad_alloc&) {

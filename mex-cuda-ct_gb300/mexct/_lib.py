@@ -85,6 +85,7 @@ SIGNATURES = {
     "mexct_mat_info": [_c.c_char_p, _c.c_char_p, _c.POINTER(_i), _c.POINTER(_c.c_longlong)],
     "mexct_mat_read": [_c.c_char_p, _c.c_char_p, _P, _c.c_longlong],
     "mexct_mat_write": [_c.c_char_p, _c.c_char_p, _P, _i, _c.POINTER(_c.c_longlong), _i],
+    "mexct_mat_write_ex": [_c.c_char_p, _c.c_char_p, _P, _i, _c.POINTER(_c.c_longlong), _i, _i],
     "mexct_vff_info": [_c.c_char_p, _c.POINTER(_i), _F, _c.POINTER(_i)],
     "mexct_vff_read": [_c.c_char_p, _P, _c.c_longlong],
     "mexct_vff_write": [_c.c_char_p, _P, _c.POINTER(_i), _F, _i],

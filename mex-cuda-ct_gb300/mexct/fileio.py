@@ -36,14 +36,19 @@ def read_mat(path, name=None) -> np.ndarray:
     return out
 
 
-def write_mat(path, name, arr, append=False) -> None:
-    """Write arr as a single-precision variable (at least 2 dimensions, as MATLAB has)."""
+FORMATS = {None: 0, "auto": 0, "v5": 5, "v7.3": 73}
+
+
+def write_mat(path, name, arr, append=False, format=None) -> None:
+    """Write arr as a single-precision variable (at least 2 dimensions, as MATLAB has).
+    format: "v5" (Level 5), "v7.3" (HDF5) or None (the appended file's format, else
+    -v7.3 for 2 GB or more)."""
     a = np.asfortranarray(np.asarray(arr, dtype=np.float32))
     if a.ndim < 2:
         a = a.reshape((1, -1) if a.ndim == 1 else (1, 1), order="F")
     dims = (ctypes.c_longlong * a.ndim)(*a.shape)
-    _lib.call("mexct_mat_write", _b(path), _b(name), ctypes.c_void_p(a.ctypes.data), a.ndim, dims,
-              1 if append else 0)
+    _lib.call("mexct_mat_write_ex", _b(path), _b(name), ctypes.c_void_p(a.ctypes.data), a.ndim,
+              dims, 1 if append else 0, FORMATS[format])
 
 
 def read_vff(path):

@@ -312,7 +312,7 @@ class Mat73Writer:
             offs.append(len(data))
             data += _pad8(n.encode() + b"\0")
         dseg = self._put(bytes(data))
-        return self._put(b"HEAP" + struct.pack("<B3x", 0) + _q(len(data), UNDEF, dseg)), offs
+        return self._put(b"HEAP" + struct.pack("<B3x", 0) + _q(len(data), 1, dseg)), offs
 
     def save(self, path, dense: bool = False):
         links = sorted(self.links)

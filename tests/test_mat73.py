@@ -204,3 +204,68 @@ def test_damaged_files_fail_cleanly(lib, tmp_path):
             assert e.status in (_lib.ERR_IO, _lib.ERR_UNSUPPORTED, _lib.ERR_ARG)
             outcomes["error"] += 1
     assert outcomes["error"] > 0
+
+
+def test_v73_writer_roundtrip_and_appends(lib, tmp_path):
+    """-v7.3 files written here: MATLAB's header and superblock position; 40
+    appended variables (the root group over several symbol table nodes), an
+    empty array, all read back; the Level 5 default is unchanged."""
+    from mexct import _lib, fileio
+
+    rng = np.random.default_rng(6)
+    p = tmp_path / "w73.mat"
+    a = rng.standard_normal((17, 9, 5)).astype(F)
+    fileio.write_mat(p, "recon", a, format="v7.3")
+    raw = p.read_bytes()
+    assert raw.startswith(b"MATLAB 7.3 MAT-file") and raw[512:520] == b"\x89HDF\r\n\x1a\n"
+    assert fileio.mat_list(p) == ["recon"]
+    np.testing.assert_array_equal(fileio.read_mat(p, "recon"), a)
+    names = ["v%02d" % i for i in range(40)]
+    for i, n in enumerate(names):
+        fileio.write_mat(p, n, np.full((3, i + 1), i, F), append=True)  # the file's format
+    fileio.write_mat(p, "empty", np.zeros((0, 4), F), append=True)
+    assert fileio.mat_list(p) == sorted(["recon", "empty"] + names)
+    for i, n in enumerate(names):
+        np.testing.assert_array_equal(fileio.read_mat(p, n), np.full((3, i + 1), i, F))
+    np.testing.assert_array_equal(fileio.read_mat(p, "recon"), a)
+    assert fileio.read_mat(p, "empty").shape == (0, 4)
+    with pytest.raises(_lib.MexctError) as ei:
+        fileio.write_mat(p, "recon", a, append=True)  # the name is taken
+    assert ei.value.status == _lib.ERR_ARG
+    with pytest.raises(_lib.MexctError) as ei:
+        fileio.write_mat(p, "x", a, append=True, format="v5")  # not into an HDF5 file
+    assert ei.value.status == _lib.ERR_ARG
+    q = tmp_path / "v5.mat"
+    fileio.write_mat(q, "x", a)
+    assert q.read_bytes().startswith(b"MATLAB 5.0 MAT-file")
+
+
+def test_append_to_a_matlab_layout_file(lib, tmp_path):
+    """A variable appended to a file in MATLAB's layout (its structs and #refs#
+    kept); files with a newer superblock are refused for appending."""
+    from mexct import _lib, fileio
+
+    rng = np.random.default_rng(7)
+    d = rng.standard_normal((6, 4))
+    w = Mat73Writer()
+    w.add("data", d)
+    w.add("vol", rng.standard_normal((8, 8, 3)).astype(F), layout="chunked", chunks=[2, 4, 4],
+          filters=(SHUFFLE, DEFLATE))
+    w.add_group("meta")
+    w.add_group("#refs#", mclass=None)
+    p = tmp_path / "ml.mat"
+    w.save(p)
+    vol = fileio.read_mat(p, "vol")
+    b = rng.standard_normal((5, 5)).astype(F)
+    fileio.write_mat(p, "added", b, append=True)
+    assert fileio.mat_list(p) == ["added", "data", "meta", "vol"]
+    np.testing.assert_array_equal(fileio.read_mat(p, "data"), d.astype(F))
+    np.testing.assert_array_equal(fileio.read_mat(p, "vol"), vol)
+    np.testing.assert_array_equal(fileio.read_mat(p, "added"), b)
+    w2 = Mat73Writer(new_style=True)
+    w2.add("x", np.ones((2, 2), F))
+    r = tmp_path / "new.mat"
+    w2.save(r)
+    with pytest.raises(_lib.MexctError) as ei:
+        fileio.write_mat(r, "y", b, append=True)
+    assert ei.value.status == _lib.ERR_UNSUPPORTED
