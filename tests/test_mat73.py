@@ -1,4 +1,5 @@
-"""MATLAB -v7.3 MAT-files (HDF5) through mexct_mat_list / _info / _read (CPU only).
+"""MATLAB -v7.3 MAT-files (HDF5) through mexct_mat_list / _info / _read and
+mexct_mat_write_ex (CPU only).
 
 The files come from tests/mat73_writer.py, a writer of the HDF5 structures that
 MATLAB's save -v7.3 produces (version 0 superblock behind the 512-byte user
@@ -10,7 +11,8 @@ ragged edge chunks, one- and two-level chunk B-trees, deflate / shuffle /
 Fletcher-32 filters and a per-chunk filter mask, a version 4 single-chunk
 layout, header continuation blocks, empty arrays (MATLAB_empty), groups
 (structs) and MATLAB's #refs#, and damaged files (an error status, never a
-crash).
+crash).  Written here: -v7.3 files read back, appends (to the library's own
+files and to files in MATLAB's layout), and the format rules.
 """
 import numpy as np
 import pytest
