@@ -597,6 +597,9 @@ mexct_status find_var73(const MatFile& mf, const char* path, const char* name,
   for (const mexct::Mat73Var& v : mf.h5vars) {
     if (name && *name) {
       if (v.name == name) {
+        if (v.unsupported)
+          return set_err(MEXCT_ERR_UNSUPPORTED, "mat: %s in %s (-v7.3 / HDF5): %s", name, path,
+                         v.unsupported);
         if (!v.numeric)
           return set_err(MEXCT_ERR_UNSUPPORTED, "mat: %s in %s is not a numeric array (%s)", name,
                          path, v.mclass.empty() ? "group" : v.mclass.c_str());

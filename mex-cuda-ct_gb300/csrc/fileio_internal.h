@@ -21,6 +21,7 @@ struct Mat73Var {
   bool numeric = false;         // a numeric or logical array this reader converts
   std::vector<long long> dims;  // MATLAB order (the HDF5 dimensions reversed)
   uint64_t header = 0;          // file offset of the dataset's object header
+  const char* unsupported = nullptr;  // an HDF5 feature of it that is not read, if any
 };
 
 // True when the file holds an HDF5 superblock where MATLAB puts it (after a

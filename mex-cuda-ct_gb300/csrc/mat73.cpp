@@ -1022,7 +1022,14 @@ Mat73Var describe(File& h, const Link& l) {
   Mat73Var v;
   v.name = l.name;
   v.header = l.header;
-  const Dataset D = dataset(h, l.header);
+  Dataset D;
+  try {
+    D = dataset(h, l.header);
+  } catch (const Bad& b) {
+    if (!b.unsupported) throw;
+    v.unsupported = b.what;  // listed; reading it reports why (the others stay readable)
+    return v;
+  }
   v.mclass = D.mclass;
   if (!D.is_dataset) return v;  // a group: struct, cell or sparse array
   v.numeric = D.have_type && D.have_layout && !D.null_space &&

@@ -169,6 +169,33 @@ def test_dense_groups_and_missing_superblock_are_reported(lib, tmp_path):
     assert "no HDF5 superblock" in _lib.last_error()
 
 
+def test_unsupported_variable_leaves_the_others_readable(lib, tmp_path):
+    """A variable stored with an HDF5 feature the reader does not follow (here a
+    version 4 chunk index other than a single chunk) is listed and reports why;
+    the file's other variables read as usual."""
+    from mexct import _lib, fileio
+
+    a = np.arange(12, dtype=F).reshape(3, 4)
+    w = Mat73Writer(new_style=True)
+    w.add("good", a)
+    w.add("odd", a, layout="single")
+    p = tmp_path / "odd.mat"
+    w.save(p)
+    raw = bytearray(p.read_bytes())
+    # the single-chunk layout message: version 4, class 2, flags, 3 dims of 4 bytes,
+    # then the index type (1) -> 3 (fixed array)
+    i = raw.index(bytes([4, 2, 0, 3, 4]))
+    assert raw[i + 5 + 12] == 1
+    raw[i + 5 + 12] = 3
+    p.write_bytes(bytes(raw))
+    assert fileio.mat_list(p) == ["good", "odd"]
+    np.testing.assert_array_equal(fileio.read_mat(p, "good"), a)
+    with pytest.raises(_lib.MexctError) as ei:
+        fileio.read_mat(p, "odd")
+    assert ei.value.status == _lib.ERR_UNSUPPORTED
+    assert "chunk index" in _lib.last_error()
+
+
 def test_damaged_files_fail_cleanly(lib, tmp_path):
     """Truncations and seeded byte corruptions of a chunked, deflated file give
     a status (an error, or data when the damage misses every structure read),
