@@ -741,7 +741,18 @@ mexct_status mexct_mat_read(const char* path, const char* name, float* out, long
   if (count != n) return set_err(MEXCT_ERR_ARG, "mat: %s holds %lld elements, not %lld",
                                  v->name.c_str(), n, count);
   if (n > 0 && !out) return set_err(MEXCT_ERR_ARG, "mat: NULL output");
-  for (long long i = 0; i < n; ++i) out[i] = (float)mi_value(v->real.data + i * es, v->real.type, v->swap);
+  const uint8_t* src = v->real.data;
+  if (v->real.type == miSINGLE && !v->swap) {  // the common cases in bulk
+    std::memcpy(out, src, 4 * (size_t)n);
+  } else if (v->real.type == miDOUBLE && !v->swap) {
+    for (long long i = 0; i < n; ++i) {
+      double d;
+      std::memcpy(&d, src + 8 * i, 8);
+      out[i] = (float)d;
+    }
+  } else {
+    for (long long i = 0; i < n; ++i) out[i] = (float)mi_value(src + i * es, v->real.type, v->swap);
+  }
   return MEXCT_OK;
 }
 
@@ -810,22 +821,13 @@ mexct_status mexct_mat_write_ex(const char* path, const char* name, const float*
   pad8(body);
   put_u32(body, miSINGLE);
   put_u32(body, (uint32_t)(4 * n));
-  const size_t at = body.size();
-  body.resize(at + 4 * (size_t)n);
-  if (n > 0) std::memcpy(body.data() + at, data, 4 * (size_t)n);  // little-endian file
-  pad8(body);
+  // the data follow body straight from the caller's array (a little-endian file)
+  const size_t tail = (8 - (4 * (size_t)n) % 8) % 8;
   std::vector<uint8_t> elem;
   put_u32(elem, miMATRIX);
-  put_u32(elem, (uint32_t)body.size());
-  FILE* f = nullptr;
-  bool header = true;
-  if (append) {
-    std::vector<uint8_t> old;
-    if (read_file(path, old) && old.size() >= 128) header = false;
-    f = std::fopen(path, header ? "wb" : "ab");
-  } else {
-    f = std::fopen(path, "wb");
-  }
+  put_u32(elem, (uint32_t)(body.size() + 4 * (size_t)n + tail));
+  const bool header = !existing;  // a new file (or one too short to hold a header)
+  FILE* f = std::fopen(path, header ? "wb" : "ab");
   if (!f) return set_err(MEXCT_ERR_IO, "mat: cannot write %s", path);
   bool ok = true;
   if (header) {
@@ -840,8 +842,11 @@ mexct_status mexct_mat_write_ex(const char* path, const char* name, const float*
     h[127] = 'M';
     ok = std::fwrite(h, 1, 128, f) == 128;
   }
+  const uint8_t zeros[8] = {};
   ok = ok && std::fwrite(elem.data(), 1, elem.size(), f) == elem.size();
   ok = ok && std::fwrite(body.data(), 1, body.size(), f) == body.size();
+  ok = ok && (n == 0 || std::fwrite(data, 4, (size_t)n, f) == (size_t)n);
+  ok = ok && std::fwrite(zeros, 1, tail, f) == tail;
   ok = (std::fclose(f) == 0) && ok;
   return ok ? MEXCT_OK : set_err(MEXCT_ERR_IO, "mat: writing %s failed", path);
 }
