@@ -140,6 +140,17 @@ mexct_status mexct_prefilter(mexct_ctx* ctx, const float* sino,
                              const float* angles, int geom, float sad,
                              int filter, float cutoff, float q, float* out);
 
+/* weightedSino = parker_weight(sino, angles, geom, q)
+ * Replaces fbp_reconstruction/parker_weight.m:1-79 (its printed notes left
+ * out): the (modified) Parker window per view and row element u of a W x W
+ * detector, computed in FP64 from MATLAB's double SAD and q, rounded to
+ * single and multiplied into the single sinogram as the reference does.
+ * Host only (no GPU).  W != H: MEXCT_ERR_UNSUPPORTED (the reference's repmat
+ * needs a square detector). */
+mexct_status mexct_parker_weight(const float* sino, int W, int H, int nP,
+                                 const float* angles, int geom, double sad,
+                                 double q, float* out);
+
 /* recon = FBP_recon(pre, post, angles, geom, filter, cutoff, q)
  * Replaces fbp_reconstruction/FBP_recon.m:1-41 on the device: log
  * transform, pre-filter and BP with no host round trip. */

@@ -762,6 +762,41 @@ mexct_status prefilter_tables(mexct_ctx* c, int W, int H, int nP, const float* a
                               float sad, int filter, float cutoff, float q, int order,
                               cudaStream_t st);
 
+// The (modified) Parker window of parker_weight.m:29-72 per view i and row
+// element u of a W x W detector, in FP64, stored as single as the reference
+// does (:72): fan / cone angle alpha_u = atan((u - W/2 + 1/2) / SAD) (0 for
+// parallel rays, :29-32), negated when the angles increase (:36-39); delta
+// half the fan angle, epsilon the overscan beyond pi + 2 delta (:42-59); the
+// window is the Wesarg et al. sum of four S terms of b = q (2 delta - 2 alpha
+// + epsilon) (:64-70, :81-99).
+void parker_table(int W, int nP, const float* angles, int geom, double sad, double q,
+                  float* out) {
+  const double pi = 3.14159265358979323846;
+  std::vector<double> alpha(W, 0.0);
+  if (geom != 0)
+    for (int j = 0; j < W; ++j) alpha[j] = std::atan((-W / 2.0 + 0.5 + j) / sad);
+  bool incr = true;
+  for (int i = 1; i < nP; ++i)
+    if (!(angles[i] - angles[i - 1] >= 0)) incr = false;
+  if (incr)
+    for (double& a : alpha) a = -a;
+  const double delta = std::fabs(alpha[W - 1] - alpha[0]) / 2;
+  const double extent = nP > 0 ? std::fabs((double)(angles[nP - 1] - angles[0])) : 0.0;
+  const double eps = std::max(extent - (pi + 2 * delta), 0.0);
+  auto b2 = [&](double a) { return q * (2 * delta - 2 * a + eps); };
+  for (int i = 0; i < nP; ++i) {
+    const double beta = std::fabs((double)(angles[i] - angles[0]));
+    for (int j = 0; j < W; ++j) {
+      const double a = alpha[j];
+      out[(size_t)i * W + j] = (float)(
+          0.5 * (s_window(beta / b2(a) - 0.5) +
+                 s_window((beta - 2 * delta + 2 * a - eps) / b2(a) + 0.5) -
+                 s_window((beta - pi + 2 * a) / b2(-a) - 0.5) -
+                 s_window((beta - pi - 2 * delta - eps) / b2(-a) + 0.5)));
+    }
+  }
+}
+
 mexct_status prefilter_dev_impl(mexct_ctx* c, const float* d_sino,
                                 const float* d_pre, int W, int H, int nP,
                                 const float* angles, int geom, float sad,
@@ -823,34 +858,14 @@ mexct_status prefilter_tables(mexct_ctx* c, int W, int H, int nP, const float* a
     c->filt_cut = cutoff;
   }
   // Parker window per (view, row element) and dbeta/2 per view.
-  std::vector<double> alpha(H, 0.0);
-  if (geom != 0)
-    for (int j = 0; j < H; ++j) alpha[j] = std::atan((-H / 2.0 + 0.5 + j) / (double)sad);
-  bool incr = true;
-  for (int i = 1; i < nP; ++i)
-    if (!(angles[i] - angles[i - 1] >= 0)) incr = false;
-  if (incr)
-    for (double& a : alpha) a = -a;
-  const double delta = std::fabs(alpha[H - 1] - alpha[0]) / 2;
-  const double extent = std::fabs((double)(angles[nP - 1] - angles[0]));
-  const double eps = std::max(extent - (pi + 2 * delta), 0.0);
-  auto b2 = [&](double a) { return (double)q * (2 * delta - 2 * a + eps); };
+  (void)pi;
   std::vector<float> tab((size_t)order + (size_t)nP * W + nP);
   std::memcpy(tab.data(), c->filt_kern.data(), sizeof(float) * order);
   float* parker = tab.data() + order;
   float* dbeta = parker + (size_t)nP * W;
-  for (int i = 0; i < nP; ++i) {
-    const double beta = std::fabs((double)(angles[i] - angles[0]));
-    for (int j = 0; j < W; ++j) {
-      const double a = alpha[j];
-      parker[(size_t)i * W + j] = (float)(
-          0.5 * (s_window(beta / b2(a) - 0.5) +
-                 s_window((beta - 2 * delta + 2 * a - eps) / b2(a) + 0.5) -
-                 s_window((beta - pi + 2 * a) / b2(-a) - 0.5) -
-                 s_window((beta - pi - 2 * delta - eps) / b2(-a) + 0.5)));
-    }
+  parker_table(W, nP, angles, geom, sad, q, parker);
+  for (int i = 0; i < nP; ++i)
     dbeta[i] = (i > 0) ? (angles[i] - angles[i - 1]) / 2 : (angles[1] - angles[0]) / 2;
-  }
   MEXCT_TRY_CUDA(c->tabs.ensure(tab.size() * sizeof(float)), "prefilter: workspace");
   // from a pageable host vector: cudaMemcpyAsync returns once the bytes are
   // staged, so the vector may go out of scope
@@ -1082,6 +1097,30 @@ mexct_status mexct_fp_det(mexct_ctx* ctx, const float* vol, int W, int H, float 
                   c->stream);
   if (s) return s;
   return finish(c, out, c->out, M * 4, "fp_det: download");
+}
+
+mexct_status mexct_parker_weight(const float* sino, int W, int H, int nP, const float* angles,
+                                 int geom, double sad, double q, float* out) {
+  if (nP > 0 && (!sino || !angles || !out))
+    return set_err(MEXCT_ERR_ARG, "parker_weight: NULL pointer");
+  if (bad_dims(W, H) || nP < 0) return set_err(MEXCT_ERR_ARG, "parker_weight: bad dims");
+  if (bad_geom(geom)) return set_err(MEXCT_ERR_ARG, "parker_weight: invalid geometry %d", geom);
+  if (W != H)
+    return set_err(MEXCT_ERR_UNSUPPORTED,
+                   "parker_weight: W (%d) != H (%d); the reference's weighting "
+                   "(parker_weight.m:73) needs a square detector", W, H);
+  if (geom != 0 && !(sad > 0.0)) return set_err(MEXCT_ERR_ARG, "parker_weight: SAD must be > 0");
+  std::vector<float> win((size_t)nP * W);
+  parker_table(W, nP, angles, geom, sad, q, win.data());
+  const size_t P = (size_t)W * H;
+  for (int i = 0; i < nP; ++i) {
+    const float* w = win.data() + (size_t)i * W;
+    for (int v = 0; v < H; ++v) {
+      const size_t r = (size_t)i * P + (size_t)v * W;
+      for (int u = 0; u < W; ++u) out[r + u] = sino[r + u] * w[u];  // :73, in single
+    }
+  }
+  return MEXCT_OK;
 }
 
 mexct_status mexct_bp_det(mexct_ctx* ctx, const float* sino, const mexct_detector* det, int nP,

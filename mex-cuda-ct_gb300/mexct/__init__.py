@@ -14,5 +14,6 @@ from .ops import (  # noqa: F401
     CUDAmex_TVmin_3D,
     FBP_recon,
     general3D_BP_matched,
+    parker_weight,
     preFilterSinogram,
 )

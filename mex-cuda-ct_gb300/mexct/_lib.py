@@ -60,6 +60,7 @@ SIGNATURES = {
     "mexct_tvmin3d": [_P, _P, _i, _i, _i, _f, _i, _P],
     "mexct_prefilter": [_P, _P, _P, _i, _i, _i, _P, _i, _f, _i, _f, _f, _P],
     "mexct_fbp": [_P, _P, _P, _i, _i, _i, _P, _i, _f, _i, _f, _f, _P],
+    "mexct_parker_weight": [_P, _i, _i, _i, _P, _i, _c.c_double, _c.c_double, _P],
     "mexct_fp_dev": [_P, _P, _i, _i, _f, _P, _i, _i, _P, _P],
     "mexct_bp_dev": [_P, _P, _i, _i, _i, _f, _P, _i, _P, _P],
     "mexct_g3d_fp_dev": [_P, _P, _i, _i, _P, _P, _i, _i, _i, _i, _P, _P],

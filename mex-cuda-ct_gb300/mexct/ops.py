@@ -3,7 +3,8 @@
 Host functions keep the reference's names, argument order and array layouts:
 numpy arrays in MATLAB shape and column-major order (``order='F'``), float32
 ("single") data, float32 angles.  Each call goes through the host entry point of
-the C ABI (copy in, GPU compute, copy out), exactly like the MEX gateways:
+the C ABI (copy in, GPU compute, copy out), exactly like the MEX gateways
+(parker_weight computes on the host):
 
 =========================  ==============================================  =====================
 function                    reference                                       C ABI
@@ -15,6 +16,7 @@ CUDAmex_general3D_BP        projection_kernels/CUDAmex_general3D_BP.cu:194  mexc
 CUDAmex_oscIter             iterative_reconstruction/CUDAmex_oscIter.cu:362 mexct_osc_iter
 CUDAmex_TVmin_3D            iterative_reconstruction/CUDAmex_TVmin_3D.cu:162 mexct_tvmin3d
 preFilterSinogram           fbp_reconstruction/preFilterSinogram.m:1        mexct_prefilter
+parker_weight               fbp_reconstruction/parker_weight.m:1            mexct_parker_weight
 FBP_recon                   fbp_reconstruction/FBP_recon.m:1                mexct_fbp
 =========================  ==============================================  =====================
 
@@ -229,6 +231,20 @@ def preFilterSinogram(sino, geom, angles, filter="ramp", frequencyCutoff=1.0, pa
     out = np.empty((W, H, nP), dtype=np.float32, order="F")
     _lib.call("mexct_prefilter", None, _ptr(sino), None, W, H, nP, _ptr(ang), g, sad,
               FILTERS[str(filter).lower()], float(frequencyCutoff), float(parker_q), _ptr(out))
+    return out
+
+
+def parker_weight(sino, angles, geom, q_value=1.0):
+    """weightedSino = parker_weight(sino, angles, geom, q_value) on the host (float32)."""
+    sino = _f32F(sino, "sino")
+    if sino.ndim == 2:
+        sino = sino[:, :, None]
+    W, H, nP = sino.shape
+    g, sad = _geom_struct(geom)
+    ang = _angles(angles, nP)
+    out = np.empty((W, H, nP), dtype=np.float32, order="F")
+    _lib.call("mexct_parker_weight", _ptr(sino), W, H, nP, _ptr(ang), g, float(sad),
+              float(q_value), _ptr(out))
     return out
 
 

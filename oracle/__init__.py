@@ -77,6 +77,7 @@ def _load():
             "orc_num_subsets": [i, i, d, i, i],
             "orc_subset_order": [i, i, I32],
             "orc_prefilter": [F, i, i, i, F, i, d, i, d, d, D],
+            "orc_parker_window": [i, i, F, i, d, d, D],
             "orc_filter_response": [i, i, d, D, i],
             "orc_set_threads": [i],
             "orc_get_threads": [],
@@ -396,6 +397,17 @@ def filter_response(W, filt="ramp", cutoff=1.0):
     if order <= 0:
         raise RuntimeError("filter_response failed")
     return buf[:order].copy()
+
+
+def parker_window(W, angles, geom, q, sad=1000.0):
+    """parker_weight.m's window per view and row element in FP64 -> [nP, W] float64."""
+    lib = _load()
+    ang = np.ascontiguousarray(np.asarray(angles, dtype=np.float32).ravel())
+    out = np.zeros((ang.size, W), dtype=np.float64)
+    rc = lib.orc_parker_window(int(W), ang.size, _p(ang, ctypes.c_float), int(geom), float(sad),
+                               float(q), _p(out, ctypes.c_double))
+    _check(rc, "parker_window")
+    return out
 
 
 def prefilter(sino, geom, angles, filt, cutoff, q, sad=1000.0):

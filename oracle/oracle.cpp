@@ -1132,6 +1132,38 @@ double s_function(double b) {  // parker_weight.m:233-240
 }
 }  // namespace
 
+// parker_weight.m:29-72: the Parker window per view i and row element j
+// (W of them: the reference computes alpha over size(sino, 2) = H = W).
+int orc_parker_window(int W, int nP, const float* angles, int geom, double sad, double q,
+                      double* out) {
+  if (!angles || !out || W <= 0 || nP < 1 || geom < 0 || geom > 2) return 1;
+  const double pi = 3.14159265358979323846;
+  std::vector<double> alpha(W, 0.0);  // :29-32
+  if (geom != 0)
+    for (int j = 0; j < W; ++j) alpha[j] = std::atan((-W / 2.0 + 0.5 + j) / sad);
+  bool incr = true;  // :36-39, all(diff(angles) >= 0)
+  for (int i = 1; i < nP; ++i)
+    if (!(angles[i] - angles[i - 1] >= 0)) incr = false;
+  if (incr)
+    for (int j = 0; j < W; ++j) alpha[j] = -alpha[j];
+  const double delta = std::fabs(alpha[W - 1] - alpha[0]) / 2;  // :42-43
+  const double extent = std::fabs((double)(angles[nP - 1] - angles[0]));
+  const double eps = std::max(extent - (pi + 2 * delta), 0.0);  // :59
+  auto b2 = [&](double a) { return q * (2 * delta - 2 * a + eps); };  // :96-99
+  for (int i = 0; i < nP; ++i) {  // :64-70
+    const double beta = std::fabs((double)(angles[i] - angles[0]));
+    for (int j = 0; j < W; ++j) {
+      const double a = alpha[j];
+      out[(size_t)i * W + j] =
+          0.5 * (s_function(beta / b2(a) - 0.5) +
+                 s_function((beta - 2 * delta + 2 * a - eps) / b2(a) + 0.5) -
+                 s_function((beta - pi + 2 * a) / b2(-a) - 0.5) -
+                 s_function((beta - pi - 2 * delta - eps) / b2(-a) + 0.5));
+    }
+  }
+  return 0;
+}
+
 // preFilterSinogram.m:29-90 with parker_weight.m:28-98.
 int orc_prefilter(const float* sino, int W, int H, int nP,
                   const float* angles, int geom, double sad, int filter,
@@ -1155,32 +1187,9 @@ int orc_prefilter(const float* sino, int W, int H, int nP,
     }
     kern[n] = acc / order;
   }
-  // Parker weights (parker_weight.m:181-228), indexed by the row u.
-  std::vector<double> alpha(H, 0.0);
-  if (geom != 0)
-    for (int j = 0; j < H; ++j)
-      alpha[j] = std::atan((-H / 2.0 + 0.5 + j) / sad);
-  bool incr = true;
-  for (int i = 1; i < nP; ++i)
-    if (!(angles[i] - angles[i - 1] >= 0)) incr = false;
-  if (incr)
-    for (int j = 0; j < H; ++j) alpha[j] = -alpha[j];
-  const double delta = std::fabs(alpha[H - 1] - alpha[0]) / 2;
-  const double extent = std::fabs((double)(angles[nP - 1] - angles[0]));
-  const double eps = std::max(extent - (pi + 2 * delta), 0.0);
-  auto b2 = [&](double a) { return q * (2 * delta - 2 * a + eps); };
+  // Parker weights (parker_weight.m:29-72), indexed by the row u.
   std::vector<double> win((size_t)nP * W);
-  for (int i = 0; i < nP; ++i) {
-    const double beta = std::fabs((double)(angles[i] - angles[0]));
-    for (int j = 0; j < W; ++j) {
-      const double a = alpha[j];
-      win[(size_t)i * W + j] =
-          0.5 * (s_function(beta / b2(a) - 0.5) +
-                 s_function((beta - 2 * delta + 2 * a - eps) / b2(a) + 0.5) -
-                 s_function((beta - pi + 2 * a) / b2(-a) - 0.5) -
-                 s_function((beta - pi - 2 * delta - eps) / b2(-a) + 0.5));
-    }
-  }
+  orc_parker_window(W, nP, angles, geom, sad, q, win.data());
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads())
   for (long long r = 0; r < (long long)H * nP; ++r) {
     const int i = (int)(r / H), v = (int)(r % H);

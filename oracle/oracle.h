@@ -114,6 +114,11 @@ int orc_num_subsets(int s_init, int s_final, double p_val, int max_iters,
                     int k);
 int orc_subset_order(int n_sub, int first_pick, int32_t* picks);
 
+/* parker_weight.m:29-72: the Parker window [nP][W] (view-major) in FP64 for a
+ * W x W detector; q = 1 original Parker, q < 1 Wesarg's modified weights. */
+int orc_parker_window(int W, int nP, const float* angles, int geom, double sad,
+                      double q, double* out);
+
 /* preFilterSinogram.m + parker_weight.m (FDK/FBP pre-filter).
  * filter: 0 none, 1 ramp, 2 shepp-logan, 3 cosine, 4 hamming, 5 hann.
  * geom 0 par3d, 1 fan3d, 2 cone3d.  Requires W == H (see parker_weight.m:225).
