@@ -17,3 +17,4 @@ from .ops import (  # noqa: F401
     parker_weight,
     preFilterSinogram,
 )
+from .solver import OSC_TV_recon  # noqa: F401
