@@ -54,17 +54,35 @@ def subset_order(n, first):
     return out
 
 
+def random_first_picks(numIter, numSubsInit, numSubsFinal, pVal, seed=None):
+    """One random first subset per iteration, 0-based, as OSC_TV_recon.m draws it
+    (randperm(numSubsets, 1), :82) for that iteration's subset count (:76-78)."""
+    rng = np.random.default_rng(seed)
+    return np.array([rng.integers(0, max(1, num_subsets(numSubsInit, numSubsFinal, pVal,
+                                                          numIter, k)))
+                     for k in range(1, int(numIter) + 1)], dtype=np.int32)
+
+
+def _picks(first_picks, numIter, numSubsInit, numSubsFinal, pVal):
+    if first_picks is None:
+        return random_first_picks(numIter, numSubsInit, numSubsFinal, pVal)
+    fp = np.ascontiguousarray(np.asarray(first_picks, dtype=np.int32).ravel())
+    if fp.size < int(numIter):
+        raise ValueError("first_picks needs one entry per iteration")
+    return fp
+
+
 def OSC_TV_recon(pre, post, scanAngles, geom, numIter, TV_constant, numSubsInit, numSubsFinal,
-                 pVal, first_picks):
-    """recon = OSC_TV_recon(...) on the GPU (host arrays in, float32 [W, W, H] out)."""
+                 pVal, first_picks=None):
+    """recon = OSC_TV_recon(...) on the GPU (host arrays in, float32 [W, W, H] out).
+    first_picks: each iteration's first subset (0-based); None draws them at random
+    as the reference does."""
     pre = _f32F(pre, "pre")
     post = _f32F(post, "post")
     W, H, nP = post.shape
     g, sad = _geom_struct(geom)
     ang = _angles(scanAngles, nP)
-    fp = np.ascontiguousarray(np.asarray(first_picks, dtype=np.int32).ravel())
-    if fp.size < int(numIter):
-        raise ValueError("first_picks needs one entry per iteration")
+    fp = _picks(first_picks, numIter, numSubsInit, numSubsFinal, pVal)
     out = np.empty((W, W, H), dtype=np.float32, order="F")
     _lib.call("mexct_osc_tv_recon", None, _ptr(pre), _ptr(post), W, H, nP, _ptr(ang), float(sad),
               g, int(numIter), float(TV_constant), int(numSubsInit), int(numSubsFinal),
@@ -86,15 +104,13 @@ def OSC_TV_recon_ooc(pre, post, scanAngles, geom, numIter, TV_constant, numSubsI
                      numSubsFinal, pVal, first_picks, budget_bytes):
     """OSC_TV_recon with mu in host memory, streamed through the device in
     z-slabs within budget_bytes of device memory.  Returns (recon, slab
-    thickness in slices)."""
+    thickness in slices); first_picks None draws them as the reference does."""
     pre = _f32F(pre, "pre")
     post = _f32F(post, "post")
     W, H, nP = post.shape
     g, sad = _geom_struct(geom)
     ang = _angles(scanAngles, nP)
-    fp = np.ascontiguousarray(np.asarray(first_picks, dtype=np.int32).ravel())
-    if fp.size < int(numIter):
-        raise ValueError("first_picks needs one entry per iteration")
+    fp = _picks(first_picks, numIter, numSubsInit, numSubsFinal, pVal)
     out = np.empty((W, W, H), dtype=np.float32, order="F")
     planes = _i(0)
     _lib.call("mexct_osc_tv_recon_ooc", None, _ptr(pre), _ptr(post), W, H, nP, _ptr(ang),

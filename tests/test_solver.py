@@ -292,3 +292,18 @@ def test_osc_tv_ellipsoid_256_per_iterate_vs_fp64_oracle(cuda, orc):
     assert f16[0] <= 1e-3 and f16[-1] <= 1e-3
     assert max(f16) <= 1e-2
     assert abs(truth["fp16 residual views"] - truth["fp32"]) <= 1e-3 * truth["fp32"]
+
+
+def test_random_first_picks_follow_the_schedule(lib):
+    """With first_picks omitted the mirror draws one first subset per iteration
+    within that iteration's subset count (OSC_TV_recon.m:76-82), reproducibly
+    for a seed."""
+    from mexct import solver
+
+    for args in [(20, 10, 2, 0.5), (5, 8, 8, 1.0), (1, 6, 3, 1.0)]:
+        n_iter, s0, s1, p = args
+        picks = solver.random_first_picks(n_iter, s0, s1, p, seed=3)
+        assert picks.dtype == np.int32 and picks.size == n_iter
+        for k in range(1, n_iter + 1):
+            assert 0 <= picks[k - 1] < solver.num_subsets(s0, s1, p, n_iter, k)
+        assert np.array_equal(picks, solver.random_first_picks(n_iter, s0, s1, p, seed=3))
