@@ -1044,6 +1044,7 @@ Mat73Var describe(File& h, const Link& l) {
     while (v.dims.size() < 2) v.dims.push_back(v.dims.empty() ? 0 : 1);
     return v;
   }
+  elements(D.dims);  // a damaged dataspace is refused here, not at the caller's allocation
   for (size_t i = D.dims.size(); i-- > 0;) v.dims.push_back((long long)D.dims[i]);
   while (v.dims.size() < 2) v.dims.push_back(1);
   return v;
