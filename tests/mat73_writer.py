@@ -314,7 +314,9 @@ class Mat73Writer:
         dseg = self._put(bytes(data))
         return self._put(b"HEAP" + struct.pack("<B3x", 0) + _q(len(data), 1, dseg)), offs
 
-    def save(self, path, dense: bool = False):
+    def save(self, path, dense: bool = False, per_node: int | None = None):
+        """per_node (old style): symbol table nodes of at most this many entries,
+        under a two-level group B-tree (a level-1 root over two level-0 nodes)."""
         links = sorted(self.links)
         if self.new:
             msgs = [(0x02, struct.pack("<BB", 0, 0) + _q(self._put(b"FRHP") if dense else UNDEF,
@@ -329,19 +331,32 @@ class Mat73Writer:
             heap, offs = self._heap([n for n, _ in links])
             ent = [struct.pack("<QQII", off, hdr, 0, 0) + b"\0" * 16
                    for off, (_, hdr) in zip(offs, links)]
-            # two symbol table nodes under one B-tree node (keys: heap offsets)
-            half = max(1, len(ent) // 2)
-            groups = [ent[:half], ent[half:]] if len(ent) > 1 else [ent]
+            # symbol table nodes (keys: heap offsets of each node's last name)
+            if per_node is None:
+                half = max(1, len(ent) // 2)
+                groups = [ent[:half], ent[half:]] if len(ent) > 1 else [ent]
+            else:
+                groups = [ent[i:i + per_node] for i in range(0, len(ent), per_node)]
             snods, keys = [], [0]
             start = 0
             for g in groups:
                 snods.append(self._put(b"SNOD" + struct.pack("<BBH", 1, 0, len(g)) + b"".join(g)))
                 start += len(g)
                 keys.append(offs[start - 1] if offs else 0)
-            body = b"TREE" + struct.pack("<BBH", 0, 0, len(snods)) + _q(UNDEF, UNDEF)
-            for k, s in zip(keys, snods):
-                body += _q(k, s)
-            bt = self._put(body + _q(keys[-1]))
+
+            def tree(level, children, ks):
+                body = b"TREE" + struct.pack("<BBH", 0, level, len(children)) + _q(UNDEF, UNDEF)
+                for k, c in zip(ks, children):
+                    body += _q(k, c)
+                return self._put(body + _q(ks[len(children)]))
+
+            if per_node is None or len(snods) < 2:
+                bt = tree(0, snods, keys)
+            else:  # two level-0 nodes under a level-1 root
+                h = len(snods) // 2
+                left = tree(0, snods[:h], keys[:h + 1])
+                right = tree(0, snods[h:], keys[h:])
+                bt = tree(1, [left, right], [keys[0], keys[h], keys[-1]])
             root = self._header([(0x11, _q(bt, heap))])
             eof = len(self.b) - self.sb
             sb = (SIG + struct.pack("<BBBBBBBB", 0, 0, 0, 0, 0, 8, 8, 0) +

@@ -151,6 +151,22 @@ def test_empty_array_and_scan_sized_names(lib, tmp_path):
         np.testing.assert_array_equal(fileio.read_mat(p, n), np.full((2, 2), i, F))
 
 
+def test_two_level_group_btree(lib, tmp_path):
+    """A root group whose symbol table spans a two-level B-tree (as MATLAB's files
+    get past a few hundred variables): every variable listed and read."""
+    from mexct import fileio
+
+    w = Mat73Writer()
+    names = ["p%03d" % i for i in range(30)]
+    for i, n in enumerate(names):
+        w.add(n, np.full((1, 3), i, np.float32))
+    p = tmp_path / "tree2.mat"
+    w.save(p, per_node=4)
+    assert fileio.mat_list(p) == names
+    for i, n in enumerate(names):
+        np.testing.assert_array_equal(fileio.read_mat(p, n), np.full((1, 3), i, F))
+
+
 def test_dense_groups_and_missing_superblock_are_reported(lib, tmp_path):
     from mexct import _lib, fileio
 
